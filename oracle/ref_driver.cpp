@@ -1,0 +1,64 @@
+// ref_driver.cpp — builds the REFERENCE ITSELF into a small shared library
+// (oracle/_ref/libref_qr.so) so that golden vectors can be generated from it
+// and the oracle restatement (qr_oracle.cpp) can be pinned against it.
+//
+// TEST INFRASTRUCTURE ONLY.  Compiled by oracle/Makefile with the reference
+// headers on the include path, where they lie (read-only); nothing of the
+// reference is copied into this repository.  It needs the reference's source
+// tree, so it is built only on a machine that has it; the golden fixtures it
+// produces are committed under tests/golden/.
+//
+// Entry points mirror the reference API:
+//   RNP::LA::QR::Factor / Factor_unblocked / MultQ / MultQ_unblocked /
+//   GenerateQ / GenerateQ_unblocked   (RNP/LA/QR.hpp:78-570)
+//   RNP::Random::GenerateVector       (RNP/Random.hpp:262-320)
+//   RNP::BLAS::SolveTrM               (RNP/BLAS/BLAS_mix.hpp:2096-2113)
+#include <RNP/LA/QR.hpp>
+#include <RNP/Random.hpp>
+#include <RNP/BLAS.hpp>
+#include <complex>
+#include <cstddef>
+
+typedef std::complex<float> cf;
+typedef std::complex<double> cd;
+
+#define REF_DEF(P, T)                                                                                                   \
+    extern "C" void ref_##P##geqrf(size_t m, size_t n, T *a, size_t lda, T *tau, size_t *lwork, T *work) {           \
+        RNP::LA::QR::Factor<T>(m, n, a, lda, tau, lwork, work);                                                       \
+    }                                                                                                                 \
+    extern "C" void ref_##P##geqr2(size_t m, size_t n, T *a, size_t lda, T *tau, T *work) {                           \
+        RNP::LA::QR::Factor_unblocked<T>(m, n, a, lda, tau, work);                                                    \
+    }                                                                                                                 \
+    extern "C" void ref_##P##unmqr(const char *side, const char *trans, size_t m, size_t n, size_t k, const T *a,     \
+                                   size_t lda, const T *tau, T *c, size_t ldc, size_t *lwork, T *work) {              \
+        RNP::LA::QR::MultQ<T>(side, trans, m, n, k, a, lda, tau, c, ldc, lwork, work);                                \
+    }                                                                                                                 \
+    extern "C" void ref_##P##unm2r(const char *side, const char *trans, size_t m, size_t n, size_t k, const T *a,     \
+                                   size_t lda, const T *tau, T *c, size_t ldc, T *work) {                             \
+        RNP::LA::QR::MultQ_unblocked<T>(side, trans, m, n, k, a, lda, tau, c, ldc, work);                             \
+    }                                                                                                                 \
+    extern "C" void ref_##P##ungqr(size_t m, size_t n, size_t k, T *a, size_t lda, const T *tau, size_t *lwork,      \
+                                   T *work) {                                                                         \
+        RNP::LA::QR::GenerateQ<T>(m, n, k, a, lda, tau, lwork, work);                                                 \
+    }                                                                                                                 \
+    extern "C" void ref_##P##ung2r(size_t m, size_t n, size_t k, T *a, size_t lda, const T *tau, T *work) {           \
+        RNP::LA::QR::GenerateQ_unblocked<T>(m, n, k, a, lda, tau, work);                                              \
+    }                                                                                                                 \
+    extern "C" void ref_##P##trsm_lunn(size_t n, size_t nrhs, const T *a, size_t lda, T *b, size_t ldb) {             \
+        RNP::BLAS::SolveTrM("L", "U", "N", "N", n, nrhs, T(1), a, lda, b, ldb);                                      \
+    }
+
+#define REF_RNG(P, T)                                                                                                   \
+    extern "C" void ref_##P##larnv(int dist, int *iseed, size_t n, T *x) {                                            \
+        RNP::Random::GenerateVector<T>((RNP::Random::Distribution::Distribution)dist, n, x, iseed);                   \
+    }
+
+REF_DEF(s, float)
+REF_DEF(d, double)
+REF_DEF(c, cf)
+REF_DEF(z, cd)
+// GenerateVector<std::complex<float> > does not compile in the reference
+// (RNP/Random.hpp:213 mixes double and float), so no "c" generator here.
+REF_RNG(s, float)
+REF_RNG(d, double)
+REF_RNG(z, cd)
