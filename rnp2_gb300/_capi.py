@@ -1,0 +1,59 @@
+"""ctypes binding of the C ABI declared in include/rnp_gpu/qr_gb300.h.
+
+The library must have been built (``python -m rnp2_gb300._build`` or
+``__graft_entry__.build()``); there is no fallback implementation, so a
+missing library raises immediately.
+"""
+import ctypes as C
+import os
+
+from ._build import LIBPATH
+
+SZ = C.c_size_t
+P = C.c_void_p
+CH = C.c_char_p
+PSZ = C.POINTER(C.c_size_t)
+
+_lib = None
+
+
+class LibraryNotBuilt(RuntimeError):
+    pass
+
+
+def _signatures():
+    sig = {}
+    for p in "sdcz":
+        sig["rnpgpu_%sgeqrf" % p] = [SZ, SZ, P, SZ, P, PSZ, P]
+        sig["rnpgpu_%sgeqr2" % p] = [SZ, SZ, P, SZ, P, P]
+        sig["rnpgpu_%sunmqr" % p] = [CH, CH, SZ, SZ, SZ, P, SZ, P, P, SZ, PSZ, P]
+        sig["rnpgpu_%sunm2r" % p] = [CH, CH, SZ, SZ, SZ, P, SZ, P, P, SZ, P]
+        sig["rnpgpu_%sungqr" % p] = [SZ, SZ, SZ, P, SZ, P, PSZ, P]
+        sig["rnpgpu_%sung2r" % p] = [SZ, SZ, SZ, P, SZ, P, P]
+    sig["rnpgpu_set_stream"] = [P]
+    sig["rnpgpu_get_stream"] = []
+    sig["rnpgpu_get_last_error"] = []
+    sig["rnpgpu_version"] = []
+    return sig
+
+
+RESTYPES = {"rnpgpu_get_stream": P, "rnpgpu_get_last_error": CH, "rnpgpu_version": CH}
+
+
+def lib():
+    """The loaded library; raises LibraryNotBuilt if it is missing."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIBPATH):
+            raise LibraryNotBuilt("%s is missing: build it with __graft_entry__.build()" % LIBPATH)
+        l = C.CDLL(LIBPATH)
+        for name, args in _signatures().items():
+            f = getattr(l, name)
+            f.argtypes = args
+            f.restype = RESTYPES.get(name, C.c_int)
+        _lib = l
+    return _lib
+
+
+def exported_names():
+    return sorted(_signatures().keys())

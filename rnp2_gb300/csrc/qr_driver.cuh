@@ -1,0 +1,518 @@
+// qr_driver.cuh — host side of the blocked Householder QR on one GB300.
+//
+// Mirrors RNP::LA::QR (RNP/LA/QR.hpp): Factor (geqrf), Factor_unblocked
+// (geqr2), MultQ (unmqr/ormqr), MultQ_unblocked (unm2r), GenerateQ
+// (ungqr/orgqr) and GenerateQ_unblocked (ung2r), with caller-owned device
+// work blocks and RNP's *lwork query.  All pointers are device pointers; work
+// is enqueued on the library's current stream and the calls return without
+// synchronizing.
+#pragma once
+#include "qr_kernels.cuh"
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+
+namespace rnpgpu {
+
+// status codes of the C ABI
+enum : int { kOk = 0, kErrCuda = 1, kErrDevice = 2 };
+
+// ---------------------------------------------------------------------------
+// Library context: current stream (per thread), last error, device facts.
+// ---------------------------------------------------------------------------
+struct DeviceFacts {
+    int sm_count = 0;
+    int panel_max_blocks[4] = {0, 0, 0, 0};  // per scalar type index
+};
+cudaStream_t current_stream();
+void set_last_error(const char *msg);
+const DeviceFacts &device_facts();
+
+template <class T> struct TypeIndex;
+template <> struct TypeIndex<float> { static constexpr int v = 0; };
+template <> struct TypeIndex<double> { static constexpr int v = 1; };
+template <> struct TypeIndex<cf32> { static constexpr int v = 2; };
+template <> struct TypeIndex<cf64> { static constexpr int v = 3; };
+
+#define RNPGPU_CHECK(call)                                                  \
+    do {                                                                    \
+        cudaError_t e_ = (call);                                            \
+        if (e_ != cudaSuccess) {                                            \
+            set_last_error(cudaGetErrorString(e_));                         \
+            return kErrCuda;                                                \
+        }                                                                   \
+    } while (0)
+#define RNPGPU_CHECK_LAUNCH() RNPGPU_CHECK(cudaGetLastError())
+
+// Tuning (RNP/LA/QR.hpp:41-51 keeps nb=32, nbmin=2, crossover=128 for the
+// CPU).  On the GPU every column block goes through the blocked path: the
+// unblocked tail of the CPU code would run level-2 work on one thread block.
+struct GpuTuning {
+    static constexpr size_t nb = kPanelMaxCols;
+};
+
+// ---------------------------------------------------------------------------
+// Workspace carving: regions aligned to 256 bytes inside the caller's block.
+// ---------------------------------------------------------------------------
+struct Carver {
+    char *base;
+    size_t off;
+    explicit Carver(void *p) : base((char *)p), off(0) {
+        size_t mis = (size_t)(uintptr_t)base & 255;
+        if (mis) off = 256 - mis;
+    }
+    template <class U> U *take(size_t count) {
+        U *p = base ? (U *)(base + off) : nullptr;
+        off += (count * sizeof(U) + 255) & ~(size_t)255;
+        return p;
+    }
+};
+// bytes -> elements of T, with the 256-byte alignment slack
+template <class T> size_t elems_for(size_t bytes) { return (bytes + 256 + sizeof(T) - 1) / sizeof(T); }
+
+// ---------------------------------------------------------------------------
+// Contraction launcher
+// ---------------------------------------------------------------------------
+template <class T> int launch_gemm(GemmArgs<T> g, int nsplit, cudaStream_t st) {
+    if (g.M <= 0 || g.N <= 0) return kOk;
+    if (g.K <= 0 && g.beta_mode == kBetaOne) return kOk;
+    if (g.kchunk <= 0) g.kchunk = g.K > 0 ? g.K : 1;
+    if (g.N <= 32) {
+        dim3 grid((g.M + 63) / 64, (g.N + 31) / 32, nsplit);
+        k_gemm<T, 64, 32, 16, 4, 2><<<grid, 256, 0, st>>>(g);
+    } else {
+        dim3 grid((g.M + 63) / 64, (g.N + 63) / 64, nsplit);
+        k_gemm<T, 64, 64, 16, 4, 4><<<grid, 256, 0, st>>>(g);
+    }
+    RNPGPU_CHECK_LAUNCH();
+    return kOk;
+}
+
+template <class T> GemmArgs<T> gemm_args(const T *A, size_t lda, int opA, int vunitA, const T *B, size_t ldb, int opB, int vunitB, T *D, size_t ldd, int M, int N, int K, T alpha, int beta_mode) {
+    GemmArgs<T> g;
+    g.A = A; g.lda = lda; g.B = B; g.ldb = ldb; g.D = D; g.ldd = ldd;
+    g.M = M; g.N = N; g.K = K;
+    g.opA = opA; g.opB = opB; g.vunitA = vunitA; g.vunitB = vunitB;
+    g.alpha = alpha; g.beta_mode = beta_mode;
+    g.kchunk = K; g.dstride = 0;
+    return g;
+}
+
+// split-K plan for a reduction of length K producing 'tiles' output tiles
+inline int choose_splits(int K, int tiles, int smax) {
+    const int sm = device_facts().sm_count > 0 ? device_facts().sm_count : 148;
+    int s = (2 * sm + tiles - 1) / std::max(tiles, 1);
+    s = std::min(s, std::max(1, K / 256));
+    s = std::min(s, smax);
+    return std::max(s, 1);
+}
+
+// ---------------------------------------------------------------------------
+// Block reflector application (ApplyBlock, storev "C", dir "F",
+// RNP/LA/Reflector.hpp:725-815).  V is the ib-column reflector block in its
+// stored form (unit diagonal implicit), T its upper triangular factor.
+//   left : C(M x N) <- H C or H^H C :  W = C^H V op(T), C -= V W^H
+//   right: C(M x N) <- C H or C H^H :  W = C V op(T),   C -= W V^H
+// P holds the split-K partials (smax * rows_of_W * ib), W the result.
+// ---------------------------------------------------------------------------
+template <class T> struct BlockWs {
+    T *P;
+    T *W;
+    int smax;
+};
+
+template <class T> int apply_block(bool left, bool notran, int M, int N, int ib, const T *V, size_t ldv, const T *Tm, int ldt, T *C, size_t ldc, const BlockWs<T> &ws, cudaStream_t st) {
+    if (M <= 0 || N <= 0 || ib <= 0) return kOk;
+    int rc;
+    if (left) {
+        // W = C^H V  (N x ib), reduction over the M rows
+        const int tiles = (N + 63) / 64;
+        const int S = choose_splits(M, tiles, ws.smax);
+        const int kchunk = ((M + S - 1) / S + 15) / 16 * 16;
+        const int nsplit = (M + kchunk - 1) / kchunk;
+        GemmArgs<T> g = gemm_args<T>(C, ldc, kOpC, 0, V, ldv, kOpN, 1, ws.P, (size_t)N, N, ib, M, T(1), kBetaZero);
+        g.kchunk = kchunk;
+        g.dstride = (size_t)N * ib;
+        if ((rc = launch_gemm(g, nsplit, st))) return rc;
+        // W := W T (H^H) or W T^H (H)
+        k_sum_times_t<T><<<(N + 7) / 8, 256, 0, st>>>(ws.P, (size_t)N, (size_t)N * ib, nsplit, N, ib, Tm, ldt, notran ? kOpC : kOpN, ws.W, (size_t)N);
+        RNPGPU_CHECK_LAUNCH();
+        // C -= V W^H
+        GemmArgs<T> u = gemm_args<T>(V, ldv, kOpN, 1, ws.W, (size_t)N, kOpC, 0, C, ldc, M, N, ib, T(-1), kBetaOne);
+        return launch_gemm(u, 1, st);
+    } else {
+        // W = C V  (M x ib), reduction over the N columns
+        const int tiles = (M + 63) / 64;
+        const int S = choose_splits(N, tiles, ws.smax);
+        const int kchunk = ((N + S - 1) / S + 15) / 16 * 16;
+        const int nsplit = (N + kchunk - 1) / kchunk;
+        GemmArgs<T> g = gemm_args<T>(C, ldc, kOpN, 0, V, ldv, kOpN, 1, ws.P, (size_t)M, M, ib, N, T(1), kBetaZero);
+        g.kchunk = kchunk;
+        g.dstride = (size_t)M * ib;
+        if ((rc = launch_gemm(g, nsplit, st))) return rc;
+        k_sum_times_t<T><<<(M + 7) / 8, 256, 0, st>>>(ws.P, (size_t)M, (size_t)M * ib, nsplit, M, ib, Tm, ldt, notran ? kOpN : kOpC, ws.W, (size_t)M);
+        RNPGPU_CHECK_LAUNCH();
+        // C -= W V^H
+        GemmArgs<T> u = gemm_args<T>(ws.W, (size_t)M, kOpN, 0, V, ldv, kOpC, 1, C, ldc, M, N, ib, T(-1), kBetaOne);
+        return launch_gemm(u, 1, st);
+    }
+}
+
+// T factor of one reflector block from V and tau (GenerateBlockTr "F","C"):
+// Gram matrix V^H V by a split-K contraction, then the recurrence.
+template <class T> int block_t(int rows, int ib, const T *V, size_t ldv, const T *tau, T *Tout, int ldt, T *Pg, int smax, cudaStream_t st) {
+    const int S = choose_splits(rows, 1, smax);
+    const int kchunk = ((rows + S - 1) / S + 15) / 16 * 16;
+    const int nsplit = (rows + kchunk - 1) / kchunk;
+    GemmArgs<T> g = gemm_args<T>(V, ldv, kOpC, 1, V, ldv, kOpN, 1, Pg, (size_t)kPanelMaxCols, ib, ib, rows, T(1), kBetaZero);
+    g.kchunk = kchunk;
+    g.dstride = (size_t)kPanelMaxCols * kPanelMaxCols;
+    int rc = launch_gemm(g, nsplit, st);
+    if (rc) return rc;
+    k_build_t<T><<<1, kPanelMaxCols, 0, st>>>(Pg, (size_t)kPanelMaxCols * kPanelMaxCols, 0, nsplit, tau, ib, ib, Tout, 0, ldt);
+    RNPGPU_CHECK_LAUNCH();
+    return kOk;
+}
+
+// ---------------------------------------------------------------------------
+// Panel factorization launcher (cooperative grid)
+// ---------------------------------------------------------------------------
+template <class T> struct PanelWs {
+    NormAcc *normp;
+    T *wp;
+    T *alpha_slot;
+    unsigned *sync;  // [0] counter, [1] error word
+    int gmax;
+};
+
+inline int panel_grid(int M, int gmax) {
+    int g = (M + 31) / 32;
+    g = std::min(g, gmax);
+    return std::max(g, 1);
+}
+
+template <class T> int panel_factor(int M, int N, T *A, size_t lda, T *tau, T *Tm, int ldt, const PanelWs<T> &ws, cudaStream_t st) {
+    const int G = panel_grid(M, ws.gmax);
+    PanelArgs<T> p;
+    p.A = A; p.lda = lda; p.M = M; p.N = N; p.tau = tau; p.Tm = Tm; p.ldt = ldt;
+    p.normp = ws.normp; p.wp = ws.wp; p.alpha_slot = ws.alpha_slot;
+    p.counter = ws.sync; p.err = (int *)(ws.sync + 1);
+    p.rows_per_cta = (M + G - 1) / G;
+    RNPGPU_CHECK(cudaMemsetAsync(ws.sync, 0, 2 * sizeof(unsigned), st));
+    void *args[] = {&p};
+    RNPGPU_CHECK(cudaLaunchCooperativeKernel((const void *)k_panel<T>, dim3(G), dim3(kPanelThreads), args, 0, st));
+    return kOk;
+}
+
+template <class T> int panel_gmax() {
+    const DeviceFacts &f = device_facts();
+    int g = f.panel_max_blocks[TypeIndex<T>::v];
+    return std::max(1, std::min(g, f.sm_count));
+}
+
+// ---------------------------------------------------------------------------
+// Workspace plans (bytes), shared by the query and the run
+// ---------------------------------------------------------------------------
+template <class T> size_t panel_ws_bytes(int gmax) {
+    return ((size_t)gmax * sizeof(NormAcc) + 255) / 256 * 256 + ((size_t)gmax * kPanelMaxCols * sizeof(T) + 255) / 256 * 256 + 256 + 256;
+}
+template <class T> PanelWs<T> carve_panel(Carver &cv, int gmax) {
+    PanelWs<T> w;
+    w.normp = cv.take<NormAcc>(gmax);
+    w.wp = cv.take<T>((size_t)gmax * kPanelMaxCols);
+    w.alpha_slot = cv.take<T>(1);
+    w.sync = cv.take<unsigned>(2);
+    w.gmax = gmax;
+    return w;
+}
+template <class T> size_t block_ws_bytes(int rows_w, int smax) {
+    return ((size_t)smax * rows_w * kPanelMaxCols * sizeof(T) + 255) / 256 * 256 + ((size_t)rows_w * kPanelMaxCols * sizeof(T) + 255) / 256 * 256;
+}
+template <class T> BlockWs<T> carve_block(Carver &cv, int rows_w, int smax) {
+    BlockWs<T> w;
+    w.P = cv.take<T>((size_t)smax * rows_w * kPanelMaxCols);
+    w.W = cv.take<T>((size_t)rows_w * kPanelMaxCols);
+    w.smax = smax;
+    return w;
+}
+inline int smax_for(size_t K) { return (int)std::max<size_t>(1, std::min<size_t>(64, K / 256)); }
+template <class T> size_t t_bytes() { return ((size_t)kPanelMaxCols * kPanelMaxCols * sizeof(T) + 255) / 256 * 256; }
+
+// ---------------------------------------------------------------------------
+// Factor (geqrf): RNP/LA/QR.hpp:129-197
+// ---------------------------------------------------------------------------
+template <class T> int geqr2(size_t m, size_t n, T *a, size_t lda, T *tau, T *work);
+
+template <class T> size_t geqrf_bytes(size_t m, size_t n, int smax) {
+    return panel_ws_bytes<T>(panel_gmax<T>()) + t_bytes<T>() + block_ws_bytes<T>((int)n, smax);
+}
+
+template <class T> int geqrf(size_t m, size_t n, T *a, size_t lda, T *tau, size_t *lwork, T *work) {
+    if (lwork == nullptr) return -6;
+    const size_t k = std::min(m, n);
+    if (k == 0) return kOk;
+    if (lda < std::max<size_t>(1, m)) return -4;
+    if (m > (size_t)INT32_MAX || n > (size_t)INT32_MAX) return -1;
+    int smax = smax_for(m);
+    if (work == nullptr || *lwork == 0) {
+        *lwork = elems_for<T>(geqrf_bytes<T>(m, n, smax));
+        return kOk;
+    }
+    if (a == nullptr) return -3;
+    if (tau == nullptr) return -5;
+    while (smax > 1 && elems_for<T>(geqrf_bytes<T>(m, n, smax)) > *lwork) smax /= 2;
+    if (elems_for<T>(geqrf_bytes<T>(m, n, smax)) > *lwork) {
+        // not enough workspace for the blocked code: level-2 code needs n
+        if (*lwork < n) return -6;
+        return geqr2<T>(m, n, a, lda, tau, work);
+    }
+    cudaStream_t st = current_stream();
+    Carver cv(work);
+    const int gmax = panel_gmax<T>();
+    PanelWs<T> pw = carve_panel<T>(cv, gmax);
+    T *Tm = cv.take<T>((size_t)kPanelMaxCols * kPanelMaxCols);
+    BlockWs<T> bw = carve_block<T>(cv, (int)n, smax);
+    const size_t nb = GpuTuning::nb;
+    for (size_t i = 0; i < k; i += nb) {
+        const int ib = (int)std::min(nb, k - i);
+        T *Ai = a + i + i * lda;
+        int rc = panel_factor<T>((int)(m - i), ib, Ai, lda, tau + i, Tm, kPanelMaxCols, pw, st);
+        if (rc) return rc;
+        if (i + ib < n) {
+            rc = apply_block<T>(true, false, (int)(m - i), (int)(n - i - ib), ib, Ai, lda, Tm, kPanelMaxCols, a + i + (i + ib) * lda, lda, bw, st);
+            if (rc) return rc;
+        }
+    }
+    return kOk;
+}
+
+// ---------------------------------------------------------------------------
+// Factor_unblocked (geqr2): RNP/LA/QR.hpp:78-102.  Level-2 kernels, work of
+// length n holds w = v^H C, as in the reference.
+// ---------------------------------------------------------------------------
+template <class T> int larf_launch(bool left, int mc, int nc, const T *v, const T *taup, bool conj_tau, T *C, size_t ldc, T *w, cudaStream_t st) {
+    if (mc <= 0 || nc <= 0) return kOk;
+    if (left) k_larf_w<T><<<(nc + 7) / 8, 256, 0, st>>>(1, mc, nc, v, C, ldc, w);
+    else k_larf_w<T><<<(mc + 255) / 256, 256, 0, st>>>(0, mc, nc, v, C, ldc, w);
+    RNPGPU_CHECK_LAUNCH();
+    dim3 grid((mc + 255) / 256, std::min(nc, 65535));
+    k_larf_update<T><<<grid, 256, 0, st>>>(left ? 1 : 0, mc, nc, v, w, taup, conj_tau ? 1 : 0, C, ldc);
+    RNPGPU_CHECK_LAUNCH();
+    return kOk;
+}
+
+template <class T> int geqr2(size_t m, size_t n, T *a, size_t lda, T *tau, T *work) {
+    const size_t k = std::min(m, n);
+    if (k == 0) return kOk;
+    if (lda < std::max<size_t>(1, m)) return -4;
+    if (a == nullptr) return -3;
+    if (tau == nullptr) return -5;
+    if (work == nullptr && n > 1) return -6;
+    if (m > (size_t)INT32_MAX || n > (size_t)INT32_MAX) return -1;
+    cudaStream_t st = current_stream();
+    for (size_t i = 0; i < k; ++i) {
+        const size_t row = std::min(i + 1, m - 1);
+        k_larfg<T><<<1, 256, 0, st>>>((int)(m - i), a + i + i * lda, a + row + i * lda, tau + i);
+        RNPGPU_CHECK_LAUNCH();
+        if (i + 1 < n) {
+            int rc = larf_launch<T>(true, (int)(m - i), (int)(n - i - 1), a + i + i * lda, tau + i, true, a + i + (i + 1) * lda, lda, work, st);
+            if (rc) return rc;
+        }
+    }
+    return kOk;
+}
+
+// ---------------------------------------------------------------------------
+// MultQ (unmqr): RNP/LA/QR.hpp:337-429.  The T factors of all blocks are
+// built once per call and kept in the workspace.
+// ---------------------------------------------------------------------------
+template <class T> int unm2r(const char *side, const char *trans, size_t m, size_t n, size_t k, const T *a, size_t lda, const T *tau, T *c, size_t ldc, T *work);
+
+template <class T> size_t unmqr_bytes(size_t nq, size_t nw, size_t k, int smax, int sgram) {
+    const size_t nblk = (k + GpuTuning::nb - 1) / GpuTuning::nb;
+    return nblk * t_bytes<T>() + ((size_t)sgram * kPanelMaxCols * kPanelMaxCols * sizeof(T) + 255) / 256 * 256 + block_ws_bytes<T>((int)nw, smax);
+}
+
+template <class T> int unmqr(const char *side, const char *trans, size_t m, size_t n, size_t k, const T *a, size_t lda, const T *tau, T *c, size_t ldc, size_t *lwork, T *work) {
+    if (side == nullptr) return -1;
+    if (trans == nullptr) return -2;
+    if (lwork == nullptr) return -11;
+    if (m == 0 || n == 0 || k == 0) return kOk;
+    const bool left = (side[0] == 'L'), notran = (trans[0] == 'N');
+    const size_t nq = left ? m : n, nw = left ? n : m;
+    if (k > nq) return -5;
+    if (lda < std::max<size_t>(1, nq)) return -7;
+    if (ldc < std::max<size_t>(1, m)) return -10;
+    if (m > (size_t)INT32_MAX || n > (size_t)INT32_MAX) return -3;
+    int smax = smax_for(nq);
+    int sgram = smax_for(nq);
+    if (work == nullptr || *lwork == 0) {
+        *lwork = elems_for<T>(unmqr_bytes<T>(nq, nw, k, smax, sgram));
+        return kOk;
+    }
+    if (a == nullptr) return -6;
+    if (tau == nullptr) return -8;
+    if (c == nullptr) return -9;
+    while ((smax > 1 || sgram > 1) && elems_for<T>(unmqr_bytes<T>(nq, nw, k, smax, sgram)) > *lwork) {
+        smax = std::max(1, smax / 2);
+        sgram = std::max(1, sgram / 2);
+    }
+    if (elems_for<T>(unmqr_bytes<T>(nq, nw, k, smax, sgram)) > *lwork) {
+        if (*lwork < nw) return -11;
+        return unm2r<T>(side, trans, m, n, k, a, lda, tau, c, ldc, work);
+    }
+    cudaStream_t st = current_stream();
+    Carver cv(work);
+    const size_t nb = GpuTuning::nb;
+    const size_t nblk = (k + nb - 1) / nb;
+    T *Tc = cv.take<T>(nblk * kPanelMaxCols * kPanelMaxCols);
+    T *Pg = cv.take<T>((size_t)sgram * kPanelMaxCols * kPanelMaxCols);
+    BlockWs<T> bw = carve_block<T>(cv, (int)nw, smax);
+    for (size_t b = 0; b < nblk; ++b) {
+        const size_t i = b * nb;
+        const int ib = (int)std::min(nb, k - i);
+        int rc = block_t<T>((int)(nq - i), ib, a + i + i * lda, lda, tau + i, Tc + b * kPanelMaxCols * kPanelMaxCols, kPanelMaxCols, Pg, sgram, st);
+        if (rc) return rc;
+    }
+    const bool forward = (left && !notran) || (!left && notran);
+    for (size_t s = 0; s < nblk; ++s) {
+        const size_t b = forward ? s : nblk - 1 - s;
+        const size_t i = b * nb;
+        const int ib = (int)std::min(nb, k - i);
+        const T *V = a + i + i * lda;
+        const T *Tb = Tc + b * kPanelMaxCols * kPanelMaxCols;
+        int rc;
+        if (left) rc = apply_block<T>(true, notran, (int)(m - i), (int)n, ib, V, lda, Tb, kPanelMaxCols, c + i, ldc, bw, st);
+        else rc = apply_block<T>(false, notran, (int)m, (int)(n - i), ib, V, lda, Tb, kPanelMaxCols, c + i * ldc, ldc, bw, st);
+        if (rc) return rc;
+    }
+    return kOk;
+}
+
+// MultQ_unblocked (unm2r): RNP/LA/QR.hpp:234-298
+template <class T> int unm2r(const char *side, const char *trans, size_t m, size_t n, size_t k, const T *a, size_t lda, const T *tau, T *c, size_t ldc, T *work) {
+    if (side == nullptr) return -1;
+    if (trans == nullptr) return -2;
+    if (m < 1 || n < 1 || k < 1) return kOk;
+    const bool left = (side[0] == 'L'), notran = (trans[0] == 'N');
+    const size_t nq = left ? m : n;
+    if (k > nq) return -5;
+    if (lda < std::max<size_t>(1, nq)) return -7;
+    if (ldc < std::max<size_t>(1, m)) return -10;
+    if (a == nullptr) return -6;
+    if (tau == nullptr) return -8;
+    if (c == nullptr) return -9;
+    if (work == nullptr) return -11;
+    if (m > (size_t)INT32_MAX || n > (size_t)INT32_MAX) return -3;
+    cudaStream_t st = current_stream();
+    const bool forward = (left && !notran) || (!left && notran);
+    for (size_t s = 0; s < k; ++s) {
+        const size_t i = forward ? s : k - 1 - s;
+        int rc;
+        if (left) rc = larf_launch<T>(true, (int)(m - i), (int)n, a + i + i * lda, tau + i, !notran, c + i, ldc, work, st);
+        else rc = larf_launch<T>(false, (int)m, (int)(n - i), a + i + i * lda, tau + i, !notran, c + i * ldc, ldc, work, st);
+        if (rc) return rc;
+    }
+    return kOk;
+}
+
+// ---------------------------------------------------------------------------
+// GenerateQ (ungqr): RNP/LA/QR.hpp:509-570.  Blocks are processed backwards;
+// block i is applied to the columns to its right (ApplyBlock "L","N") and
+// its own columns become  I - V (T V1^H).
+// ---------------------------------------------------------------------------
+template <class T> int ung2r(size_t m, size_t n, size_t k, T *a, size_t lda, const T *tau, T *work);
+
+template <class T> size_t ungqr_bytes(size_t m, size_t n, int smax, int sgram) {
+    return 2 * t_bytes<T>() + ((size_t)sgram * kPanelMaxCols * kPanelMaxCols * sizeof(T) + 255) / 256 * 256 + block_ws_bytes<T>((int)n, smax);
+}
+
+template <class T> int ungqr(size_t m, size_t n, size_t k, T *a, size_t lda, const T *tau, size_t *lwork, T *work) {
+    if (lwork == nullptr) return -7;
+    if (n == 0) return kOk;
+    if (k > n) return -3;
+    if (n > m) return -2;
+    if (lda < std::max<size_t>(1, m)) return -5;
+    if (m > (size_t)INT32_MAX) return -1;
+    int smax = smax_for(m), sgram = smax_for(m);
+    if (work == nullptr || *lwork == 0) {
+        *lwork = elems_for<T>(ungqr_bytes<T>(m, n, smax, sgram));
+        return kOk;
+    }
+    if (a == nullptr) return -4;
+    if (tau == nullptr && k > 0) return -6;
+    while ((smax > 1 || sgram > 1) && elems_for<T>(ungqr_bytes<T>(m, n, smax, sgram)) > *lwork) {
+        smax = std::max(1, smax / 2);
+        sgram = std::max(1, sgram / 2);
+    }
+    if (elems_for<T>(ungqr_bytes<T>(m, n, smax, sgram)) > *lwork) {
+        if (*lwork < n) return -7;
+        return ung2r<T>(m, n, k, a, lda, tau, work);
+    }
+    cudaStream_t st = current_stream();
+    Carver cv(work);
+    T *Tm = cv.take<T>((size_t)kPanelMaxCols * kPanelMaxCols);
+    T *Y = cv.take<T>((size_t)kPanelMaxCols * kPanelMaxCols);
+    T *Pg = cv.take<T>((size_t)sgram * kPanelMaxCols * kPanelMaxCols);
+    BlockWs<T> bw = carve_block<T>(cv, (int)n, smax);
+    if (k < n) {
+        dim3 grid((unsigned)std::min<size_t>((m + 255) / 256, 1024), (unsigned)std::min<size_t>(n - k, 65535));
+        k_identity_cols<T><<<grid, 256, 0, st>>>((int)m, (int)k, (int)n, a, lda);
+        RNPGPU_CHECK_LAUNCH();
+    }
+    const size_t nb = GpuTuning::nb;
+    const size_t nblk = (k + nb - 1) / nb;
+    for (size_t s = 0; s < nblk; ++s) {
+        const size_t b = nblk - 1 - s;
+        const size_t i = b * nb;
+        const int ib = (int)std::min(nb, k - i);
+        T *V = a + i + i * lda;
+        int rc = block_t<T>((int)(m - i), ib, V, lda, tau + i, Tm, kPanelMaxCols, Pg, sgram, st);
+        if (rc) return rc;
+        if (i + ib < n) {
+            rc = apply_block<T>(true, true, (int)(m - i), (int)(n - i - ib), ib, V, lda, Tm, kPanelMaxCols, a + i + (i + ib) * lda, lda, bw, st);
+            if (rc) return rc;
+        }
+        k_t_v1h<T><<<1, kPanelMaxCols * kPanelMaxCols, 0, st>>>(Tm, kPanelMaxCols, V, lda, ib, Y, kPanelMaxCols);
+        RNPGPU_CHECK_LAUNCH();
+        // V block columns <- I - V Y  (in place: each thread block owns whole rows)
+        GemmArgs<T> g = gemm_args<T>(V, lda, kOpN, 1, Y, (size_t)kPanelMaxCols, kOpN, 0, V, lda, (int)(m - i), ib, ib, T(-1), kBetaIdentity);
+        if ((rc = launch_gemm(g, 1, st))) return rc;
+        if (i > 0) {
+            dim3 grid((unsigned)std::min<size_t>((i + 255) / 256, 1024), (unsigned)ib);
+            k_zero_rows<T><<<grid, 256, 0, st>>>((int)i, (int)i, (int)i + ib, a, lda);
+            RNPGPU_CHECK_LAUNCH();
+        }
+    }
+    return kOk;
+}
+
+// GenerateQ_unblocked (ung2r): RNP/LA/QR.hpp:451-485
+template <class T> int ung2r(size_t m, size_t n, size_t k, T *a, size_t lda, const T *tau, T *work) {
+    if (n < 1) return kOk;
+    if (k > n) return -3;
+    if (n > m) return -2;
+    if (lda < std::max<size_t>(1, m)) return -5;
+    if (a == nullptr) return -4;
+    if (tau == nullptr && k > 0) return -6;
+    if (work == nullptr && n > 1) return -7;
+    if (m > (size_t)INT32_MAX) return -1;
+    cudaStream_t st = current_stream();
+    if (k < n) {
+        dim3 grid((unsigned)std::min<size_t>((m + 255) / 256, 1024), (unsigned)std::min<size_t>(n - k, 65535));
+        k_identity_cols<T><<<grid, 256, 0, st>>>((int)m, (int)k, (int)n, a, lda);
+        RNPGPU_CHECK_LAUNCH();
+    }
+    for (size_t s = 0; s < k; ++s) {
+        const size_t i = k - 1 - s;
+        if (i + 1 < n) {
+            int rc = larf_launch<T>(true, (int)(m - i), (int)(n - i - 1), a + i + i * lda, tau + i, false, a + i + (i + 1) * lda, lda, work, st);
+            if (rc) return rc;
+        }
+        k_ung2r_col<T><<<(unsigned)std::min<size_t>((m + 255) / 256, 1024), 256, 0, st>>>((int)m, (int)i, a, lda, tau);
+        RNPGPU_CHECK_LAUNCH();
+    }
+    return kOk;
+}
+
+} // namespace rnpgpu

@@ -1,0 +1,556 @@
+// qr_kernels.cuh — device kernels of the blocked Householder QR path.
+//
+//   k_panel        panel factorization (geqr2 on an M x ib panel) across a
+//                  cooperative grid, reflector generation with safe-scaled
+//                  norms (RNP/LA/Reflector.hpp:117-158, Generate), the
+//                  in-panel applications (Reflector.hpp:191-236, Apply) and
+//                  the compact-WY T factor (Reflector.hpp:580-626,
+//                  GenerateBlockTr "F","C"), all in one launch
+//   k_gemm         tiled contraction  D = alpha*op(A)*op(B) (+ D | + I),
+//                  split-K capable; every step of ApplyBlock
+//                  (Reflector.hpp:725-815) and the Gram matrix of
+//                  GenerateBlockTr is one call of it
+//   k_sum_times_t  W = (sum of split-K partials) * op(T)
+//   k_build_t      T recurrence from a Gram matrix and tau
+//   k_larfg / k_larf_*   level-2 kernels for the *_unblocked entry points
+#pragma once
+#include "rnp_common.cuh"
+
+namespace rnpgpu {
+
+constexpr int kPanelMaxCols = 32;
+constexpr int kPanelThreads = 256;
+
+template <class T> __device__ __forceinline__ T ldcg(const T *p) { return *(volatile const T *)p; }
+__device__ __forceinline__ double ldcg(const double *p) { return __ldcg(p); }
+__device__ __forceinline__ float ldcg(const float *p) { return __ldcg(p); }
+__device__ __forceinline__ cf64 ldcg(const cf64 *p) { double2 v = __ldcg((const double2 *)p); return cf64(v.x, v.y); }
+__device__ __forceinline__ cf32 ldcg(const cf32 *p) { float2 v = __ldcg((const float2 *)p); return cf32(v.x, v.y); }
+
+template <class T> __device__ __forceinline__ T tzero() { return T(0); }
+template <class T> __device__ __forceinline__ T tone() { return T(1); }
+
+// ---------------------------------------------------------------------------
+// Reflector scalars from (alpha, ||x||):  beta = -sign(Re alpha)*||[alpha;x]||,
+// tau = (beta-alpha)/beta, scal = 1/(alpha-beta), including the safmin
+// rescaling of Reflector.hpp:133-148.  Computed in FP64 for every type.
+// ---------------------------------------------------------------------------
+template <class T> struct ReflScalars {
+    T tau, scal;      // scal multiplies x after 'knt' multiplications by rsafmn
+    double sr, si;    // scal in FP64 (the FP32 forms scale x in FP64)
+    double beta;      // final beta (already scaled back)
+    int knt;
+    bool identity;    // tau == 0: H = I, x and alpha untouched
+};
+
+template <class T> __device__ ReflScalars<T> reflector_scalars(T alpha, const NormAcc &nacc) {
+    typedef typename Tr<T>::R R;
+    ReflScalars<T> s;
+    const double xnorm = nacc.result();
+    double ar = (double)Tr<T>::re(alpha), ai = (double)Tr<T>::im(alpha);
+    s.knt = 0;
+    if (xnorm == 0.0 && ai == 0.0) {
+        s.identity = true;
+        s.tau = T(0);
+        s.scal = T(1);
+        s.sr = 1.0;
+        s.si = 0.0;
+        s.beta = ar;
+        return s;
+    }
+    s.identity = false;
+    double beta = hypot3(ar, ai, xnorm);
+    if (ar > 0.0) beta = -beta;
+    // The FP32 forms carry beta in FP64, where FP32 magnitudes never reach the
+    // safmin region; the rescaling only ever triggers for FP64 data.
+    const bool is64 = sizeof(R) == 8;
+    if (is64) {
+        const double safmin = 0x1p-1022 / (2.0 * 0x1p-52);
+        const double rsafmn = 1.0 / safmin;
+        if (fabs(beta) < safmin) {
+            // as the reference, rescale x and alpha by 1/safmin until beta is
+            // representable accurately; the norm of the rescaled x comes from
+            // the accumulators scaled by the same power of two
+            double mult = 1.0;
+            do {
+                ++s.knt;
+                beta *= rsafmn;
+                ar *= rsafmn;
+                ai *= rsafmn;
+                mult *= rsafmn;
+            } while (fabs(beta) < safmin && s.knt < 1);
+            const double xn = nacc.result_scaled(mult);
+            beta = hypot3(ar, ai, xn);
+            if (ar > 0.0) beta = -beta;
+        }
+    }
+    double tr = (beta - ar) / beta, ti = -ai / beta;
+    double sr, si;
+    if (Tr<T>::is_complex) {
+        crecip(ar - beta, ai, sr, si);
+    } else {
+        sr = 1.0 / (ar - beta);
+        si = 0.0;
+    }
+    s.tau = Tr<T>::make((R)tr, (R)ti);
+    s.scal = Tr<T>::make((R)sr, (R)si);
+    s.sr = sr;
+    s.si = si;
+    if (s.knt) {
+        const double safmin = 0x1p-1022 / (2.0 * 0x1p-52);
+        for (int q = 0; q < s.knt; ++q) beta *= safmin;
+    }
+    s.beta = beta;
+    return s;
+}
+
+template <class T> __device__ __forceinline__ T scale_x(T x, const ReflScalars<T> &s) {
+    typedef typename Tr<T>::R R;
+    if (sizeof(R) == 8) {
+        for (int q = 0; q < s.knt; ++q) x = x * (R)(1.0 / (0x1p-1022 / (2.0 * 0x1p-52)));
+        return x * s.scal;
+    }
+    return x * s.scal;
+}
+// FP32 types: v = x/(alpha-beta) evaluated in FP64 and rounded once
+__device__ __forceinline__ float scale_x(float x, const ReflScalars<float> &s) { return (float)((double)x * s.sr); }
+__device__ __forceinline__ cf32 scale_x(cf32 x, const ReflScalars<cf32> &s) {
+    double xr = x.x, xi = x.y;
+    return cf32((float)(xr * s.sr - xi * s.si), (float)(xr * s.si + xi * s.sr));
+}
+
+// ---------------------------------------------------------------------------
+// Panel factorization across a cooperative grid.
+// Rows [b*R, min(M,(b+1)*R)) of the panel belong to block b.  Per column j:
+//   barrier 1: every block combines the norm partials of x = A[j+1:M, j]
+//              and forms beta/tau/scal identically; scales its rows of x;
+//              accumulates, over its rows, w_c = v^H A[:,c] (c > j) and the
+//              Gram column g_c = V[:,c]^H v (c < j)
+//   barrier 2: every block combines w and applies H^H to its rows of the
+//              trailing panel columns, then accumulates the norm partials of
+//              the next column; block 0 extends T by one column.
+// Two grid barriers per column; no atomics on data, so the result is
+// deterministic for a given grid size.
+// ---------------------------------------------------------------------------
+template <class T> struct PanelArgs {
+    T *A;
+    size_t lda;
+    int M, N;            // panel rows and columns, N <= kPanelMaxCols, M >= N
+    T *tau;              // N
+    T *Tm;               // N x N upper triangular T factor (ldt); may be null
+    int ldt;
+    NormAcc *normp;      // [gridDim.x]
+    T *wp;               // [gridDim.x][kPanelMaxCols]
+    T *alpha_slot;       // [1]
+    unsigned *counter;   // zeroed before launch
+    int *err;            // zeroed before launch
+    int rows_per_cta;
+};
+
+template <class T> __global__ void __launch_bounds__(kPanelThreads) k_panel(PanelArgs<T> p) {
+    const int G = gridDim.x, b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nwarps = kPanelThreads / 32;
+    const int r0 = b * p.rows_per_cta;
+    const int r1 = min(p.M, r0 + p.rows_per_cta);
+    const size_t lda = p.lda;
+    T *A = p.A;
+    GridBarrier bar{p.counter, p.err, (unsigned)G, 0u};
+
+    __shared__ T s_T[kPanelMaxCols][kPanelMaxCols + 1];
+    __shared__ T s_w[kPanelMaxCols];
+    __shared__ NormAcc s_nacc[kPanelThreads / 32];
+    __shared__ ReflScalars<T> s_refl;
+
+    auto norm_partial = [&](int col) {
+        NormAcc acc;
+        acc.zero();
+        for (int r = max(r0, col + 1) + tid; r < r1; r += kPanelThreads) acc.add(A[r + (size_t)col * lda]);
+        acc.warp_reduce();
+        if (lane == 0) s_nacc[warp] = acc;
+        __syncthreads();
+        if (tid == 0) {
+            NormAcc t = s_nacc[0];
+            for (int w = 1; w < nwarps; ++w) t.merge(s_nacc[w]);
+            p.normp[b] = t;
+            if (col >= r0 && col < r1) *p.alpha_slot = A[col + (size_t)col * lda];
+        }
+    };
+
+    norm_partial(0);
+    if (!bar.sync()) return;
+
+    for (int j = 0; j < p.N; ++j) {
+        // (1) combine norm partials; reflector scalars (identical in every block)
+        if (warp == 0) {
+            NormAcc acc;
+            acc.zero();
+            for (int q = lane; q < G; q += 32) {
+                NormAcc t;
+                t.sml = __ldcg(&p.normp[q].sml);
+                t.med = __ldcg(&p.normp[q].med);
+                t.big = __ldcg(&p.normp[q].big);
+                acc.merge(t);
+            }
+            acc.warp_reduce();
+            if (lane == 0) s_refl = reflector_scalars<T>(ldcg(p.alpha_slot), acc);
+        }
+        __syncthreads();
+        const ReflScalars<T> rs = s_refl;
+        // (2) scale x into v on own rows; beta into the diagonal; tau
+        if (!rs.identity) {
+            for (int r = max(r0, j + 1) + tid; r < r1; r += kPanelThreads) {
+                T x = A[r + (size_t)j * lda];
+                A[r + (size_t)j * lda] = scale_x(x, rs);
+            }
+            if (tid == 0 && j >= r0 && j < r1) A[j + (size_t)j * lda] = Tr<T>::make((typename Tr<T>::R)rs.beta, 0);
+        }
+        if (b == 0 && tid == 0) p.tau[j] = rs.tau;
+        __syncthreads();
+        // (3) partial sums over own rows r >= j (v_j = 1):
+        //     c > j: w_c = sum conj(v_r) A[r,c];  c < j: g_c = sum conj(V[r,c]) v_r
+        for (int c = warp; c < p.N; c += nwarps) {
+            if (c == j) continue;
+            T acc = T(0);
+            for (int r = max(r0, j) + lane; r < r1; r += 32) {
+                T v = (r == j) ? T(1) : A[r + (size_t)j * lda];
+                T a = A[r + (size_t)c * lda];
+                acc = (c > j) ? fmac(Tr<T>::conj(v), a, acc) : fmac(Tr<T>::conj(a), v, acc);
+            }
+            acc = warp_sum(acc);
+            if (lane == 0) p.wp[(size_t)b * kPanelMaxCols + c] = acc;
+        }
+        if (!bar.sync()) return;
+        // (4) combine w/g
+        for (int c = warp; c < p.N; c += nwarps) {
+            if (c == j) continue;
+            T acc = T(0);
+            for (int q = lane; q < G; q += 32) acc = acc + ldcg(&p.wp[(size_t)q * kPanelMaxCols + c]);
+            acc = warp_sum(acc);
+            if (lane == 0) s_w[c] = acc;
+        }
+        __syncthreads();
+        if (!rs.identity && j + 1 < p.N) {
+            const T ctau = Tr<T>::conj(rs.tau);
+            for (int r = max(r0, j) + tid; r < r1; r += kPanelThreads) {
+                T v = (r == j) ? T(1) : A[r + (size_t)j * lda];
+                T cv = ctau * v;
+                for (int c = j + 1; c < p.N; ++c) {
+                    T a = A[r + (size_t)c * lda];
+                    A[r + (size_t)c * lda] = fmac(-cv, s_w[c], a);
+                }
+            }
+        }
+        if (b == 0) {
+            // T(0:j, j) = -tau_j * T(0:j, 0:j) * g(0:j);  T(j, j) = tau_j
+            if (tid < j) {
+                T acc = T(0);
+                for (int l = tid; l < j; ++l) acc = fmac(s_T[tid][l], s_w[l], acc);
+                s_T[tid][j] = rs.identity ? T(0) : (-rs.tau) * acc;
+            }
+            if (tid == 0) s_T[j][j] = rs.tau;
+        }
+        if (j + 1 < p.N) {
+            __syncthreads();
+            norm_partial(j + 1);
+            if (!bar.sync()) return;
+        }
+    }
+    if (b == 0 && p.Tm != nullptr) {
+        __syncthreads();
+        for (int idx = tid; idx < p.N * p.N; idx += kPanelThreads) {
+            int r = idx % p.N, c = idx / p.N;
+            if (r <= c) p.Tm[r + (size_t)c * p.ldt] = s_T[r][c];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Generic tiled contraction on CUDA cores.
+//   D(m,n) = alpha * sum_k opA(m,k) * opB(k,n)  [+ D(m,n) | + delta(m,n)]
+// op: 0 = N, 1 = T, 2 = C (conjugate transpose).  An operand flagged
+// "vunit" is a Householder block V read in its stored coordinates (row,col):
+// zero above the diagonal, one on it (RNP/LA/Reflector.hpp:530-545).
+// blockIdx.z splits K into chunks of 'kchunk'; chunk z writes D + z*dstride.
+// ---------------------------------------------------------------------------
+enum { kOpN = 0, kOpT = 1, kOpC = 2 };
+enum { kBetaZero = 0, kBetaOne = 1, kBetaIdentity = 2 };
+
+template <class T> struct GemmArgs {
+    const T *A;
+    size_t lda;
+    const T *B;
+    size_t ldb;
+    T *D;
+    size_t ldd;
+    int M, N, K;
+    int opA, opB;
+    int vunitA, vunitB;
+    T alpha;
+    int beta_mode;
+    int kchunk;
+    size_t dstride;
+};
+
+template <class T> __device__ __forceinline__ T load_op(const T *X, size_t ldx, int op, int vunit, int i, int k) {
+    // element (i,k) of op(X): stored coordinates (row, col)
+    int row = (op == kOpN) ? i : k, col = (op == kOpN) ? k : i;
+    T v;
+    if (vunit && row <= col) v = (row == col) ? T(1) : T(0);
+    else v = X[row + (size_t)col * ldx];
+    return (op == kOpC) ? Tr<T>::conj(v) : v;
+}
+
+template <class T, int BM, int BN, int BK, int TM, int TN>
+__global__ void __launch_bounds__((BM / TM) * (BN / TN)) k_gemm(GemmArgs<T> g) {
+    constexpr int NT = (BM / TM) * (BN / TN);
+    constexpr int TX = BN / TN;  // threads along n
+    __shared__ T sA[BK][BM + 1];
+    __shared__ T sB[BK][BN + 1];
+    const int tid = threadIdx.x;
+    const int tx = tid % TX, ty = tid / TX;
+    const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
+    const int kbeg = blockIdx.z * g.kchunk;
+    const int kend = min(g.K, kbeg + g.kchunk);
+    T acc[TM][TN];
+#pragma unroll
+    for (int i = 0; i < TM; ++i)
+#pragma unroll
+        for (int j = 0; j < TN; ++j) acc[i][j] = T(0);
+
+    for (int k0 = kbeg; k0 < kend; k0 += BK) {
+        // A tile: BM x BK of op(A); coalesce along the stored leading dimension
+        for (int idx = tid; idx < BM * BK; idx += NT) {
+            int mi, ki;
+            if (g.opA == kOpN) { mi = idx % BM; ki = idx / BM; }
+            else { ki = idx % BK; mi = idx / BK; }
+            int gm = m0 + mi, gk = k0 + ki;
+            sA[ki][mi] = (gm < g.M && gk < kend) ? load_op(g.A, g.lda, g.opA, g.vunitA, gm, gk) : T(0);
+        }
+        for (int idx = tid; idx < BN * BK; idx += NT) {
+            int ni, ki;
+            if (g.opB == kOpN) { ki = idx % BK; ni = idx / BK; }
+            else { ni = idx % BN; ki = idx / BN; }
+            int gn = n0 + ni, gk = k0 + ki;
+            sB[ki][ni] = (gn < g.N && gk < kend) ? load_op(g.B, g.ldb, g.opB, g.vunitB, gk, gn) : T(0);
+        }
+        __syncthreads();
+#pragma unroll 4
+        for (int kk = 0; kk < BK; ++kk) {
+            T a[TM], bb[TN];
+#pragma unroll
+            for (int i = 0; i < TM; ++i) a[i] = sA[kk][ty + i * (BM / TM)];
+#pragma unroll
+            for (int j = 0; j < TN; ++j) bb[j] = sB[kk][tx + j * TX];
+#pragma unroll
+            for (int i = 0; i < TM; ++i)
+#pragma unroll
+                for (int j = 0; j < TN; ++j) acc[i][j] = fmac(a[i], bb[j], acc[i][j]);
+        }
+        __syncthreads();
+    }
+    T *D = g.D + (size_t)blockIdx.z * g.dstride;
+#pragma unroll
+    for (int i = 0; i < TM; ++i) {
+        int gm = m0 + ty + i * (BM / TM);
+        if (gm >= g.M) continue;
+#pragma unroll
+        for (int j = 0; j < TN; ++j) {
+            int gn = n0 + tx + j * TX;
+            if (gn >= g.N) continue;
+            T v = g.alpha * acc[i][j];
+            T *dp = &D[gm + (size_t)gn * g.ldd];
+            if (g.beta_mode == kBetaOne) v = v + *dp;
+            else if (g.beta_mode == kBetaIdentity && gm == gn) v = v + T(1);
+            *dp = v;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// W(r, :) = (sum_s P_s(r, :)) * op(T), T upper triangular k x k.
+// op 0: T, op 2: T^H.   P_s has leading dimension ldp, stride pstride.
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void __launch_bounds__(256) k_sum_times_t(const T *P, size_t ldp, size_t pstride, int nsplit, int rows, int k, const T *Tm, int ldt, int opT, T *W, size_t ldw) {
+    __shared__ T sT[kPanelMaxCols][kPanelMaxCols + 1];
+    __shared__ T sW[8][kPanelMaxCols + 1];
+    const int tid = threadIdx.x;
+    for (int idx = tid; idx < k * k; idx += 256) {
+        int r = idx % k, c = idx / k;
+        sT[r][c] = (r <= c) ? Tm[r + (size_t)c * ldt] : T(0);
+    }
+    const int rl = tid / kPanelMaxCols, j = tid % kPanelMaxCols;
+    const int row = blockIdx.x * 8 + rl;
+    T s = T(0);
+    if (row < rows && j < k)
+        for (int q = 0; q < nsplit; ++q) s = s + P[(size_t)q * pstride + row + (size_t)j * ldp];
+    sW[rl][j] = s;
+    __syncthreads();
+    if (row < rows && j < k) {
+        T acc = T(0);
+        if (opT == kOpN) {
+            for (int l = 0; l <= j; ++l) acc = fmac(sW[rl][l], sT[l][j], acc);
+        } else {
+            for (int l = j; l < k; ++l) acc = fmac(sW[rl][l], Tr<T>::conj(sT[j][l]), acc);
+        }
+        W[row + (size_t)j * ldw] = acc;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// T factors from Gram matrices (GenerateBlockTr "F","C" recurrence,
+// RNP/LA/Reflector.hpp:588-622):  for i = 0..k-1,
+//   T(0:i, i) = -tau_i * T(0:i,0:i) * G(0:i, i),  T(i,i) = tau_i
+// with G = V^H V (sum of nsplit partials).  One block per reflector block.
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void __launch_bounds__(kPanelMaxCols) k_build_t(const T *P, size_t pstride_split, size_t pstride_blk, int nsplit, const T *tau, int nb, int k_total, T *Tout, size_t tstride, int ldt) {
+    __shared__ T sG[kPanelMaxCols][kPanelMaxCols + 1];
+    __shared__ T sT[kPanelMaxCols][kPanelMaxCols + 1];
+    const int blk = blockIdx.x, tid = threadIdx.x;
+    const int i0 = blk * nb;
+    const int k = min(nb, k_total - i0);
+    const T *Pb = P + (size_t)blk * pstride_blk;
+    for (int c = 0; c < k; ++c) {
+        if (tid < k) {
+            T s = T(0);
+            for (int q = 0; q < nsplit; ++q) s = s + Pb[(size_t)q * pstride_split + tid + (size_t)c * kPanelMaxCols];
+            sG[tid][c] = s;
+        }
+    }
+    __syncthreads();
+    for (int i = 0; i < k; ++i) {
+        T ti = tau[i0 + i];
+        if (tid < i) {
+            T acc = T(0);
+            for (int l = tid; l < i; ++l) acc = fmac(sT[tid][l], sG[l][i], acc);
+            sT[tid][i] = (ti == T(0)) ? T(0) : (-ti) * acc;
+        }
+        if (tid == 0) sT[i][i] = ti;
+        __syncthreads();
+    }
+    T *To = Tout + (size_t)blk * tstride;
+    for (int c = 0; c < k; ++c)
+        if (tid <= c) To[tid + (size_t)c * ldt] = sT[tid][c];
+}
+
+// Y = T * V1^H (k x k) with V1 the unit lower triangular top of V (stored at
+// v with leading dimension ldv).  One block of kPanelMaxCols^2 threads.
+template <class T>
+__global__ void __launch_bounds__(1024) k_t_v1h(const T *Tm, int ldt, const T *v, size_t ldv, int k, T *Y, int ldy) {
+    const int r = threadIdx.x % kPanelMaxCols, c = threadIdx.x / kPanelMaxCols;
+    if (r >= k || c >= k) return;
+    // Y(r,c) = sum_l T(r,l) * conj(V1(c,l)),  T(r,l)=0 for l<r, V1(c,l)=0 for l>c, V1(c,c)=1
+    T acc = T(0);
+    for (int l = r; l <= c; ++l) {
+        T vcl = (l == c) ? T(1) : v[c + (size_t)l * ldv];
+        acc = fmac(Tm[r + (size_t)l * ldt], Tr<T>::conj(vcl), acc);
+    }
+    Y[r + (size_t)c * ldy] = acc;
+}
+
+// ---------------------------------------------------------------------------
+// Level-2 kernels for the *_unblocked entry points
+// ---------------------------------------------------------------------------
+
+// larfg on one column: alpha = *alpha_p, x = x[0..n-1) with stride 1.
+template <class T> __global__ void __launch_bounds__(256) k_larfg(int n, T *alpha_p, T *x, T *tau_p) {
+    __shared__ NormAcc s_nacc[8];
+    __shared__ ReflScalars<T> s_refl;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (n <= 0) {
+        if (tid == 0) *tau_p = T(0);
+        return;
+    }
+    NormAcc acc;
+    acc.zero();
+    for (int r = tid; r < n - 1; r += 256) acc.add(x[r]);
+    acc.warp_reduce();
+    if (lane == 0) s_nacc[warp] = acc;
+    __syncthreads();
+    if (tid == 0) {
+        NormAcc t = s_nacc[0];
+        for (int w = 1; w < 8; ++w) t.merge(s_nacc[w]);
+        s_refl = reflector_scalars<T>(*alpha_p, t);
+    }
+    __syncthreads();
+    const ReflScalars<T> rs = s_refl;
+    if (!rs.identity)
+        for (int r = tid; r < n - 1; r += 256) x[r] = scale_x(x[r], rs);
+    if (tid == 0) {
+        *tau_p = rs.tau;
+        if (!rs.identity) *alpha_p = Tr<T>::make((typename Tr<T>::R)rs.beta, 0);
+    }
+}
+
+// side L:  w_c = sum_r conj(v_r) C[r,c]   (v_0 = 1), c < nc, r < mc
+// side R:  w_r = sum_c C[r,c] v_c         (v_0 = 1), r < mc, c < nc
+template <class T> __global__ void __launch_bounds__(256) k_larf_w(int left, int mc, int nc, const T *v, const T *C, size_t ldc, T *w) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (left) {
+        int c = blockIdx.x * 8 + warp;
+        if (c >= nc) return;
+        T acc = T(0);
+        for (int r = lane; r < mc; r += 32) {
+            T vr = (r == 0) ? T(1) : v[r];
+            acc = fmac(Tr<T>::conj(vr), C[r + (size_t)c * ldc], acc);
+        }
+        acc = warp_sum(acc);
+        if (lane == 0) w[c] = acc;
+    } else {
+        int r = blockIdx.x * 256 + tid;
+        if (r >= mc) return;
+        T acc = T(0);
+        for (int c = 0; c < nc; ++c) {
+            T vc = (c == 0) ? T(1) : v[c];
+            acc = fmac(C[r + (size_t)c * ldc], vc, acc);
+        }
+        w[r] = acc;
+    }
+}
+
+// side L:  C[r,c] -= tau * v_r * w_c ;  side R:  C[r,c] -= tau * w_r * conj(v_c)
+// tau = *taup, conjugated when conj_tau is set
+template <class T> __global__ void __launch_bounds__(256) k_larf_update(int left, int mc, int nc, const T *v, const T *w, const T *taup, int conj_tau, T *C, size_t ldc) {
+    const int r = blockIdx.x * 256 + threadIdx.x;
+    if (r >= mc) return;
+    const T tau = conj_tau ? Tr<T>::conj(*taup) : *taup;
+    if (tau == T(0)) return;
+    for (int c = blockIdx.y; c < nc; c += gridDim.y) {
+        T upd;
+        if (left) {
+            T vr = (r == 0) ? T(1) : v[r];
+            upd = tau * vr * w[c];
+        } else {
+            T vc = (c == 0) ? T(1) : v[c];
+            upd = tau * w[r] * Tr<T>::conj(vc);
+        }
+        C[r + (size_t)c * ldc] = C[r + (size_t)c * ldc] - upd;
+    }
+}
+
+// GenerateQ_unblocked column finish (RNP/LA/QR.hpp:475-483):
+// A[i+1:m, i] *= -tau_i;  A[i,i] = 1 - tau_i;  A[0:i, i] = 0
+template <class T> __global__ void __launch_bounds__(256) k_ung2r_col(int m, int i, T *A, size_t lda, const T *tau) {
+    const T t = tau[i];
+    T *col = A + (size_t)i * lda;
+    for (int r = blockIdx.x * 256 + threadIdx.x; r < m; r += gridDim.x * 256) {
+        if (r < i) col[r] = T(0);
+        else if (r == i) col[r] = T(1) - t;
+        else col[r] = (-t) * col[r];
+    }
+}
+
+// columns [j0, j1) of an m-row matrix set to the identity's columns
+template <class T> __global__ void __launch_bounds__(256) k_identity_cols(int m, int j0, int j1, T *A, size_t lda) {
+    for (int c = j0 + blockIdx.y; c < j1; c += gridDim.y)
+        for (int r = blockIdx.x * 256 + threadIdx.x; r < m; r += gridDim.x * 256) A[r + (size_t)c * lda] = (r == c) ? T(1) : T(0);
+}
+
+// rows [0, r1) of columns [c0, c1) set to zero
+template <class T> __global__ void __launch_bounds__(256) k_zero_rows(int r1, int c0, int c1, T *A, size_t lda) {
+    for (int c = c0 + blockIdx.y; c < c1; c += gridDim.y)
+        for (int r = blockIdx.x * 256 + threadIdx.x; r < r1; r += gridDim.x * 256) A[r + (size_t)c * lda] = T(0);
+}
+
+} // namespace rnpgpu

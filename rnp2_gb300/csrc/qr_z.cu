@@ -1,0 +1,5 @@
+// qr_z.cu — rnpgpu::cf64 instantiation of the QR path and its C ABI entry points.
+#define RNPGPU_T rnpgpu::cf64
+#define RNPGPU_CT rnpgpu_complex_double
+#define RNPGPU_P z
+#include "qr_type.inc"

@@ -1,0 +1,235 @@
+// rnp_common.cuh — scalar types, reductions and the bounded grid barrier
+// shared by every QR kernel of the GB300 library.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstddef>
+#include <cstdint>
+
+namespace rnpgpu {
+
+// ---------------------------------------------------------------------------
+// Complex scalar, layout-compatible with std::complex<R> (re, im).
+// ---------------------------------------------------------------------------
+template <class R> struct alignas(2 * sizeof(R)) cplx {
+    R x, y;
+    cplx() = default;
+    __host__ __device__ cplx(R a) : x(a), y(R(0)) {}
+    __host__ __device__ cplx(R a, R b) : x(a), y(b) {}
+};
+template <class R> __host__ __device__ inline cplx<R> operator+(cplx<R> a, cplx<R> b) { return cplx<R>(a.x + b.x, a.y + b.y); }
+template <class R> __host__ __device__ inline cplx<R> operator-(cplx<R> a, cplx<R> b) { return cplx<R>(a.x - b.x, a.y - b.y); }
+template <class R> __host__ __device__ inline cplx<R> operator-(cplx<R> a) { return cplx<R>(-a.x, -a.y); }
+template <class R> __host__ __device__ inline cplx<R> operator*(cplx<R> a, cplx<R> b) { return cplx<R>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+template <class R> __host__ __device__ inline cplx<R> operator*(cplx<R> a, R b) { return cplx<R>(a.x * b, a.y * b); }
+template <class R> __host__ __device__ inline cplx<R> operator*(R b, cplx<R> a) { return cplx<R>(a.x * b, a.y * b); }
+template <class R> __host__ __device__ inline cplx<R> operator/(cplx<R> a, R b) { return cplx<R>(a.x / b, a.y / b); }
+template <class R> __host__ __device__ inline bool operator==(cplx<R> a, cplx<R> b) { return a.x == b.x && a.y == b.y; }
+template <class R> __host__ __device__ inline bool operator!=(cplx<R> a, cplx<R> b) { return !(a == b); }
+
+typedef cplx<float> cf32;
+typedef cplx<double> cf64;
+
+// ---------------------------------------------------------------------------
+// Scalar traits.  AccR is the real type used for Householder norms and
+// beta/tau: FP64 for every scalar type (the FP32 forms keep the norm and the
+// beta scaling in FP64).
+// ---------------------------------------------------------------------------
+template <class T> struct Tr;
+template <> struct Tr<double> {
+    typedef double R;
+    static constexpr bool is_complex = false;
+    __host__ __device__ static double conj(double v) { return v; }
+    __host__ __device__ static double re(double v) { return v; }
+    __host__ __device__ static double im(double) { return 0.0; }
+    __host__ __device__ static double make(double a, double) { return a; }
+};
+template <> struct Tr<float> {
+    typedef float R;
+    static constexpr bool is_complex = false;
+    __host__ __device__ static float conj(float v) { return v; }
+    __host__ __device__ static float re(float v) { return v; }
+    __host__ __device__ static float im(float) { return 0.0f; }
+    __host__ __device__ static float make(float a, float) { return a; }
+};
+template <class Rr> struct Tr<cplx<Rr> > {
+    typedef Rr R;
+    static constexpr bool is_complex = true;
+    __host__ __device__ static cplx<Rr> conj(cplx<Rr> v) { return cplx<Rr>(v.x, -v.y); }
+    __host__ __device__ static Rr re(cplx<Rr> v) { return v.x; }
+    __host__ __device__ static Rr im(cplx<Rr> v) { return v.y; }
+    __host__ __device__ static cplx<Rr> make(Rr a, Rr b) { return cplx<Rr>(a, b); }
+};
+
+// fused multiply-add c + a*b for every scalar type
+__device__ __forceinline__ double fmac(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ float fmac(float a, float b, float c) { return fmaf(a, b, c); }
+template <class R> __device__ __forceinline__ cplx<R> fmac(cplx<R> a, cplx<R> b, cplx<R> c) {
+    return cplx<R>(fmac(-a.y, b.y, fmac(a.x, b.x, c.x)), fmac(a.y, b.x, fmac(a.x, b.y, c.y)));
+}
+
+// ---------------------------------------------------------------------------
+// Warp / block sums
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double warp_sum(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ float warp_sum(float v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+template <class R> __device__ __forceinline__ cplx<R> warp_sum(cplx<R> v) {
+    return cplx<R>(warp_sum(v.x), warp_sum(v.y));
+}
+
+// ---------------------------------------------------------------------------
+// Safe 2-norm accumulation without divisions (three accumulators for tiny,
+// medium and huge magnitudes, after Blue 1978 and Anderson, ACM TOMS
+// Algorithm 978, 2017).  The thresholds and scale factors follow from the
+// IEEE double format (minexponent -1021, maxexponent 1024, 53 digits):
+//   tsml = 2^ceil((-1021-1)/2)       = 2^-511
+//   tbig = 2^floor((1024-53+1)/2)    = 2^486
+//   ssml = 2^-floor((-1021-53)/2)    = 2^537
+//   sbig = 2^-ceil((1024+53-1)/2)    = 2^-538
+// Squares of FP32 values never leave the double range, so FP32 inputs use
+// the medium accumulator only.
+// ---------------------------------------------------------------------------
+struct NormAcc {
+    double sml, med, big;
+    __device__ __forceinline__ void zero() { sml = 0.0; med = 0.0; big = 0.0; }
+    __device__ __forceinline__ void add(double v) {
+        const double tsml = 0x1p-511, tbig = 0x1p486, ssml = 0x1p537, sbig = 0x1p-538;
+        double a = fabs(v);
+        if (a > tbig) {
+            double s = a * sbig;
+            big = fma(s, s, big);
+        } else if (a < tsml) {
+            double s = a * ssml;
+            sml = fma(s, s, sml);
+        } else {
+            med = fma(a, a, med);
+        }
+    }
+    __device__ __forceinline__ void add(float v) {
+        double a = (double)v;
+        med = fma(a, a, med);
+    }
+    template <class R> __device__ __forceinline__ void add(cplx<R> v) { add(v.x); add(v.y); }
+    __device__ __forceinline__ void merge(const NormAcc &o) { sml += o.sml; med += o.med; big += o.big; }
+    __device__ __forceinline__ void warp_reduce() { sml = warp_sum(sml); med = warp_sum(med); big = warp_sum(big); }
+    __device__ double result() const { return result_scaled(1.0); }
+    // mult * ||x|| for a power-of-two mult, without rounding through the
+    // subnormal range when ||x|| itself is subnormal
+    __device__ double result_scaled(double mult) const {
+        const double ssml = 0x1p537, sbig = 0x1p-538;
+        double scl, sumsq;
+        if (big > 0.0) {
+            double b = big;
+            if (med > 0.0 || med != med) b += (med * sbig) * sbig;
+            scl = 1.0 / sbig;
+            sumsq = b;
+        } else if (sml > 0.0) {
+            if (med > 0.0 || med != med) {
+                double ymed = sqrt(med), ysml = sqrt(sml) / ssml;
+                double ymin = ymed < ysml ? ymed : ysml, ymax = ymed < ysml ? ysml : ymed;
+                double q = ymin / ymax;
+                scl = 1.0;
+                sumsq = ymax * ymax * (1.0 + q * q);
+            } else {
+                scl = 1.0 / ssml;
+                sumsq = sml;
+            }
+        } else {
+            scl = 1.0;
+            sumsq = med;
+        }
+        return (scl * mult) * sqrt(sumsq);
+    }
+};
+
+// sqrt(x^2+y^2+z^2) without unnecessary overflow (RNP/Types.hpp:73-92)
+__device__ __forceinline__ double hypot3(double x, double y, double z) {
+    double xa = fabs(x), ya = fabs(y), za = fabs(z);
+    double w = fmax(fmax(xa, ya), za);
+    if (xa != xa || ya != ya || za != za) return xa + ya + za;
+    if (w == 0.0) return xa + ya + za;
+    xa /= w; ya /= w; za /= w;
+    return w * sqrt(xa * xa + ya * ya + za * za);
+}
+
+// 1/(a+ib) by Smith's algorithm (Smith, CACM 5(8), 1962)
+__device__ __forceinline__ void crecip(double a, double b, double &rx, double &ry) {
+    if (fabs(b) <= fabs(a)) {
+        double r = b / a, d = a + b * r;
+        rx = 1.0 / d;
+        ry = -r / d;
+    } else {
+        double r = a / b, d = b + a * r;
+        rx = r / d;
+        ry = -1.0 / d;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Bounded grid barrier for cooperative launches.  The counter is zeroed by
+// the host before the launch; every barrier generation adds one arrival per
+// block.  A wait that exceeds kSpinLimit cycles (about 2 s at 2 GHz) sets the
+// launch's error word and the kernel returns instead of hanging; a block that
+// sees the error word set stops waiting too.
+// ---------------------------------------------------------------------------
+static constexpr long long kSpinLimit = 4000000000LL;
+
+enum DeviceStatus : int { kStatusOk = 0, kStatusBarrierTimeout = 1 };
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ int ld_volatile(const int *p) {
+    int v;
+    asm volatile("ld.volatile.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void red_release_add(unsigned *p, unsigned v) {
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+struct GridBarrier {
+    unsigned *counter;
+    int *err;
+    unsigned nblocks;
+    unsigned gen;
+    long long spin_limit = kSpinLimit;
+    // returns false when this launch must stop (timeout or an error elsewhere)
+    __device__ bool sync() {
+        __shared__ int s_ok;
+        __syncthreads();
+        if (nblocks > 1) {
+            if (threadIdx.x == 0) {
+                ++gen;
+                const unsigned target = gen * nblocks;
+                __threadfence();
+                red_release_add(counter, 1u);
+                int ok = 1;
+                const long long t0 = clock64();
+                while (ld_acquire(counter) < target) {
+                    if (ld_volatile(err) != 0) { ok = 0; break; }
+                    if (clock64() - t0 > spin_limit) {
+                        atomicExch(err, (int)kStatusBarrierTimeout);
+                        ok = 0;
+                        break;
+                    }
+                    __nanosleep(32);
+                }
+                __threadfence();
+                s_ok = ok;
+            }
+            __syncthreads();
+            return s_ok != 0;
+        }
+        return true;
+    }
+};
+
+} // namespace rnpgpu
