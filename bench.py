@@ -1,0 +1,379 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 QR path on the tall-skinny least-squares workload.
+
+Workload: min ||A x - b|| with A 65536 x 512 real double, A = U diag(s) V^T
+(U, V from the QR of seeded Gaussian matrices, s geometric from 1 to 1e-6,
+cond 1e6), b = A x_true + 1e-10 N(0,1), 16 right-hand sides.  A step is one
+complete FP64-accurate solve of that problem.
+
+  value   mixed form (FP32 factor, FP64 refinement, rnpgpu_dsgels) with A, b
+          resident in HBM: solves/s
+  e2e     the same through the C ABI with host buffers: pinned host A, b
+          copied in and x copied out inside every timed step
+  plain   the FP64 drop-in path (rnpgpu_dgels: Factor, MultQ, triangular
+          solve) on the same problem, for the mixed-vs-plain ratio
+
+``--impl reference`` times the CPU restatement of the reference's QR least
+squares (Factor, MultQ("L","C"), SolveTrM), with OpenBLAS for level-3, on the
+host cores.  Under torchrun each rank solves its own replica (the workload does
+not shard); rank 0 prints one JSON line.
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+M, N, NRHS = 65536, 512, 16
+METRIC = "FP64-accurate least-squares solves/s, 65536x512 real, 16 RHS, cond 1e6"
+UNIT = "solves/s"
+WORKLOAD = "ls_65536x512_nrhs16_cond1e6"
+DATA = "synthetic: A = U diag(s) V^T, U,V from QR of seeded N(0,1) matrices, s = 10^(-6 i/511); b = A x + 1e-10 N(0,1)"
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def solve_flops(m, n, nrhs):
+    """Algorithmic flops of one QR least-squares solve: Factor 2mn^2 - 2n^3/3,
+    MultQ("L","C") 2 nrhs n (2m - n), triangular solve n^2 nrhs."""
+    return 2.0 * m * n * n - 2.0 * n ** 3 / 3.0 + 2.0 * nrhs * n * (2.0 * m - n) + float(n) * n * nrhs
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    FIELDS = "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.lines = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_problem(torch, device, seed=0):
+    """A = U diag(s) V^T and b, built on the GPU with this library's QR."""
+    from rnp2_gb300 import qr as gq
+
+    g = torch.Generator(device=device).manual_seed(seed)
+    G1 = torch.randn((N, M), generator=g, dtype=torch.float64, device=device).t()
+    t1 = gq.factor(G1)
+    gq.generate_q(G1, t1)
+    G2 = torch.randn((N, N), generator=g, dtype=torch.float64, device=device).t()
+    t2 = gq.factor(G2)
+    gq.generate_q(G2, t2)
+    s = 10.0 ** (-6.0 * torch.arange(N, dtype=torch.float64, device=device) / (N - 1))
+    A = gq.to_colmajor((G1 * s) @ G2.t())
+    xt = torch.randn((NRHS, N), generator=g, dtype=torch.float64, device=device).t()
+    noise = torch.randn((NRHS, M), generator=g, dtype=torch.float64, device=device).t()
+    b = gq.to_colmajor(A @ xt + 1e-10 * noise)
+    del G1, G2
+    return A, b
+
+
+def ls_errors(torch, A, b, x):
+    """(max_j ||A^T r_j|| / (||A||_F (||A||_F ||x_j|| + ||b_j||)), ||r||) in FP64 (torch, reporting only)."""
+    r = b - A @ x
+    g = A.t() @ r
+    an = torch.linalg.norm(A)
+    eta = torch.linalg.norm(g, dim=0) / (an * (an * torch.linalg.norm(x, dim=0) + torch.linalg.norm(b, dim=0)))
+    return float(eta.max()), float(torch.linalg.norm(r))
+
+
+def cpu_solve(A_np, b_np, threads):
+    """One FP64 QR least-squares solve with the CPU oracle (+ OpenBLAS)."""
+    import numpy as np
+
+    import oracle as orc
+
+    o = orc.load()
+    blas = orc.find_openblas()
+    kind_blas = "none"
+    if blas and orc.use_blas(o, blas, "scipy_", threads) == 0:
+        kind_blas = os.path.basename(blas)
+    a = np.asfortranarray(A_np.copy())
+    bb = np.asfortranarray(b_np.copy())
+    t0 = time.perf_counter()
+    o.gels("d", a.shape[0], a.shape[1], bb.shape[1], a, bb)
+    dt = time.perf_counter() - t0
+    return bb[: a.shape[1]].copy(), dt, kind_blas
+
+
+def cpu_arm(args, rank, world):
+    """--impl reference: the reference's QR least squares restated on the CPU."""
+    import numpy as np
+
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    rng = np.random.default_rng(0)
+    U, _ = np.linalg.qr(rng.standard_normal((M, N)))
+    V, _ = np.linalg.qr(rng.standard_normal((N, N)))
+    s = 10.0 ** (-6.0 * np.arange(N) / (N - 1))
+    A = np.asfortranarray((U * s) @ V.T)
+    b = np.asfortranarray(A @ rng.standard_normal((N, NRHS)) + 1e-10 * rng.standard_normal((M, NRHS)))
+    times = []
+    for i in range(args.warmup + args.steps):
+        _, dt, kind_blas = cpu_solve(A, b, threads)
+        if i >= args.warmup:
+            times.append(dt)
+    tot = sum(times)
+    val = len(times) / tot
+    line = {
+        "impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * tot / len(times), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": DATA,
+        "config": {"workload": WORKLOAD, "m": M, "n": N, "nrhs": NRHS},
+        "cpu_baseline": {"value": val, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": "full 65536x512x16 FP64 QR least-squares solve per step (oracle restatement of Factor + MultQ + SolveTrM, level-3 via %s)" % kind_blas},
+        "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def gpu_arm(args, rank, world, local):
+    import torch
+
+    import rnp2_gb300
+    from rnp2_gb300 import _capi
+    from rnp2_gb300 import ls as gls
+    from rnp2_gb300 import qr as gq
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    lib = rnp2_gb300.lib()
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    A, b = make_problem(torch, dev)
+    X = gq.empty_colmajor(N, NRHS, torch.float64, dev)
+    work = torch.empty(gls.refine_workspace(A, NRHS), dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream()
+
+    # ---------------- mixed form, inputs resident -------------------------
+    info = None
+    for _ in range(args.warmup):
+        _, info = gls.gels_refine(A, b, X, work=work)
+    barrier()
+    launches0 = lib.rnpgpu_launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            _, info = gls.gels_refine(A, b, X, work=work)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    launches = lib.rnpgpu_launch_count() - launches0
+    ms = e0.elapsed_time(e1) / args.steps
+    if dist is not None:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t)
+    value = world * 1e3 / ms
+    eta_mixed, _ = ls_errors(torch, A, b, X)
+    x_mixed = X.clone()
+
+    # ---------------- e2e through host buffers ------------------------------
+    A_h = A.cpu().pin_memory()
+    b_h = b.cpu().pin_memory()
+    x_h = torch.empty((NRHS, N), dtype=torch.float64).pin_memory().t()
+    A_d = gq.empty_colmajor(M, N, torch.float64, dev)
+    b_d = gq.empty_colmajor(M, NRHS, torch.float64, dev)
+    for _ in range(max(1, args.warmup)):
+        A_d.copy_(A_h, non_blocking=True)
+        b_d.copy_(b_h, non_blocking=True)
+        gls.gels_refine(A_d, b_d, X, work=work)
+        x_h.copy_(X, non_blocking=True)
+    barrier()
+    e0.record(stream)
+    for _ in range(args.steps):
+        A_d.copy_(A_h, non_blocking=True)
+        b_d.copy_(b_h, non_blocking=True)
+        gls.gels_refine(A_d, b_d, X, work=work)
+        x_h.copy_(X, non_blocking=True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_e2e = e0.elapsed_time(e1) / args.steps
+    if dist is not None:
+        t = torch.tensor([ms_e2e], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_e2e = float(t)
+    del A_d, b_d
+
+    # ---------------- plain FP64 drop-in on the same problem ----------------
+    Ap = gq.empty_colmajor(M, N, torch.float64, dev)
+    bp = gq.empty_colmajor(M, NRHS, torch.float64, dev)
+    tau = torch.zeros(N, dtype=torch.float64, device=dev)
+    lw = C.c_size_t(0)
+    lib.rnpgpu_dgels(M, N, NRHS, None, M, None, None, M, C.byref(lw), None)
+    pwork = torch.empty(lw.value, dtype=torch.float64, device=dev)
+    plain_steps = max(2, min(args.steps, 5))
+    plain_ms = []
+    for i in range(1 + plain_steps):
+        Ap.copy_(A)
+        bp.copy_(b)
+        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s0.record(stream)
+        gls.gels(Ap, bp, tau, work=pwork)
+        s1.record(stream)
+        torch.cuda.synchronize()
+        if i > 0:
+            plain_ms.append(s0.elapsed_time(s1))
+    ms_plain = statistics.mean(plain_ms)
+    x_plain = bp[:N].clone()
+    eta_plain, _ = ls_errors(torch, A, b, x_plain)
+    ferr_mixed_vs_plain = float(torch.linalg.norm(x_mixed - x_plain) / torch.linalg.norm(x_plain))
+    del Ap, bp, pwork
+
+    # ---------------- per-kernel profile of the mixed step ------------------
+    lib.rnpgpu_timing_enable(1)
+    _capi.timing_report()
+    prof_steps = 2
+    for _ in range(prof_steps):
+        gls.gels_refine(A, b, X, work=work)
+    torch.cuda.synchronize()
+    prof = _capi.timing_report()
+    lib.rnpgpu_timing_enable(0)
+    scratch = torch.empty(torch.cuda.get_device_properties(dev).multi_processor_count * 8 * 256, dtype=torch.float64, device=dev)
+    peak64 = C.c_double(0)
+    lib.rnpgpu_probe_peak(0, C.c_void_p(scratch.data_ptr()), scratch.numel() * 8, C.byref(peak64))
+    tot_ms = sum(v[1] for v in prof.values())
+    top = max(prof.items(), key=lambda kv: kv[1][1]) if prof else ("none", (0, 0.0))
+    res = prof.get("residual_fp64", (0, 0.0))
+    roofline = None
+    if res[0] > 0:
+        per_launch_flops = 2.0 * M * N * NRHS
+        avg_s = res[1] / res[0] * 1e-3
+        achieved = per_launch_flops / avg_s / 1e12
+        roofline = {
+            "kernel": "residual_fp64 (k_gemm<double,128,16>: r = b - A x)",
+            "bound": "tensor", "pipe": "fp64 (DFMA)", "achieved": achieved, "peak": peak64.value, "unit": "TFLOP/s",
+            "frac": achieved / peak64.value if peak64.value else None, "traffic": None,
+            "peak_source": "FP64 FMA throughput measured in this run (rnpgpu_probe_peak); MEASURED_PEAKS.json has no FP64 figure",
+            "algorithmic_flops_per_launch": per_launch_flops,
+            "share_of_step": res[1] / tot_ms if tot_ms else None,
+        }
+
+    # ---------------- CPU baseline (rank 0) ---------------------------------
+    cpu = None
+    ferr_vs_cpu = None
+    if rank == 0 and not args.no_cpu:
+        import numpy as np
+
+        A_np = np.asfortranarray(A.cpu().numpy())
+        b_np = np.asfortranarray(b.cpu().numpy())
+        threads = os.cpu_count() or 1
+        x_cpu, dt, kind_blas = cpu_solve(A_np, b_np, threads)
+        x_cpu, dt2, _ = cpu_solve(A_np, b_np, threads)
+        dt = min(dt, dt2)
+        cpu = {"value": 1.0 / dt, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": "2 full solves of the same problem, best taken (oracle restatement of Factor + MultQ + SolveTrM; level-3 via %s)" % kind_blas}
+        xm = x_mixed.cpu().numpy()
+        ferr_vs_cpu = float(np.linalg.norm(xm - x_cpu) / np.linalg.norm(x_cpu))
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 factor + f64 refinement",
+        "data": DATA,
+        "config": {"workload": WORKLOAD, "m": M, "n": N, "nrhs": NRHS, "parallelism": "replicas" if world > 1 else "single GPU",
+                   "l2": "inputs larger than L2 (A is 268 MB in FP64)"},
+        "e2e": {"value": world * 1e3 / ms_e2e, "unit": UNIT, "ms_per_step": ms_e2e,
+                "h2d_bytes_per_step": A.numel() * 8 + b.numel() * 8, "d2h_bytes_per_step": X.numel() * 8},
+        "gpu_launches": int(launches),
+        "mixed": {"iterations": info["iterations"] if info else None, "converged": info["converged"] if info else None,
+                  "backward_error": eta_mixed, "backward_error_bound": 10 * N * 2.0 ** -52,
+                  "forward_error_vs_cpu_fp64_oracle": ferr_vs_cpu, "forward_error_vs_plain_gpu": ferr_mixed_vs_plain},
+        "plain_fp64": {"solves_per_s": 1e3 / ms_plain, "ms_per_solve": ms_plain, "backward_error": eta_plain,
+                       "tflops": solve_flops(M, N, NRHS) / (ms_plain * 1e-3) / 1e12},
+        "speedup_mixed_vs_plain": ms_plain / ms,
+        "profile_ms_per_step": {k: v[1] / prof_steps for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])},
+        "top_kernel": top[0],
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "clocks": clk.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        return cpu_arm(args, rank, world)
+    return gpu_arm(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

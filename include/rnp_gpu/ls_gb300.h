@@ -1,0 +1,68 @@
+/* ls_gb300.h — C ABI of the least-squares layer on the GB300 QR.
+ *
+ * Conventions as in qr_gb300.h: column-major DEVICE arrays, caller-owned
+ * workspace with the *lwork query (work == NULL or *lwork == 0), asynchronous
+ * on the stream set by rnpgpu_set_stream, int status (0 ok, -i bad argument
+ * i, > 0 CUDA error).
+ */
+#ifndef RNP_GPU_LS_GB300_H
+#define RNP_GPU_LS_GB300_H
+
+#include <stddef.h>
+#include "qr_gb300.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- Upper triangular solve B <- R^{-1} B (R n x n non-unit, B n x nrhs):
+ *      replaces RNP::BLAS::SolveTrM("L","U","N","N", n, nrhs, 1, a, lda, b, ldb)
+ *      (RNP/BLAS/BLAS_mix.hpp:2096-2113, forwarded to dtrsm_ at src/BLAS_mix.cpp:682) ---- */
+int rnpgpu_strsm_lunn(size_t n, size_t nrhs, const float *a, size_t lda, float *b, size_t ldb);
+int rnpgpu_dtrsm_lunn(size_t n, size_t nrhs, const double *a, size_t lda, double *b, size_t ldb);
+int rnpgpu_ctrsm_lunn(size_t n, size_t nrhs, const rnpgpu_complex_float *a, size_t lda, rnpgpu_complex_float *b, size_t ldb);
+int rnpgpu_ztrsm_lunn(size_t n, size_t nrhs, const rnpgpu_complex_double *a, size_t lda, rnpgpu_complex_double *b, size_t ldb);
+
+/* ---- Least squares min ||A x - B|| (m >= n, full column rank) by QR: the
+ *      composition a caller of the reference writes — QR::Factor, then
+ *      QR::MultQ("L","C") on B, then SolveTrM("L","U","N","N") (no single
+ *      reference routine).  On exit A holds the factorization, tau the
+ *      reflector scalars and B(0:n, :) the solution. ---- */
+int rnpgpu_sgels(size_t m, size_t n, size_t nrhs, float *a, size_t lda, float *tau, float *b, size_t ldb, size_t *lwork, float *work);
+int rnpgpu_dgels(size_t m, size_t n, size_t nrhs, double *a, size_t lda, double *tau, double *b, size_t ldb, size_t *lwork, double *work);
+int rnpgpu_cgels(size_t m, size_t n, size_t nrhs, rnpgpu_complex_float *a, size_t lda, rnpgpu_complex_float *tau, rnpgpu_complex_float *b, size_t ldb, size_t *lwork, rnpgpu_complex_float *work);
+int rnpgpu_zgels(size_t m, size_t n, size_t nrhs, rnpgpu_complex_double *a, size_t lda, rnpgpu_complex_double *tau, rnpgpu_complex_double *b, size_t ldb, size_t *lwork, rnpgpu_complex_double *work);
+
+/* ---- Mixed-precision least squares with iterative refinement (no reference
+ *      counterpart): A is factored in FP32 (a working copy; A and B are not
+ *      modified); the residual r = b - A x, the solution x and the error
+ *      metrics are computed in FP64.  Steps  x += R^{-1} (Q^H r)(0:n)  run
+ *      until the least-squares backward error bound
+ *          max_j ||R^{-H} A^H r_j|| / ||x_j||
+ *      (an upper bound of the Karlson-Walden estimate) and the normal-equation
+ *      residual  max_j ||A^H r_j|| / (||A||_F (||A||_F ||x_j|| + ||b_j||))
+ *      are both at most 10 n eps, the correction stops halving, or max_iter
+ *      steps are taken (max_iter <= 0: 10).
+ *      flags bit 0 (RNPGPU_REFINE_FORWARD): continue with corrected
+ *      seminormal-equation steps  x += R^{-1} R^{-H} A^H r  until the
+ *      correction stops shrinking, for FP64-level forward accuracy.
+ *      The loop reads a few norms back per step, so these calls synchronize
+ *      their stream. ---- */
+#define RNPGPU_REFINE_FORWARD 1
+typedef struct {
+    int iterations;         /* refinement steps taken */
+    int converged;          /* 1 if both error measures reached 10 n eps */
+    double backward_error;  /* max_j ||R^{-H} A^H r_j|| / ||x_j|| */
+    double normal_residual; /* max_j ||A^H r_j|| / (||A||_F (||A||_F ||x_j|| + ||b_j||)) */
+    double correction;      /* max_j ||d_j|| / ||x_j|| of the last step */
+    double anorm;           /* ||A||_F */
+} rnpgpu_refine_info;
+
+int rnpgpu_dsgels(size_t m, size_t n, size_t nrhs, const double *a, size_t lda, const double *b, size_t ldb, double *x, size_t ldx, int max_iter, int flags, rnpgpu_refine_info *info, size_t *lwork, double *work);
+int rnpgpu_zcgels(size_t m, size_t n, size_t nrhs, const rnpgpu_complex_double *a, size_t lda, const rnpgpu_complex_double *b, size_t ldb, rnpgpu_complex_double *x, size_t ldx, int max_iter, int flags, rnpgpu_refine_info *info, size_t *lwork, rnpgpu_complex_double *work);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RNP_GPU_LS_GB300_H */

@@ -86,6 +86,17 @@ void *rnpgpu_get_stream(void);
 const char *rnpgpu_get_last_error(void);
 /* Library version string. */
 const char *rnpgpu_version(void);
+/* Number of kernels this library has launched in this process. */
+unsigned long long rnpgpu_launch_count(void);
+/* Per-kernel-class timing with CUDA events on the launching stream, for the
+ * calling thread: enable/disable, then read "name count total_ms" lines
+ * (since the last report) into buf; returns the report's length. */
+int rnpgpu_timing_enable(int on);
+int rnpgpu_timing_report(char *buf, size_t len);
+/* Measured FMA throughput of the current device in TFLOP/s (kind 0: FP64,
+ * kind 1: FP32), using scratch (>= SMs*8*256 doubles) for the probe's
+ * outputs; synchronous.  Used as the roofline denominator of FP64 work. */
+int rnpgpu_probe_peak(int kind, void *scratch, size_t scratch_bytes, double *tflops);
 
 #ifdef __cplusplus
 }

@@ -17,6 +17,22 @@ PSZ = C.POINTER(C.c_size_t)
 _lib = None
 
 
+class RefineInfo(C.Structure):
+    """rnpgpu_refine_info (include/rnp_gpu/ls_gb300.h)"""
+
+    _fields_ = [
+        ("iterations", C.c_int),
+        ("converged", C.c_int),
+        ("backward_error", C.c_double),
+        ("normal_residual", C.c_double),
+        ("correction", C.c_double),
+        ("anorm", C.c_double),
+    ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class LibraryNotBuilt(RuntimeError):
     pass
 
@@ -30,14 +46,33 @@ def _signatures():
         sig["rnpgpu_%sunm2r" % p] = [CH, CH, SZ, SZ, SZ, P, SZ, P, P, SZ, P]
         sig["rnpgpu_%sungqr" % p] = [SZ, SZ, SZ, P, SZ, P, PSZ, P]
         sig["rnpgpu_%sung2r" % p] = [SZ, SZ, SZ, P, SZ, P, P]
+        sig["rnpgpu_%strsm_lunn" % p] = [SZ, SZ, P, SZ, P, SZ]
+        sig["rnpgpu_%sgels" % p] = [SZ, SZ, SZ, P, SZ, P, P, SZ, PSZ, P]
+    for name in ("rnpgpu_dsgels", "rnpgpu_zcgels"):
+        sig[name] = [SZ, SZ, SZ, P, SZ, P, SZ, P, SZ, C.c_int, C.c_int, C.POINTER(RefineInfo), PSZ, P]
     sig["rnpgpu_set_stream"] = [P]
     sig["rnpgpu_get_stream"] = []
     sig["rnpgpu_get_last_error"] = []
     sig["rnpgpu_version"] = []
+    sig["rnpgpu_launch_count"] = []
+    sig["rnpgpu_timing_enable"] = [C.c_int]
+    sig["rnpgpu_timing_report"] = [C.c_char_p, SZ]
+    sig["rnpgpu_probe_peak"] = [C.c_int, P, SZ, C.POINTER(C.c_double)]
     return sig
 
 
-RESTYPES = {"rnpgpu_get_stream": P, "rnpgpu_get_last_error": CH, "rnpgpu_version": CH}
+RESTYPES = {"rnpgpu_get_stream": P, "rnpgpu_get_last_error": CH, "rnpgpu_version": CH, "rnpgpu_launch_count": C.c_ulonglong}
+
+
+def timing_report():
+    """{kernel class: (launches, total ms)} since the last report."""
+    buf = C.create_string_buffer(1 << 16)
+    lib().rnpgpu_timing_report(buf, len(buf))
+    out = {}
+    for line in buf.value.decode().splitlines():
+        name, cnt, ms = line.split()
+        out[name] = (int(cnt), float(ms))
+    return out
 
 
 def lib():

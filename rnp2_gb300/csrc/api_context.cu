@@ -2,8 +2,13 @@
 // library-level C ABI entry points (rnpgpu_set_stream & co.).
 #include "qr_driver.cuh"
 #include "../../include/rnp_gpu/qr_gb300.h"
+#include <algorithm>
+#include <atomic>
+#include <cstring>
 #include <cstdio>
+#include <map>
 #include <string>
+#include <vector>
 
 namespace rnpgpu {
 
@@ -12,6 +17,66 @@ static thread_local std::string t_last_error;
 
 cudaStream_t current_stream() { return t_stream; }
 void set_last_error(const char *msg) { t_last_error = msg ? msg : ""; }
+
+// ---------------------------------------------------------------------------
+// launch accounting and per-kernel-class event timing
+// ---------------------------------------------------------------------------
+static std::atomic<unsigned long long> g_launches{0};
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+struct TimedLaunch {
+    const char *name;
+    cudaEvent_t start, stop;
+};
+struct KTimer {
+    bool on = false;
+    std::vector<TimedLaunch> done;
+    std::vector<TimedLaunch> open;
+    std::vector<cudaEvent_t> pool;
+    cudaEvent_t get() {
+        if (!pool.empty()) {
+            cudaEvent_t e = pool.back();
+            pool.pop_back();
+            return e;
+        }
+        cudaEvent_t e = nullptr;
+        cudaEventCreate(&e);
+        return e;
+    }
+};
+static thread_local KTimer t_timer;
+
+void ktimer_begin(const char *name, cudaStream_t st) {
+    if (!t_timer.on) return;
+    TimedLaunch t{name, t_timer.get(), t_timer.get()};
+    cudaEventRecord(t.start, st);
+    t_timer.open.push_back(t);
+}
+void ktimer_end(cudaStream_t st) {
+    if (!t_timer.on || t_timer.open.empty()) return;
+    TimedLaunch t = t_timer.open.back();
+    t_timer.open.pop_back();
+    cudaEventRecord(t.stop, st);
+    t_timer.done.push_back(t);
+}
+
+// FP64 / FP32 FMA throughput probe (independent FMA chains, full occupancy)
+__global__ void k_probe_dfma(double *out, int iters, double b, double c) {
+    double a0 = threadIdx.x, a1 = a0 + 1, a2 = a0 + 2, a3 = a0 + 3, a4 = a0 + 4, a5 = a0 + 5, a6 = a0 + 6, a7 = a0 + 7;
+    for (int i = 0; i < iters; ++i) {
+        a0 = fma(a0, b, c); a1 = fma(a1, b, c); a2 = fma(a2, b, c); a3 = fma(a3, b, c);
+        a4 = fma(a4, b, c); a5 = fma(a5, b, c); a6 = fma(a6, b, c); a7 = fma(a7, b, c);
+    }
+    out[blockIdx.x * blockDim.x + threadIdx.x] = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+}
+__global__ void k_probe_ffma(float *out, int iters, float b, float c) {
+    float a0 = threadIdx.x, a1 = a0 + 1, a2 = a0 + 2, a3 = a0 + 3, a4 = a0 + 4, a5 = a0 + 5, a6 = a0 + 6, a7 = a0 + 7;
+    for (int i = 0; i < iters; ++i) {
+        a0 = fmaf(a0, b, c); a1 = fmaf(a1, b, c); a2 = fmaf(a2, b, c); a3 = fmaf(a3, b, c);
+        a4 = fmaf(a4, b, c); a5 = fmaf(a5, b, c); a6 = fmaf(a6, b, c); a7 = fmaf(a7, b, c);
+    }
+    out[blockIdx.x * blockDim.x + threadIdx.x] = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+}
 
 // per-type occupancy of the panel kernel (defined in the per-type units)
 int panel_blocks_per_sm_s();
@@ -50,5 +115,76 @@ int rnpgpu_set_stream(void *stream) {
 void *rnpgpu_get_stream(void) { return (void *)rnpgpu::t_stream; }
 const char *rnpgpu_get_last_error(void) { return rnpgpu::t_last_error.c_str(); }
 const char *rnpgpu_version(void) { return "rnp2_gb300 0.1 (sm_103a)"; }
+
+unsigned long long rnpgpu_launch_count(void) { return rnpgpu::g_launches.load(); }
+
+int rnpgpu_timing_enable(int on) {
+    rnpgpu::t_timer.on = (on != 0);
+    return 0;
+}
+
+// "name count total_ms\n" per kernel class since the last report; resets.
+int rnpgpu_timing_report(char *buf, size_t len) {
+    using namespace rnpgpu;
+    std::map<std::string, std::pair<long, double> > acc;
+    for (auto &t : t_timer.done) {
+        cudaEventSynchronize(t.stop);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, t.start, t.stop);
+        auto &a = acc[t.name];
+        a.first += 1;
+        a.second += ms;
+        t_timer.pool.push_back(t.start);
+        t_timer.pool.push_back(t.stop);
+    }
+    t_timer.done.clear();
+    std::string out;
+    char line[256];
+    for (auto &kv : acc) {
+        snprintf(line, sizeof(line), "%s %ld %.6f\n", kv.first.c_str(), kv.second.first, kv.second.second);
+        out += line;
+    }
+    if (buf && len) {
+        size_t n = std::min(len - 1, out.size());
+        memcpy(buf, out.data(), n);
+        buf[n] = 0;
+    }
+    return (int)out.size();
+}
+
+// Measured FMA throughput of the current device in TFLOP/s
+// (kind 0: FP64 DFMA, kind 1: FP32 FFMA); synchronous.
+int rnpgpu_probe_peak(int kind, void *scratch, size_t scratch_bytes, double *tflops) {
+    using namespace rnpgpu;
+    const DeviceFacts &f = device_facts();
+    const int blocks = f.sm_count * 8, threads = 256;
+    if (scratch_bytes < (size_t)blocks * threads * sizeof(double) || tflops == nullptr) return -2;
+    cudaStream_t st = current_stream();
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    const int iters = kind == 0 ? 4096 : 65536;
+    double best = 0.0;
+    for (int rep = 0; rep < 3; ++rep) {
+        cudaEventRecord(e0, st);
+        if (kind == 0) k_probe_dfma<<<blocks, threads, 0, st>>>((double *)scratch, iters, 0.999, 1e-3);
+        else k_probe_ffma<<<blocks, threads, 0, st>>>((float *)scratch, iters, 0.999f, 1e-3f);
+        cudaEventRecord(e1, st);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        double fl = 2.0 * 8 * (double)iters * blocks * threads;
+        if (ms > 0) best = std::max(best, fl / (ms * 1e-3) / 1e12);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        set_last_error(cudaGetErrorString(e));
+        return 1;
+    }
+    *tflops = best;
+    return 0;
+}
 
 } // extern "C"

@@ -1,0 +1,292 @@
+// ls_driver.cuh — least squares on the QR path.
+//
+//  gels<T>          min ||A x - b|| by Factor, MultQ("L","C") and the upper
+//                   triangular solve, the composition a caller of the
+//                   reference writes (RNP/LA/QR.hpp:129-197, 337-429;
+//                   BLAS::SolveTrM, RNP/BLAS/BLAS_mix.hpp:2096-2113)
+//  gels_refine<H,L> the mixed form: Factor in the low precision L (FP32),
+//                   then refinement  x += R^{-1} Q^H (b - A x)  with the
+//                   residual, the solution and the error metrics in H
+//                   (FP64).  Loop shape and stop rule follow the reference's
+//                   LU::RefineSolution (RNP/LA/LU.hpp:244-311): stop when the
+//                   backward error is small enough or the correction stops
+//                   halving, at most max_iter steps.
+#pragma once
+#include "ls_kernels.cuh"
+#include "qr_driver.cuh"
+#include <cmath>
+#include <vector>
+
+namespace rnpgpu {
+
+struct RefineInfo {
+    int iterations;
+    int converged;
+    double backward_error;   // max_j ||R^{-H} A^H r_j|| / ||x_j||  (LS backward error bound)
+    double normal_residual;  // max_j ||A^H r_j|| / (||A||_F (||A||_F ||x_j|| + ||b_j||))
+    double correction;       // max_j ||d_j|| / ||x_j|| of the last step
+    double anorm;            // ||A||_F
+};
+
+template <class T> int trsm_upper(size_t n, size_t nrhs, const T *a, size_t lda, T *b, size_t ldb, cudaStream_t st) {
+    if (n == 0 || nrhs == 0) return kOk;
+    KScope ks("trsm", st);
+    k_trsm_upper<T><<<(unsigned)std::min<size_t>(nrhs, 65535), 256, 0, st>>>((int)n, (int)nrhs, a, lda, b, ldb);
+    RNPGPU_CHECK_LAUNCH();
+    return kOk;
+}
+
+template <class T> int trsm_upper_ct(size_t n, size_t nrhs, const T *a, size_t lda, T *b, size_t ldb, cudaStream_t st) {
+    if (n == 0 || nrhs == 0) return kOk;
+    KScope ks("trsm", st);
+    k_trsm_upper_ct<T><<<(unsigned)std::min<size_t>(nrhs, 65535), 256, 0, st>>>((int)n, (int)nrhs, a, lda, b, ldb);
+    RNPGPU_CHECK_LAUNCH();
+    return kOk;
+}
+
+template <class T> int trsm_lunn(size_t n, size_t nrhs, const T *a, size_t lda, T *b, size_t ldb) {
+    if (n == 0 || nrhs == 0) return kOk;
+    if (lda < n) return -4;
+    if (ldb < n) return -6;
+    if (a == nullptr) return -3;
+    if (b == nullptr) return -5;
+    if (n > (size_t)INT32_MAX || nrhs > (size_t)INT32_MAX) return -1;
+    return trsm_upper<T>(n, nrhs, a, lda, b, ldb, current_stream());
+}
+
+// ---------------------------------------------------------------------------
+// plain least squares
+// ---------------------------------------------------------------------------
+template <class T> size_t gels_bytes(size_t m, size_t n, size_t nrhs) {
+    size_t f = geqrf_bytes<T>(m, n, smax_for(m));
+    size_t q = unmqr_bytes<T>(m, nrhs, n, smax_for(m), smax_for(m));
+    return std::max(f, q);
+}
+
+template <class T> int gels(size_t m, size_t n, size_t nrhs, T *a, size_t lda, T *tau, T *b, size_t ldb, size_t *lwork, T *work) {
+    if (lwork == nullptr) return -9;
+    if (n > m) return -2;
+    if (m == 0 || n == 0 || nrhs == 0) return kOk;
+    if (lda < m) return -5;
+    if (ldb < m) return -8;
+    if (m > (size_t)INT32_MAX || nrhs > (size_t)INT32_MAX) return -1;
+    const size_t need = elems_for<T>(gels_bytes<T>(m, n, nrhs));
+    if (work == nullptr || *lwork == 0) {
+        *lwork = need;
+        return kOk;
+    }
+    if (a == nullptr) return -4;
+    if (tau == nullptr) return -6;
+    if (b == nullptr) return -7;
+    size_t lw = *lwork;
+    int rc = geqrf<T>(m, n, a, lda, tau, &lw, work);
+    if (rc) return rc < 0 ? -9 : rc;
+    lw = *lwork;
+    rc = unmqr<T>("L", "C", m, nrhs, n, a, lda, tau, b, ldb, &lw, work);
+    if (rc) return rc < 0 ? -9 : rc;
+    return trsm_upper<T>(n, nrhs, a, lda, b, ldb, current_stream());
+}
+
+// ---------------------------------------------------------------------------
+// mixed precision least squares with iterative refinement
+// ---------------------------------------------------------------------------
+template <class TH, class TL> struct RefinePlan {
+    size_t af, tauf, wq, r, rf, p, g, norms, total;
+    int split;
+    RefinePlan(size_t m, size_t n, size_t nrhs) {
+        auto al = [](size_t b) { return (b + 255) / 256 * 256; };
+        af = al(m * n * sizeof(TL));
+        tauf = al(n * sizeof(TL));
+        wq = al(std::max(geqrf_bytes<TL>(m, n, smax_for(m)), unmqr_bytes<TL>(m, nrhs, n, smax_for(m), smax_for(m))) + 256);
+        r = al(m * nrhs * sizeof(TH));
+        rf = al(m * nrhs * sizeof(TL));
+        split = smax_for(m);
+        p = al((size_t)split * n * nrhs * sizeof(TH));
+        g = al(n * nrhs * sizeof(TH));
+        norms = al((n + 6 * nrhs) * sizeof(double));
+        rf = std::max(rf, al(n * nrhs * sizeof(TL)));
+        total = af + tauf + wq + r + rf + p + g + norms;
+    }
+};
+
+template <class TH, class TL>
+int gels_refine(size_t m, size_t n, size_t nrhs, const TH *a, size_t lda, const TH *b, size_t ldb, TH *x, size_t ldx, int max_iter, int flags, RefineInfo *info, size_t *lwork, TH *work) {
+    if (lwork == nullptr) return -13;
+    if (n > m) return -2;
+    if (m == 0 || n == 0 || nrhs == 0) return kOk;
+    if (lda < m) return -5;
+    if (ldb < m) return -7;
+    if (ldx < n) return -9;
+    if (m > (size_t)INT32_MAX || nrhs > (size_t)INT32_MAX) return -1;
+    RefinePlan<TH, TL> plan(m, n, nrhs);
+    const size_t need = elems_for<TH>(plan.total);
+    if (work == nullptr || *lwork == 0) {
+        *lwork = need;
+        return kOk;
+    }
+    if (a == nullptr) return -4;
+    if (b == nullptr) return -6;
+    if (x == nullptr) return -8;
+    if (*lwork < need) return -13;
+    if (max_iter <= 0) max_iter = 10;
+    const bool forward = (flags & 1) != 0;
+    cudaStream_t st = current_stream();
+    Carver cv(work);
+    TL *Af = cv.take<TL>(plan.af / sizeof(TL));
+    TL *tauf = cv.take<TL>(plan.tauf / sizeof(TL));
+    TL *wq = cv.take<TL>(plan.wq / sizeof(TL));
+    TH *r = cv.take<TH>(plan.r / sizeof(TH));
+    TL *rf = cv.take<TL>(plan.rf / sizeof(TL));
+    TH *P = cv.take<TH>(plan.p / sizeof(TH));
+    TH *g = cv.take<TH>(plan.g / sizeof(TH));
+    double *dn = cv.take<double>(plan.norms / sizeof(double));
+    const size_t lwq = plan.wq / sizeof(TL);
+    const dim3 gmn((unsigned)std::min<size_t>((m + 255) / 256, 2048), (unsigned)std::min<size_t>(n, 65535));
+    const dim3 gmr((unsigned)std::min<size_t>((m + 255) / 256, 2048), (unsigned)std::min<size_t>(nrhs, 65535));
+    const dim3 gnr((unsigned)std::min<size_t>((n + 255) / 256, 2048), (unsigned)std::min<size_t>(nrhs, 65535));
+    const unsigned cb = (unsigned)std::min<size_t>(std::max(n, nrhs), 4096);
+    int rc;
+
+    // low-precision working copy and its factorization
+    k_convert<TH, TL><<<gmn, 256, 0, st>>>((int)m, (int)n, a, lda, Af, m);
+    RNPGPU_CHECK_LAUNCH();
+    size_t lw = lwq;
+    if ((rc = geqrf<TL>(m, n, Af, m, tauf, &lw, wq))) return rc < 0 ? -13 : rc;
+
+    // ||A||_F and ||b_j|| in FP64
+    std::vector<double> h(n + 6 * nrhs);
+    k_col_sumsq<TH><<<cb, 256, 0, st>>>((int)m, (int)n, a, lda, dn);
+    RNPGPU_CHECK_LAUNCH();
+    k_col_sumsq<TH><<<cb, 256, 0, st>>>((int)m, (int)nrhs, b, ldb, dn + n);
+    RNPGPU_CHECK_LAUNCH();
+    RNPGPU_CHECK(cudaMemcpyAsync(h.data(), dn, (n + nrhs) * sizeof(double), cudaMemcpyDeviceToHost, st));
+    RNPGPU_CHECK(cudaStreamSynchronize(st));
+    double asq = 0.0;
+    for (size_t j = 0; j < n; ++j) asq += h[j];
+    const double anorm = std::sqrt(asq);
+    std::vector<double> bn(nrhs);
+    for (size_t j = 0; j < nrhs; ++j) bn[j] = std::sqrt(h[n + j]);
+
+    // x = 0, r = b
+    RNPGPU_CHECK(cudaMemset2DAsync(x, ldx * sizeof(TH), 0, n * sizeof(TH), nrhs, st));
+    RNPGPU_CHECK(cudaMemcpy2DAsync(r, m * sizeof(TH), b, ldb * sizeof(TH), m * sizeof(TH), nrhs, cudaMemcpyDeviceToDevice, st));
+
+    const double eps = 0x1p-52;
+    const double tol = 10.0 * (double)n * eps;  // 10 n eps
+    TL *gf = rf;                                // n x nrhs low-precision copy of A^H r
+    auto correction_size = [&](double &corr_out) -> int {
+        RNPGPU_CHECK(cudaMemcpyAsync(h.data() + n + nrhs, dn + n + nrhs, 2 * nrhs * sizeof(double), cudaMemcpyDeviceToHost, st));
+        RNPGPU_CHECK(cudaStreamSynchronize(st));
+        corr_out = 0.0;
+        for (size_t j = 0; j < nrhs; ++j) {
+            double xs = h[n + 2 * nrhs + j], ds = h[n + nrhs + j];
+            corr_out = std::max(corr_out, xs > 0.0 ? std::sqrt(ds / xs) : (ds > 0.0 ? HUGE_VAL : 0.0));
+        }
+        return kOk;
+    };
+    // g = A^H r (FP64); y = R_f^{-H} g (low precision, in gf);
+    // eta = max_j ||g_j|| / (||A||_F (||A||_F ||x_j|| + ||b_j||)),
+    // mu  = max_j ||y_j|| / ||x_j||   (an upper bound of the Karlson-Walden
+    //                                   estimate of the LS backward error)
+    double eta = HUGE_VAL, mu = HUGE_VAL;
+    auto check = [&]() -> int {
+        const int S = choose_splits((int)m, ((int)n + 127) / 128, plan.split);
+        const int kchunk = (((int)m + S - 1) / S + 15) / 16 * 16;
+        const int nsplit = ((int)m + kchunk - 1) / kchunk;
+        GemmArgs<TH> ga = gemm_args<TH>(a, lda, kOpC, 0, r, m, kOpN, 0, P, n, (int)n, (int)nrhs, (int)m, TH(1), kBetaZero);
+        ga.kchunk = kchunk;
+        ga.dstride = n * nrhs;
+        int rc2 = launch_gemm(ga, nsplit, st, "normal_eq_fp64");
+        if (rc2) return rc2;
+        k_sum_partials<TH><<<gnr, 256, 0, st>>>(P, n, n * nrhs, nsplit, (int)n, (int)nrhs, g, n);
+        RNPGPU_CHECK_LAUNCH();
+        k_col_sumsq<TH><<<(unsigned)std::min<size_t>(nrhs, 4096), 256, 0, st>>>((int)n, (int)nrhs, g, n, dn + n + 3 * nrhs);
+        RNPGPU_CHECK_LAUNCH();
+        k_convert<TH, TL><<<gnr, 256, 0, st>>>((int)n, (int)nrhs, g, n, gf, n);
+        RNPGPU_CHECK_LAUNCH();
+        if ((rc2 = trsm_upper_ct<TL>(n, nrhs, Af, m, gf, n, st))) return rc2;
+        k_col_sumsq<TL><<<(unsigned)std::min<size_t>(nrhs, 4096), 256, 0, st>>>((int)n, (int)nrhs, gf, n, dn + n + 4 * nrhs);
+        RNPGPU_CHECK_LAUNCH();
+        RNPGPU_CHECK(cudaMemcpyAsync(h.data() + n + 3 * nrhs, dn + n + 3 * nrhs, 2 * nrhs * sizeof(double), cudaMemcpyDeviceToHost, st));
+        RNPGPU_CHECK(cudaStreamSynchronize(st));
+        eta = 0.0;
+        mu = 0.0;
+        for (size_t j = 0; j < nrhs; ++j) {
+            const double xn = std::sqrt(h[n + 2 * nrhs + j]);
+            const double den = anorm * (anorm * xn + bn[j]);
+            eta = std::max(eta, den > 0.0 ? std::sqrt(h[n + 3 * nrhs + j]) / den : 0.0);
+            mu = std::max(mu, xn > 0.0 ? std::sqrt(h[n + 4 * nrhs + j]) / xn : 0.0);
+        }
+        return kOk;
+    };
+
+    // Steps: "Q" steps d = R^{-1} (Q^H r)(0:n) until the LS backward error
+    // bound mu reaches 10 n eps; in forward mode then "CSNE" steps
+    // d = R^{-1} R^{-H} A^H r (corrected seminormal equations, whose fixed
+    // point satisfies A^H r = 0 exactly) until the correction stops shrinking.
+    bool csne = false, checked = false;
+    double prev_corr = HUGE_VAL, corr = 0.0;
+    int it = 0, converged = 0;
+    for (it = 0; it < max_iter;) {
+        if (!csne) {
+            k_convert<TH, TL><<<gmr, 256, 0, st>>>((int)m, (int)nrhs, r, m, rf, m);
+            RNPGPU_CHECK_LAUNCH();
+            lw = lwq;
+            if ((rc = unmqr<TL>("L", "C", m, nrhs, n, Af, m, tauf, rf, m, &lw, wq))) return rc < 0 ? -13 : rc;
+            if ((rc = trsm_upper<TL>(n, nrhs, Af, m, rf, m, st))) return rc;
+        } else {
+            // gf already holds R^{-H} A^H r from the last check
+            if ((rc = trsm_upper<TL>(n, nrhs, Af, m, gf, n, st))) return rc;
+        }
+        const size_t ldd = csne ? n : m;
+        k_add_correction<TL, TH><<<gnr, 256, 0, st>>>((int)n, (int)nrhs, rf, ldd, x, ldx);
+        RNPGPU_CHECK_LAUNCH();
+        k_col_sumsq<TL><<<(unsigned)std::min<size_t>(nrhs, 4096), 256, 0, st>>>((int)n, (int)nrhs, rf, ldd, dn + n + nrhs);
+        RNPGPU_CHECK_LAUNCH();
+        k_col_sumsq<TH><<<(unsigned)std::min<size_t>(nrhs, 4096), 256, 0, st>>>((int)n, (int)nrhs, x, ldx, dn + n + 2 * nrhs);
+        RNPGPU_CHECK_LAUNCH();
+        // r = b - A x in FP64
+        RNPGPU_CHECK(cudaMemcpy2DAsync(r, m * sizeof(TH), b, ldb * sizeof(TH), m * sizeof(TH), nrhs, cudaMemcpyDeviceToDevice, st));
+        GemmArgs<TH> gr = gemm_args<TH>(a, lda, kOpN, 0, x, ldx, kOpN, 0, r, m, (int)m, (int)nrhs, (int)n, TH(-1), kBetaOne);
+        if ((rc = launch_gemm(gr, 1, st, "residual_fp64"))) return rc;
+        ++it;
+        if ((rc = correction_size(corr))) return rc;
+        const bool stagnated = (it >= 2 && corr > 0.5 * prev_corr);
+        const bool last = (it == max_iter);
+        prev_corr = corr;
+        checked = false;
+        if (corr <= 1e-5 || stagnated || last || csne) {
+            if ((rc = check())) return rc;
+            checked = true;
+            const bool backward_ok = (mu <= tol) && (eta <= tol);
+            converged = backward_ok ? 1 : 0;
+            if (last) break;
+            if (!csne) {
+                // Q steps converge to the point where Q_f^H r = 0 for the FP32
+                // factor's Q_f; when that stalls above the bound (or forward
+                // accuracy is asked for) switch to the CSNE steps, whose
+                // fixed point is the least-squares solution itself.
+                if (backward_ok && !forward) break;
+                if (backward_ok || stagnated) {
+                    csne = true;
+                    prev_corr = HUGE_VAL;
+                }
+            } else {
+                if (backward_ok && !forward) break;
+                if (stagnated || corr <= 2.0 * eps) break;
+            }
+        }
+    }
+    if (!checked && (rc = check())) return rc;
+    if (info) {
+        info->iterations = it;
+        info->converged = converged;
+        info->backward_error = mu;
+        info->normal_residual = eta;
+        info->correction = corr;
+        info->anorm = anorm;
+    }
+    return kOk;
+}
+
+} // namespace rnpgpu

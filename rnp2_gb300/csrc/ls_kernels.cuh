@@ -1,0 +1,130 @@
+// ls_kernels.cuh — kernels of the least-squares layer built on the QR path:
+// upper-triangular solve (the reference's BLAS::SolveTrM "L","U","N","N",
+// RNP/BLAS/BLAS_mix.hpp:2096-2113 -> dtrsm_), precision conversion, column
+// norms and the FP64 accumulation of refinement corrections.
+#pragma once
+#include "qr_kernels.cuh"
+
+namespace rnpgpu {
+
+// X = R^{-1} Y in place (Y is n x nrhs with leading dimension ldb), R upper
+// triangular non-unit (leading dimension ldr).  One block per right-hand
+// side; 32 x 32 diagonal blocks solved by one warp with shuffles, the rows
+// above updated by the whole block.
+template <class T> __global__ void __launch_bounds__(256) k_trsm_upper(int n, int nrhs, const T *R, size_t ldr, T *B, size_t ldb) {
+    __shared__ T xs[32];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int col = blockIdx.x; col < nrhs; col += gridDim.x) {
+        T *y = B + (size_t)col * ldb;
+        for (int i1 = n; i1 > 0; i1 -= 32) {
+            const int i0 = max(0, i1 - 32), nbk = i1 - i0;
+            if (warp == 0) {
+                T yv = (lane < nbk) ? y[i0 + lane] : T(0);
+                for (int i = nbk - 1; i >= 0; --i) {
+                    if (lane == i) yv = yv / R[(i0 + i) + (size_t)(i0 + i) * ldr];
+                    const T xi = shfl(yv, i);
+                    if (lane < i) yv = yv - R[(i0 + lane) + (size_t)(i0 + i) * ldr] * xi;
+                }
+                if (lane < nbk) {
+                    y[i0 + lane] = yv;
+                    xs[lane] = yv;
+                }
+            }
+            __syncthreads();
+            for (int r = tid; r < i0; r += blockDim.x) {
+                T acc = y[r];
+                for (int c = 0; c < nbk; ++c) acc = fmac(-R[r + (size_t)(i0 + c) * ldr], xs[c], acc);
+                y[r] = acc;
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// Y = R^{-H} G in place: forward substitution with the conjugate transpose of
+// an upper triangular R (the lower triangular system R^H y = g).
+template <class T> __global__ void __launch_bounds__(256) k_trsm_upper_ct(int n, int nrhs, const T *R, size_t ldr, T *B, size_t ldb) {
+    __shared__ T xs[32];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int col = blockIdx.x; col < nrhs; col += gridDim.x) {
+        T *y = B + (size_t)col * ldb;
+        for (int i0 = 0; i0 < n; i0 += 32) {
+            const int nbk = min(32, n - i0), i1 = i0 + nbk;
+            if (warp == 0) {
+                T yv = (lane < nbk) ? y[i0 + lane] : T(0);
+                for (int i = 0; i < nbk; ++i) {
+                    if (lane == i) yv = yv / Tr<T>::conj(R[(i0 + i) + (size_t)(i0 + i) * ldr]);
+                    const T xi = shfl(yv, i);
+                    if (lane > i && lane < nbk) yv = yv - Tr<T>::conj(R[(i0 + i) + (size_t)(i0 + lane) * ldr]) * xi;
+                }
+                if (lane < nbk) {
+                    y[i0 + lane] = yv;
+                    xs[lane] = yv;
+                }
+            }
+            __syncthreads();
+            for (int r = i1 + tid; r < n; r += blockDim.x) {
+                T acc = y[r];
+                const T *rc = R + (size_t)r * ldr + i0;
+                for (int c = 0; c < nbk; ++c) acc = fmac(-Tr<T>::conj(rc[c]), xs[c], acc);
+                y[r] = acc;
+            }
+            __syncthreads();
+        }
+    }
+}
+
+template <class Tin, class Tout> __device__ __forceinline__ Tout convert_scalar(Tin v);
+template <> __device__ __forceinline__ float convert_scalar<double, float>(double v) { return (float)v; }
+template <> __device__ __forceinline__ double convert_scalar<float, double>(float v) { return (double)v; }
+template <> __device__ __forceinline__ double convert_scalar<double, double>(double v) { return v; }
+template <> __device__ __forceinline__ float convert_scalar<float, float>(float v) { return v; }
+template <> __device__ __forceinline__ cf32 convert_scalar<cf64, cf32>(cf64 v) { return cf32((float)v.x, (float)v.y); }
+template <> __device__ __forceinline__ cf64 convert_scalar<cf32, cf64>(cf32 v) { return cf64((double)v.x, (double)v.y); }
+template <> __device__ __forceinline__ cf64 convert_scalar<cf64, cf64>(cf64 v) { return v; }
+template <> __device__ __forceinline__ cf32 convert_scalar<cf32, cf32>(cf32 v) { return v; }
+
+// B(0:m, 0:n) = (Tout) A(0:m, 0:n)
+template <class Tin, class Tout> __global__ void __launch_bounds__(256) k_convert(int m, int n, const Tin *A, size_t lda, Tout *B, size_t ldb) {
+    for (int c = blockIdx.y; c < n; c += gridDim.y)
+        for (int r = blockIdx.x * 256 + threadIdx.x; r < m; r += gridDim.x * 256)
+            B[r + (size_t)c * ldb] = convert_scalar<Tin, Tout>(A[r + (size_t)c * lda]);
+}
+
+// X(0:n, j) += (Th) D(0:n, j)
+template <class Tl, class Th> __global__ void __launch_bounds__(256) k_add_correction(int n, int nrhs, const Tl *D, size_t ldd, Th *X, size_t ldx) {
+    for (int c = blockIdx.y; c < nrhs; c += gridDim.y)
+        for (int r = blockIdx.x * 256 + threadIdx.x; r < n; r += gridDim.x * 256)
+            X[r + (size_t)c * ldx] = X[r + (size_t)c * ldx] + convert_scalar<Tl, Th>(D[r + (size_t)c * ldd]);
+}
+
+// out[j] = ||A(0:m, j)||_2^2 accumulated in FP64 (error metrics only)
+template <class T> __global__ void __launch_bounds__(256) k_col_sumsq(int m, int n, const T *A, size_t lda, double *out) {
+    __shared__ double s[8];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int c = blockIdx.x; c < n; c += gridDim.x) {
+        double acc = 0.0;
+        for (int r = tid; r < m; r += 256) acc += abs2(A[r + (size_t)c * lda]);
+        acc = warp_sum(acc);
+        if (lane == 0) s[warp] = acc;
+        __syncthreads();
+        if (tid == 0) {
+            double t = 0.0;
+            for (int w = 0; w < 8; ++w) t += s[w];
+            out[c] = t;
+        }
+        __syncthreads();
+    }
+}
+
+// out(0:rows, 0:cols) = sum over q < nsplit of P_q  (P_q = P + q*pstride)
+template <class T> __global__ void __launch_bounds__(256) k_sum_partials(const T *P, size_t ldp, size_t pstride, int nsplit, int rows, int cols, T *out, size_t ldo) {
+    for (int c = blockIdx.y; c < cols; c += gridDim.y)
+        for (int r = blockIdx.x * 256 + threadIdx.x; r < rows; r += gridDim.x * 256) {
+            T acc = T(0);
+            for (int q = 0; q < nsplit; ++q) acc = acc + P[(size_t)q * pstride + r + (size_t)c * ldp];
+            out[r + (size_t)c * ldo] = acc;
+        }
+}
+
+} // namespace rnpgpu

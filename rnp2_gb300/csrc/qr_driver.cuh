@@ -28,6 +28,22 @@ cudaStream_t current_stream();
 void set_last_error(const char *msg);
 const DeviceFacts &device_facts();
 
+// Launch accounting and optional per-kernel-class timing (CUDA events on the
+// launching stream; only while rnpgpu_timing_enable(1) is in effect).
+void note_launch();
+void ktimer_begin(const char *name, cudaStream_t st);
+void ktimer_end(cudaStream_t st);
+struct KScope {
+    cudaStream_t st;
+    KScope(const char *name, cudaStream_t s) : st(s) { ktimer_begin(name, s); }
+    ~KScope() { ktimer_end(st); }
+};
+template <class T> struct TypeName;
+template <> struct TypeName<float> { static constexpr const char *v = "f32"; };
+template <> struct TypeName<double> { static constexpr const char *v = "f64"; };
+template <> struct TypeName<cf32> { static constexpr const char *v = "c32"; };
+template <> struct TypeName<cf64> { static constexpr const char *v = "c64"; };
+
 template <class T> struct TypeIndex;
 template <> struct TypeIndex<float> { static constexpr int v = 0; };
 template <> struct TypeIndex<double> { static constexpr int v = 1; };
@@ -42,7 +58,11 @@ template <> struct TypeIndex<cf64> { static constexpr int v = 3; };
             return kErrCuda;                                                \
         }                                                                   \
     } while (0)
-#define RNPGPU_CHECK_LAUNCH() RNPGPU_CHECK(cudaGetLastError())
+#define RNPGPU_CHECK_LAUNCH()            \
+    do {                                 \
+        note_launch();                   \
+        RNPGPU_CHECK(cudaGetLastError()); \
+    } while (0)
 
 // Tuning (RNP/LA/QR.hpp:41-51 keeps nb=32, nbmin=2, crossover=128 for the
 // CPU).  On the GPU every column block goes through the blocked path: the
@@ -73,11 +93,15 @@ template <class T> size_t elems_for(size_t bytes) { return (bytes + 256 + sizeof
 // ---------------------------------------------------------------------------
 // Contraction launcher
 // ---------------------------------------------------------------------------
-template <class T> int launch_gemm(GemmArgs<T> g, int nsplit, cudaStream_t st) {
+template <class T> int launch_gemm(GemmArgs<T> g, int nsplit, cudaStream_t st, const char *tag = "gemm") {
     if (g.M <= 0 || g.N <= 0) return kOk;
     if (g.K <= 0 && g.beta_mode == kBetaOne) return kOk;
     if (g.kchunk <= 0) g.kchunk = g.K > 0 ? g.K : 1;
-    if (g.N <= 32) {
+    KScope ks(tag, st);
+    if (g.N <= 16) {
+        dim3 grid((g.M + 127) / 128, (g.N + 15) / 16, nsplit);
+        k_gemm<T, 128, 16, 16, 8, 1><<<grid, 256, 0, st>>>(g);
+    } else if (g.N <= 32) {
         dim3 grid((g.M + 63) / 64, (g.N + 31) / 32, nsplit);
         k_gemm<T, 64, 32, 16, 4, 2><<<grid, 256, 0, st>>>(g);
     } else {
@@ -133,13 +157,13 @@ template <class T> int apply_block(bool left, bool notran, int M, int N, int ib,
         GemmArgs<T> g = gemm_args<T>(C, ldc, kOpC, 0, V, ldv, kOpN, 1, ws.P, (size_t)N, N, ib, M, T(1), kBetaZero);
         g.kchunk = kchunk;
         g.dstride = (size_t)N * ib;
-        if ((rc = launch_gemm(g, nsplit, st))) return rc;
+        if ((rc = launch_gemm(g, nsplit, st, "larfb_w"))) return rc;
         // W := W T (H^H) or W T^H (H)
         k_sum_times_t<T><<<(N + 7) / 8, 256, 0, st>>>(ws.P, (size_t)N, (size_t)N * ib, nsplit, N, ib, Tm, ldt, notran ? kOpC : kOpN, ws.W, (size_t)N);
         RNPGPU_CHECK_LAUNCH();
         // C -= V W^H
         GemmArgs<T> u = gemm_args<T>(V, ldv, kOpN, 1, ws.W, (size_t)N, kOpC, 0, C, ldc, M, N, ib, T(-1), kBetaOne);
-        return launch_gemm(u, 1, st);
+        return launch_gemm(u, 1, st, "larfb_update");
     } else {
         // W = C V  (M x ib), reduction over the N columns
         const int tiles = (M + 63) / 64;
@@ -149,12 +173,12 @@ template <class T> int apply_block(bool left, bool notran, int M, int N, int ib,
         GemmArgs<T> g = gemm_args<T>(C, ldc, kOpN, 0, V, ldv, kOpN, 1, ws.P, (size_t)M, M, ib, N, T(1), kBetaZero);
         g.kchunk = kchunk;
         g.dstride = (size_t)M * ib;
-        if ((rc = launch_gemm(g, nsplit, st))) return rc;
+        if ((rc = launch_gemm(g, nsplit, st, "larfb_w"))) return rc;
         k_sum_times_t<T><<<(M + 7) / 8, 256, 0, st>>>(ws.P, (size_t)M, (size_t)M * ib, nsplit, M, ib, Tm, ldt, notran ? kOpN : kOpC, ws.W, (size_t)M);
         RNPGPU_CHECK_LAUNCH();
         // C -= W V^H
         GemmArgs<T> u = gemm_args<T>(ws.W, (size_t)M, kOpN, 0, V, ldv, kOpC, 1, C, ldc, M, N, ib, T(-1), kBetaOne);
-        return launch_gemm(u, 1, st);
+        return launch_gemm(u, 1, st, "larfb_update");
     }
 }
 
@@ -167,7 +191,7 @@ template <class T> int block_t(int rows, int ib, const T *V, size_t ldv, const T
     GemmArgs<T> g = gemm_args<T>(V, ldv, kOpC, 1, V, ldv, kOpN, 1, Pg, (size_t)kPanelMaxCols, ib, ib, rows, T(1), kBetaZero);
     g.kchunk = kchunk;
     g.dstride = (size_t)kPanelMaxCols * kPanelMaxCols;
-    int rc = launch_gemm(g, nsplit, st);
+    int rc = launch_gemm(g, nsplit, st, "larft_gram");
     if (rc) return rc;
     k_build_t<T><<<1, kPanelMaxCols, 0, st>>>(Pg, (size_t)kPanelMaxCols * kPanelMaxCols, 0, nsplit, tau, ib, ib, Tout, 0, ldt);
     RNPGPU_CHECK_LAUNCH();
@@ -200,7 +224,9 @@ template <class T> int panel_factor(int M, int N, T *A, size_t lda, T *tau, T *T
     p.rows_per_cta = (M + G - 1) / G;
     RNPGPU_CHECK(cudaMemsetAsync(ws.sync, 0, 2 * sizeof(unsigned), st));
     void *args[] = {&p};
+    KScope ks("panel", st);
     RNPGPU_CHECK(cudaLaunchCooperativeKernel((const void *)k_panel<T>, dim3(G), dim3(kPanelThreads), args, 0, st));
+    note_launch();
     return kOk;
 }
 

@@ -23,6 +23,15 @@ template <class R> __host__ __device__ inline cplx<R> operator*(cplx<R> a, cplx<
 template <class R> __host__ __device__ inline cplx<R> operator*(cplx<R> a, R b) { return cplx<R>(a.x * b, a.y * b); }
 template <class R> __host__ __device__ inline cplx<R> operator*(R b, cplx<R> a) { return cplx<R>(a.x * b, a.y * b); }
 template <class R> __host__ __device__ inline cplx<R> operator/(cplx<R> a, R b) { return cplx<R>(a.x / b, a.y / b); }
+// a/b by Smith's algorithm (Smith, CACM 5(8), 1962)
+template <class R> __host__ __device__ inline cplx<R> operator/(cplx<R> a, cplx<R> b) {
+    if ((b.y < 0 ? -b.y : b.y) <= (b.x < 0 ? -b.x : b.x)) {
+        R r = b.y / b.x, d = b.x + b.y * r;
+        return cplx<R>((a.x + a.y * r) / d, (a.y - a.x * r) / d);
+    }
+    R r = b.x / b.y, d = b.y + b.x * r;
+    return cplx<R>((a.x * r + a.y) / d, (a.y * r - a.x) / d);
+}
 template <class R> __host__ __device__ inline bool operator==(cplx<R> a, cplx<R> b) { return a.x == b.x && a.y == b.y; }
 template <class R> __host__ __device__ inline bool operator!=(cplx<R> a, cplx<R> b) { return !(a == b); }
 
@@ -81,6 +90,12 @@ __device__ __forceinline__ float warp_sum(float v) {
 template <class R> __device__ __forceinline__ cplx<R> warp_sum(cplx<R> v) {
     return cplx<R>(warp_sum(v.x), warp_sum(v.y));
 }
+__device__ __forceinline__ double shfl(double v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+__device__ __forceinline__ float shfl(float v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+template <class R> __device__ __forceinline__ cplx<R> shfl(cplx<R> v, int src) { return cplx<R>(shfl(v.x, src), shfl(v.y, src)); }
+__device__ __forceinline__ double abs2(double v) { return v * v; }
+__device__ __forceinline__ double abs2(float v) { return (double)v * (double)v; }
+template <class R> __device__ __forceinline__ double abs2(cplx<R> v) { return (double)v.x * (double)v.x + (double)v.y * (double)v.y; }
 
 // ---------------------------------------------------------------------------
 // Safe 2-norm accumulation without divisions (three accumulators for tiny,

@@ -1,0 +1,76 @@
+"""Least squares on the GB300 QR (include/rnp_gpu/ls_gb300.h), for torch CUDA
+tensors in column-major layout (see rnp2_gb300.qr).
+
+  gels(A, B)            plain: Factor, MultQ("L","C"), triangular solve; in place
+  gels_refine(A, B)     mixed: FP32 factor + FP64 iterative refinement
+  trsm_upper(R, B)      B <- R^{-1} B, R upper triangular (SolveTrM "L","U","N","N")
+"""
+import ctypes as C
+
+import torch
+
+from ._capi import RefineInfo, lib
+from .qr import _PREFIX, _bind_stream, _check, colmajor, empty_colmajor
+
+
+def trsm_upper(R, B):
+    p = _PREFIX[B.dtype]
+    n = R.shape[1]
+    r, ldr = colmajor(R)
+    b, ldb = colmajor(B)
+    _bind_stream()
+    _check("trsm_lunn", getattr(lib(), "rnpgpu_%strsm_lunn" % p)(n, B.shape[1], r, ldr, b, ldb))
+    return B
+
+
+def gels(A, B, tau=None, work=None):
+    """min ||A X - B||: A (m x n, m >= n) and B (m x nrhs) are overwritten;
+    returns the solution view B[:n]."""
+    p = _PREFIX[A.dtype]
+    m, n = A.shape
+    nrhs = B.shape[1]
+    if tau is None:
+        tau = torch.zeros(max(n, 1), dtype=A.dtype, device=A.device)
+    a, lda = colmajor(A)
+    b, ldb = colmajor(B)
+    fn = getattr(lib(), "rnpgpu_%sgels" % p)
+    _bind_stream()
+    if work is None:
+        lw = C.c_size_t(0)
+        _check("gels", fn(m, n, nrhs, a, lda, tau.data_ptr(), b, ldb, C.byref(lw), None))
+        work = torch.empty(max(lw.value, 1), dtype=A.dtype, device=A.device)
+    lw = C.c_size_t(work.numel())
+    _check("gels", fn(m, n, nrhs, a, lda, tau.data_ptr(), b, ldb, C.byref(lw), work.data_ptr()))
+    return B[:n]
+
+
+def refine_workspace(A, nrhs):
+    p = {torch.float64: "ds", torch.complex128: "zc"}[A.dtype]
+    m, n = A.shape
+    lw = C.c_size_t(0)
+    fn = getattr(lib(), "rnpgpu_%sgels" % p)
+    _check("gels_refine", fn(m, n, nrhs, None, max(m, 1), None, max(m, 1), None, max(n, 1), 0, 0, None, C.byref(lw), None))
+    return lw.value
+
+
+def gels_refine(A, B, X=None, max_iter=10, work=None, forward=False):
+    """Mixed-precision least squares (FP32 factor, FP64 refinement) of an FP64
+    (or complex128) problem; A and B are not modified.  forward=True adds the
+    corrected seminormal-equation steps for FP64 forward accuracy.
+    Returns (X, info)."""
+    p = {torch.float64: "ds", torch.complex128: "zc"}[A.dtype]
+    m, n = A.shape
+    nrhs = B.shape[1]
+    if X is None:
+        X = empty_colmajor(n, nrhs, A.dtype, A.device)
+    a, lda = colmajor(A)
+    b, ldb = colmajor(B)
+    x, ldx = colmajor(X)
+    fn = getattr(lib(), "rnpgpu_%sgels" % p)
+    _bind_stream()
+    if work is None:
+        work = torch.empty(max(refine_workspace(A, nrhs), 1), dtype=A.dtype, device=A.device)
+    info = RefineInfo()
+    lw = C.c_size_t(work.numel())
+    _check("gels_refine", fn(m, n, nrhs, a, lda, b, ldb, x, ldx, int(max_iter), 1 if forward else 0, C.byref(info), C.byref(lw), work.data_ptr()))
+    return X, info.as_dict()
