@@ -47,6 +47,16 @@ int rnpgpu_dgeqrf(size_t m, size_t n, double *a, size_t lda, double *tau, size_t
 int rnpgpu_cgeqrf(size_t m, size_t n, rnpgpu_complex_float *a, size_t lda, rnpgpu_complex_float *tau, size_t *lwork, rnpgpu_complex_float *work);
 int rnpgpu_zgeqrf(size_t m, size_t n, rnpgpu_complex_double *a, size_t lda, rnpgpu_complex_double *tau, size_t *lwork, rnpgpu_complex_double *work);
 
+/* ---- Factor without a work block (no counterpart in the reference): the
+ *      same factorization as rnpgpu_dgeqrf for callers that cannot allocate
+ *      device memory (frameworks that own and pre-budget it, fixed-budget
+ *      real-time loops).  It uses an 8 MiB scratch array built into the
+ *      library, so n is limited to about 16,000 columns (status -2 beyond,
+ *      message in rnpgpu_get_last_error()).  The first call on a device looks
+ *      up the array's address and should come before any stream capture;
+ *      calls that overlap on the GPU share the array and race. ---- */
+int rnpgpu_dgeqrf_noalloc(size_t m, size_t n, double *a, size_t lda, double *tau);
+
 /* ---- Factor_unblocked: RNP::LA::QR::Factor_unblocked (RNP/LA/QR.hpp:78-102), _geqr2; work: n ---- */
 int rnpgpu_sgeqr2(size_t m, size_t n, float *a, size_t lda, float *tau, float *work);
 int rnpgpu_dgeqr2(size_t m, size_t n, double *a, size_t lda, double *tau, double *work);
