@@ -234,6 +234,14 @@ def gpu_arm(args, rank, world, local):
     eta_mixed, _ = ls_errors(torch, A, b, X)
     x_mixed = X.clone()
 
+    if args.phase == "mixed":
+        # profiling runs (ncu launch lists): the mixed solves only
+        if rank == 0:
+            print(json.dumps({"phase": "mixed", "ms_per_step": ms, "value": value, "gpu_launches": int(launches)}), flush=True)
+        if dist is not None:
+            dist.destroy_process_group()
+        return 0
+
     # ---------------- e2e through host buffers ------------------------------
     A_h = A.cpu().pin_memory()
     b_h = b.cpu().pin_memory()
@@ -367,6 +375,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--phase", default="all", choices=["all", "mixed"], help="'mixed': only the timed mixed solves (for profiler runs)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
     rank, world, local = dist_env()

@@ -42,7 +42,7 @@ int rnpgpu_zgels(size_t m, size_t n, size_t nrhs, rnpgpu_complex_double *a, size
  *      (an upper bound of the Karlson-Walden estimate) and the normal-equation
  *      residual  max_j ||A^H r_j|| / (||A||_F (||A||_F ||x_j|| + ||b_j||))
  *      are both at most 10 n eps, the correction stops halving, or max_iter
- *      steps are taken (max_iter <= 0: 10).
+ *      steps are taken (max_iter <= 0: 10, or 30 in forward mode).
  *      flags bit 0 (RNPGPU_REFINE_FORWARD): continue with corrected
  *      seminormal-equation steps  x += R^{-1} R^{-H} A^H r  until the
  *      correction stops shrinking, for FP64-level forward accuracy.

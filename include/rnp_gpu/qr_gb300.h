@@ -96,6 +96,15 @@ void *rnpgpu_get_stream(void);
 const char *rnpgpu_get_last_error(void);
 /* Library version string. */
 const char *rnpgpu_version(void);
+/* Device-side status of the tensor-core kernels: nonzero if one of their
+ * bounded waits gave up (its results are then not valid); reset != 0 clears
+ * it.  Synchronous. */
+int rnpgpu_device_status(int reset);
+/* C = alpha op(A) op(B) + beta C in FP32 on the tensor cores (each operand
+ * split into three BF16 terms, six products, FP32 accumulation); op "N" or
+ * "T", beta 0 or 1.  No counterpart in the reference: the contraction of the
+ * FP32 trailing updates, exported for checking. */
+int rnpgpu_sgemm_tc(const char *transa, const char *transb, size_t m, size_t n, size_t k, float alpha, const float *a, size_t lda, const float *b, size_t ldb, float beta, float *c, size_t ldc);
 /* Number of kernels this library has launched in this process. */
 unsigned long long rnpgpu_launch_count(void);
 /* Per-kernel-class timing with CUDA events on the launching stream, for the

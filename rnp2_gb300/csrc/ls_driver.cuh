@@ -57,10 +57,12 @@ template <class T> int trsm_lunn(size_t n, size_t nrhs, const T *a, size_t lda, 
 // ---------------------------------------------------------------------------
 // plain least squares
 // ---------------------------------------------------------------------------
+template <class T> size_t tstore_bytes(size_t n) { return ((n + GpuTuning::nb - 1) / GpuTuning::nb) * t_bytes<T>(); }
+
 template <class T> size_t gels_bytes(size_t m, size_t n, size_t nrhs) {
     size_t f = geqrf_bytes<T>(m, n, smax_for(m));
     size_t q = unmqr_bytes<T>(m, nrhs, n, smax_for(m), smax_for(m));
-    return std::max(f, q);
+    return std::max(f, q) + tstore_bytes<T>(n) + 512;
 }
 
 template <class T> int gels(size_t m, size_t n, size_t nrhs, T *a, size_t lda, T *tau, T *b, size_t ldb, size_t *lwork, T *work) {
@@ -78,11 +80,16 @@ template <class T> int gels(size_t m, size_t n, size_t nrhs, T *a, size_t lda, T
     if (a == nullptr) return -4;
     if (tau == nullptr) return -6;
     if (b == nullptr) return -7;
-    size_t lw = *lwork;
-    int rc = geqrf<T>(m, n, a, lda, tau, &lw, work);
+    if (*lwork < need) return -9;
+    // the T factors of the factorization are kept for MultQ
+    Carver cv(work);
+    T *Ts = cv.take<T>(tstore_bytes<T>(n) / sizeof(T));
+    T *wrest = cv.take<T>(0);
+    size_t lw = *lwork - (size_t)(wrest - work);
+    int rc = geqrf<T>(m, n, a, lda, tau, &lw, wrest, Ts);
     if (rc) return rc < 0 ? -9 : rc;
-    lw = *lwork;
-    rc = unmqr<T>("L", "C", m, nrhs, n, a, lda, tau, b, ldb, &lw, work);
+    lw = *lwork - (size_t)(wrest - work);
+    rc = unmqr<T>("L", "C", m, nrhs, n, a, lda, tau, b, ldb, &lw, wrest, Ts);
     if (rc) return rc < 0 ? -9 : rc;
     return trsm_upper<T>(n, nrhs, a, lda, b, ldb, current_stream());
 }
@@ -91,12 +98,13 @@ template <class T> int gels(size_t m, size_t n, size_t nrhs, T *a, size_t lda, T
 // mixed precision least squares with iterative refinement
 // ---------------------------------------------------------------------------
 template <class TH, class TL> struct RefinePlan {
-    size_t af, tauf, wq, r, rf, p, g, norms, total;
+    size_t af, tauf, ts, wq, r, rf, p, g, norms, total;
     int split;
     RefinePlan(size_t m, size_t n, size_t nrhs) {
         auto al = [](size_t b) { return (b + 255) / 256 * 256; };
         af = al(m * n * sizeof(TL));
         tauf = al(n * sizeof(TL));
+        ts = al(tstore_bytes<TL>(n));
         wq = al(std::max(geqrf_bytes<TL>(m, n, smax_for(m)), unmqr_bytes<TL>(m, nrhs, n, smax_for(m), smax_for(m))) + 256);
         r = al(m * nrhs * sizeof(TH));
         rf = al(m * nrhs * sizeof(TL));
@@ -105,7 +113,7 @@ template <class TH, class TL> struct RefinePlan {
         g = al(n * nrhs * sizeof(TH));
         norms = al((n + 6 * nrhs) * sizeof(double));
         rf = std::max(rf, al(n * nrhs * sizeof(TL)));
-        total = af + tauf + wq + r + rf + p + g + norms;
+        total = af + tauf + ts + wq + r + rf + p + g + norms;
     }
 };
 
@@ -128,12 +136,13 @@ int gels_refine(size_t m, size_t n, size_t nrhs, const TH *a, size_t lda, const 
     if (b == nullptr) return -6;
     if (x == nullptr) return -8;
     if (*lwork < need) return -13;
-    if (max_iter <= 0) max_iter = 10;
     const bool forward = (flags & 1) != 0;
+    if (max_iter <= 0) max_iter = forward ? 30 : 10;
     cudaStream_t st = current_stream();
     Carver cv(work);
     TL *Af = cv.take<TL>(plan.af / sizeof(TL));
     TL *tauf = cv.take<TL>(plan.tauf / sizeof(TL));
+    TL *Tf = cv.take<TL>(plan.ts / sizeof(TL));
     TL *wq = cv.take<TL>(plan.wq / sizeof(TL));
     TH *r = cv.take<TH>(plan.r / sizeof(TH));
     TL *rf = cv.take<TL>(plan.rf / sizeof(TL));
@@ -151,7 +160,7 @@ int gels_refine(size_t m, size_t n, size_t nrhs, const TH *a, size_t lda, const 
     k_convert<TH, TL><<<gmn, 256, 0, st>>>((int)m, (int)n, a, lda, Af, m);
     RNPGPU_CHECK_LAUNCH();
     size_t lw = lwq;
-    if ((rc = geqrf<TL>(m, n, Af, m, tauf, &lw, wq))) return rc < 0 ? -13 : rc;
+    if ((rc = geqrf<TL>(m, n, Af, m, tauf, &lw, wq, Tf))) return rc < 0 ? -13 : rc;
 
     // ||A||_F and ||b_j|| in FP64
     std::vector<double> h(n + 6 * nrhs);
@@ -232,7 +241,7 @@ int gels_refine(size_t m, size_t n, size_t nrhs, const TH *a, size_t lda, const 
             k_convert<TH, TL><<<gmr, 256, 0, st>>>((int)m, (int)nrhs, r, m, rf, m);
             RNPGPU_CHECK_LAUNCH();
             lw = lwq;
-            if ((rc = unmqr<TL>("L", "C", m, nrhs, n, Af, m, tauf, rf, m, &lw, wq))) return rc < 0 ? -13 : rc;
+            if ((rc = unmqr<TL>("L", "C", m, nrhs, n, Af, m, tauf, rf, m, &lw, wq, Tf))) return rc < 0 ? -13 : rc;
             if ((rc = trsm_upper<TL>(n, nrhs, Af, m, rf, m, st))) return rc;
         } else {
             // gf already holds R^{-H} A^H r from the last check
@@ -251,7 +260,10 @@ int gels_refine(size_t m, size_t n, size_t nrhs, const TH *a, size_t lda, const 
         if ((rc = launch_gemm(gr, 1, st, "residual_fp64"))) return rc;
         ++it;
         if ((rc = correction_size(corr))) return rc;
-        const bool stagnated = (it >= 2 && corr > 0.5 * prev_corr);
+        // Q steps contract fast, so failing to halve means they have stalled;
+        // CSNE steps contract more slowly and count as stalled only when the
+        // correction no longer shrinks noticeably
+        const bool stagnated = (it >= 2 && corr > (csne ? 0.9 : 0.5) * prev_corr);
         const bool last = (it == max_iter);
         prev_corr = corr;
         checked = false;

@@ -9,21 +9,27 @@ namespace rnpgpu {
 
 // X = R^{-1} Y in place (Y is n x nrhs with leading dimension ldb), R upper
 // triangular non-unit (leading dimension ldr).  One block per right-hand
-// side; 32 x 32 diagonal blocks solved by one warp with shuffles, the rows
-// above updated by the whole block.
+// side; each 32 x 32 diagonal block is staged in shared memory and solved by
+// one warp with shuffles, the rows above are updated by the whole block.
 template <class T> __global__ void __launch_bounds__(256) k_trsm_upper(int n, int nrhs, const T *R, size_t ldr, T *B, size_t ldb) {
     __shared__ T xs[32];
+    __shared__ T sR[32][33];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     for (int col = blockIdx.x; col < nrhs; col += gridDim.x) {
         T *y = B + (size_t)col * ldb;
         for (int i1 = n; i1 > 0; i1 -= 32) {
             const int i0 = max(0, i1 - 32), nbk = i1 - i0;
+            for (int idx = tid; idx < nbk * nbk; idx += blockDim.x) {
+                const int r = idx % nbk, c = idx / nbk;
+                sR[r][c] = (r <= c) ? R[(i0 + r) + (size_t)(i0 + c) * ldr] : T(0);
+            }
+            __syncthreads();
             if (warp == 0) {
                 T yv = (lane < nbk) ? y[i0 + lane] : T(0);
                 for (int i = nbk - 1; i >= 0; --i) {
-                    if (lane == i) yv = yv / R[(i0 + i) + (size_t)(i0 + i) * ldr];
+                    if (lane == i) yv = yv / sR[i][i];
                     const T xi = shfl(yv, i);
-                    if (lane < i) yv = yv - R[(i0 + lane) + (size_t)(i0 + i) * ldr] * xi;
+                    if (lane < i) yv = yv - sR[lane][i] * xi;
                 }
                 if (lane < nbk) {
                     y[i0 + lane] = yv;
@@ -45,17 +51,23 @@ template <class T> __global__ void __launch_bounds__(256) k_trsm_upper(int n, in
 // an upper triangular R (the lower triangular system R^H y = g).
 template <class T> __global__ void __launch_bounds__(256) k_trsm_upper_ct(int n, int nrhs, const T *R, size_t ldr, T *B, size_t ldb) {
     __shared__ T xs[32];
+    __shared__ T sR[32][33];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     for (int col = blockIdx.x; col < nrhs; col += gridDim.x) {
         T *y = B + (size_t)col * ldb;
         for (int i0 = 0; i0 < n; i0 += 32) {
             const int nbk = min(32, n - i0), i1 = i0 + nbk;
+            for (int idx = tid; idx < nbk * nbk; idx += blockDim.x) {
+                const int r = idx % nbk, c = idx / nbk;
+                sR[r][c] = (r <= c) ? R[(i0 + r) + (size_t)(i0 + c) * ldr] : T(0);
+            }
+            __syncthreads();
             if (warp == 0) {
                 T yv = (lane < nbk) ? y[i0 + lane] : T(0);
                 for (int i = 0; i < nbk; ++i) {
-                    if (lane == i) yv = yv / Tr<T>::conj(R[(i0 + i) + (size_t)(i0 + i) * ldr]);
+                    if (lane == i) yv = yv / Tr<T>::conj(sR[i][i]);
                     const T xi = shfl(yv, i);
-                    if (lane > i && lane < nbk) yv = yv - Tr<T>::conj(R[(i0 + i) + (size_t)(i0 + lane) * ldr]) * xi;
+                    if (lane > i && lane < nbk) yv = yv - Tr<T>::conj(sR[i][lane]) * xi;
                 }
                 if (lane < nbk) {
                     y[i0 + lane] = yv;
@@ -121,9 +133,16 @@ template <class T> __global__ void __launch_bounds__(256) k_col_sumsq(int m, int
 template <class T> __global__ void __launch_bounds__(256) k_sum_partials(const T *P, size_t ldp, size_t pstride, int nsplit, int rows, int cols, T *out, size_t ldo) {
     for (int c = blockIdx.y; c < cols; c += gridDim.y)
         for (int r = blockIdx.x * 256 + threadIdx.x; r < rows; r += gridDim.x * 256) {
-            T acc = T(0);
-            for (int q = 0; q < nsplit; ++q) acc = acc + P[(size_t)q * pstride + r + (size_t)c * ldp];
-            out[r + (size_t)c * ldo] = acc;
+            T a[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) a[u] = T(0);
+            int q = 0;
+            for (; q + 8 <= nsplit; q += 8) {
+#pragma unroll
+                for (int u = 0; u < 8; ++u) a[u] = a[u] + P[(size_t)(q + u) * pstride + r + (size_t)c * ldp];
+            }
+            for (int u = 0; q < nsplit; ++q, ++u) a[u] = a[u] + P[(size_t)q * pstride + r + (size_t)c * ldp];
+            out[r + (size_t)c * ldo] = ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7]));
         }
 }
 

@@ -8,7 +8,9 @@
 // synchronizing.
 #pragma once
 #include "qr_kernels.cuh"
+#include "tc_gemm.cuh"
 #include <algorithm>
+#include <type_traits>
 #include <cstring>
 #include <mutex>
 
@@ -93,11 +95,45 @@ template <class T> size_t elems_for(size_t bytes) { return (bytes + 256 + sizeof
 // ---------------------------------------------------------------------------
 // Contraction launcher
 // ---------------------------------------------------------------------------
+// error word of the tensor-core kernels' bounded waits (per translation unit)
+static __device__ int g_tc_status;
+
+template <int BN> int launch_gemm_tc_bn(const GemmArgs<float> &g, int nsplit, cudaStream_t st) {
+    static std::once_flag once;
+    static cudaError_t attr = cudaSuccess;
+    std::call_once(once, []() {
+        attr = cudaFuncSetAttribute((const void *)tc::k_gemm_tc<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SmemLayout<BN>::kBytes);
+    });
+    RNPGPU_CHECK(attr);
+    int *err = nullptr;
+    RNPGPU_CHECK(cudaGetSymbolAddress((void **)&err, g_tc_status));
+    dim3 grid((g.M + tc::kBM - 1) / tc::kBM, (g.N + BN - 1) / BN, nsplit);
+    tc::k_gemm_tc<BN><<<grid, tc::kThreads, tc::SmemLayout<BN>::kBytes, st>>>(g, err);
+    RNPGPU_CHECK_LAUNCH();
+    return kOk;
+}
+
+// FP32 updates with a short contraction (the rank-32 trailing and MultQ
+// updates C -= V W^H, K <= 64) and at least one full 128-row tile run on the
+// tensor cores (three-term BF16 split); long reductions (W = C^H V over all
+// rows) stay on FP32 FMA, whose round-to-nearest accumulation is more
+// accurate over long K than the tensor-core accumulator and, for these
+// skinny shapes, faster.
+inline bool use_tensor_cores(const GemmArgs<float> &g) { return g.M >= 128 && g.K >= 16 && g.K <= 64; }
+template <class T> bool use_tensor_cores(const GemmArgs<T> &) { return false; }
+
+inline int launch_gemm_tc(const GemmArgs<float> &g, int nsplit, cudaStream_t st) {
+    if (g.N <= 32) return launch_gemm_tc_bn<32>(g, nsplit, st);
+    return launch_gemm_tc_bn<64>(g, nsplit, st);
+}
+template <class T> int launch_gemm_tc(const GemmArgs<T> &, int, cudaStream_t) { return kErrDevice; }
+
 template <class T> int launch_gemm(GemmArgs<T> g, int nsplit, cudaStream_t st, const char *tag = "gemm") {
     if (g.M <= 0 || g.N <= 0) return kOk;
     if (g.K <= 0 && g.beta_mode == kBetaOne) return kOk;
     if (g.kchunk <= 0) g.kchunk = g.K > 0 ? g.K : 1;
     KScope ks(tag, st);
+    if (use_tensor_cores(g)) return launch_gemm_tc(g, nsplit, st);
     if (g.N <= 16) {
         dim3 grid((g.M + 127) / 128, (g.N + 15) / 16, nsplit);
         k_gemm<T, 128, 16, 16, 8, 1><<<grid, 256, 0, st>>>(g);
@@ -152,7 +188,13 @@ template <class T> int apply_block(bool left, bool notran, int M, int N, int ib,
         // W = C^H V  (N x ib), reduction over the M rows
         const int tiles = (N + 63) / 64;
         const int S = choose_splits(M, tiles, ws.smax);
-        const int kchunk = ((M + S - 1) / S + 15) / 16 * 16;
+        int kchunk = ((M + S - 1) / S + 15) / 16 * 16;
+        if (std::is_same<T, float>::value) {
+            // tensor-core path: at most ~1024 rows per accumulator, within
+            // the partial buffer's smax slots
+            const int floor_chunk = ((M + ws.smax - 1) / ws.smax + 15) / 16 * 16;
+            kchunk = std::max(floor_chunk, std::min(kchunk, 1024));
+        }
         const int nsplit = (M + kchunk - 1) / kchunk;
         GemmArgs<T> g = gemm_args<T>(C, ldc, kOpC, 0, V, ldv, kOpN, 1, ws.P, (size_t)N, N, ib, M, T(1), kBetaZero);
         g.kchunk = kchunk;
@@ -202,10 +244,8 @@ template <class T> int block_t(int rows, int ib, const T *V, size_t ldv, const T
 // Panel factorization launcher (cooperative grid)
 // ---------------------------------------------------------------------------
 template <class T> struct PanelWs {
-    NormAcc *normp;
-    T *wp;
-    T *alpha_slot;
-    unsigned *sync;  // [0] counter, [1] error word
+    PanelRec<T> *rec;  // [2][gmax]
+    unsigned *sync;    // [0] counter, [1] error word
     int gmax;
 };
 
@@ -215,17 +255,30 @@ inline int panel_grid(int M, int gmax) {
     return std::max(g, 1);
 }
 
+// shared-memory budget for a block's rows of the panel
+constexpr size_t kPanelSmemMax = 180 * 1024;
+
 template <class T> int panel_factor(int M, int N, T *A, size_t lda, T *tau, T *Tm, int ldt, const PanelWs<T> &ws, cudaStream_t st) {
     const int G = panel_grid(M, ws.gmax);
+    static std::once_flag attr_once;
+    static cudaError_t attr_err = cudaSuccess;
+    std::call_once(attr_once, []() {
+        attr_err = cudaFuncSetAttribute((const void *)k_panel<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPanelSmemMax);
+    });
+    RNPGPU_CHECK(attr_err);
     PanelArgs<T> p;
     p.A = A; p.lda = lda; p.M = M; p.N = N; p.tau = tau; p.Tm = Tm; p.ldt = ldt;
-    p.normp = ws.normp; p.wp = ws.wp; p.alpha_slot = ws.alpha_slot;
+    p.rec = ws.rec;
     p.counter = ws.sync; p.err = (int *)(ws.sync + 1);
     p.rows_per_cta = (M + G - 1) / G;
     RNPGPU_CHECK(cudaMemsetAsync(ws.sync, 0, 2 * sizeof(unsigned), st));
     void *args[] = {&p};
     KScope ks("panel", st);
-    RNPGPU_CHECK(cudaLaunchCooperativeKernel((const void *)k_panel<T>, dim3(G), dim3(kPanelThreads), args, 0, st));
+    const size_t smem = (size_t)p.rows_per_cta * N * sizeof(T);
+    if (smem <= kPanelSmemMax && G <= device_facts().sm_count)
+        RNPGPU_CHECK(cudaLaunchCooperativeKernel((const void *)k_panel<T, true>, dim3(G), dim3(kPanelThreads), args, smem, st));
+    else
+        RNPGPU_CHECK(cudaLaunchCooperativeKernel((const void *)k_panel<T, false>, dim3(G), dim3(kPanelThreads), args, 0, st));
     note_launch();
     return kOk;
 }
@@ -240,13 +293,11 @@ template <class T> int panel_gmax() {
 // Workspace plans (bytes), shared by the query and the run
 // ---------------------------------------------------------------------------
 template <class T> size_t panel_ws_bytes(int gmax) {
-    return ((size_t)gmax * sizeof(NormAcc) + 255) / 256 * 256 + ((size_t)gmax * kPanelMaxCols * sizeof(T) + 255) / 256 * 256 + 256 + 256;
+    return ((size_t)2 * gmax * sizeof(PanelRec<T>) + 255) / 256 * 256 + 256;
 }
 template <class T> PanelWs<T> carve_panel(Carver &cv, int gmax) {
     PanelWs<T> w;
-    w.normp = cv.take<NormAcc>(gmax);
-    w.wp = cv.take<T>((size_t)gmax * kPanelMaxCols);
-    w.alpha_slot = cv.take<T>(1);
+    w.rec = cv.take<PanelRec<T> >((size_t)2 * gmax);
     w.sync = cv.take<unsigned>(2);
     w.gmax = gmax;
     return w;
@@ -273,7 +324,9 @@ template <class T> size_t geqrf_bytes(size_t m, size_t n, int smax) {
     return panel_ws_bytes<T>(panel_gmax<T>()) + t_bytes<T>() + block_ws_bytes<T>((int)n, smax);
 }
 
-template <class T> int geqrf(size_t m, size_t n, T *a, size_t lda, T *tau, size_t *lwork, T *work) {
+// Tstore (optional): receives the 32 x 32 T factor of every column block
+// (block b at Tstore + b*32*32, leading dimension 32) for later MultQ calls.
+template <class T> int geqrf(size_t m, size_t n, T *a, size_t lda, T *tau, size_t *lwork, T *work, T *Tstore = nullptr) {
     if (lwork == nullptr) return -6;
     const size_t k = std::min(m, n);
     if (k == 0) return kOk;
@@ -302,10 +355,11 @@ template <class T> int geqrf(size_t m, size_t n, T *a, size_t lda, T *tau, size_
     for (size_t i = 0; i < k; i += nb) {
         const int ib = (int)std::min(nb, k - i);
         T *Ai = a + i + i * lda;
-        int rc = panel_factor<T>((int)(m - i), ib, Ai, lda, tau + i, Tm, kPanelMaxCols, pw, st);
+        T *Tb = Tstore ? Tstore + (i / nb) * kPanelMaxCols * kPanelMaxCols : Tm;
+        int rc = panel_factor<T>((int)(m - i), ib, Ai, lda, tau + i, Tb, kPanelMaxCols, pw, st);
         if (rc) return rc;
         if (i + ib < n) {
-            rc = apply_block<T>(true, false, (int)(m - i), (int)(n - i - ib), ib, Ai, lda, Tm, kPanelMaxCols, a + i + (i + ib) * lda, lda, bw, st);
+            rc = apply_block<T>(true, false, (int)(m - i), (int)(n - i - ib), ib, Ai, lda, Tb, kPanelMaxCols, a + i + (i + ib) * lda, lda, bw, st);
             if (rc) return rc;
         }
     }
@@ -359,7 +413,9 @@ template <class T> size_t unmqr_bytes(size_t nq, size_t nw, size_t k, int smax, 
     return nblk * t_bytes<T>() + ((size_t)sgram * kPanelMaxCols * kPanelMaxCols * sizeof(T) + 255) / 256 * 256 + block_ws_bytes<T>((int)nw, smax);
 }
 
-template <class T> int unmqr(const char *side, const char *trans, size_t m, size_t n, size_t k, const T *a, size_t lda, const T *tau, T *c, size_t ldc, size_t *lwork, T *work) {
+// Tcache (optional): the T factors of the reflector blocks as stored by
+// geqrf(..., Tstore); when given they are not rebuilt.
+template <class T> int unmqr(const char *side, const char *trans, size_t m, size_t n, size_t k, const T *a, size_t lda, const T *tau, T *c, size_t ldc, size_t *lwork, T *work, const T *Tcache = nullptr) {
     if (side == nullptr) return -1;
     if (trans == nullptr) return -2;
     if (lwork == nullptr) return -11;
@@ -394,19 +450,22 @@ template <class T> int unmqr(const char *side, const char *trans, size_t m, size
     T *Tc = cv.take<T>(nblk * kPanelMaxCols * kPanelMaxCols);
     T *Pg = cv.take<T>((size_t)sgram * kPanelMaxCols * kPanelMaxCols);
     BlockWs<T> bw = carve_block<T>(cv, (int)nw, smax);
-    for (size_t b = 0; b < nblk; ++b) {
-        const size_t i = b * nb;
-        const int ib = (int)std::min(nb, k - i);
-        int rc = block_t<T>((int)(nq - i), ib, a + i + i * lda, lda, tau + i, Tc + b * kPanelMaxCols * kPanelMaxCols, kPanelMaxCols, Pg, sgram, st);
-        if (rc) return rc;
+    if (Tcache == nullptr) {
+        for (size_t b = 0; b < nblk; ++b) {
+            const size_t i = b * nb;
+            const int ib = (int)std::min(nb, k - i);
+            int rc = block_t<T>((int)(nq - i), ib, a + i + i * lda, lda, tau + i, Tc + b * kPanelMaxCols * kPanelMaxCols, kPanelMaxCols, Pg, sgram, st);
+            if (rc) return rc;
+        }
     }
+    const T *Tuse = Tcache ? Tcache : Tc;
     const bool forward = (left && !notran) || (!left && notran);
     for (size_t s = 0; s < nblk; ++s) {
         const size_t b = forward ? s : nblk - 1 - s;
         const size_t i = b * nb;
         const int ib = (int)std::min(nb, k - i);
         const T *V = a + i + i * lda;
-        const T *Tb = Tc + b * kPanelMaxCols * kPanelMaxCols;
+        const T *Tb = Tuse + b * kPanelMaxCols * kPanelMaxCols;
         int rc;
         if (left) rc = apply_block<T>(true, notran, (int)(m - i), (int)n, ib, V, lda, Tb, kPanelMaxCols, c + i, ldc, bw, st);
         else rc = apply_block<T>(false, notran, (int)m, (int)(n - i), ib, V, lda, Tb, kPanelMaxCols, c + i * ldc, ldc, bw, st);

@@ -121,17 +121,32 @@ __device__ __forceinline__ cf32 scale_x(cf32 x, const ReflScalars<cf32> &s) {
 
 // ---------------------------------------------------------------------------
 // Panel factorization across a cooperative grid.
-// Rows [b*R, min(M,(b+1)*R)) of the panel belong to block b.  Per column j:
-//   barrier 1: every block combines the norm partials of x = A[j+1:M, j]
-//              and forms beta/tau/scal identically; scales its rows of x;
-//              accumulates, over its rows, w_c = v^H A[:,c] (c > j) and the
-//              Gram column g_c = V[:,c]^H v (c < j)
-//   barrier 2: every block combines w and applies H^H to its rows of the
-//              trailing panel columns, then accumulates the norm partials of
-//              the next column; block 0 extends T by one column.
-// Two grid barriers per column; no atomics on data, so the result is
-// deterministic for a given grid size.
+// Rows [b*R, min(M,(b+1)*R)) of the panel belong to block b.  One grid
+// barrier per column j: after it every block holds the combined partial sums
+// of the previous phase and
+//   1. applies H[j-1]^H (tau[j-1], v[j-1], w[j-1] = v^H A) to its rows of the
+//      panel columns right of j-1; block 0 extends T by column j-1;
+//   2. forms ||x|| of column j below the diagonal by downdating
+//      ||a - c v||^2 = s1 - 2 Re(c conj(s2)) + |c|^2 s3  (c = conj(tau) w_j)
+//      from sums gathered in the previous phase; when that would cancel
+//      (result < delta * s1) or the column holds magnitudes outside the safe
+//      squaring range, an extra barrier recomputes the norm exactly with the
+//      three-accumulator scheme;
+//   3. forms beta/tau/1/(alpha-beta) identically in every block (FP64) and
+//      scales its rows of x into v;
+//   4. accumulates over its rows w_c = v^H A[:,c] (c > j), the Gram column
+//      g_c = V[:,c]^H v (c < j) and the downdating sums of column j+1, and
+//      writes them into the partial record of the next phase.
+// Records are double-buffered by phase parity and combined by all threads in
+// a fixed order: the result is deterministic for a given grid size.
 // ---------------------------------------------------------------------------
+constexpr int kRecT = kPanelMaxCols + 2;  // w/g[32], alpha of the next column, v at its row
+constexpr int kRecD = 6;                  // s1, s3, unsafe, Re s2, Im s2 | exact: sml, med, big
+template <class T> struct PanelRec {
+    T v[kRecT];
+    double d[kRecD];
+};
+
 template <class T> struct PanelArgs {
     T *A;
     size_t lda;
@@ -139,15 +154,27 @@ template <class T> struct PanelArgs {
     T *tau;              // N
     T *Tm;               // N x N upper triangular T factor (ldt); may be null
     int ldt;
-    NormAcc *normp;      // [gridDim.x]
-    T *wp;               // [gridDim.x][kPanelMaxCols]
-    T *alpha_slot;       // [1]
+    PanelRec<T> *rec;    // [2][gridDim.x]
     unsigned *counter;   // zeroed before launch
     int *err;            // zeroed before launch
     int rows_per_cta;
 };
 
-template <class T> __global__ void __launch_bounds__(kPanelThreads) k_panel(PanelArgs<T> p) {
+__device__ __forceinline__ double re_of(double v) { return v; }
+__device__ __forceinline__ double re_of(float v) { return v; }
+template <class R> __device__ __forceinline__ double re_of(cplx<R> v) { return v.x; }
+__device__ __forceinline__ double im_of(double) { return 0.0; }
+__device__ __forceinline__ double im_of(float) { return 0.0; }
+template <class R> __device__ __forceinline__ double im_of(cplx<R> v) { return v.y; }
+
+// SMEM = true: the block's rows of the panel live in dynamic shared memory
+// for the whole launch (loaded once, written back at the end); SMEM = false:
+// they are read and written in place in global memory (panels too tall for
+// shared memory).
+template <class T, bool SMEM> __global__ void __launch_bounds__(kPanelThreads) k_panel(PanelArgs<T> p) {
+    typedef typename Tr<T>::R R;
+    const bool is64 = sizeof(R) == 8;
+    const double delta = is64 ? 0.5 : 1e-4;
     const int G = gridDim.x, b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nwarps = kPanelThreads / 32;
     const int r0 = b * p.rows_per_cta;
@@ -157,106 +184,239 @@ template <class T> __global__ void __launch_bounds__(kPanelThreads) k_panel(Pane
     GridBarrier bar{p.counter, p.err, (unsigned)G, 0u};
 
     __shared__ T s_T[kPanelMaxCols][kPanelMaxCols + 1];
-    __shared__ T s_w[kPanelMaxCols];
-    __shared__ NormAcc s_nacc[kPanelThreads / 32];
+    __shared__ T s_w[kPanelMaxCols];   // w of the reflector to apply next
+    __shared__ T s_cv[kRecT];          // combined record
+    __shared__ double s_cd[kRecD];
+    __shared__ T s_pv[6][kRecT];
+    __shared__ double s_pd[6][kRecD];
+    __shared__ double s_red[kPanelThreads / 32][6];
     __shared__ ReflScalars<T> s_refl;
+    extern __shared__ __align__(16) unsigned char s_dyn[];
+    T *sP = reinterpret_cast<T *>(s_dyn);
+    const int ldp = p.rows_per_cta;
+    auto at = [&](int r, int c) -> T & {
+        if (SMEM) return sP[(size_t)c * ldp + (r - r0)];
+        return A[r + (size_t)c * lda];
+    };
+    if (SMEM) {
+        for (int c = 0; c < p.N; ++c)
+            for (int r = r0 + tid; r < r1; r += kPanelThreads) sP[(size_t)c * ldp + (r - r0)] = A[r + (size_t)c * lda];
+    }
+    __syncthreads();
 
-    auto norm_partial = [&](int col) {
+    int phase = 0;  // records of phase k live in buffer k & 1
+    auto my_rec = [&]() -> PanelRec<T> & { return p.rec[(size_t)(phase & 1) * G + b]; };
+    // combine the records of the current phase into s_cv / s_cd (all threads)
+    auto combine = [&]() {
+        const int nslot = kRecT + kRecD;
+        const int slot = tid % nslot, grp = tid / nslot;
+        const PanelRec<T> *rb = p.rec + (size_t)(phase & 1) * G;
+        // eight independent loads in flight per thread (fixed summation order)
+        if (grp < 6) {
+            if (slot < kRecT) {
+                T a[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) a[u] = T(0);
+                int q = grp;
+                for (; q + 42 < G; q += 48) {
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) a[u] = a[u] + ldcg(&rb[q + 6 * u].v[slot]);
+                }
+                for (int u = 0; q < G; q += 6, ++u) a[u & 7] = a[u & 7] + ldcg(&rb[q].v[slot]);
+                s_pv[grp][slot] = ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7]));
+            } else {
+                double a[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) a[u] = 0.0;
+                int q = grp;
+                for (; q + 42 < G; q += 48) {
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) a[u] += __ldcg(&rb[q + 6 * u].d[slot - kRecT]);
+                }
+                for (int u = 0; q < G; q += 6, ++u) a[u & 7] += __ldcg(&rb[q].d[slot - kRecT]);
+                s_pd[grp][slot - kRecT] = ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7]));
+            }
+        }
+        __syncthreads();
+        if (tid < kRecT) {
+            T a = s_pv[0][tid];
+            for (int g = 1; g < 6; ++g) a = a + s_pv[g][tid];
+            s_cv[tid] = a;
+        } else if (tid < kRecT + kRecD) {
+            double a = s_pd[0][tid - kRecT];
+            for (int g = 1; g < 6; ++g) a += s_pd[g][tid - kRecT];
+            s_cd[tid - kRecT] = a;
+        }
+        __syncthreads();
+    };
+    // exact norm record of column col (rows > col) and its diagonal element
+    auto exact_record = [&](int col) {
         NormAcc acc;
         acc.zero();
-        for (int r = max(r0, col + 1) + tid; r < r1; r += kPanelThreads) acc.add(A[r + (size_t)col * lda]);
+        for (int r = max(r0, col + 1) + tid; r < r1; r += kPanelThreads) acc.add(at(r, col));
         acc.warp_reduce();
-        if (lane == 0) s_nacc[warp] = acc;
+        if (lane == 0) {
+            s_red[warp][0] = acc.sml;
+            s_red[warp][1] = acc.med;
+            s_red[warp][2] = acc.big;
+        }
         __syncthreads();
-        if (tid == 0) {
-            NormAcc t = s_nacc[0];
-            for (int w = 1; w < nwarps; ++w) t.merge(s_nacc[w]);
-            p.normp[b] = t;
-            if (col >= r0 && col < r1) *p.alpha_slot = A[col + (size_t)col * lda];
+        ++phase;
+        PanelRec<T> &rc = my_rec();
+        if (tid < kRecT) rc.v[tid] = (tid == kPanelMaxCols && col >= r0 && col < r1) ? at(col, col) : T(0);
+        if (tid < kRecD) {
+            double t = 0.0;
+            if (tid < 3)
+                for (int w = 0; w < nwarps; ++w) t += s_red[w][tid];
+            rc.d[tid] = t;
         }
     };
+    auto exact_norm = [&](NormAcc &nacc, T &alpha) {
+        nacc.sml = s_cd[0];
+        nacc.med = s_cd[1];
+        nacc.big = s_cd[2];
+        alpha = s_cv[kPanelMaxCols];
+    };
 
-    norm_partial(0);
+    // prologue: exact norm of column 0
+    exact_record(0);
     if (!bar.sync()) return;
+    combine();
+    NormAcc nacc;
+    T alpha;
+    exact_norm(nacc, alpha);
+    ReflScalars<T> prev;
+    prev.identity = true;
+    prev.tau = T(0);
 
     for (int j = 0; j < p.N; ++j) {
-        // (1) combine norm partials; reflector scalars (identical in every block)
-        if (warp == 0) {
-            NormAcc acc;
-            acc.zero();
-            for (int q = lane; q < G; q += 32) {
-                NormAcc t;
-                t.sml = __ldcg(&p.normp[q].sml);
-                t.med = __ldcg(&p.normp[q].med);
-                t.big = __ldcg(&p.normp[q].big);
-                acc.merge(t);
+        if (j > 0) {
+            // 1. apply H[j-1]^H to own rows r >= j-1 of columns j..N-1
+            if (!prev.identity) {
+                const T ctau = Tr<T>::conj(prev.tau);
+                for (int r = max(r0, j - 1) + tid; r < r1; r += kPanelThreads) {
+                    const T v = (r == j - 1) ? T(1) : at(r, j - 1);
+                    const T cv = ctau * v;
+                    for (int c = j; c < p.N; ++c) at(r, c) = fmac(-cv, s_w[c], at(r, c));
+                }
             }
-            acc.warp_reduce();
-            if (lane == 0) s_refl = reflector_scalars<T>(ldcg(p.alpha_slot), acc);
+            // 2. norm of column j by downdating, exact when that is unsafe
+            const double s1 = s_cd[0], s3 = s_cd[1], unsafe = s_cd[2];
+            const T a_pre = s_cv[kPanelMaxCols], vn = s_cv[kPanelMaxCols + 1];
+            double n2 = s1;
+            alpha = a_pre;
+            if (!prev.identity) {
+                const T ctau = Tr<T>::conj(prev.tau);
+                const T wj = s_w[j];
+                alpha = fmac(-(ctau * vn), wj, a_pre);
+                const T c = ctau * wj;
+                const double cr = re_of(c), ci = im_of(c);
+                // Re(c * conj(s2)) = cr*s2r + ci*s2i
+                n2 = s1 - 2.0 * (cr * s_cd[3] + ci * s_cd[4]) + (cr * cr + ci * ci) * s3;
+            }
+            __syncthreads();
+            if (unsafe != 0.0 || !(n2 >= delta * s1) || !(n2 < 1e300)) {
+                exact_record(j);
+                if (!bar.sync()) return;
+                combine();
+                exact_norm(nacc, alpha);
+            } else {
+                nacc.zero();
+                nacc.med = n2;
+            }
         }
+        // 3. reflector scalars, identical in every block
+        if (tid == 0) s_refl = reflector_scalars<T>(alpha, nacc);
         __syncthreads();
         const ReflScalars<T> rs = s_refl;
-        // (2) scale x into v on own rows; beta into the diagonal; tau
         if (!rs.identity) {
-            for (int r = max(r0, j + 1) + tid; r < r1; r += kPanelThreads) {
-                T x = A[r + (size_t)j * lda];
-                A[r + (size_t)j * lda] = scale_x(x, rs);
-            }
-            if (tid == 0 && j >= r0 && j < r1) A[j + (size_t)j * lda] = Tr<T>::make((typename Tr<T>::R)rs.beta, 0);
+            for (int r = max(r0, j + 1) + tid; r < r1; r += kPanelThreads) at(r, j) = scale_x(at(r, j), rs);
+            if (tid == 0 && j >= r0 && j < r1) at(j, j) = Tr<T>::make((R)rs.beta, 0);
         }
         if (b == 0 && tid == 0) p.tau[j] = rs.tau;
         __syncthreads();
-        // (3) partial sums over own rows r >= j (v_j = 1):
-        //     c > j: w_c = sum conj(v_r) A[r,c];  c < j: g_c = sum conj(V[r,c]) v_r
+        // 4. partial record of this phase
+        ++phase;
+        PanelRec<T> &rc = my_rec();
         for (int c = warp; c < p.N; c += nwarps) {
-            if (c == j) continue;
             T acc = T(0);
-            for (int r = max(r0, j) + lane; r < r1; r += 32) {
-                T v = (r == j) ? T(1) : A[r + (size_t)j * lda];
-                T a = A[r + (size_t)c * lda];
-                acc = (c > j) ? fmac(Tr<T>::conj(v), a, acc) : fmac(Tr<T>::conj(a), v, acc);
+            if (c != j) {
+                for (int r = max(r0, j) + lane; r < r1; r += 32) {
+                    const T v = (r == j) ? T(1) : at(r, j);
+                    const T a = at(r, c);
+                    acc = (c > j) ? fmac(Tr<T>::conj(v), a, acc) : fmac(Tr<T>::conj(a), v, acc);
+                }
+                acc = warp_sum(acc);
             }
-            acc = warp_sum(acc);
-            if (lane == 0) p.wp[(size_t)b * kPanelMaxCols + c] = acc;
+            if (lane == 0) rc.v[c] = acc;
         }
-        if (!bar.sync()) return;
-        // (4) combine w/g
-        for (int c = warp; c < p.N; c += nwarps) {
-            if (c == j) continue;
-            T acc = T(0);
-            for (int q = lane; q < G; q += 32) acc = acc + ldcg(&p.wp[(size_t)q * kPanelMaxCols + c]);
-            acc = warp_sum(acc);
-            if (lane == 0) s_w[c] = acc;
-        }
-        __syncthreads();
-        if (!rs.identity && j + 1 < p.N) {
-            const T ctau = Tr<T>::conj(rs.tau);
-            for (int r = max(r0, j) + tid; r < r1; r += kPanelThreads) {
-                T v = (r == j) ? T(1) : A[r + (size_t)j * lda];
-                T cv = ctau * v;
-                for (int c = j + 1; c < p.N; ++c) {
-                    T a = A[r + (size_t)c * lda];
-                    A[r + (size_t)c * lda] = fmac(-cv, s_w[c], a);
+        for (int c = p.N + tid; c < kPanelMaxCols; c += kPanelThreads) rc.v[c] = T(0);
+        double e1 = 0.0, e3 = 0.0, eu = 0.0, e2r = 0.0, e2i = 0.0;
+        T anext = T(0), vnext = T(0);
+        if (j + 1 < p.N) {
+            const double tsml = 0x1p-511, tbig = 0x1p486;
+            for (int r = max(r0, j + 2) + tid; r < r1; r += kPanelThreads) {
+                const T a = at(r, j + 1), v = at(r, j);
+                const double ar = re_of(a), ai = im_of(a), vr = re_of(v), vi = im_of(v);
+                e1 = fma(ar, ar, fma(ai, ai, e1));
+                e3 = fma(vr, vr, fma(vi, vi, e3));
+                // conj(v) a
+                e2r = fma(vr, ar, fma(vi, ai, e2r));
+                e2i = fma(vr, ai, fma(-vi, ar, e2i));
+                if (is64) {
+                    const double m = fmax(fabs(ar), fabs(ai));
+                    if (m > tbig || (m < tsml && m != 0.0)) eu = 1.0;
                 }
             }
+            if (j + 1 >= r0 && j + 1 < r1 && tid == 0) {
+                anext = at(j + 1, j + 1);
+                vnext = at(j + 1, j);
+            }
         }
+        e1 = warp_sum(e1);
+        e3 = warp_sum(e3);
+        eu = warp_sum(eu);
+        e2r = warp_sum(e2r);
+        e2i = warp_sum(e2i);
+        if (lane == 0) {
+            s_red[warp][0] = e1;
+            s_red[warp][1] = e3;
+            s_red[warp][2] = eu;
+            s_red[warp][3] = e2r;
+            s_red[warp][4] = e2i;
+        }
+        __syncthreads();
+        if (tid < 5) {
+            double t = 0.0;
+            for (int w = 0; w < nwarps; ++w) t += s_red[w][tid];
+            rc.d[tid] = t;
+        }
+        if (tid == 5) rc.d[5] = 0.0;
+        if (tid == 0) {
+            rc.v[kPanelMaxCols] = anext;
+            rc.v[kPanelMaxCols + 1] = vnext;
+        }
+        if (!bar.sync()) return;
+        combine();
+        // w of H[j] for the next step; T column j from the Gram column (block 0)
+        if (tid < kPanelMaxCols) s_w[tid] = s_cv[tid];
         if (b == 0) {
             // T(0:j, j) = -tau_j * T(0:j, 0:j) * g(0:j);  T(j, j) = tau_j
             if (tid < j) {
                 T acc = T(0);
-                for (int l = tid; l < j; ++l) acc = fmac(s_T[tid][l], s_w[l], acc);
+                for (int l = tid; l < j; ++l) acc = fmac(s_T[tid][l], s_cv[l], acc);
                 s_T[tid][j] = rs.identity ? T(0) : (-rs.tau) * acc;
             }
             if (tid == 0) s_T[j][j] = rs.tau;
         }
-        if (j + 1 < p.N) {
-            __syncthreads();
-            norm_partial(j + 1);
-            if (!bar.sync()) return;
-        }
+        prev = rs;
+        __syncthreads();
+    }
+    if (SMEM) {
+        for (int c = 0; c < p.N; ++c)
+            for (int r = r0 + tid; r < r1; r += kPanelThreads) A[r + (size_t)c * lda] = sP[(size_t)c * ldp + (r - r0)];
     }
     if (b == 0 && p.Tm != nullptr) {
-        __syncthreads();
         for (int idx = tid; idx < p.N * p.N; idx += kPanelThreads) {
             int r = idx % p.N, c = idx / p.N;
             if (r <= c) p.Tm[r + (size_t)c * p.ldt] = s_T[r][c];
@@ -304,6 +464,7 @@ template <class T, int BM, int BN, int BK, int TM, int TN>
 __global__ void __launch_bounds__((BM / TM) * (BN / TN)) k_gemm(GemmArgs<T> g) {
     constexpr int NT = (BM / TM) * (BN / TN);
     constexpr int TX = BN / TN;  // threads along n
+    constexpr int LA = (BM * BK + NT - 1) / NT, LB = (BN * BK + NT - 1) / NT;
     __shared__ T sA[BK][BM + 1];
     __shared__ T sB[BK][BN + 1];
     const int tid = threadIdx.x;
@@ -317,23 +478,55 @@ __global__ void __launch_bounds__((BM / TM) * (BN / TN)) k_gemm(GemmArgs<T> g) {
 #pragma unroll
         for (int j = 0; j < TN; ++j) acc[i][j] = T(0);
 
-    for (int k0 = kbeg; k0 < kend; k0 += BK) {
-        // A tile: BM x BK of op(A); coalesce along the stored leading dimension
-        for (int idx = tid; idx < BM * BK; idx += NT) {
+    // the next tile is fetched into registers while the current one is used
+    T ra[LA], rb[LB];
+    auto fetch = [&](int k0) {
+#pragma unroll
+        for (int u = 0; u < LA; ++u) {
+            const int idx = tid + u * NT;
             int mi, ki;
             if (g.opA == kOpN) { mi = idx % BM; ki = idx / BM; }
             else { ki = idx % BK; mi = idx / BK; }
-            int gm = m0 + mi, gk = k0 + ki;
-            sA[ki][mi] = (gm < g.M && gk < kend) ? load_op(g.A, g.lda, g.opA, g.vunitA, gm, gk) : T(0);
+            const int gm = m0 + mi, gk = k0 + ki;
+            ra[u] = (idx < BM * BK && gm < g.M && gk < kend) ? load_op(g.A, g.lda, g.opA, g.vunitA, gm, gk) : T(0);
         }
-        for (int idx = tid; idx < BN * BK; idx += NT) {
+#pragma unroll
+        for (int u = 0; u < LB; ++u) {
+            const int idx = tid + u * NT;
             int ni, ki;
             if (g.opB == kOpN) { ki = idx % BK; ni = idx / BK; }
             else { ni = idx % BN; ki = idx / BN; }
-            int gn = n0 + ni, gk = k0 + ki;
-            sB[ki][ni] = (gn < g.N && gk < kend) ? load_op(g.B, g.ldb, g.opB, g.vunitB, gk, gn) : T(0);
+            const int gn = n0 + ni, gk = k0 + ki;
+            rb[u] = (idx < BN * BK && gn < g.N && gk < kend) ? load_op(g.B, g.ldb, g.opB, g.vunitB, gk, gn) : T(0);
         }
+    };
+    auto stash = [&]() {
+#pragma unroll
+        for (int u = 0; u < LA; ++u) {
+            const int idx = tid + u * NT;
+            if (idx < BM * BK) {
+                int mi, ki;
+                if (g.opA == kOpN) { mi = idx % BM; ki = idx / BM; }
+                else { ki = idx % BK; mi = idx / BK; }
+                sA[ki][mi] = ra[u];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < LB; ++u) {
+            const int idx = tid + u * NT;
+            if (idx < BN * BK) {
+                int ni, ki;
+                if (g.opB == kOpN) { ki = idx % BK; ni = idx / BK; }
+                else { ni = idx % BN; ki = idx / BN; }
+                sB[ki][ni] = rb[u];
+            }
+        }
+    };
+    if (kbeg < kend) fetch(kbeg);
+    for (int k0 = kbeg; k0 < kend; k0 += BK) {
+        stash();
         __syncthreads();
+        if (k0 + BK < kend) fetch(k0 + BK);
 #pragma unroll 4
         for (int kk = 0; kk < BK; ++kk) {
             T a[TM], bb[TN];
@@ -382,8 +575,18 @@ __global__ void __launch_bounds__(256) k_sum_times_t(const T *P, size_t ldp, siz
     const int rl = tid / kPanelMaxCols, j = tid % kPanelMaxCols;
     const int row = blockIdx.x * 8 + rl;
     T s = T(0);
-    if (row < rows && j < k)
-        for (int q = 0; q < nsplit; ++q) s = s + P[(size_t)q * pstride + row + (size_t)j * ldp];
+    if (row < rows && j < k) {
+        T a[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) a[u] = T(0);
+        int q = 0;
+        for (; q + 8 <= nsplit; q += 8) {
+#pragma unroll
+            for (int u = 0; u < 8; ++u) a[u] = a[u] + P[(size_t)(q + u) * pstride + row + (size_t)j * ldp];
+        }
+        for (int u = 0; q < nsplit; ++q, ++u) a[u] = a[u] + P[(size_t)q * pstride + row + (size_t)j * ldp];
+        s = ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7]));
+    }
     sW[rl][j] = s;
     __syncthreads();
     if (row < rows && j < k) {

@@ -53,10 +53,11 @@ def refine_workspace(A, nrhs):
     return lw.value
 
 
-def gels_refine(A, B, X=None, max_iter=10, work=None, forward=False):
+def gels_refine(A, B, X=None, max_iter=0, work=None, forward=False):
     """Mixed-precision least squares (FP32 factor, FP64 refinement) of an FP64
     (or complex128) problem; A and B are not modified.  forward=True adds the
     corrected seminormal-equation steps for FP64 forward accuracy.
+    max_iter <= 0 selects the default (10 steps, 30 in forward mode).
     Returns (X, info)."""
     p = {torch.float64: "ds", torch.complex128: "zc"}[A.dtype]
     m, n = A.shape
