@@ -37,7 +37,8 @@ template <class T> __device__ __forceinline__ T tone() { return T(1); }
 // ---------------------------------------------------------------------------
 template <class T> struct ReflScalars {
     T tau, scal;      // scal multiplies x after 'knt' multiplications by rsafmn
-    double sr, si;    // scal in FP64 (the FP32 forms scale x in FP64)
+    double sr, si;    // scal in FP64
+    float sr_hi, sr_lo, si_hi, si_lo;  // FP32 hi/lo parts of scal (FP32 forms)
     double beta;      // final beta (already scaled back)
     int knt;
     bool identity;    // tau == 0: H = I, x and alpha untouched
@@ -55,6 +56,7 @@ template <class T> __device__ ReflScalars<T> reflector_scalars(T alpha, const No
         s.scal = T(1);
         s.sr = 1.0;
         s.si = 0.0;
+        s.sr_hi = 1.0f; s.sr_lo = 0.0f; s.si_hi = 0.0f; s.si_lo = 0.0f;
         s.beta = ar;
         return s;
     }
@@ -84,11 +86,14 @@ template <class T> __device__ ReflScalars<T> reflector_scalars(T alpha, const No
             if (ar > 0.0) beta = -beta;
         }
     }
-    double tr = (beta - ar) / beta, ti = -ai / beta;
-    double sr, si;
+    double tr, ti = 0.0, sr, si;
     if (Tr<T>::is_complex) {
+        const double rb = 1.0 / beta;
+        tr = (beta - ar) * rb;
+        ti = -ai * rb;
         crecip(ar - beta, ai, sr, si);
     } else {
+        tr = (beta - ar) / beta;
         sr = 1.0 / (ar - beta);
         si = 0.0;
     }
@@ -96,6 +101,10 @@ template <class T> __device__ ReflScalars<T> reflector_scalars(T alpha, const No
     s.scal = Tr<T>::make((R)sr, (R)si);
     s.sr = sr;
     s.si = si;
+    s.sr_hi = (float)sr;
+    s.sr_lo = (float)(sr - (double)s.sr_hi);
+    s.si_hi = (float)si;
+    s.si_lo = (float)(si - (double)s.si_hi);
     if (s.knt) {
         const double safmin = 0x1p-1022 / (2.0 * 0x1p-52);
         for (int q = 0; q < s.knt; ++q) beta *= safmin;
@@ -112,11 +121,13 @@ template <class T> __device__ __forceinline__ T scale_x(T x, const ReflScalars<T
     }
     return x * s.scal;
 }
-// FP32 types: v = x/(alpha-beta) evaluated in FP64 and rounded once
-__device__ __forceinline__ float scale_x(float x, const ReflScalars<float> &s) { return (float)((double)x * s.sr); }
+// FP32 types: v = x/(alpha-beta) with the FP64 scale factor applied as an
+// FP32 hi + lo pair (FP32 pipe; within an ulp of the FP64 product rounded)
+__device__ __forceinline__ float scale_x(float x, const ReflScalars<float> &s) { return fmaf(x, s.sr_lo, x * s.sr_hi); }
 __device__ __forceinline__ cf32 scale_x(cf32 x, const ReflScalars<cf32> &s) {
-    double xr = x.x, xi = x.y;
-    return cf32((float)(xr * s.sr - xi * s.si), (float)(xr * s.si + xi * s.sr));
+    const float re = fmaf(x.x, s.sr_lo, x.x * s.sr_hi) - fmaf(x.y, s.si_lo, x.y * s.si_hi);
+    const float im = fmaf(x.x, s.si_lo, x.x * s.si_hi) + fmaf(x.y, s.sr_lo, x.y * s.sr_hi);
+    return cf32(re, im);
 }
 
 // ---------------------------------------------------------------------------
@@ -353,31 +364,62 @@ template <class T, bool SMEM> __global__ void __launch_bounds__(kPanelThreads) k
         for (int c = p.N + tid; c < kPanelMaxCols; c += kPanelThreads) rc.v[c] = T(0);
         double e1 = 0.0, e3 = 0.0, eu = 0.0, e2r = 0.0, e2i = 0.0;
         T anext = T(0), vnext = T(0);
-        if (j + 1 < p.N) {
-            const double tsml = 0x1p-511, tbig = 0x1p486;
-            for (int r = max(r0, j + 2) + tid; r < r1; r += kPanelThreads) {
-                const T a = at(r, j + 1), v = at(r, j);
-                const double ar = re_of(a), ai = im_of(a), vr = re_of(v), vi = im_of(v);
-                e1 = fma(ar, ar, fma(ai, ai, e1));
-                e3 = fma(vr, vr, fma(vi, vi, e3));
-                // conj(v) a
-                e2r = fma(vr, ar, fma(vi, ai, e2r));
-                e2i = fma(vr, ai, fma(-vi, ar, e2i));
-                if (is64) {
+        if (is64) {
+            if (j + 1 < p.N) {
+                const double tsml = 0x1p-511, tbig = 0x1p486;
+                for (int r = max(r0, j + 2) + tid; r < r1; r += kPanelThreads) {
+                    const T a = at(r, j + 1), v = at(r, j);
+                    const double ar = re_of(a), ai = im_of(a), vr = re_of(v), vi = im_of(v);
+                    e1 = fma(ar, ar, fma(ai, ai, e1));
+                    e3 = fma(vr, vr, fma(vi, vi, e3));
+                    // conj(v) a
+                    e2r = fma(vr, ar, fma(vi, ai, e2r));
+                    e2i = fma(vr, ai, fma(-vi, ar, e2i));
                     const double m = fmax(fabs(ar), fabs(ai));
                     if (m > tbig || (m < tsml && m != 0.0)) eu = 1.0;
                 }
             }
-            if (j + 1 >= r0 && j + 1 < r1 && tid == 0) {
-                anext = at(j + 1, j + 1);
-                vnext = at(j + 1, j);
+            e1 = warp_sum(e1);
+            e3 = warp_sum(e3);
+            eu = warp_sum(eu);
+            e2r = warp_sum(e2r);
+            e2i = warp_sum(e2i);
+        } else {
+            // FP32 data: error-free FP32 accumulation, converted to FP64 once
+            // per warp (FP32 magnitudes never need the range checks)
+            float h1 = 0.f, l1 = 0.f, h3 = 0.f, l3 = 0.f, h2r = 0.f, l2r = 0.f, h2i = 0.f, l2i = 0.f;
+            if (j + 1 < p.N) {
+                for (int r = max(r0, j + 2) + tid; r < r1; r += kPanelThreads) {
+                    const T a = at(r, j + 1), v = at(r, j);
+                    const float ar = (float)re_of(a), vr = (float)re_of(v);
+                    df_add_prod(h1, l1, ar, ar);
+                    df_add_prod(h3, l3, vr, vr);
+                    df_add_prod(h2r, l2r, vr, ar);
+                    if (Tr<T>::is_complex) {
+                        const float ai = (float)im_of(a), vi = (float)im_of(v);
+                        df_add_prod(h1, l1, ai, ai);
+                        df_add_prod(h3, l3, vi, vi);
+                        df_add_prod(h2r, l2r, vi, ai);
+                        df_add_prod(h2i, l2i, vr, ai);
+                        df_add_prod(h2i, l2i, -vi, ar);
+                    }
+                }
+            }
+            df_warp_sum(h1, l1);
+            df_warp_sum(h3, l3);
+            df_warp_sum(h2r, l2r);
+            if (Tr<T>::is_complex) df_warp_sum(h2i, l2i);
+            if (lane == 0) {
+                e1 = (double)h1 + (double)l1;
+                e3 = (double)h3 + (double)l3;
+                e2r = (double)h2r + (double)l2r;
+                e2i = (double)h2i + (double)l2i;
             }
         }
-        e1 = warp_sum(e1);
-        e3 = warp_sum(e3);
-        eu = warp_sum(eu);
-        e2r = warp_sum(e2r);
-        e2i = warp_sum(e2i);
+        if (j + 1 < p.N && j + 1 >= r0 && j + 1 < r1 && tid == 0) {
+            anext = at(j + 1, j + 1);
+            vnext = at(j + 1, j);
+        }
         if (lane == 0) {
             s_red[warp][0] = e1;
             s_red[warp][1] = e3;

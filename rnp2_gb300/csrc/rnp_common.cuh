@@ -163,13 +163,45 @@ struct NormAcc {
 };
 
 // sqrt(x^2+y^2+z^2) without unnecessary overflow (RNP/Types.hpp:73-92)
+// The components are scaled by the power of two nearest below max|.| (exact)
+// instead of divided by the max: the same overflow protection without
+// divisions, which are long instruction sequences on the FP64 pipe.
 __device__ __forceinline__ double hypot3(double x, double y, double z) {
     double xa = fabs(x), ya = fabs(y), za = fabs(z);
     double w = fmax(fmax(xa, ya), za);
     if (xa != xa || ya != ya || za != za) return xa + ya + za;
     if (w == 0.0) return xa + ya + za;
-    xa /= w; ya /= w; za /= w;
-    return w * sqrt(xa * xa + ya * ya + za * za);
+    if (w < 0x1p-1000 || w > 0x1p1000) {
+        // extreme magnitudes (2^-e would leave the double range): divide
+        xa /= w; ya /= w; za /= w;
+        return w * sqrt(xa * xa + ya * ya + za * za);
+    }
+    int e;
+    frexp(w, &e);
+    const double sc = ldexp(1.0, -e);
+    xa *= sc; ya *= sc; za *= sc;
+    return ldexp(sqrt(xa * xa + ya * ya + za * za), e);
+}
+
+// Error-free FP32 accumulation (TwoProduct by FMA, TwoSum): (hi, lo) carries a
+// sum to about 2^-48 relative, on the FP32 pipe.
+__device__ __forceinline__ void df_add(float &hi, float &lo, float x) {
+    const float s = hi + x, bp = s - hi;
+    lo += (hi - (s - bp)) + (x - bp);
+    hi = s;
+}
+__device__ __forceinline__ void df_add_prod(float &hi, float &lo, float a, float b) {
+    const float p = a * b;
+    const float e = fmaf(a, b, -p);
+    df_add(hi, lo, p);
+    lo += e;
+}
+__device__ __forceinline__ void df_warp_sum(float &hi, float &lo) {
+    for (int o = 16; o > 0; o >>= 1) {
+        const float oh = __shfl_xor_sync(0xffffffffu, hi, o), ol = __shfl_xor_sync(0xffffffffu, lo, o);
+        df_add(hi, lo, oh);
+        lo += ol;
+    }
 }
 
 // 1/(a+ib) by Smith's algorithm (Smith, CACM 5(8), 1962)
