@@ -184,6 +184,143 @@ def cpu_arm(args, rank, world):
     return 0
 
 
+def timed(torch, fn, reps):
+    """min over reps of one call's CUDA-event time in ms (fn sets up untimed state)."""
+    best = None
+    for _ in range(reps):
+        pre, call = fn()
+        if pre is not None:
+            pre()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        call()
+        e1.record()
+        torch.cuda.synchronize()
+        t = e0.elapsed_time(e1)
+        best = t if best is None else min(best, t)
+    return best
+
+
+def batched_config(torch, dev, gq, lib, peak64, count=20000, loop_sample=200, check_sample=40):
+    """Batched FP64 QR of `count` matrices, m ~ U[16,256], n ~ U[8,m], N(0,1)
+    entries, packed with lda = m: the tuned plan's run captured in a CUDA
+    graph and replayed, against looping the plain Factor over a sample."""
+    import numpy as np
+
+    import oracle as orc
+    from rnp2_gb300.batched import BatchedQR
+
+    rng = np.random.default_rng(0)
+    ms = rng.integers(16, 257, count)
+    ns = np.array([rng.integers(8, m + 1) for m in ms])
+    b = BatchedQR(ms, ns, torch.float64, dev)
+    g = torch.Generator(device=dev).manual_seed(11)
+    a0 = torch.randn(b.a.numel(), generator=g, dtype=torch.float64, device=dev)
+    b.a.copy_(a0)
+    tune_ms = b.tune()
+    cfg = [b.config(0), b.config(1)]
+    # capture one run in a CUDA graph
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        b.a.copy_(a0)
+        b.factor()
+    torch.cuda.current_stream().wait_stream(s)
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        b.factor()
+    times = []
+    for _ in range(4):
+        b.a.copy_(a0)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        graph.replay()
+        e1.record()
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    ms_batched = min(times[1:])
+    flops = float(sum(2.0 * m * min(m, n) * n - min(m, n) ** 2 * (m + n) + 2.0 * min(m, n) ** 3 / 3 for m, n in zip(ms, ns)))
+    # every R of a sample against the CPU oracle
+    o = orc.load()
+    worst = 0.0
+    for i in rng.choice(count, check_sample, replace=False):
+        i = int(i)
+        m, n = int(ms[i]), int(ns[i])
+        x = np.asfortranarray(a0[int(b.a_off[i]):int(b.a_off[i]) + m * n].view(n, m).t().cpu().numpy())
+        o.geqrf("d", m, n, x)
+        k = min(m, n)
+        rg = np.triu(b.matrix(i).cpu().numpy()[:k])
+        ro = np.triu(x[:k])
+        worst = max(worst, float(np.linalg.norm(rg - ro) / np.linalg.norm(ro)))
+    # looping the plain Factor over a sample of the same matrices
+    idx = [int(i) for i in rng.choice(count, loop_sample, replace=False)]
+    mats = [gq.to_colmajor(a0[int(b.a_off[i]):int(b.a_off[i]) + int(ms[i]) * int(ns[i])].view(int(ns[i]), int(ms[i])).t()) for i in idx]
+    copies = [x.clone() for x in mats]
+    taus = [torch.zeros(min(x.shape), dtype=torch.float64, device=dev) for x in mats]
+    works = [torch.empty(gq.workspace_query("geqrf", torch.float64, *x.shape), dtype=torch.float64, device=dev) for x in mats]
+    for x, t, w in zip(copies, taus, works):
+        gq.factor(x, t, w)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for x, t, w in zip(copies, taus, works):
+        gq.factor(x, t, w)
+    e1.record()
+    torch.cuda.synchronize()
+    loop_ms_per = e0.elapsed_time(e1) / loop_sample
+    sample_flops = float(sum(2.0 * ms[i] * min(ms[i], ns[i]) * ns[i] - min(ms[i], ns[i]) ** 2 * (ms[i] + ns[i]) + 2.0 * min(ms[i], ns[i]) ** 3 / 3 for i in idx))
+    # the loop's time scaled from the sample to the batch by flops
+    loop_ms_total = e0.elapsed_time(e1) * flops / sample_flops
+    del b
+    return {
+        "workload": "batched_qr_20000_f64_m16-256",
+        "solves_per_s": count / (ms_batched * 1e-3), "ms": ms_batched, "tflops": flops / (ms_batched * 1e-3) / 1e12,
+        "frac_of_fp64_peak": flops / (ms_batched * 1e-3) / 1e12 / peak64 if peak64 else None,
+        "graph_captured": True, "autotune_ms": tune_ms, "class_configs": cfg,
+        "loop_plain_solves_per_s": count / (loop_ms_total * 1e-3), "loop_plain_ms_per_matrix": loop_ms_per,
+        "loop_sample": "plain Factor looped over %d random matrices of the batch, scaled to the batch by flops" % loop_sample,
+        "speedup_vs_loop": loop_ms_total / ms_batched,
+        "r_max_rel_err_vs_oracle": worst, "r_check_sample": check_sample,
+    }
+
+
+def other_configs(torch, dev, gq, lib, peak64):
+    """The plain FP64 drop-in on the reference's other configurations:
+    1024x256 real Factor + GenerateQ, and 4096x4096 complex Factor followed by
+    MultQ("L","C") on a 4096x64 block (FP64 throughout)."""
+    out = {}
+    g = torch.Generator(device=dev).manual_seed(7)
+    # 1024 x 256 real, entries uniform[-1, 1]
+    A0 = gq.to_colmajor(2 * torch.rand((1024, 256), generator=g, dtype=torch.float64, device=dev) - 1)
+    A = gq.to_colmajor(A0)
+    tau = torch.zeros(256, dtype=torch.float64, device=dev)
+    wf = torch.empty(gq.workspace_query("geqrf", torch.float64, 1024, 256), dtype=torch.float64, device=dev)
+    wq = torch.empty(gq.workspace_query("ungqr", torch.float64, 1024, 256, 256), dtype=torch.float64, device=dev)
+    ms_f = timed(torch, lambda: ((lambda: A.copy_(A0)), (lambda: gq.factor(A, tau, wf))), 5)
+    ms_q = timed(torch, lambda: ((lambda: (A.copy_(A0), gq.factor(A, tau, wf))), (lambda: gq.generate_q(A, tau, 256, wq))), 5)
+    f1 = 2.0 * 1024 * 256 ** 2 - 2.0 * 256 ** 3 / 3
+    q1 = 4.0 * 1024 * 256 * 256 - 2.0 * (1024 + 256) * 256 ** 2 + 4.0 * 256 ** 3 / 3
+    out["qr_1024x256_f64"] = {"factor_ms": ms_f, "generate_q_ms": ms_q, "factor_gflops": f1 / ms_f / 1e6, "generate_q_gflops": q1 / ms_q / 1e6}
+    # 4096 x 4096 complex, re/im N(0,1); MultQ("L","C") on 4096 x 64
+    n = 4096
+    Z0 = gq.to_colmajor(torch.complex(torch.randn((n, n), generator=g, dtype=torch.float64, device=dev), torch.randn((n, n), generator=g, dtype=torch.float64, device=dev)))
+    Z = gq.to_colmajor(Z0)
+    tz = torch.zeros(n, dtype=torch.complex128, device=dev)
+    wz = torch.empty(gq.workspace_query("geqrf", torch.complex128, n, n), dtype=torch.complex128, device=dev)
+    ms_z = timed(torch, lambda: ((lambda: Z.copy_(Z0)), (lambda: gq.factor(Z, tz, wz))), 2)
+    C0 = gq.to_colmajor(torch.complex(torch.randn((n, 64), generator=g, dtype=torch.float64, device=dev), torch.randn((n, 64), generator=g, dtype=torch.float64, device=dev)))
+    Cc = gq.to_colmajor(C0)
+    wm = torch.empty(gq.workspace_query("unmqr", torch.complex128, n, 64, n, side="L", trans="C"), dtype=torch.complex128, device=dev)
+    ms_m = timed(torch, lambda: ((lambda: Cc.copy_(C0)), (lambda: gq.mult_q("L", "C", Z, tz, Cc, n, wm))), 3)
+    fz = 4.0 * (2.0 * n ** 3 - 2.0 * n ** 3 / 3)
+    fm = 4.0 * 2.0 * 64 * n * (2.0 * n - n)
+    out["qr_4096x4096_c128"] = {"factor_ms": ms_z, "factor_tflops": fz / ms_z / 1e9, "factor_frac_of_fp64_peak": fz / ms_z / 1e9 / peak64 if peak64 else None,
+                                "multq_4096x64_ms": ms_m, "multq_tflops": fm / ms_m / 1e9}
+    del Z, Z0, wz
+    return out
+
+
 def gpu_arm(args, rank, world, local):
     import torch
 
@@ -289,6 +426,18 @@ def gpu_arm(args, rank, world, local):
         if i > 0:
             plain_ms.append(s0.elapsed_time(s1))
     ms_plain = statistics.mean(plain_ms)
+    # per-kernel-class profile of one plain solve
+    Ap.copy_(A)
+    bp.copy_(b)
+    lib.rnpgpu_timing_enable(1)
+    _capi.timing_report()
+    gls.gels(Ap, bp, tau, work=pwork)
+    torch.cuda.synchronize()
+    prof_plain = _capi.timing_report()
+    lib.rnpgpu_timing_enable(0)
+    Ap.copy_(A)
+    bp.copy_(b)
+    gls.gels(Ap, bp, tau, work=pwork)
     x_plain = bp[:N].clone()
     eta_plain, _ = ls_errors(torch, A, b, x_plain)
     ferr_mixed_vs_plain = float(torch.linalg.norm(x_mixed - x_plain) / torch.linalg.norm(x_plain))
@@ -323,6 +472,11 @@ def gpu_arm(args, rank, world, local):
             "share_of_step": res[1] / tot_ms if tot_ms else None,
         }
 
+    # ---------------- the other plain configurations ------------------------
+    others = {} if args.no_configs else other_configs(torch, dev, gq, lib, peak64.value)
+    if not args.no_configs:
+        others["batched"] = batched_config(torch, dev, gq, lib, peak64.value)
+
     # ---------------- CPU baseline (rank 0) ---------------------------------
     cpu = None
     ferr_vs_cpu = None
@@ -353,11 +507,13 @@ def gpu_arm(args, rank, world, local):
                   "backward_error": eta_mixed, "backward_error_bound": 10 * N * 2.0 ** -52,
                   "forward_error_vs_cpu_fp64_oracle": ferr_vs_cpu, "forward_error_vs_plain_gpu": ferr_mixed_vs_plain},
         "plain_fp64": {"solves_per_s": 1e3 / ms_plain, "ms_per_solve": ms_plain, "backward_error": eta_plain,
-                       "tflops": solve_flops(M, N, NRHS) / (ms_plain * 1e-3) / 1e12},
+                       "tflops": solve_flops(M, N, NRHS) / (ms_plain * 1e-3) / 1e12,
+                       "profile_ms": {k: v[1] for k, v in sorted(prof_plain.items(), key=lambda kv: -kv[1][1])}},
         "speedup_mixed_vs_plain": ms_plain / ms,
         "profile_ms_per_step": {k: v[1] / prof_steps for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])},
         "top_kernel": top[0],
         "roofline": roofline,
+        "configs": others,
         "cpu_baseline": cpu,
         "clocks": clk.summary(),
     }
@@ -375,6 +531,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-configs", action="store_true", help="skip the other plain configurations")
     ap.add_argument("--phase", default="all", choices=["all", "mixed"], help="'mixed': only the timed mixed solves (for profiler runs)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup

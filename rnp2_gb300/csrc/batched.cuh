@@ -1,0 +1,182 @@
+// batched.cuh — thousands of small, uneven QR factorizations in one
+// persistent launch.
+//
+// Each matrix of the batch is factored exactly as RNP::LA::QR::Factor would
+// (same reflector convention, RNP/LA/QR.hpp:78-197), by one thread block:
+// a blocked right-looking Householder QR whose NB-column panel is factored in
+// shared memory (Generate / Apply per column, RNP/LA/Reflector.hpp:117-236,
+// with the compact-WY T grown from the Gram column as in GenerateBlockTr,
+// Reflector.hpp:580-626), followed by the trailing update
+// C -= V (T^H (V^H C))... applied in column tiles staged in shared memory.
+// Blocks take matrices from a work queue (one atomic counter) in the order of
+// the descriptor array, which the host sorts by decreasing cost so the tail
+// of the launch is made of small matrices.
+#pragma once
+#include "qr_kernels.cuh"
+
+namespace rnpgpu {
+
+struct BatchDesc {
+    long long a_off;    // element offset of the matrix in the packed buffer
+    long long tau_off;  // element offset of its tau
+    int m, n, lda, index;
+};
+
+constexpr int kBatchMaxRows = 256;  // rows of the largest matrix a block stages
+constexpr int kBatchTile = 32;      // trailing-update column tile
+
+template <class T, int NB> struct BatchSmem {
+    static constexpr size_t kP = (size_t)kBatchMaxRows * NB;          // panel
+    static constexpr size_t kC = (size_t)kBatchMaxRows * kBatchTile;  // trailing tile
+    static constexpr size_t kW = (size_t)kBatchTile * NB;
+    static constexpr size_t kBytes = (kP + kC + kW + NB * NB + 2 * NB) * sizeof(T);
+};
+
+template <class T, int NT, int NB>
+__global__ void __launch_bounds__(NT) k_geqrf_batched(const BatchDesc *__restrict__ desc, int count, T *A, T *tau, unsigned *queue) {
+    typedef typename Tr<T>::R R;
+    extern __shared__ __align__(16) unsigned char s_raw[];
+    typedef BatchSmem<T, NB> L;
+    T *sP = reinterpret_cast<T *>(s_raw);  // panel, column-major, ld kBatchMaxRows
+    T *sC = sP + L::kP;                    // trailing tile, column-major, ld kBatchMaxRows
+    T *sW = sC + L::kC;                    // W (kBatchTile x NB), ld kBatchTile
+    T *sT = sW + L::kW;                    // T (NB x NB), ld NB
+    T *sG = sT + NB * NB;                  // w / Gram column (NB)
+    __shared__ NormAcc s_nacc[NT / 32];
+    __shared__ ReflScalars<T> s_refl;
+    __shared__ int s_idx;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    constexpr int NW = NT / 32;
+
+    for (;;) {
+        if (tid == 0) s_idx = (int)atomicAdd(queue, 1u);
+        __syncthreads();
+        const int idx = s_idx;
+        __syncthreads();
+        if (idx >= count) break;
+        const BatchDesc d = desc[idx];
+        T *a = A + d.a_off;
+        T *tp = tau + d.tau_off;
+        const int m = d.m, n = d.n, lda = d.lda;
+        const int k = min(m, n);
+        for (int j0 = 0; j0 < k; j0 += NB) {
+            const int jb = min(NB, k - j0), mp = m - j0;
+            // ---- panel into shared memory
+            for (int e = tid; e < mp * jb; e += NT) {
+                const int r = e % mp, c = e / mp;
+                sP[c * kBatchMaxRows + r] = a[(j0 + r) + (size_t)(j0 + c) * lda];
+            }
+            __syncthreads();
+            // ---- factor the panel column by column
+            for (int jj = 0; jj < jb; ++jj) {
+                T *col = sP + jj * kBatchMaxRows;
+                NormAcc acc;
+                acc.zero();
+                for (int r = jj + 1 + tid; r < mp; r += NT) acc.add(col[r]);
+                acc.warp_reduce();
+                if (lane == 0) s_nacc[warp] = acc;
+                __syncthreads();
+                if (tid == 0) {
+                    NormAcc t = s_nacc[0];
+                    for (int w = 1; w < NW; ++w) t.merge(s_nacc[w]);
+                    s_refl = reflector_scalars<T>(col[jj], t);
+                }
+                __syncthreads();
+                const ReflScalars<T> rs = s_refl;
+                if (!rs.identity)
+                    for (int r = jj + 1 + tid; r < mp; r += NT) col[r] = scale_x(col[r], rs);
+                __syncthreads();
+                // w_c = v^H P[:,c] (c > jj) and Gram g_c = V[:,c]^H v (c < jj), rows >= jj
+                for (int c = warp; c < jb; c += NW) {
+                    if (c == jj) continue;
+                    const T *pc = sP + c * kBatchMaxRows;
+                    T s = T(0);
+                    for (int r = jj + lane; r < mp; r += 32) {
+                        const T v = (r == jj) ? T(1) : col[r];
+                        s = (c > jj) ? fmac(Tr<T>::conj(v), pc[r], s) : fmac(Tr<T>::conj(pc[r]), v, s);
+                    }
+                    s = warp_sum(s);
+                    if (lane == 0) sG[c] = s;
+                }
+                __syncthreads();
+                if (!rs.identity && jj + 1 < jb) {
+                    const T ctau = Tr<T>::conj(rs.tau);
+                    for (int e = tid; e < (mp - jj) * (jb - jj - 1); e += NT) {
+                        const int r = jj + e % (mp - jj), c = jj + 1 + e / (mp - jj);
+                        const T v = (r == jj) ? T(1) : col[r];
+                        sP[c * kBatchMaxRows + r] = fmac(-(ctau * v), sG[c], sP[c * kBatchMaxRows + r]);
+                    }
+                }
+                // T(0:jj, jj) = -tau T(0:jj, 0:jj) g(0:jj), T(jj, jj) = tau
+                if (tid < jj) {
+                    T s = T(0);
+                    for (int l = tid; l < jj; ++l) s = fmac(sT[tid + l * NB], sG[l], s);
+                    sT[tid + jj * NB] = rs.identity ? T(0) : (-rs.tau) * s;
+                }
+                if (tid == 0) {
+                    sT[jj + jj * NB] = rs.tau;
+                    tp[j0 + jj] = rs.tau;
+                    if (!rs.identity) col[jj] = Tr<T>::make((R)rs.beta, 0);
+                }
+                __syncthreads();
+            }
+            // ---- panel back to global memory
+            for (int e = tid; e < mp * jb; e += NT) {
+                const int r = e % mp, c = e / mp;
+                a[(j0 + r) + (size_t)(j0 + c) * lda] = sP[c * kBatchMaxRows + r];
+            }
+            // ---- trailing update, one column tile at a time:  C -= V (T^H ... ) : W = C^H V T, C -= V W^H
+            for (int c0 = j0 + jb; c0 < n; c0 += kBatchTile) {
+                const int ct = min(kBatchTile, n - c0);
+                for (int e = tid; e < mp * ct; e += NT) {
+                    const int r = e % mp, c = e / mp;
+                    sC[c * kBatchMaxRows + r] = a[(j0 + r) + (size_t)(c0 + c) * lda];
+                }
+                __syncthreads();
+                // W(c, l) = sum_r conj(C(r, c)) V(r, l), V unit lower trapezoidal
+                for (int e = tid; e < ct * jb; e += NT) {
+                    const int c = e % ct, l = e / ct;
+                    const T *vc = sP + l * kBatchMaxRows;
+                    const T *cc = sC + c * kBatchMaxRows;
+                    T s = Tr<T>::conj(cc[l]);
+                    for (int r = l + 1; r < mp; ++r) s = fmac(Tr<T>::conj(cc[r]), vc[r], s);
+                    sW[c + l * kBatchTile] = s;
+                }
+                __syncthreads();
+                // W := W T (upper triangular, in place by columns from the right)
+                for (int c = tid; c < ct; c += NT) {
+                    T w[NB];
+#pragma unroll
+                    for (int l = 0; l < NB; ++l) w[l] = (l < jb) ? sW[c + l * kBatchTile] : T(0);
+                    for (int l = jb - 1; l >= 0; --l) {
+                        T s = T(0);
+                        for (int q = 0; q <= l; ++q) s = fmac(w[q], sT[q + l * NB], s);
+                        sW[c + l * kBatchTile] = s;
+                    }
+                }
+                __syncthreads();
+                // C(r, c) -= sum_l V(r, l) conj(W(c, l))
+                for (int r = tid; r < mp; r += NT) {
+                    T v[NB];
+#pragma unroll
+                    for (int l = 0; l < NB; ++l) v[l] = (l < jb && r >= l) ? (r == l ? T(1) : sP[l * kBatchMaxRows + r]) : T(0);
+                    for (int c = 0; c < ct; ++c) {
+                        T s = sC[c * kBatchMaxRows + r];
+#pragma unroll
+                        for (int l = 0; l < NB; ++l) s = fmac(-v[l], Tr<T>::conj(sW[c + l * kBatchTile]), s);
+                        sC[c * kBatchMaxRows + r] = s;
+                    }
+                }
+                __syncthreads();
+                for (int e = tid; e < mp * ct; e += NT) {
+                    const int r = e % mp, c = e / mp;
+                    a[(j0 + r) + (size_t)(c0 + c) * lda] = sC[c * kBatchMaxRows + r];
+                }
+                __syncthreads();
+            }
+            __syncthreads();
+        }
+    }
+}
+
+} // namespace rnpgpu
