@@ -31,7 +31,7 @@ struct RefineInfo {
 template <class T> int trsm_upper(size_t n, size_t nrhs, const T *a, size_t lda, T *b, size_t ldb, cudaStream_t st) {
     if (n == 0 || nrhs == 0) return kOk;
     KScope ks("trsm", st);
-    k_trsm_upper<T><<<(unsigned)std::min<size_t>(nrhs, 65535), 256, 0, st>>>((int)n, (int)nrhs, a, lda, b, ldb);
+    k_trsm_upper<T><<<(unsigned)std::min<size_t>(nrhs, 65535), 512, 0, st>>>((int)n, (int)nrhs, a, lda, b, ldb);
     RNPGPU_CHECK_LAUNCH();
     return kOk;
 }
@@ -39,7 +39,7 @@ template <class T> int trsm_upper(size_t n, size_t nrhs, const T *a, size_t lda,
 template <class T> int trsm_upper_ct(size_t n, size_t nrhs, const T *a, size_t lda, T *b, size_t ldb, cudaStream_t st) {
     if (n == 0 || nrhs == 0) return kOk;
     KScope ks("trsm", st);
-    k_trsm_upper_ct<T><<<(unsigned)std::min<size_t>(nrhs, 65535), 256, 0, st>>>((int)n, (int)nrhs, a, lda, b, ldb);
+    k_trsm_upper_ct<T><<<(unsigned)std::min<size_t>(nrhs, 65535), 512, 0, st>>>((int)n, (int)nrhs, a, lda, b, ldb);
     RNPGPU_CHECK_LAUNCH();
     return kOk;
 }

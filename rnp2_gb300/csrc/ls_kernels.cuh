@@ -11,7 +11,7 @@ namespace rnpgpu {
 // triangular non-unit (leading dimension ldr).  One block per right-hand
 // side; each 32 x 32 diagonal block is staged in shared memory and solved by
 // one warp with shuffles, the rows above are updated by the whole block.
-template <class T> __global__ void __launch_bounds__(256) k_trsm_upper(int n, int nrhs, const T *R, size_t ldr, T *B, size_t ldb) {
+template <class T> __global__ void __launch_bounds__(512) k_trsm_upper(int n, int nrhs, const T *R, size_t ldr, T *B, size_t ldb) {
     __shared__ T xs[32];
     __shared__ T sR[32][33];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -37,10 +37,16 @@ template <class T> __global__ void __launch_bounds__(256) k_trsm_upper(int n, in
                 }
             }
             __syncthreads();
+            // rows above: 32 independent loads in flight per thread
             for (int r = tid; r < i0; r += blockDim.x) {
-                T acc = y[r];
-                for (int c = 0; c < nbk; ++c) acc = fmac(-R[r + (size_t)(i0 + c) * ldr], xs[c], acc);
-                y[r] = acc;
+                T a[4] = {T(0), T(0), T(0), T(0)};
+                if (nbk == 32 && sizeof(T) <= 8) {
+#pragma unroll
+                    for (int c = 0; c < 32; ++c) a[c & 3] = fmac(R[r + (size_t)(i0 + c) * ldr], xs[c], a[c & 3]);
+                } else {
+                    for (int c = 0; c < nbk; ++c) a[0] = fmac(R[r + (size_t)(i0 + c) * ldr], xs[c], a[0]);
+                }
+                y[r] = y[r] - ((a[0] + a[1]) + (a[2] + a[3]));
             }
             __syncthreads();
         }
@@ -49,7 +55,7 @@ template <class T> __global__ void __launch_bounds__(256) k_trsm_upper(int n, in
 
 // Y = R^{-H} G in place: forward substitution with the conjugate transpose of
 // an upper triangular R (the lower triangular system R^H y = g).
-template <class T> __global__ void __launch_bounds__(256) k_trsm_upper_ct(int n, int nrhs, const T *R, size_t ldr, T *B, size_t ldb) {
+template <class T> __global__ void __launch_bounds__(512) k_trsm_upper_ct(int n, int nrhs, const T *R, size_t ldr, T *B, size_t ldb) {
     __shared__ T xs[32];
     __shared__ T sR[32][33];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -76,10 +82,15 @@ template <class T> __global__ void __launch_bounds__(256) k_trsm_upper_ct(int n,
             }
             __syncthreads();
             for (int r = i1 + tid; r < n; r += blockDim.x) {
-                T acc = y[r];
                 const T *rc = R + (size_t)r * ldr + i0;
-                for (int c = 0; c < nbk; ++c) acc = fmac(-Tr<T>::conj(rc[c]), xs[c], acc);
-                y[r] = acc;
+                T a[4] = {T(0), T(0), T(0), T(0)};
+                if (nbk == 32 && sizeof(T) <= 8) {
+#pragma unroll
+                    for (int c = 0; c < 32; ++c) a[c & 3] = fmac(Tr<T>::conj(rc[c]), xs[c], a[c & 3]);
+                } else {
+                    for (int c = 0; c < nbk; ++c) a[0] = fmac(Tr<T>::conj(rc[c]), xs[c], a[0]);
+                }
+                y[r] = y[r] - ((a[0] + a[1]) + (a[2] + a[3]));
             }
             __syncthreads();
         }

@@ -1,0 +1,273 @@
+// multq_thin.cuh — MultQ("L", trans) on a thin C (at most kThinMaxCols
+// columns) in one cooperative launch, and the T factors of all reflector
+// blocks of a MultQ call in two launches.
+//
+// RNP::LA::QR::MultQ (RNP/LA/QR.hpp:337-429) applies the reflector blocks one
+// after another, each by ApplyBlock (RNP/LA/Reflector.hpp:725-815):
+//   Q^H C:  C -= V_b (T_b^H (V_b^H C)),  b = 0, 1, ...
+//   Q   C:  C -= V_b (T_b   (V_b^H C)),  b = ..., 1, 0
+// For a thin C every block is a long reduction (V_b^H C over all rows)
+// followed by a rank-32 update, far too little work for a launch of its own.
+// Here thread block g owns rows [g R, (g+1) R) of C for the whole launch (in
+// shared memory when they fit) and, per reflector block,
+//   1. accumulates its part of V_b^H C over its rows (lanes along rows, a
+//      4 x 4 tile of (reflector, column) per warp, reduced by shuffles),
+//   2. writes it to its slot of the partial buffer;  grid barrier;
+//   3. sums a slice of the (reflector, column) entries over all blocks in a
+//      fixed order into the reduced buffer;  grid barrier;
+//   4. reads V_b^H C back and forms Y = op(T_b) (V_b^H C) in shared memory,
+//   5. updates its rows: C -= V_b Y.
+// The summation order depends only on the grid size: results are
+// deterministic.  Every barrier wait is bounded (GridBarrier).
+#pragma once
+#include "qr_kernels.cuh"
+
+namespace rnpgpu {
+
+constexpr int kThinMaxCols = 64;
+constexpr int kThinThreads = 512;
+constexpr int kThinWarps = kThinThreads / 32;
+
+template <class T> struct ThinArgs {
+    const T *A;
+    size_t lda;
+    const T *Tf;  // T of block b at Tf + b * kPanelMaxCols^2, leading dimension kPanelMaxCols
+    T *C;
+    size_t ldc;
+    int m, n, k, nblk;
+    int forward;  // 1: Q^H C (blocks ascending, op(T) = T^H); 0: Q C (descending, op(T) = T)
+    T *part;      // [gridDim.x][kPanelMaxCols * n]
+    T *wred;      // [kPanelMaxCols * n]
+    unsigned *counter;
+    int *err;
+    int rows_per_cta;
+};
+
+// shared memory of the thin kernel: W, Y, T, VBUF staging buffers for the
+// block's rows of V_b (column-major, leading dimension rows) and, when CSMEM,
+// the block's rows of C (row-major, leading dimension n + 1)
+template <class T> inline size_t thin_smem_bytes(int rows, int n, bool csmem, int vbuf) {
+    size_t e = (size_t)2 * kPanelMaxCols * n + (size_t)kPanelMaxCols * (kPanelMaxCols + 1);
+    e += (size_t)vbuf * kPanelMaxCols * rows;
+    if (csmem) e += (size_t)rows * (n + 1);
+    return e * sizeof(T);
+}
+
+// V_b element (row r, column l) in stored form: zero above the diagonal of
+// the block, one on it
+template <class T> __device__ __forceinline__ T vload(const T *A, size_t lda, int i, int r, int l) {
+    const int d = r - (i + l);
+    if (d < 0) return T(0);
+    if (d == 0) return T(1);
+    return A[r + (size_t)(i + l) * lda];
+}
+
+// one element global -> shared by cp.async, per real component (complex
+// elements need only the alignment of their real type)
+template <class T> __device__ __forceinline__ void stage_elem(T *dst, const T *src) {
+    typedef typename Tr<T>::R R;
+    constexpr int nc = sizeof(T) / sizeof(R);
+#pragma unroll
+    for (int q = 0; q < nc; ++q) cp_async<sizeof(R)>(reinterpret_cast<R *>(dst) + q, reinterpret_cast<const R *>(src) + q);
+}
+
+// VBUF: 0 = V read from global memory, 1 = V_b staged in shared memory before
+// its use, 2 = V_{b+1} staged during block b's barriers (double buffer)
+template <class T, bool CSMEM, int VBUF> __global__ void __launch_bounds__(kThinThreads) k_multq_thin(ThinArgs<T> p) {
+    extern __shared__ __align__(16) unsigned char s_dyn[];
+    const int n = p.n, ldsc = n + 1, R = p.rows_per_cta;
+    T *sW = reinterpret_cast<T *>(s_dyn);                   // 32 x n (ld 32): V^H C
+    T *sY = sW + kPanelMaxCols * n;                         // 32 x n (ld 32): op(T) V^H C
+    T *sT = sY + kPanelMaxCols * n;                         // 32 x 33
+    T *sV0 = sT + kPanelMaxCols * (kPanelMaxCols + 1);      // 32 x R (ld R)
+    T *sV1 = sV0 + (VBUF >= 1 ? (size_t)kPanelMaxCols * R : 0);
+    T *sC = sV0 + (size_t)VBUF * kPanelMaxCols * R;         // R x (n+1), row-major
+    const int G = gridDim.x, g = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int r0 = g * R;
+    const int r1 = min(p.m, r0 + R);
+    GridBarrier bar{p.counter, p.err, (unsigned)G, 0u};
+    auto cref = [&](int r, int c) -> T & {
+        if (CSMEM) return sC[(size_t)(r - r0) * ldsc + c];
+        return p.C[r + (size_t)c * p.ldc];
+    };
+    auto block_of = [&](int s) { return p.forward ? s : p.nblk - 1 - s; };
+    // rows [max(r0, i_b), r1) of V_b into buf; entries above the diagonal of
+    // the block and columns beyond its width as zeros, the diagonal as ones
+    auto stage_v = [&](int bb, T *buf) {
+        const int i = bb * kPanelMaxCols, ib = min(kPanelMaxCols, p.k - i), rs = max(r0, i);
+        const int nr = r1 - rs;
+        for (int e = tid; e < nr * kPanelMaxCols; e += kThinThreads) {
+            const int rr = e % nr, l = e / nr, r = rs + rr;
+            T *dst = buf + (size_t)l * R + (r - r0);
+            if (l >= ib || r < i + l) *dst = T(0);
+            else if (r == i + l) *dst = T(1);
+            else stage_elem(dst, p.A + r + (size_t)(i + l) * p.lda);
+        }
+        cp_async_commit();
+    };
+    auto vget = [&](const T *buf, int i, int r, int l) -> T {
+        if (VBUF > 0) return buf[(size_t)l * R + (r - r0)];
+        return vload(p.A, p.lda, i, r, l);
+    };
+    if (CSMEM) {
+        for (int c = 0; c < n; ++c)
+            for (int r = r0 + tid; r < r1; r += kThinThreads) sC[(size_t)(r - r0) * ldsc + c] = p.C[r + (size_t)c * p.ldc];
+    }
+    if (VBUF > 0 && p.nblk > 0) stage_v(block_of(0), sV0);
+
+    const int nw = kPanelMaxCols * n;          // entries of V^H C
+    const int ctiles = (n + 3) / 4;
+    const int ntiles = (kPanelMaxCols / 4) * ctiles;
+    const int slice = (nw + G - 1) / G;        // entries this block reduces
+    for (int s = 0; s < p.nblk; ++s) {
+        const int b = block_of(s);
+        const int i = b * kPanelMaxCols;
+        const int ib = min(kPanelMaxCols, p.k - i);
+        const int rs = max(r0, i);
+        const T *sV = (VBUF == 2 && (s & 1)) ? sV1 : sV0;
+        if (VBUF > 0) cp_async_wait_all();
+        __syncthreads();
+        // 1. partial V^H C over own rows; tile t = (reflectors 4*(t % 8) .., columns 4*(t / 8) ..)
+        T *mine = p.part + (size_t)g * nw;
+        for (int t = warp; t < ntiles; t += kThinWarps) {
+            const int l0 = 4 * (t % (kPanelMaxCols / 4)), c0 = 4 * (t / (kPanelMaxCols / 4));
+            T acc[4][4];
+#pragma unroll
+            for (int a = 0; a < 4; ++a)
+#pragma unroll
+                for (int q = 0; q < 4; ++q) acc[a][q] = T(0);
+            if (l0 < ib) {
+                for (int r = rs + lane; r < r1; r += 32) {
+                    T v[4], c[4];
+#pragma unroll
+                    for (int a = 0; a < 4; ++a) v[a] = (VBUF > 0 || l0 + a < ib) ? Tr<T>::conj(vget(sV, i, r, l0 + a)) : T(0);
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) c[q] = (c0 + q < n) ? cref(r, c0 + q) : T(0);
+#pragma unroll
+                    for (int a = 0; a < 4; ++a)
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) acc[a][q] = fmac(v[a], c[q], acc[a][q]);
+                }
+            }
+#pragma unroll
+            for (int a = 0; a < 4; ++a)
+#pragma unroll
+                for (int q = 0; q < 4; ++q) acc[a][q] = warp_sum(acc[a][q]);
+            if (lane < 16) {
+                const int a = lane & 3, q = lane >> 2;
+                T val = T(0);
+#pragma unroll
+                for (int aa = 0; aa < 4; ++aa)
+#pragma unroll
+                    for (int qq = 0; qq < 4; ++qq)
+                        if (aa == a && qq == q) val = acc[aa][qq];
+                if (c0 + q < n) mine[(l0 + a) + (size_t)(c0 + q) * kPanelMaxCols] = val;
+            }
+        }
+        // the next block's V streams in while this one waits at the barriers
+        if (VBUF == 2 && s + 1 < p.nblk) stage_v(block_of(s + 1), (s & 1) ? sV0 : sV1);
+        if (!bar.sync()) return;
+        // 3. this block's slice of the reduction, fixed order over blocks
+        for (int e = g * slice + warp; e < min(nw, (g + 1) * slice); e += kThinWarps) {
+            T a = T(0);
+            for (int q = lane; q < G; q += 32) a = a + ldcg(&p.part[(size_t)q * nw + e]);
+            a = warp_sum(a);
+            if (lane == 0) p.wred[e] = a;
+        }
+        if (!bar.sync()) return;
+        // 4. Y = op(T) (V^H C)
+        for (int e = tid; e < nw; e += kThinThreads) sW[e] = ldcg(&p.wred[e]);
+        const T *Tb = p.Tf + (size_t)b * kPanelMaxCols * kPanelMaxCols;
+        for (int e = tid; e < kPanelMaxCols * kPanelMaxCols; e += kThinThreads) {
+            const int r = e % kPanelMaxCols, c = e / kPanelMaxCols;
+            sT[r * (kPanelMaxCols + 1) + c] = (r <= c && c < ib) ? Tb[r + (size_t)c * kPanelMaxCols] : T(0);
+        }
+        __syncthreads();
+        for (int e = tid; e < nw; e += kThinThreads) {
+            const int l = e % kPanelMaxCols, c = e / kPanelMaxCols;
+            T acc = T(0);
+            if (l < ib) {
+                if (p.forward) {
+                    // (T^H W)(l, c) = sum_{j <= l} conj(T(j, l)) W(j, c)
+                    for (int j = 0; j <= l; ++j) acc = fmac(Tr<T>::conj(sT[j * (kPanelMaxCols + 1) + l]), sW[j + c * kPanelMaxCols], acc);
+                } else {
+                    // (T W)(l, c) = sum_{j >= l} T(l, j) W(j, c)
+                    for (int j = l; j < ib; ++j) acc = fmac(sT[l * (kPanelMaxCols + 1) + j], sW[j + c * kPanelMaxCols], acc);
+                }
+            }
+            sY[e] = acc;
+        }
+        __syncthreads();
+        // 5. C(r, c) -= sum_l V(r, l) Y(l, c) on own rows
+        const int nrc = (r1 > rs) ? (r1 - rs + 31) / 32 : 0;
+        for (int w = warp; w < nrc * ctiles; w += kThinWarps) {
+            const int rc = w % nrc, c0 = 4 * (w / nrc);
+            const int r = rs + rc * 32 + lane;
+            if (r < r1) {
+                T acc[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) acc[q] = (c0 + q < n) ? cref(r, c0 + q) : T(0);
+                const int lmax = min(ib, r - i + 1);  // V(r, l) = 0 for l > r - i
+                for (int l0 = 0; l0 < lmax; l0 += 8) {
+                    T v[8];
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) v[u] = (l0 + u < lmax) ? -vget(sV, i, r, l0 + u) : T(0);
+#pragma unroll
+                    for (int u = 0; u < 8; ++u)
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) acc[q] = fmac(v[u], sY[l0 + u + min(c0 + q, n - 1) * kPanelMaxCols], acc[q]);
+                }
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                    if (c0 + q < n) cref(r, c0 + q) = acc[q];
+            }
+        }
+        if (VBUF == 1 && s + 1 < p.nblk) {
+            __syncthreads();
+            stage_v(block_of(s + 1), sV0);
+        }
+    }
+    __syncthreads();
+    if (CSMEM) {
+        for (int c = 0; c < n; ++c)
+            for (int r = r0 + tid; r < r1; r += kThinThreads) p.C[r + (size_t)c * p.ldc] = sC[(size_t)(r - r0) * ldsc + c];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Gram matrices V_b^H V_b of all reflector blocks, split over row chunks:
+// block (s, b) sums rows [i_b + s*chunk, i_b + (s+1)*chunk) of block b and
+// writes the 32 x 32 partial at P + (b * S + s) * 32 * 32 (leading dimension
+// 32).  k_build_t then runs the GenerateBlockTr recurrence on every block.
+// ---------------------------------------------------------------------------
+template <class T> __global__ void __launch_bounds__(256) k_gram_blocks(const T *A, size_t lda, int m, int k, int chunk, T *P) {
+    __shared__ T sV[64][kPanelMaxCols + 1];
+    const int s = blockIdx.x, b = blockIdx.y, S = gridDim.x, tid = threadIdx.x;
+    const int i = b * kPanelMaxCols;
+    const int ib = min(kPanelMaxCols, k - i);
+    const int rb = i + s * chunk, re = min(m, rb + chunk);
+    // thread: row l1 = tid % 32 of the Gram matrix, columns l2 = tid / 32 + 8 q
+    const int l1 = tid % kPanelMaxCols, lq = tid / kPanelMaxCols;
+    T acc[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) acc[q] = T(0);
+    for (int c0 = rb; c0 < re; c0 += 64) {
+        const int rows = min(64, re - c0);
+        __syncthreads();
+        for (int e = tid; e < 64 * kPanelMaxCols; e += 256) {
+            const int r = e % 64, l = e / 64;
+            sV[r][l] = (r < rows && l < ib) ? vload(A, lda, i, c0 + r, l) : T(0);
+        }
+        __syncthreads();
+        for (int r = 0; r < rows; ++r) {
+            const T a = Tr<T>::conj(sV[r][l1]);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) acc[q] = fmac(a, sV[r][lq + 8 * q], acc[q]);
+        }
+    }
+    T *out = P + ((size_t)b * S + s) * kPanelMaxCols * kPanelMaxCols;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) out[l1 + (size_t)(lq + 8 * q) * kPanelMaxCols] = acc[q];
+}
+
+} // namespace rnpgpu

@@ -8,6 +8,7 @@
 // synchronizing.
 #pragma once
 #include "qr_kernels.cuh"
+#include "multq_thin.cuh"
 #include "tc_gemm.cuh"
 #include <algorithm>
 #include <type_traits>
@@ -403,14 +404,108 @@ template <class T> int geqr2(size_t m, size_t n, T *a, size_t lda, T *tau, T *wo
 }
 
 // ---------------------------------------------------------------------------
+// T factors of all reflector blocks of a call (GenerateBlockTr "F","C" for
+// every block, RNP/LA/Reflector.hpp:580-626): the Gram matrices of all blocks
+// in one launch (row chunks of every block in parallel), then the
+// recurrence for all blocks in one launch.
+// ---------------------------------------------------------------------------
+inline int gram_splits(size_t rows, size_t nblk, int scap) {
+    size_t s = std::min<size_t>((size_t)std::max(scap, 1), std::max<size_t>(1, (rows + 511) / 512));
+    s = std::min<size_t>(s, std::max<size_t>(1, 4096 / std::max<size_t>(nblk, 1)));
+    return (int)std::max<size_t>(s, 1);
+}
+template <class T> size_t gram_bytes(size_t rows, size_t nblk, int scap) {
+    return (nblk * (size_t)gram_splits(rows, nblk, scap) * kPanelMaxCols * kPanelMaxCols * sizeof(T) + 255) / 256 * 256;
+}
+template <class T> int build_all_t(size_t rows, size_t k, const T *a, size_t lda, const T *tau, T *Tout, T *Pg, int scap, cudaStream_t st) {
+    const size_t nblk = (k + kPanelMaxCols - 1) / kPanelMaxCols;
+    if (nblk == 0) return kOk;
+    const int S = gram_splits(rows, nblk, scap);
+    const int chunk = (int)((rows + S - 1) / S);
+    KScope ks("larft_all", st);
+    k_gram_blocks<T><<<dim3((unsigned)S, (unsigned)nblk), 256, 0, st>>>(a, lda, (int)rows, (int)k, chunk, Pg);
+    RNPGPU_CHECK_LAUNCH();
+    k_build_t<T><<<(unsigned)nblk, kPanelMaxCols, 0, st>>>(Pg, (size_t)kPanelMaxCols * kPanelMaxCols, (size_t)S * kPanelMaxCols * kPanelMaxCols, S, tau, kPanelMaxCols, (int)k,
+                                                           Tout, (size_t)kPanelMaxCols * kPanelMaxCols, kPanelMaxCols);
+    RNPGPU_CHECK_LAUNCH();
+    return kOk;
+}
+
+// ---------------------------------------------------------------------------
+// Thin left MultQ in one cooperative launch (multq_thin.cuh)
+// ---------------------------------------------------------------------------
+struct ThinPlan {
+    bool csmem;
+    int vbuf;
+    int grid, rows;
+    size_t smem;
+};
+constexpr size_t kThinSmemMax = 200 * 1024;
+
+template <class T> size_t thin_ws_bytes(size_t n) {
+    const int G = std::max(1, device_facts().sm_count);
+    return ((size_t)(G + 1) * kPanelMaxCols * n * sizeof(T) + 255) / 256 * 256 + 1024;
+}
+// C's rows and two V staging buffers in shared memory when they fit, then one
+// buffer, then C alone, then neither
+template <class T> ThinPlan thin_plan(size_t m, size_t n) {
+    ThinPlan tp;
+    const int sms = std::max(1, device_facts().sm_count);
+    tp.grid = (int)std::max<size_t>(1, std::min<size_t>((size_t)sms, (m + 31) / 32));
+    tp.rows = (int)((m + tp.grid - 1) / tp.grid);
+    static const int modes[4][2] = {{1, 2}, {1, 1}, {1, 0}, {0, 0}};
+    for (int q = 0; q < 4; ++q) {
+        tp.csmem = modes[q][0] != 0;
+        tp.vbuf = modes[q][1];
+        tp.smem = thin_smem_bytes<T>(tp.rows, (int)n, tp.csmem, tp.vbuf);
+        if (tp.smem <= kThinSmemMax) break;
+    }
+    return tp;
+}
+template <class T, bool CS, int VB> const void *thin_kernel() { return (const void *)k_multq_thin<T, CS, VB>; }
+template <class T> int multq_thin(bool notran, size_t m, size_t n, size_t k, const T *a, size_t lda, const T *Tf, T *c, size_t ldc, void *ws, cudaStream_t st) {
+    const ThinPlan tp = thin_plan<T>(m, n);
+    const void *kern = tp.csmem ? (tp.vbuf == 2 ? thin_kernel<T, true, 2>() : tp.vbuf == 1 ? thin_kernel<T, true, 1>() : thin_kernel<T, true, 0>()) : thin_kernel<T, false, 0>();
+    static std::once_flag once;
+    static cudaError_t attr = cudaSuccess;
+    std::call_once(once, []() {
+        const void *ks[4] = {thin_kernel<T, true, 2>(), thin_kernel<T, true, 1>(), thin_kernel<T, true, 0>(), thin_kernel<T, false, 0>()};
+        for (int q = 0; q < 4 && attr == cudaSuccess; ++q) attr = cudaFuncSetAttribute(ks[q], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kThinSmemMax);
+    });
+    RNPGPU_CHECK(attr);
+    Carver cv(ws);
+    ThinArgs<T> p;
+    p.A = a; p.lda = lda; p.Tf = Tf; p.C = c; p.ldc = ldc;
+    p.m = (int)m; p.n = (int)n; p.k = (int)k;
+    p.nblk = (int)((k + kPanelMaxCols - 1) / kPanelMaxCols);
+    p.forward = notran ? 0 : 1;
+    p.part = cv.take<T>((size_t)tp.grid * kPanelMaxCols * n);
+    p.wred = cv.take<T>((size_t)kPanelMaxCols * n);
+    unsigned *sync = cv.take<unsigned>(2);
+    p.counter = sync;
+    p.err = (int *)(sync + 1);
+    p.rows_per_cta = tp.rows;
+    RNPGPU_CHECK(cudaMemsetAsync(sync, 0, 2 * sizeof(unsigned), st));
+    void *args[] = {&p};
+    KScope ks("multq_thin", st);
+    RNPGPU_CHECK(cudaLaunchCooperativeKernel(kern, dim3(tp.grid), dim3(kThinThreads), args, tp.smem, st));
+    note_launch();
+    return kOk;
+}
+
+// ---------------------------------------------------------------------------
 // MultQ (unmqr): RNP/LA/QR.hpp:337-429.  The T factors of all blocks are
-// built once per call and kept in the workspace.
+// built once per call (or taken from the factorization) and kept in the
+// workspace.  A thin C on the left (at most kThinMaxCols columns) goes
+// through the one-launch kernel; otherwise every block is one ApplyBlock.
 // ---------------------------------------------------------------------------
 template <class T> int unm2r(const char *side, const char *trans, size_t m, size_t n, size_t k, const T *a, size_t lda, const T *tau, T *c, size_t ldc, T *work);
 
 template <class T> size_t unmqr_bytes(size_t nq, size_t nw, size_t k, int smax, int sgram) {
     const size_t nblk = (k + GpuTuning::nb - 1) / GpuTuning::nb;
-    return nblk * t_bytes<T>() + ((size_t)sgram * kPanelMaxCols * kPanelMaxCols * sizeof(T) + 255) / 256 * 256 + block_ws_bytes<T>((int)nw, smax);
+    size_t uni = std::max(block_ws_bytes<T>((int)nw, smax), gram_bytes<T>(nq, nblk, sgram));
+    if (nw <= (size_t)kThinMaxCols) uni = std::max(uni, thin_ws_bytes<T>(nw));
+    return nblk * t_bytes<T>() + uni;
 }
 
 // Tcache (optional): the T factors of the reflector blocks as stored by
@@ -439,6 +534,7 @@ template <class T> int unmqr(const char *side, const char *trans, size_t m, size
         smax = std::max(1, smax / 2);
         sgram = std::max(1, sgram / 2);
     }
+    const bool thin = left && n <= (size_t)kThinMaxCols;
     if (elems_for<T>(unmqr_bytes<T>(nq, nw, k, smax, sgram)) > *lwork) {
         if (*lwork < nw) return -11;
         return unm2r<T>(side, trans, m, n, k, a, lda, tau, c, ldc, work);
@@ -448,17 +544,15 @@ template <class T> int unmqr(const char *side, const char *trans, size_t m, size
     const size_t nb = GpuTuning::nb;
     const size_t nblk = (k + nb - 1) / nb;
     T *Tc = cv.take<T>(nblk * kPanelMaxCols * kPanelMaxCols);
-    T *Pg = cv.take<T>((size_t)sgram * kPanelMaxCols * kPanelMaxCols);
-    BlockWs<T> bw = carve_block<T>(cv, (int)nw, smax);
-    if (Tcache == nullptr) {
-        for (size_t b = 0; b < nblk; ++b) {
-            const size_t i = b * nb;
-            const int ib = (int)std::min(nb, k - i);
-            int rc = block_t<T>((int)(nq - i), ib, a + i + i * lda, lda, tau + i, Tc + b * kPanelMaxCols * kPanelMaxCols, kPanelMaxCols, Pg, sgram, st);
-            if (rc) return rc;
-        }
-    }
+    // one region shared by the Gram partials (used first) and the apply workspace
+    const size_t mark = cv.off;
+    T *Pg = cv.take<T>(gram_bytes<T>(nq, nblk, sgram) / sizeof(T));
+    cv.off = mark;
+    int rc;
+    if (Tcache == nullptr && (rc = build_all_t<T>(nq, k, a, lda, tau, Tc, Pg, sgram, st))) return rc;
     const T *Tuse = Tcache ? Tcache : Tc;
+    if (thin) return multq_thin<T>(notran, m, n, k, a, lda, Tuse, c, ldc, cv.take<T>(0), st);
+    BlockWs<T> bw = carve_block<T>(cv, (int)nw, smax);
     const bool forward = (left && !notran) || (!left && notran);
     for (size_t s = 0; s < nblk; ++s) {
         const size_t b = forward ? s : nblk - 1 - s;
@@ -466,7 +560,6 @@ template <class T> int unmqr(const char *side, const char *trans, size_t m, size
         const int ib = (int)std::min(nb, k - i);
         const T *V = a + i + i * lda;
         const T *Tb = Tuse + b * kPanelMaxCols * kPanelMaxCols;
-        int rc;
         if (left) rc = apply_block<T>(true, notran, (int)(m - i), (int)n, ib, V, lda, Tb, kPanelMaxCols, c + i, ldc, bw, st);
         else rc = apply_block<T>(false, notran, (int)m, (int)(n - i), ib, V, lda, Tb, kPanelMaxCols, c + i * ldc, ldc, bw, st);
         if (rc) return rc;
@@ -508,8 +601,9 @@ template <class T> int unm2r(const char *side, const char *trans, size_t m, size
 // ---------------------------------------------------------------------------
 template <class T> int ung2r(size_t m, size_t n, size_t k, T *a, size_t lda, const T *tau, T *work);
 
-template <class T> size_t ungqr_bytes(size_t m, size_t n, int smax, int sgram) {
-    return 2 * t_bytes<T>() + ((size_t)sgram * kPanelMaxCols * kPanelMaxCols * sizeof(T) + 255) / 256 * 256 + block_ws_bytes<T>((int)n, smax);
+template <class T> size_t ungqr_bytes(size_t m, size_t n, size_t k, int smax, int sgram) {
+    const size_t nblk = (k + GpuTuning::nb - 1) / GpuTuning::nb;
+    return (nblk + 1) * t_bytes<T>() + std::max(gram_bytes<T>(m, nblk, sgram), block_ws_bytes<T>((int)n, smax));
 }
 
 template <class T> int ungqr(size_t m, size_t n, size_t k, T *a, size_t lda, const T *tau, size_t *lwork, T *work) {
@@ -521,39 +615,44 @@ template <class T> int ungqr(size_t m, size_t n, size_t k, T *a, size_t lda, con
     if (m > (size_t)INT32_MAX) return -1;
     int smax = smax_for(m), sgram = smax_for(m);
     if (work == nullptr || *lwork == 0) {
-        *lwork = elems_for<T>(ungqr_bytes<T>(m, n, smax, sgram));
+        *lwork = elems_for<T>(ungqr_bytes<T>(m, n, k, smax, sgram));
         return kOk;
     }
     if (a == nullptr) return -4;
     if (tau == nullptr && k > 0) return -6;
-    while ((smax > 1 || sgram > 1) && elems_for<T>(ungqr_bytes<T>(m, n, smax, sgram)) > *lwork) {
+    while ((smax > 1 || sgram > 1) && elems_for<T>(ungqr_bytes<T>(m, n, k, smax, sgram)) > *lwork) {
         smax = std::max(1, smax / 2);
         sgram = std::max(1, sgram / 2);
     }
-    if (elems_for<T>(ungqr_bytes<T>(m, n, smax, sgram)) > *lwork) {
+    if (elems_for<T>(ungqr_bytes<T>(m, n, k, smax, sgram)) > *lwork) {
         if (*lwork < n) return -7;
         return ung2r<T>(m, n, k, a, lda, tau, work);
     }
     cudaStream_t st = current_stream();
     Carver cv(work);
-    T *Tm = cv.take<T>((size_t)kPanelMaxCols * kPanelMaxCols);
+    const size_t nb = GpuTuning::nb;
+    const size_t nblk = (k + nb - 1) / nb;
+    T *Tall = cv.take<T>(nblk * kPanelMaxCols * kPanelMaxCols);
     T *Y = cv.take<T>((size_t)kPanelMaxCols * kPanelMaxCols);
-    T *Pg = cv.take<T>((size_t)sgram * kPanelMaxCols * kPanelMaxCols);
+    // the Gram partials (used first) and the block workspace share one region
+    const size_t mark = cv.off;
+    T *Pg = cv.take<T>(gram_bytes<T>(m, nblk, sgram) / sizeof(T));
+    cv.off = mark;
     BlockWs<T> bw = carve_block<T>(cv, (int)n, smax);
     if (k < n) {
         dim3 grid((unsigned)std::min<size_t>((m + 255) / 256, 1024), (unsigned)std::min<size_t>(n - k, 65535));
         k_identity_cols<T><<<grid, 256, 0, st>>>((int)m, (int)k, (int)n, a, lda);
         RNPGPU_CHECK_LAUNCH();
     }
-    const size_t nb = GpuTuning::nb;
-    const size_t nblk = (k + nb - 1) / nb;
+    // T of every block from the untouched reflectors, before any is overwritten
+    int rc = build_all_t<T>(m, k, a, lda, tau, Tall, Pg, sgram, st);
+    if (rc) return rc;
     for (size_t s = 0; s < nblk; ++s) {
         const size_t b = nblk - 1 - s;
         const size_t i = b * nb;
         const int ib = (int)std::min(nb, k - i);
         T *V = a + i + i * lda;
-        int rc = block_t<T>((int)(m - i), ib, V, lda, tau + i, Tm, kPanelMaxCols, Pg, sgram, st);
-        if (rc) return rc;
+        const T *Tm = Tall + b * kPanelMaxCols * kPanelMaxCols;
         if (i + ib < n) {
             rc = apply_block<T>(true, true, (int)(m - i), (int)(n - i - ib), ib, V, lda, Tm, kPanelMaxCols, a + i + (i + ib) * lda, lda, bw, st);
             if (rc) return rc;

@@ -19,7 +19,7 @@
 namespace rnpgpu {
 
 constexpr int kPanelMaxCols = 32;
-constexpr int kPanelThreads = 256;
+constexpr int kPanelThreads = 512;
 
 template <class T> __device__ __forceinline__ T ldcg(const T *p) { return *(volatile const T *)p; }
 __device__ __forceinline__ double ldcg(const double *p) { return __ldcg(p); }
@@ -38,11 +38,30 @@ template <class T> __device__ __forceinline__ T tone() { return T(1); }
 template <class T> struct ReflScalars {
     T tau, scal;      // scal multiplies x after 'knt' multiplications by rsafmn
     double sr, si;    // scal in FP64
-    float sr_hi, sr_lo, si_hi, si_lo;  // FP32 hi/lo parts of scal (FP32 forms)
+    float sr_hi, sr_lo, si_hi, si_lo;  // FP32 forms: scal = (hi + lo) * 2^sh
+    int sh;
     double beta;      // final beta (already scaled back)
     int knt;
     bool identity;    // tau == 0: H = I, x and alpha untouched
 };
+
+// FP32 hi/lo parts of the FP64 scale factor, with a power-of-two shift when
+// its magnitude leaves [2^-100, 2^100] (columns of extreme magnitude), so
+// that neither part overflows or loses bits in the FP32 range
+template <class T> __device__ __forceinline__ void set_f32_scale(ReflScalars<T> &s, double sr, double si) {
+    const double mx = fmax(fabs(sr), fabs(si));
+    int e = 0;
+    if (mx > 0x1p100 || (mx < 0x1p-100 && mx > 0.0)) {
+        frexp(mx, &e);
+        sr = ldexp(sr, -e);
+        si = ldexp(si, -e);
+    }
+    s.sh = e;
+    s.sr_hi = (float)sr;
+    s.sr_lo = (float)(sr - (double)s.sr_hi);
+    s.si_hi = (float)si;
+    s.si_lo = (float)(si - (double)s.si_hi);
+}
 
 template <class T> __device__ ReflScalars<T> reflector_scalars(T alpha, const NormAcc &nacc) {
     typedef typename Tr<T>::R R;
@@ -57,6 +76,7 @@ template <class T> __device__ ReflScalars<T> reflector_scalars(T alpha, const No
         s.sr = 1.0;
         s.si = 0.0;
         s.sr_hi = 1.0f; s.sr_lo = 0.0f; s.si_hi = 0.0f; s.si_lo = 0.0f;
+        s.sh = 0;
         s.beta = ar;
         return s;
     }
@@ -101,10 +121,7 @@ template <class T> __device__ ReflScalars<T> reflector_scalars(T alpha, const No
     s.scal = Tr<T>::make((R)sr, (R)si);
     s.sr = sr;
     s.si = si;
-    s.sr_hi = (float)sr;
-    s.sr_lo = (float)(sr - (double)s.sr_hi);
-    s.si_hi = (float)si;
-    s.si_lo = (float)(si - (double)s.si_hi);
+    set_f32_scale(s, sr, si);
     if (s.knt) {
         const double safmin = 0x1p-1022 / (2.0 * 0x1p-52);
         for (int q = 0; q < s.knt; ++q) beta *= safmin;
@@ -122,12 +139,66 @@ template <class T> __device__ __forceinline__ T scale_x(T x, const ReflScalars<T
     return x * s.scal;
 }
 // FP32 types: v = x/(alpha-beta) with the FP64 scale factor applied as an
-// FP32 hi + lo pair (FP32 pipe; within an ulp of the FP64 product rounded)
-__device__ __forceinline__ float scale_x(float x, const ReflScalars<float> &s) { return fmaf(x, s.sr_lo, x * s.sr_hi); }
+// FP32 hi + lo pair (FP32 pipe; within an ulp of the FP64 product rounded),
+// then the power-of-two shift in two exact steps
+__device__ __forceinline__ float pow2f(int e) { return __int_as_float((e + 127) << 23); }  // |e| <= 126
+__device__ __forceinline__ float shift_f32(float v, int sh) {
+    if (sh == 0) return v;
+    const int h = sh / 2;
+    return (v * pow2f(h)) * pow2f(sh - h);
+}
+// (an upward shift goes first, so that tiny x are scaled out of the
+// subnormal range before the product; a downward one last)
+__device__ __forceinline__ float scale_x(float x, const ReflScalars<float> &s) {
+    if (s.sh > 0) x = shift_f32(x, s.sh);
+    const float v = fmaf(x, s.sr_lo, x * s.sr_hi);
+    return s.sh < 0 ? shift_f32(v, s.sh) : v;
+}
 __device__ __forceinline__ cf32 scale_x(cf32 x, const ReflScalars<cf32> &s) {
+    if (s.sh > 0) x = cf32(shift_f32(x.x, s.sh), shift_f32(x.y, s.sh));
     const float re = fmaf(x.x, s.sr_lo, x.x * s.sr_hi) - fmaf(x.y, s.si_lo, x.y * s.si_hi);
     const float im = fmaf(x.x, s.si_lo, x.x * s.si_hi) + fmaf(x.y, s.sr_lo, x.y * s.sr_hi);
-    return cf32(re, im);
+    return s.sh < 0 ? cf32(shift_f32(re, s.sh), shift_f32(im, s.sh)) : cf32(re, im);
+}
+
+// FP32 data: the reflector scalars from alpha and the squared norm n2 of x
+// (FP64).  Squares of FP32 magnitudes neither overflow nor underflow in FP64,
+// so beta = -sign(Re alpha) sqrt(|alpha|^2 + n2) needs no scaling, and
+// 1/beta and 1/(alpha - beta) come from one FP64 division:
+//   inv = 1/(beta |alpha - beta|^2),  1/beta = |alpha - beta|^2 inv,
+//   1/(alpha - beta) = conj(alpha - beta) beta inv.
+template <class T> __device__ ReflScalars<T> reflector_scalars_sq(T alpha, double n2) {
+    typedef typename Tr<T>::R R;
+    ReflScalars<T> s;
+    const double ar = (double)Tr<T>::re(alpha), ai = (double)Tr<T>::im(alpha);
+    s.knt = 0;
+    if (n2 == 0.0 && ai == 0.0) {
+        s.identity = true;
+        s.tau = T(0);
+        s.scal = T(1);
+        s.sr = 1.0;
+        s.si = 0.0;
+        s.sr_hi = 1.0f; s.sr_lo = 0.0f; s.si_hi = 0.0f; s.si_lo = 0.0f;
+        s.sh = 0;
+        s.beta = ar;
+        return s;
+    }
+    s.identity = false;
+    double beta = sqrt(fma(ar, ar, fma(ai, ai, n2)));
+    if (ar > 0.0) beta = -beta;
+    const double dr = ar - beta;
+    const double z2 = fma(dr, dr, ai * ai);
+    const double inv = 1.0 / (beta * z2);
+    const double rb = z2 * inv, rz = beta * inv;
+    const double tr = (beta - ar) * rb, ti = -ai * rb;
+    const double sr = dr * rz, si = -ai * rz;
+    s.tau = Tr<T>::make((R)tr, (R)ti);
+    s.scal = Tr<T>::make((R)sr, (R)si);
+    s.sr = sr;
+    s.si = si;
+    set_f32_scale(s, sr, si);
+    s.beta = beta;
+    return s;
 }
 
 // ---------------------------------------------------------------------------
@@ -135,27 +206,33 @@ __device__ __forceinline__ cf32 scale_x(cf32 x, const ReflScalars<cf32> &s) {
 // Rows [b*R, min(M,(b+1)*R)) of the panel belong to block b.  One grid
 // barrier per column j: after it every block holds the combined partial sums
 // of the previous phase and
-//   1. applies H[j-1]^H (tau[j-1], v[j-1], w[j-1] = v^H A) to its rows of the
-//      panel columns right of j-1; block 0 extends T by column j-1;
-//   2. forms ||x|| of column j below the diagonal by downdating
+//   1. (thread 0) forms ||x|| of column j below the diagonal by downdating
 //      ||a - c v||^2 = s1 - 2 Re(c conj(s2)) + |c|^2 s3  (c = conj(tau) w_j)
-//      from sums gathered in the previous phase; when that would cancel
-//      (result < delta * s1) or the column holds magnitudes outside the safe
-//      squaring range, an extra barrier recomputes the norm exactly with the
-//      three-accumulator scheme;
-//   3. forms beta/tau/1/(alpha-beta) identically in every block (FP64) and
-//      scales its rows of x into v;
+//      from the sums gathered in the previous phase, and from it beta, tau
+//      and 1/(alpha-beta) (FP64, identical in every block); when the
+//      downdating would cancel (result < delta * s1) or the column holds
+//      magnitudes outside the safe squaring range, an extra barrier
+//      recomputes the norm exactly with the three-accumulator scheme;
+//   2. (all threads, meanwhile) applies H[j-1]^H (tau[j-1], v[j-1],
+//      w[j-1] = v^H A) to its rows of the panel columns right of j-1;
+//   3. scales its rows of x into v;
 //   4. accumulates over its rows w_c = v^H A[:,c] (c > j), the Gram column
 //      g_c = V[:,c]^H v (c < j) and the downdating sums of column j+1, and
-//      writes them into the partial record of the next phase.
+//      writes them into the partial record of the next phase; after the
+//      barrier block 0 extends T by column j from the Gram column.
+// FP32 panels accumulate the downdating sums error-free in FP32 (hi + lo
+// pairs, about 2^-48 relative) and keep the FP64 pipe to thread 0.
 // Records are double-buffered by phase parity and combined by all threads in
-// a fixed order: the result is deterministic for a given grid size.
+// a fixed order with all loads of a thread in flight at once: the result is
+// deterministic for a given grid size.
 // ---------------------------------------------------------------------------
 constexpr int kRecT = kPanelMaxCols + 2;  // w/g[32], alpha of the next column, v at its row
 constexpr int kRecD = 6;                  // s1, s3, unsafe, Re s2, Im s2 | exact: sml, med, big
 template <class T> struct PanelRec {
     T v[kRecT];
-    double d[kRecD];
+    double d[kRecD];  // FP64 sums (FP64 data, and exact norms of every type)
+    float fh[kRecD];  // FP32 data: the downdating sums as hi + lo pairs
+    float fl[kRecD];
 };
 
 template <class T> struct PanelArgs {
@@ -177,6 +254,21 @@ template <class R> __device__ __forceinline__ double re_of(cplx<R> v) { return v
 __device__ __forceinline__ double im_of(double) { return 0.0; }
 __device__ __forceinline__ double im_of(float) { return 0.0; }
 template <class R> __device__ __forceinline__ double im_of(cplx<R> v) { return v.y; }
+__device__ __forceinline__ float re_f(float v) { return v; }
+__device__ __forceinline__ float re_f(cf32 v) { return v.x; }
+__device__ __forceinline__ float im_f(float) { return 0.f; }
+__device__ __forceinline__ float im_f(cf32 v) { return v.y; }
+template <class T> __device__ __forceinline__ float re_f(T v) { return (float)re_of(v); }
+template <class T> __device__ __forceinline__ float im_f(T v) { return (float)im_of(v); }
+
+// pairwise sum of N values in a fixed order
+template <class U, int N> __device__ __forceinline__ U tree_sum(U (&v)[N]) {
+#pragma unroll
+    for (int w = N / 2; w >= 1; w /= 2)
+#pragma unroll
+        for (int i = 0; i < w; ++i) v[i] = v[i] + v[i + w];
+    return v[0];
+}
 
 // SMEM = true: the block's rows of the panel live in dynamic shared memory
 // for the whole launch (loaded once, written back at the end); SMEM = false:
@@ -184,10 +276,13 @@ template <class R> __device__ __forceinline__ double im_of(cplx<R> v) { return v
 // shared memory).
 template <class T, bool SMEM> __global__ void __launch_bounds__(kPanelThreads) k_panel(PanelArgs<T> p) {
     typedef typename Tr<T>::R R;
-    const bool is64 = sizeof(R) == 8;
+    constexpr bool is64 = sizeof(R) == 8;
+    constexpr int nwarps = kPanelThreads / 32;
+    constexpr int kSlots = kRecT + kRecD;            // one thread per record entry ...
+    constexpr int kGroups = kPanelThreads / kSlots;  // ... and kGroups subsets of the records
+    constexpr int UNR = (sizeof(T) <= 4) ? 32 : (sizeof(T) <= 8 ? 16 : 8);
     const double delta = is64 ? 0.5 : 1e-4;
     const int G = gridDim.x, b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int nwarps = kPanelThreads / 32;
     const int r0 = b * p.rows_per_cta;
     const int r1 = min(p.M, r0 + p.rows_per_cta);
     const size_t lda = p.lda;
@@ -195,13 +290,16 @@ template <class T, bool SMEM> __global__ void __launch_bounds__(kPanelThreads) k
     GridBarrier bar{p.counter, p.err, (unsigned)G, 0u};
 
     __shared__ T s_T[kPanelMaxCols][kPanelMaxCols + 1];
-    __shared__ T s_w[kPanelMaxCols];   // w of the reflector to apply next
     __shared__ T s_cv[kRecT];          // combined record
-    __shared__ double s_cd[kRecD];
-    __shared__ T s_pv[6][kRecT];
-    __shared__ double s_pd[6][kRecD];
-    __shared__ double s_red[kPanelThreads / 32][6];
+    __shared__ double s_cd[kRecD];     // combined FP64 sums
+    __shared__ float s_ch[kRecD], s_cl[kRecD];  // combined FP32 pair sums
+    __shared__ T s_pv[kGroups][kRecT];
+    __shared__ double s_pd[kGroups][kRecD];
+    __shared__ float s_ph[kGroups][kRecD], s_pl[kGroups][kRecD];
+    __shared__ double s_red[nwarps][6];
+    __shared__ float s_rh[nwarps][6], s_rl[nwarps][6];
     __shared__ ReflScalars<T> s_refl;
+    __shared__ int s_exact;
     extern __shared__ __align__(16) unsigned char s_dyn[];
     T *sP = reinterpret_cast<T *>(s_dyn);
     const int ldp = p.rows_per_cta;
@@ -217,46 +315,78 @@ template <class T, bool SMEM> __global__ void __launch_bounds__(kPanelThreads) k
 
     int phase = 0;  // records of phase k live in buffer k & 1
     auto my_rec = [&]() -> PanelRec<T> & { return p.rec[(size_t)(phase & 1) * G + b]; };
-    // combine the records of the current phase into s_cv / s_cd (all threads)
-    auto combine = [&]() {
-        const int nslot = kRecT + kRecD;
-        const int slot = tid % nslot, grp = tid / nslot;
+    // combine the records of the current phase into s_cv and s_cd (FP64
+    // sums) or s_ch/s_cl (FP32 pair sums)
+    auto combine = [&](bool pairs) {
+        const int slot = tid % kSlots, grp = tid / kSlots;
         const PanelRec<T> *rb = p.rec + (size_t)(phase & 1) * G;
-        // eight independent loads in flight per thread (fixed summation order)
-        if (grp < 6) {
+        if (grp < kGroups) {
             if (slot < kRecT) {
-                T a[8];
+                T a = T(0);
+                for (int base = grp; base < G; base += UNR * kGroups) {
+                    T v[UNR];
 #pragma unroll
-                for (int u = 0; u < 8; ++u) a[u] = T(0);
-                int q = grp;
-                for (; q + 42 < G; q += 48) {
-#pragma unroll
-                    for (int u = 0; u < 8; ++u) a[u] = a[u] + ldcg(&rb[q + 6 * u].v[slot]);
+                    for (int u = 0; u < UNR; ++u) {
+                        const int q = base + u * kGroups;
+                        v[u] = (q < G) ? ldcg(&rb[q].v[slot]) : T(0);
+                    }
+                    a = a + tree_sum(v);
                 }
-                for (int u = 0; q < G; q += 6, ++u) a[u & 7] = a[u & 7] + ldcg(&rb[q].v[slot]);
-                s_pv[grp][slot] = ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7]));
+                s_pv[grp][slot] = a;
+            } else if (pairs) {
+                const int d = slot - kRecT;
+                float h = 0.f, l = 0.f;
+                for (int base = grp; base < G; base += 16 * kGroups) {
+                    float vh[16], vl[16];
+#pragma unroll
+                    for (int u = 0; u < 16; ++u) {
+                        const int q = base + u * kGroups;
+                        vh[u] = (q < G) ? __ldcg(&rb[q].fh[d]) : 0.f;
+                        vl[u] = (q < G) ? __ldcg(&rb[q].fl[d]) : 0.f;
+                    }
+#pragma unroll
+                    for (int u = 0; u < 16; ++u) {
+                        df_add(h, l, vh[u]);
+                        l += vl[u];
+                    }
+                }
+                s_ph[grp][d] = h;
+                s_pl[grp][d] = l;
             } else {
-                double a[8];
+                const int d = slot - kRecT;
+                double a = 0.0;
+                for (int base = grp; base < G; base += 16 * kGroups) {
+                    double v[16];
 #pragma unroll
-                for (int u = 0; u < 8; ++u) a[u] = 0.0;
-                int q = grp;
-                for (; q + 42 < G; q += 48) {
-#pragma unroll
-                    for (int u = 0; u < 8; ++u) a[u] += __ldcg(&rb[q + 6 * u].d[slot - kRecT]);
+                    for (int u = 0; u < 16; ++u) {
+                        const int q = base + u * kGroups;
+                        v[u] = (q < G) ? __ldcg(&rb[q].d[d]) : 0.0;
+                    }
+                    a += tree_sum(v);
                 }
-                for (int u = 0; q < G; q += 6, ++u) a[u & 7] += __ldcg(&rb[q].d[slot - kRecT]);
-                s_pd[grp][slot - kRecT] = ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7]));
+                s_pd[grp][d] = a;
             }
         }
         __syncthreads();
         if (tid < kRecT) {
             T a = s_pv[0][tid];
-            for (int g = 1; g < 6; ++g) a = a + s_pv[g][tid];
+            for (int g = 1; g < kGroups; ++g) a = a + s_pv[g][tid];
             s_cv[tid] = a;
-        } else if (tid < kRecT + kRecD) {
-            double a = s_pd[0][tid - kRecT];
-            for (int g = 1; g < 6; ++g) a += s_pd[g][tid - kRecT];
-            s_cd[tid - kRecT] = a;
+        } else if (tid < kSlots) {
+            const int d = tid - kRecT;
+            if (pairs) {
+                float h = s_ph[0][d], l = s_pl[0][d];
+                for (int g = 1; g < kGroups; ++g) {
+                    df_add(h, l, s_ph[g][d]);
+                    l += s_pl[g][d];
+                }
+                s_ch[d] = h;
+                s_cl[d] = l;
+            } else {
+                double a = s_pd[0][d];
+                for (int g = 1; g < kGroups; ++g) a += s_pd[g][d];
+                s_cd[d] = a;
+            }
         }
         __syncthreads();
     };
@@ -282,63 +412,84 @@ template <class T, bool SMEM> __global__ void __launch_bounds__(kPanelThreads) k
             rc.d[tid] = t;
         }
     };
-    auto exact_norm = [&](NormAcc &nacc, T &alpha) {
-        nacc.sml = s_cd[0];
-        nacc.med = s_cd[1];
-        nacc.big = s_cd[2];
-        alpha = s_cv[kPanelMaxCols];
+    // thread 0: reflector scalars from the combined exact record
+    auto scalars_from_exact = [&]() {
+        if (tid == 0) {
+            NormAcc nacc;
+            nacc.sml = s_cd[0];
+            nacc.med = s_cd[1];
+            nacc.big = s_cd[2];
+            s_refl = reflector_scalars<T>(s_cv[kPanelMaxCols], nacc);
+        }
+        __syncthreads();
     };
 
     // prologue: exact norm of column 0
     exact_record(0);
     if (!bar.sync()) return;
-    combine();
-    NormAcc nacc;
-    T alpha;
-    exact_norm(nacc, alpha);
+    combine(false);
+    scalars_from_exact();
     ReflScalars<T> prev;
     prev.identity = true;
     prev.tau = T(0);
 
     for (int j = 0; j < p.N; ++j) {
         if (j > 0) {
-            // 1. apply H[j-1]^H to own rows r >= j-1 of columns j..N-1
+            // 1. thread 0: downdated norm of column j and its reflector scalars
+            if (tid == 0) {
+                double s1, s3, unsafe, s2r, s2i;
+                if (is64) {
+                    s1 = s_cd[0]; s3 = s_cd[1]; unsafe = s_cd[2]; s2r = s_cd[3]; s2i = s_cd[4];
+                } else {
+                    s1 = (double)s_ch[0] + (double)s_cl[0];
+                    s3 = (double)s_ch[1] + (double)s_cl[1];
+                    unsafe = (double)s_ch[2];
+                    s2r = (double)s_ch[3] + (double)s_cl[3];
+                    s2i = (double)s_ch[4] + (double)s_cl[4];
+                }
+                const T a_pre = s_cv[kPanelMaxCols], vn = s_cv[kPanelMaxCols + 1];
+                double n2 = s1;
+                T alpha = a_pre;
+                if (!prev.identity) {
+                    const T ctau = Tr<T>::conj(prev.tau);
+                    const T wj = s_cv[j];
+                    alpha = fmac(-(ctau * vn), wj, a_pre);
+                    const T c = ctau * wj;
+                    const double cr = re_of(c), ci = im_of(c);
+                    // Re(c * conj(s2)) = cr*s2r + ci*s2i
+                    n2 = s1 - 2.0 * (cr * s2r + ci * s2i) + (cr * cr + ci * ci) * s3;
+                }
+                const int exact = (unsafe != 0.0 || !(n2 >= delta * s1) || !(n2 < 1e300)) ? 1 : 0;
+                s_exact = exact;
+                if (!exact) {
+                    if (is64) {
+                        NormAcc nacc;
+                        nacc.zero();
+                        nacc.med = n2;
+                        s_refl = reflector_scalars<T>(alpha, nacc);
+                    } else {
+                        s_refl = reflector_scalars_sq<T>(alpha, n2);
+                    }
+                }
+            }
+            // 2. apply H[j-1]^H to own rows r >= j-1 of columns j..N-1
             if (!prev.identity) {
                 const T ctau = Tr<T>::conj(prev.tau);
                 for (int r = max(r0, j - 1) + tid; r < r1; r += kPanelThreads) {
                     const T v = (r == j - 1) ? T(1) : at(r, j - 1);
                     const T cv = ctau * v;
-                    for (int c = j; c < p.N; ++c) at(r, c) = fmac(-cv, s_w[c], at(r, c));
+                    for (int c = j; c < p.N; ++c) at(r, c) = fmac(-cv, s_cv[c], at(r, c));
                 }
             }
-            // 2. norm of column j by downdating, exact when that is unsafe
-            const double s1 = s_cd[0], s3 = s_cd[1], unsafe = s_cd[2];
-            const T a_pre = s_cv[kPanelMaxCols], vn = s_cv[kPanelMaxCols + 1];
-            double n2 = s1;
-            alpha = a_pre;
-            if (!prev.identity) {
-                const T ctau = Tr<T>::conj(prev.tau);
-                const T wj = s_w[j];
-                alpha = fmac(-(ctau * vn), wj, a_pre);
-                const T c = ctau * wj;
-                const double cr = re_of(c), ci = im_of(c);
-                // Re(c * conj(s2)) = cr*s2r + ci*s2i
-                n2 = s1 - 2.0 * (cr * s_cd[3] + ci * s_cd[4]) + (cr * cr + ci * ci) * s3;
-            }
             __syncthreads();
-            if (unsafe != 0.0 || !(n2 >= delta * s1) || !(n2 < 1e300)) {
+            if (s_exact) {
                 exact_record(j);
                 if (!bar.sync()) return;
-                combine();
-                exact_norm(nacc, alpha);
-            } else {
-                nacc.zero();
-                nacc.med = n2;
+                combine(false);
+                scalars_from_exact();
             }
         }
-        // 3. reflector scalars, identical in every block
-        if (tid == 0) s_refl = reflector_scalars<T>(alpha, nacc);
-        __syncthreads();
+        // 3. scale x into v
         const ReflScalars<T> rs = s_refl;
         if (!rs.identity) {
             for (int r = max(r0, j + 1) + tid; r < r1; r += kPanelThreads) at(r, j) = scale_x(at(r, j), rs);
@@ -362,9 +513,9 @@ template <class T, bool SMEM> __global__ void __launch_bounds__(kPanelThreads) k
             if (lane == 0) rc.v[c] = acc;
         }
         for (int c = p.N + tid; c < kPanelMaxCols; c += kPanelThreads) rc.v[c] = T(0);
-        double e1 = 0.0, e3 = 0.0, eu = 0.0, e2r = 0.0, e2i = 0.0;
         T anext = T(0), vnext = T(0);
         if (is64) {
+            double e1 = 0.0, e3 = 0.0, eu = 0.0, e2r = 0.0, e2i = 0.0;
             if (j + 1 < p.N) {
                 const double tsml = 0x1p-511, tbig = 0x1p486;
                 for (int r = max(r0, j + 2) + tid; r < r1; r += kPanelThreads) {
@@ -384,19 +535,28 @@ template <class T, bool SMEM> __global__ void __launch_bounds__(kPanelThreads) k
             eu = warp_sum(eu);
             e2r = warp_sum(e2r);
             e2i = warp_sum(e2i);
+            if (lane == 0) {
+                s_red[warp][0] = e1;
+                s_red[warp][1] = e3;
+                s_red[warp][2] = eu;
+                s_red[warp][3] = e2r;
+                s_red[warp][4] = e2i;
+            }
         } else {
-            // FP32 data: error-free FP32 accumulation, converted to FP64 once
-            // per warp (FP32 magnitudes never need the range checks)
-            float h1 = 0.f, l1 = 0.f, h3 = 0.f, l3 = 0.f, h2r = 0.f, l2r = 0.f, h2i = 0.f, l2i = 0.f;
+            // FP32 data: error-free FP32 accumulation; magnitudes outside
+            // [2^-40, 2^48] (squares that could leave the FP32 range or lose
+            // their low parts) send the column to the exact FP64 norm
+            float h1 = 0.f, l1 = 0.f, h3 = 0.f, l3 = 0.f, h2r = 0.f, l2r = 0.f, h2i = 0.f, l2i = 0.f, eu = 0.f;
             if (j + 1 < p.N) {
                 for (int r = max(r0, j + 2) + tid; r < r1; r += kPanelThreads) {
                     const T a = at(r, j + 1), v = at(r, j);
-                    const float ar = (float)re_of(a), vr = (float)re_of(v);
+                    const float ar = re_f(a), vr = re_f(v), ai = im_f(a), vi = im_f(v);
+                    const float m = fmaxf(fabsf(ar), fabsf(ai));
+                    if (m > 0x1p48f || (m < 0x1p-40f && m != 0.f)) eu = 1.f;
                     df_add_prod(h1, l1, ar, ar);
                     df_add_prod(h3, l3, vr, vr);
                     df_add_prod(h2r, l2r, vr, ar);
                     if (Tr<T>::is_complex) {
-                        const float ai = (float)im_of(a), vi = (float)im_of(v);
                         df_add_prod(h1, l1, ai, ai);
                         df_add_prod(h3, l3, vi, vi);
                         df_add_prod(h2r, l2r, vi, ai);
@@ -409,41 +569,49 @@ template <class T, bool SMEM> __global__ void __launch_bounds__(kPanelThreads) k
             df_warp_sum(h3, l3);
             df_warp_sum(h2r, l2r);
             if (Tr<T>::is_complex) df_warp_sum(h2i, l2i);
+            eu = warp_sum(eu);
             if (lane == 0) {
-                e1 = (double)h1 + (double)l1;
-                e3 = (double)h3 + (double)l3;
-                e2r = (double)h2r + (double)l2r;
-                e2i = (double)h2i + (double)l2i;
+                s_rh[warp][0] = h1; s_rl[warp][0] = l1;
+                s_rh[warp][1] = h3; s_rl[warp][1] = l3;
+                s_rh[warp][2] = eu; s_rl[warp][2] = 0.f;
+                s_rh[warp][3] = h2r; s_rl[warp][3] = l2r;
+                s_rh[warp][4] = h2i; s_rl[warp][4] = l2i;
             }
         }
         if (j + 1 < p.N && j + 1 >= r0 && j + 1 < r1 && tid == 0) {
             anext = at(j + 1, j + 1);
             vnext = at(j + 1, j);
         }
-        if (lane == 0) {
-            s_red[warp][0] = e1;
-            s_red[warp][1] = e3;
-            s_red[warp][2] = eu;
-            s_red[warp][3] = e2r;
-            s_red[warp][4] = e2i;
-        }
         __syncthreads();
         if (tid < 5) {
-            double t = 0.0;
-            for (int w = 0; w < nwarps; ++w) t += s_red[w][tid];
-            rc.d[tid] = t;
+            if (is64) {
+                double t = 0.0;
+                for (int w = 0; w < nwarps; ++w) t += s_red[w][tid];
+                rc.d[tid] = t;
+            } else {
+                float h = s_rh[0][tid], l = s_rl[0][tid];
+                for (int w = 1; w < nwarps; ++w) {
+                    df_add(h, l, s_rh[w][tid]);
+                    l += s_rl[w][tid];
+                }
+                rc.fh[tid] = h;
+                rc.fl[tid] = l;
+            }
         }
-        if (tid == 5) rc.d[5] = 0.0;
+        if (tid == 5) {
+            rc.d[5] = 0.0;
+            rc.fh[5] = 0.f;
+            rc.fl[5] = 0.f;
+        }
         if (tid == 0) {
             rc.v[kPanelMaxCols] = anext;
             rc.v[kPanelMaxCols + 1] = vnext;
         }
         if (!bar.sync()) return;
-        combine();
-        // w of H[j] for the next step; T column j from the Gram column (block 0)
-        if (tid < kPanelMaxCols) s_w[tid] = s_cv[tid];
+        combine(!is64);
+        // T column j from the Gram column (block 0):
+        // T(0:j, j) = -tau_j * T(0:j, 0:j) * g(0:j);  T(j, j) = tau_j
         if (b == 0) {
-            // T(0:j, j) = -tau_j * T(0:j, 0:j) * g(0:j);  T(j, j) = tau_j
             if (tid < j) {
                 T acc = T(0);
                 for (int l = tid; l < j; ++l) acc = fmac(s_T[tid][l], s_cv[l], acc);
@@ -452,8 +620,8 @@ template <class T, bool SMEM> __global__ void __launch_bounds__(kPanelThreads) k
             if (tid == 0) s_T[j][j] = rs.tau;
         }
         prev = rs;
-        __syncthreads();
     }
+    __syncthreads();
     if (SMEM) {
         for (int c = 0; c < p.N; ++c)
             for (int r = r0 + tid; r < r1; r += kPanelThreads) A[r + (size_t)c * lda] = sP[(size_t)c * ldp + (r - r0)];

@@ -204,6 +204,14 @@ __device__ __forceinline__ void df_warp_sum(float &hi, float &lo) {
     }
 }
 
+// Asynchronous global -> shared copies (cp.async, 4/8/16 bytes, cached in
+// L1); both addresses aligned to the copy size.
+template <int BYTES> __device__ __forceinline__ void cp_async(void *smem_dst, const void *gsrc) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"((uint32_t)__cvta_generic_to_shared(smem_dst)), "l"(gsrc), "n"(BYTES) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 // 1/(a+ib) by Smith's algorithm (Smith, CACM 5(8), 1962)
 __device__ __forceinline__ void crecip(double a, double b, double &rx, double &ry) {
     if (fabs(b) <= fabs(a)) {

@@ -4,7 +4,8 @@
 // Every FP32 operand element x is split as x = x0 + x1 + x2 with
 // x0 = bf16(x), x1 = bf16(x - x0), x2 = bf16(x - x0 - x1) (Henry, Tang and
 // Heinecke, "Leveraging the bfloat16 artificial intelligence datatype for
-// higher-precision computations", 2019).  The product a*b is formed from the
+// higher-precision computations", 2019); x1 and x2 are stored scaled by 2^8
+// and 2^16 so that they do not underflow for small x.  The product a*b is formed from the
 // six terms of order <= 2^-16 relative, each a BF16 x BF16 MMA.  The three
 // magnitude classes accumulate in separate FP32 accumulators in tensor
 // memory (a0b0 | a0b1 + a1b0 | a0b2 + a1b1 + a2b0), so the low-order bits
@@ -112,11 +113,14 @@ __device__ __forceinline__ uint32_t tile_off(int row, int k) {
     return (uint32_t)(((row >> 3) * (kBK / 8) + (k >> 3)) * 128 + (row & 7) * 16 + (k & 7) * 2);
 }
 
+// x = h0 + 2^-8 h1 + 2^-16 h2: each remainder is scaled up by 2^8 (exactly)
+// before it is rounded, so the low slices stay as far from the bottom of the
+// exponent range as x itself; the accumulator of class c carries 2^(8c)
 __device__ __forceinline__ void split3(float x, __nv_bfloat16 &h0, __nv_bfloat16 &h1, __nv_bfloat16 &h2) {
     h0 = __float2bfloat16_rn(x);
-    float r = x - __bfloat162float(h0);
+    float r = (x - __bfloat162float(h0)) * 256.0f;
     h1 = __float2bfloat16_rn(r);
-    r = r - __bfloat162float(h1);
+    r = (r - __bfloat162float(h1)) * 256.0f;
     h2 = __float2bfloat16_rn(r);
 }
 
@@ -281,7 +285,7 @@ template <int BN> __global__ void __launch_bounds__(kThreads) k_gemm_tc(GemmArgs
                 tmem_ld16(lane_base + BN, mid);
                 tmem_ld16(lane_base + 2 * BN, small);
 #pragma unroll
-                for (int i = 0; i < 16; ++i) v[i] = big[i] + (mid[i] + small[i]);
+                for (int i = 0; i < 16; ++i) v[i] = big[i] + fmaf(small[i], 0x1p-16f, mid[i] * 0x1p-8f);
             } else {
 #pragma unroll
                 for (int i = 0; i < 16; ++i) v[i] = 0.f;

@@ -190,3 +190,55 @@ def test_empty_inputs_are_quick_returns():
     c = gq.empty_colmajor(5, 0, torch.float64)
     gq.mult_q("L", "N", gq.empty_colmajor(5, 2, torch.float64), torch.zeros(2, dtype=torch.float64, device="cuda"), c, 2)
     del a
+
+
+# MultQ on the left with a thin C goes through the one-launch kernel; C's
+# rows are held in shared memory or, when they do not fit, in place.
+THIN = [("d", 3000, 1, 70), ("d", 2000, 16, 256), ("s", 5000, 33, 100), ("z", 40000, 64, 64), ("c", 700, 64, 45), ("z", 129, 7, 129)]
+
+
+@pytest.mark.parametrize("p,m,nrhs,k", THIN)
+def test_mult_q_thin_against_oracle(oracle, p, m, nrhs, k):
+    q = "z" if p == "c" else p
+    vals, _ = oracle.larnv(q, 2, [3, 1, 4, 1], m * k)
+    a = np.asfortranarray(vals.astype(NP[p]).reshape(k, m).T)
+    fac, tau = run_factor(a, p, m, k)
+    cv, _ = oracle.larnv(q, 2, [5, 9, 2, 7], m * nrhs)
+    c0 = np.asfortranarray(cv.astype(NP[p]).reshape(nrhs, m).T)
+    t = torch.from_numpy(np.ascontiguousarray(tau)).cuda()
+    A = to_dev(fac)
+    tol = 1e-12 if p in "dz" else 1e-5
+    for trans in ("N", "C"):
+        co = c0.copy(order="F")
+        oracle.unmqr(p, "L", trans, m, nrhs, k, fac, tau, co)
+        dc = to_dev(c0)
+        gq.mult_q("L", trans, A, t, dc, k)
+        torch.cuda.synchronize()
+        assert rel(from_dev(dc), co) <= tol, trans
+
+
+# FP32 panels sum squares error-free in FP32; columns whose magnitudes leave
+# the safe squaring range take the exact FP64 norm, and the reflector scale
+# factor carries a power-of-two shift at the ends of the FP32 range.
+@pytest.mark.parametrize("p", ["s", "c"])
+@pytest.mark.parametrize("scale", [2.0 ** -120, 2.0 ** -70, 2.0 ** 55, 2.0 ** 100, "mixed"])
+def test_fp32_factor_extreme_magnitudes(oracle, p, scale):
+    m, n = 700, 40
+    q = "z" if p == "c" else p
+    vals, _ = oracle.larnv(q, 2, [7, 7, 7, 7], m * n)
+    hi = np.complex128 if p == "c" else np.float64
+    a64 = np.asfortranarray(vals.astype(hi).reshape(n, m).T)
+    if scale == "mixed":
+        s = 2.0 ** np.linspace(-110, 110, n)
+    else:
+        s = np.full(n, scale)
+    a = np.asfortranarray((a64 * s[None, :]).astype(NP[p]))
+    fac, tau = run_factor(a, p, m, n)
+    assert np.all(np.isfinite(fac)) and np.all(np.isfinite(tau))
+    fo = np.asfortranarray(a.astype(hi))
+    oracle.geqrf("z" if p == "c" else "d", m, n, fo)
+    R, _ = split_factor(fac, m, n)
+    Ro, _ = split_factor(fo, m, n)
+    # compare column by column (columns differ by up to 2^220 in the mixed case)
+    for j in range(n):
+        assert rel(R[:, j], Ro[:, j]) <= 1e-4, j
