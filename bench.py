@@ -218,7 +218,7 @@ def batched_config(torch, dev, gq, lib, peak64, count=20000, loop_sample=200, ch
     a0 = torch.randn(b.a.numel(), generator=g, dtype=torch.float64, device=dev)
     b.a.copy_(a0)
     tune_ms = b.tune()
-    cfg = [b.config(0), b.config(1)]
+    cfg = [b.config(c) for c in range(3)]
     # capture one run in a CUDA graph
     s = torch.cuda.Stream()
     s.wait_stream(torch.cuda.current_stream())
@@ -283,6 +283,122 @@ def batched_config(torch, dev, gq, lib, peak64, count=20000, loop_sample=200, ch
         "speedup_vs_loop": loop_ms_total / ms_batched,
         "r_max_rel_err_vs_oracle": worst, "r_check_sample": check_sample,
     }
+
+
+def batched_ls_problems(torch, dev, count, seed):
+    """C5 inputs: m ~ U[32,512], n ~ U[8,m/2], A = U diag(s) V^H with U, V
+    Householder reflectors of seeded complex Gaussian vectors and s
+    log-uniform on [1e-4, 1] (cond 1e4); b = A x + 1e-10 N(0,1), x N(0,1)."""
+    import numpy as np
+
+    from rnp2_gb300.batched import BatchedLS
+
+    rng = np.random.default_rng(seed)
+    ms = rng.integers(32, 513, count)
+    ns = np.array([rng.integers(8, m // 2 + 1) for m in ms])
+    ls = BatchedLS(ms, ns, torch.complex128, dev)
+    g = torch.Generator(device=dev).manual_seed(seed + 100)
+
+    def cgauss(*shape):
+        return torch.complex(torch.randn(shape, generator=g, dtype=torch.float64, device=dev), torch.randn(shape, generator=g, dtype=torch.float64, device=dev))
+
+    for i in range(count):
+        m, n = int(ms[i]), int(ns[i])
+        s = 10.0 ** (-4.0 * torch.rand(n, generator=g, dtype=torch.float64, device=dev))
+        u, w = cgauss(m), cgauss(n)
+        Vh = torch.eye(n, dtype=torch.complex128, device=dev) - 2.0 * torch.outer(w, w.conj()) / torch.vdot(w, w).real
+        D = torch.zeros((m, n), dtype=torch.complex128, device=dev)
+        D[:n] = s[:, None].to(torch.complex128) * Vh
+        A = D - 2.0 * torch.outer(u, u.conj() @ D) / torch.vdot(u, u).real
+        x = cgauss(n)
+        ls.matrix(i).copy_(A)
+        ls.rhs(i).copy_(A @ x + 1e-10 * cgauss(m))
+    return ls, ms, ns
+
+
+def batched_ls_config(torch, dev, count=4096, check_sample=32):
+    """Batched mixed-precision complex least squares (C5): FP32 complex
+    batched factorization + FP64 refinement per problem, against the batched
+    plain FP64 form, both captured in CUDA graphs."""
+    import numpy as np
+
+    import oracle as orc
+
+    ls, ms, ns = batched_ls_problems(torch, dev, count, 5)
+    tune_ms = ls.tune_mixed()
+    cfg = [ls.config(c) for c in range(3)]
+
+    def graph_time(fn, reps=4):
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(s):
+            fn()
+        torch.cuda.current_stream().wait_stream(s)
+        torch.cuda.synchronize()
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph):
+            fn()
+        ts = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            graph.replay()
+            e1.record()
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return min(ts[1:]), graph
+
+    ms_mixed, _ = graph_time(lambda: ls.solve_mixed())
+    x_mixed = ls.x.clone()
+    iters = ls.iters[:count].cpu().numpy()
+    berr = ls.berr[:count].cpu().numpy()
+    eta = ls.eta[:count].cpu().numpy()
+    bound = 10.0 * ns * 2.0 ** -52
+    # plain FP64 batched form: factor a copy (refreshed outside the timed graph) and solve
+    fa = ls.a.clone()
+    ft = torch.empty(ls.ntau, dtype=torch.complex128, device=dev)
+    ts = []
+    for _ in range(3):
+        fa.copy_(ls.a)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        ls.solve_plain(fa, ft)
+        e1.record()
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    ms_plain = min(ts[1:])
+    x_plain = ls.x.clone()
+    # forward error of a sample against the CPU FP64 oracle (QR least squares)
+    o = orc.load()
+    rng = np.random.default_rng(1)
+    fwd = 0.0
+    for i in rng.choice(count, check_sample, replace=False):
+        i = int(i)
+        m, n = int(ms[i]), int(ns[i])
+        A = np.asfortranarray(ls.matrix(i).cpu().numpy())
+        bb = np.asfortranarray(ls.rhs(i).cpu().numpy().reshape(m, 1))
+        o.gels("z", m, n, 1, A, bb)
+        xo = bb[:n, 0]
+        xg = x_mixed[int(ls.x_off[i]):int(ls.x_off[i]) + n].cpu().numpy()
+        fwd = max(fwd, float(np.linalg.norm(xg - xo) / np.linalg.norm(xo)))
+    flops = float(sum(4.0 * (2.0 * m * n * n - 2.0 * n ** 3 / 3.0) for m, n in zip(ms, ns)))
+    out = {
+        "workload": "batched_ls_4096_c128_m32-512_cond1e4_nrhs1",
+        "solves_per_s": count / (ms_mixed * 1e-3), "ms": ms_mixed,
+        "plain_fp64_solves_per_s": count / (ms_plain * 1e-3), "plain_fp64_ms": ms_plain,
+        "speedup_vs_batched_plain_fp64": ms_plain / ms_mixed,
+        "factor_gflop_real_equivalent": flops / 1e9,
+        "graph_captured": True, "autotune_ms": tune_ms, "class_configs": cfg,
+        "iterations_max": int(iters.max()), "iterations_mean": float(iters.mean()),
+        "backward_error_max": float(berr.max()), "normal_residual_max": float(eta.max()),
+        "problems_within_10n_eps": int(np.sum((berr <= bound) & (eta <= bound))), "problems": count,
+        "forward_error_vs_cpu_fp64_oracle_max": fwd, "forward_check_sample": check_sample,
+        "mixed_vs_plain_x_rel_diff": float(torch.linalg.norm(x_mixed - x_plain) / torch.linalg.norm(x_plain)),
+        "data": "synthetic: A = U diag(s) V^H, U,V Householder reflectors of seeded complex Gaussian vectors, s log-uniform on [1e-4,1]; b = A x + 1e-10 N(0,1)",
+    }
+    del ls, fa
+    return out
 
 
 def other_configs(torch, dev, gq, lib, peak64):
@@ -476,6 +592,7 @@ def gpu_arm(args, rank, world, local):
     others = {} if args.no_configs else other_configs(torch, dev, gq, lib, peak64.value)
     if not args.no_configs:
         others["batched"] = batched_config(torch, dev, gq, lib, peak64.value)
+        others["batched_ls"] = batched_ls_config(torch, dev)
 
     # ---------------- CPU baseline (rank 0) ---------------------------------
     cpu = None

@@ -21,7 +21,7 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2", "--expt-relaxed-constexpr", "-I" + INCLUDE]
 
-UNITS = ["api_context.cu", "qr_s.cu", "qr_d.cu", "qr_c.cu", "qr_z.cu", "qr_noalloc.cu", "batched.cu"]
+UNITS = ["api_context.cu", "qr_s.cu", "qr_d.cu", "qr_c.cu", "qr_z.cu", "qr_noalloc.cu", "batched.cu", "batched_s.cu", "batched_d.cu", "batched_c.cu", "batched_z.cu"]
 
 
 def _nvcc():

@@ -19,27 +19,30 @@ namespace rnpgpu {
 struct BatchDesc {
     long long a_off;    // element offset of the matrix in the packed buffer
     long long tau_off;  // element offset of its tau
+    long long b_off;    // least squares: element offsets of b (m) and x (n)
+    long long x_off;
     int m, n, lda, index;
 };
 
-constexpr int kBatchMaxRows = 256;  // rows of the largest matrix a block stages
-constexpr int kBatchTile = 32;      // trailing-update column tile
+constexpr int kBatchMaxRows = 512;  // rows of the largest matrix a block stages
 
-template <class T, int NB> struct BatchSmem {
-    static constexpr size_t kP = (size_t)kBatchMaxRows * NB;          // panel
-    static constexpr size_t kC = (size_t)kBatchMaxRows * kBatchTile;  // trailing tile
-    static constexpr size_t kW = (size_t)kBatchTile * NB;
+// MR: rows a block stages (the class's largest m); TILE: trailing-update
+// column tile
+template <class T, int NB, int MR, int TILE> struct BatchSmem {
+    static constexpr size_t kP = (size_t)MR * NB;    // panel
+    static constexpr size_t kC = (size_t)MR * TILE;  // trailing tile
+    static constexpr size_t kW = (size_t)TILE * NB;
     static constexpr size_t kBytes = (kP + kC + kW + NB * NB + 2 * NB) * sizeof(T);
 };
 
-template <class T, int NT, int NB>
+template <class T, int NT, int NB, int MR, int TILE>
 __global__ void __launch_bounds__(NT) k_geqrf_batched(const BatchDesc *__restrict__ desc, int count, T *A, T *tau, unsigned *queue) {
     typedef typename Tr<T>::R R;
     extern __shared__ __align__(16) unsigned char s_raw[];
-    typedef BatchSmem<T, NB> L;
-    T *sP = reinterpret_cast<T *>(s_raw);  // panel, column-major, ld kBatchMaxRows
-    T *sC = sP + L::kP;                    // trailing tile, column-major, ld kBatchMaxRows
-    T *sW = sC + L::kC;                    // W (kBatchTile x NB), ld kBatchTile
+    typedef BatchSmem<T, NB, MR, TILE> L;
+    T *sP = reinterpret_cast<T *>(s_raw);  // panel, column-major, ld MR
+    T *sC = sP + L::kP;                    // trailing tile, column-major, ld MR
+    T *sW = sC + L::kC;                    // W (TILE x NB), ld TILE
     T *sT = sW + L::kW;                    // T (NB x NB), ld NB
     T *sG = sT + NB * NB;                  // w / Gram column (NB)
     __shared__ NormAcc s_nacc[NT / 32];
@@ -64,12 +67,12 @@ __global__ void __launch_bounds__(NT) k_geqrf_batched(const BatchDesc *__restric
             // ---- panel into shared memory
             for (int e = tid; e < mp * jb; e += NT) {
                 const int r = e % mp, c = e / mp;
-                sP[c * kBatchMaxRows + r] = a[(j0 + r) + (size_t)(j0 + c) * lda];
+                sP[c * MR + r] = a[(j0 + r) + (size_t)(j0 + c) * lda];
             }
             __syncthreads();
             // ---- factor the panel column by column
             for (int jj = 0; jj < jb; ++jj) {
-                T *col = sP + jj * kBatchMaxRows;
+                T *col = sP + jj * MR;
                 NormAcc acc;
                 acc.zero();
                 for (int r = jj + 1 + tid; r < mp; r += NT) acc.add(col[r]);
@@ -89,7 +92,7 @@ __global__ void __launch_bounds__(NT) k_geqrf_batched(const BatchDesc *__restric
                 // w_c = v^H P[:,c] (c > jj) and Gram g_c = V[:,c]^H v (c < jj), rows >= jj
                 for (int c = warp; c < jb; c += NW) {
                     if (c == jj) continue;
-                    const T *pc = sP + c * kBatchMaxRows;
+                    const T *pc = sP + c * MR;
                     T s = T(0);
                     for (int r = jj + lane; r < mp; r += 32) {
                         const T v = (r == jj) ? T(1) : col[r];
@@ -104,7 +107,7 @@ __global__ void __launch_bounds__(NT) k_geqrf_batched(const BatchDesc *__restric
                     for (int e = tid; e < (mp - jj) * (jb - jj - 1); e += NT) {
                         const int r = jj + e % (mp - jj), c = jj + 1 + e / (mp - jj);
                         const T v = (r == jj) ? T(1) : col[r];
-                        sP[c * kBatchMaxRows + r] = fmac(-(ctau * v), sG[c], sP[c * kBatchMaxRows + r]);
+                        sP[c * MR + r] = fmac(-(ctau * v), sG[c], sP[c * MR + r]);
                     }
                 }
                 // T(0:jj, jj) = -tau T(0:jj, 0:jj) g(0:jj), T(jj, jj) = tau
@@ -123,35 +126,35 @@ __global__ void __launch_bounds__(NT) k_geqrf_batched(const BatchDesc *__restric
             // ---- panel back to global memory
             for (int e = tid; e < mp * jb; e += NT) {
                 const int r = e % mp, c = e / mp;
-                a[(j0 + r) + (size_t)(j0 + c) * lda] = sP[c * kBatchMaxRows + r];
+                a[(j0 + r) + (size_t)(j0 + c) * lda] = sP[c * MR + r];
             }
             // ---- trailing update, one column tile at a time:  C -= V (T^H ... ) : W = C^H V T, C -= V W^H
-            for (int c0 = j0 + jb; c0 < n; c0 += kBatchTile) {
-                const int ct = min(kBatchTile, n - c0);
+            for (int c0 = j0 + jb; c0 < n; c0 += TILE) {
+                const int ct = min(TILE, n - c0);
                 for (int e = tid; e < mp * ct; e += NT) {
                     const int r = e % mp, c = e / mp;
-                    sC[c * kBatchMaxRows + r] = a[(j0 + r) + (size_t)(c0 + c) * lda];
+                    sC[c * MR + r] = a[(j0 + r) + (size_t)(c0 + c) * lda];
                 }
                 __syncthreads();
                 // W(c, l) = sum_r conj(C(r, c)) V(r, l), V unit lower trapezoidal
                 for (int e = tid; e < ct * jb; e += NT) {
                     const int c = e % ct, l = e / ct;
-                    const T *vc = sP + l * kBatchMaxRows;
-                    const T *cc = sC + c * kBatchMaxRows;
+                    const T *vc = sP + l * MR;
+                    const T *cc = sC + c * MR;
                     T s = Tr<T>::conj(cc[l]);
                     for (int r = l + 1; r < mp; ++r) s = fmac(Tr<T>::conj(cc[r]), vc[r], s);
-                    sW[c + l * kBatchTile] = s;
+                    sW[c + l * TILE] = s;
                 }
                 __syncthreads();
                 // W := W T (upper triangular, in place by columns from the right)
                 for (int c = tid; c < ct; c += NT) {
                     T w[NB];
 #pragma unroll
-                    for (int l = 0; l < NB; ++l) w[l] = (l < jb) ? sW[c + l * kBatchTile] : T(0);
+                    for (int l = 0; l < NB; ++l) w[l] = (l < jb) ? sW[c + l * TILE] : T(0);
                     for (int l = jb - 1; l >= 0; --l) {
                         T s = T(0);
                         for (int q = 0; q <= l; ++q) s = fmac(w[q], sT[q + l * NB], s);
-                        sW[c + l * kBatchTile] = s;
+                        sW[c + l * TILE] = s;
                     }
                 }
                 __syncthreads();
@@ -159,18 +162,18 @@ __global__ void __launch_bounds__(NT) k_geqrf_batched(const BatchDesc *__restric
                 for (int r = tid; r < mp; r += NT) {
                     T v[NB];
 #pragma unroll
-                    for (int l = 0; l < NB; ++l) v[l] = (l < jb && r >= l) ? (r == l ? T(1) : sP[l * kBatchMaxRows + r]) : T(0);
+                    for (int l = 0; l < NB; ++l) v[l] = (l < jb && r >= l) ? (r == l ? T(1) : sP[l * MR + r]) : T(0);
                     for (int c = 0; c < ct; ++c) {
-                        T s = sC[c * kBatchMaxRows + r];
+                        T s = sC[c * MR + r];
 #pragma unroll
-                        for (int l = 0; l < NB; ++l) s = fmac(-v[l], Tr<T>::conj(sW[c + l * kBatchTile]), s);
-                        sC[c * kBatchMaxRows + r] = s;
+                        for (int l = 0; l < NB; ++l) s = fmac(-v[l], Tr<T>::conj(sW[c + l * TILE]), s);
+                        sC[c * MR + r] = s;
                     }
                 }
                 __syncthreads();
                 for (int e = tid; e < mp * ct; e += NT) {
                     const int r = e % mp, c = e / mp;
-                    a[(j0 + r) + (size_t)(c0 + c) * lda] = sC[c * kBatchMaxRows + r];
+                    a[(j0 + r) + (size_t)(c0 + c) * lda] = sC[c * MR + r];
                 }
                 __syncthreads();
             }

@@ -1,6 +1,9 @@
 """Batched QR: every matrix of an uneven batch must match the oracle's
 Factor (R, V and tau), across size classes, block shapes chosen by the
-autotuner, and when the run is captured into a CUDA graph and replayed."""
+autotuner, and when the run is captured into a CUDA graph and replayed.
+Batched least squares: the plain solve matches the oracle's QR least squares
+per problem; the mixed solve (FP32 factorization, FP64 refinement) reaches
+FP64-level backward error on every problem."""
 import numpy as np
 import pytest
 
@@ -12,18 +15,18 @@ torch = pytest.importorskip("torch")
 if not torch.cuda.is_available():
     pytest.skip("no CUDA device", allow_module_level=True)
 
-from rnp2_gb300.batched import BatchedQR  # noqa: E402
+from rnp2_gb300.batched import BatchedLS, BatchedQR  # noqa: E402
 
 NP = {torch.float32: np.float32, torch.float64: np.float64, torch.complex64: np.complex64, torch.complex128: np.complex128}
 PFX = {torch.float32: "s", torch.float64: "d", torch.complex64: "c", torch.complex128: "z"}
 
 
-def make_batch(count, dtype, seed=0, mmax=256):
+def make_batch(count, dtype, seed=0, mmax=512):
     rng = np.random.default_rng(seed)
     ms = rng.integers(16, mmax + 1, count)
-    ns = np.array([rng.integers(8, m + 1) for m in ms])
-    ms[:3] = [1, 256, 40]
-    ns[:3] = [1, 256, 200]
+    ns = np.array([rng.integers(8, min(m, 300) + 1) for m in ms])
+    ms[:5] = [1, 256, 40, 512, 65]
+    ns[:5] = [1, 256, 200, 300, 64]
     b = BatchedQR(ms, ns, dtype)
     vals = []
     for i in range(count):
@@ -62,8 +65,8 @@ def test_batched_autotuned_and_graph_replayed(oracle):
     b, vals = make_batch(200, dtype, seed=2)
     a0 = b.a.clone()
     b.tune()
-    cfg = [b.config(0), b.config(1)]
-    assert cfg[0]["count"] + cfg[1]["count"] == 200
+    cfg = [b.config(c) for c in range(3)]
+    assert sum(c["count"] for c in cfg) == 200 and all(c["count"] > 0 for c in cfg)
     # capture one run into a CUDA graph, replay it twice on fresh inputs
     s = torch.cuda.Stream()
     s.wait_stream(torch.cuda.current_stream())
@@ -80,3 +83,107 @@ def test_batched_autotuned_and_graph_replayed(oracle):
         g.replay()
     torch.cuda.synchronize()
     check(b, vals, oracle, dtype)
+
+
+def ls_problems(count, dtype, seed, cond=1e4, mmax=512, noise=1e-10):
+    """A = U diag(s) V^H (U, V Householder reflectors of Gaussian vectors, s
+    log-uniform on [1/cond, 1]), b = A x + noise N(0,1)."""
+    rng = np.random.default_rng(seed)
+    ms = rng.integers(32, mmax + 1, count)
+    ns = np.array([rng.integers(8, m // 2 + 1) for m in ms])
+    ms[:3] = [32, 512, 33]
+    ns[:3] = [8, 256, 33]
+    cplx = dtype.is_complex
+
+    def gauss(*shape):
+        x = rng.standard_normal(shape)
+        return x + 1j * rng.standard_normal(shape) if cplx else x
+
+    probs = []
+    for m, n in zip(ms, ns):
+        s = 10.0 ** (-np.log10(cond) * rng.random(n))
+        u = gauss(m)
+        w = gauss(n)
+        V = np.eye(n) - 2.0 * np.outer(w, w.conj()) / np.vdot(w, w).real
+        D = np.zeros((m, n), dtype=complex if cplx else float)
+        D[:n] = s[:, None] * V.conj().T
+        A = D - 2.0 * np.outer(u, u.conj() @ D) / np.vdot(u, u).real
+        x = gauss(n)
+        b = A @ x + noise * gauss(m)
+        probs.append((np.asfortranarray(A.astype(NP[dtype])), b.astype(NP[dtype])))
+    return ms, ns, probs
+
+
+def fill(ls, probs):
+    for i, (A, b) in enumerate(probs):
+        ls.matrix(i).copy_(torch.from_numpy(A))
+        ls.rhs(i).copy_(torch.from_numpy(b))
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.complex128, torch.float32, torch.complex64])
+def test_batched_ls_plain_matches_oracle(oracle, dtype):
+    ms, ns, probs = ls_problems(48, dtype, seed=3, cond=1e2)
+    ls = BatchedLS(ms, ns, dtype)
+    fill(ls, probs)
+    ls.solve_plain()
+    torch.cuda.synchronize()
+    p = PFX[dtype]
+    tol = 1e-11 if p in "dz" else 1e-3
+    for i, (A, b) in enumerate(probs):
+        m, n = A.shape
+        ao = A.copy(order="F")
+        bo = np.asfortranarray(b.reshape(m, 1).copy())
+        oracle.gels(p, m, n, 1, ao, bo)
+        assert rel(ls.solution(i).cpu().numpy(), bo[:n, 0]) <= tol, (i, m, n)
+
+
+@pytest.mark.parametrize("dtype", [torch.complex128, torch.float64])
+def test_batched_ls_mixed_reaches_fp64_backward_error(oracle, dtype):
+    ms, ns, probs = ls_problems(64, dtype, seed=4, cond=1e4)
+    ls = BatchedLS(ms, ns, dtype)
+    fill(ls, probs)
+    ls.tune_mixed()
+    ls.solve_mixed()
+    torch.cuda.synchronize()
+    eps = np.finfo(np.float64).eps
+    berr = ls.berr.cpu().numpy()
+    eta = ls.eta.cpu().numpy()
+    iters = ls.iters.cpu().numpy()
+    p = PFX[dtype]
+    for i, (A, b) in enumerate(probs):
+        m, n = A.shape
+        assert berr[i] <= 10 * n * eps and eta[i] <= 10 * n * eps, (i, m, n, berr[i], eta[i])
+        assert 1 <= iters[i] <= 10
+        # forward error against the FP64 oracle solution: cond 1e4
+        ao = A.copy(order="F")
+        bo = np.asfortranarray(b.reshape(m, 1).copy())
+        oracle.gels(p, m, n, 1, ao, bo)
+        assert rel(ls.solution(i).cpu().numpy(), bo[:n, 0]) <= 1e-10, (i, m, n)
+        # the FP64 backward error measured independently in numpy
+        x = ls.solution(i).cpu().numpy()
+        r = b - A @ x
+        an = np.linalg.norm(A)
+        assert np.linalg.norm(A.conj().T @ r) / (an * (an * np.linalg.norm(x) + np.linalg.norm(b))) <= 10 * n * eps
+
+
+def test_batched_ls_mixed_graph_replay():
+    dtype = torch.complex128
+    ms, ns, probs = ls_problems(40, dtype, seed=5)
+    ls = BatchedLS(ms, ns, dtype)
+    fill(ls, probs)
+    ls.solve_mixed()
+    torch.cuda.synchronize()
+    x0 = ls.x.clone()
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        ls.solve_mixed()
+    torch.cuda.current_stream().wait_stream(s)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        ls.solve_mixed()
+    ls.x.zero_()
+    g.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(ls.x, x0)
