@@ -88,6 +88,21 @@ static constexpr int kMaxDevices = 64;
 static DeviceFacts g_facts[kMaxDevices];
 static std::once_flag g_facts_once[kMaxDevices];
 
+// Library-wide device status word: set by any kernel whose bounded wait
+// expired (tensor-core pipelines, grid barriers); read by
+// rnpgpu_device_status.  One file-scope variable, so no allocation.
+static __device__ int g_device_status;
+int *device_status_ptr() {
+    static int *ptr[kMaxDevices] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) dev = 0;
+    if (ptr[dev] == nullptr) {
+        void *p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_device_status) == cudaSuccess) ptr[dev] = (int *)p;
+    }
+    return ptr[dev];
+}
+
 const DeviceFacts &device_facts() {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) dev = 0;
@@ -107,6 +122,18 @@ const DeviceFacts &device_facts() {
 } // namespace rnpgpu
 
 extern "C" {
+
+// Device status word (nonzero if a bounded wait of some kernel expired since
+// the last reset): returns it and, if reset is nonzero, clears it; synchronous.
+int rnpgpu_device_status(int reset) {
+    int v = 0;
+    if (cudaMemcpyFromSymbol(&v, rnpgpu::g_device_status, sizeof(int)) != cudaSuccess) return -1;
+    if (reset) {
+        const int z = 0;
+        cudaMemcpyToSymbol(rnpgpu::g_device_status, &z, sizeof(int));
+    }
+    return v;
+}
 
 int rnpgpu_set_stream(void *stream) {
     rnpgpu::t_stream = (cudaStream_t)stream;

@@ -40,6 +40,7 @@ template <class T> struct ThinArgs {
     T *wred;      // [kPanelMaxCols * n]
     unsigned *counter;
     int *err;
+    int *status;  // library-wide status word
     int rows_per_cta;
 };
 
@@ -86,6 +87,7 @@ template <class T, bool CSMEM, int VBUF> __global__ void __launch_bounds__(kThin
     const int r0 = g * R;
     const int r1 = min(p.m, r0 + R);
     GridBarrier bar{p.counter, p.err, (unsigned)G, 0u};
+    bar.status = p.status;
     auto cref = [&](int r, int c) -> T & {
         if (CSMEM) return sC[(size_t)(r - r0) * ldsc + c];
         return p.C[r + (size_t)c * p.ldc];

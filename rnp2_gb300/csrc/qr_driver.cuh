@@ -30,6 +30,7 @@ struct DeviceFacts {
 cudaStream_t current_stream();
 void set_last_error(const char *msg);
 const DeviceFacts &device_facts();
+int *device_status_ptr();  // library-wide device status word
 
 // Launch accounting and optional per-kernel-class timing (CUDA events on the
 // launching stream; only while rnpgpu_timing_enable(1) is in effect).
@@ -96,9 +97,6 @@ template <class T> size_t elems_for(size_t bytes) { return (bytes + 256 + sizeof
 // ---------------------------------------------------------------------------
 // Contraction launcher
 // ---------------------------------------------------------------------------
-// error word of the tensor-core kernels' bounded waits (per translation unit)
-static __device__ int g_tc_status;
-
 template <int BN> int launch_gemm_tc_bn(const GemmArgs<float> &g, int nsplit, cudaStream_t st) {
     static std::once_flag once;
     static cudaError_t attr = cudaSuccess;
@@ -106,8 +104,8 @@ template <int BN> int launch_gemm_tc_bn(const GemmArgs<float> &g, int nsplit, cu
         attr = cudaFuncSetAttribute((const void *)tc::k_gemm_tc<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SmemLayout<BN>::kBytes);
     });
     RNPGPU_CHECK(attr);
-    int *err = nullptr;
-    RNPGPU_CHECK(cudaGetSymbolAddress((void **)&err, g_tc_status));
+    int *err = device_status_ptr();
+    if (err == nullptr) return kErrCuda;
     dim3 grid((g.M + tc::kBM - 1) / tc::kBM, (g.N + BN - 1) / BN, nsplit);
     tc::k_gemm_tc<BN><<<grid, tc::kThreads, tc::SmemLayout<BN>::kBytes, st>>>(g, err);
     RNPGPU_CHECK_LAUNCH();
@@ -123,7 +121,34 @@ template <int BN> int launch_gemm_tc_bn(const GemmArgs<float> &g, int nsplit, cu
 inline bool use_tensor_cores(const GemmArgs<float> &g) { return g.M >= 128 && g.K >= 16 && g.K <= 64; }
 template <class T> bool use_tensor_cores(const GemmArgs<T> &) { return false; }
 
+// The trailing update C -= V W^T (V unit-lower, K <= 32, N <= 512) goes to
+// the persistent kernel that keeps W's slices resident (one CTA per SM: the
+// request for more than half an SM's shared memory keeps a second CTA, and
+// its TMEM allocation, off the SM).
+inline bool is_trailing_update(const GemmArgs<float> &g, int nsplit) {
+    return nsplit == 1 && g.opA == kOpN && g.vunitA && (g.opB == kOpC || g.opB == kOpT) && !g.vunitB && g.beta_mode == kBetaOne && g.alpha == -1.0f && g.K <= 32 &&
+           g.N <= tc::kUpdMaxN && g.M >= 128;
+}
+inline int launch_update_tc(const GemmArgs<float> &g, cudaStream_t st) {
+    const size_t smem = std::max<size_t>(tc::upd_smem_bytes(g.N), 116 * 1024);
+    static std::once_flag once;
+    static cudaError_t attr = cudaSuccess;
+    std::call_once(once, []() { attr = cudaFuncSetAttribute((const void *)tc::k_update_tc<tc::kUpdChunk>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); });
+    RNPGPU_CHECK(attr);
+    int *err = device_status_ptr();
+    if (err == nullptr) return kErrCuda;
+    tc::UpdArgs u;
+    u.V = g.A; u.ldv = g.lda; u.W = g.B; u.ldw = g.ldb; u.C = g.D; u.ldc = g.ldd;
+    u.M = g.M; u.N = g.N; u.K = g.K;
+    const int ntiles = (g.M + tc::kBM - 1) / tc::kBM;
+    const int grid = std::max(1, std::min(ntiles, device_facts().sm_count));
+    tc::k_update_tc<tc::kUpdChunk><<<grid, tc::kThreads, smem, st>>>(u, err);
+    RNPGPU_CHECK_LAUNCH();
+    return kOk;
+}
+
 inline int launch_gemm_tc(const GemmArgs<float> &g, int nsplit, cudaStream_t st) {
+    if (is_trailing_update(g, nsplit)) return launch_update_tc(g, st);
     if (g.N <= 32) return launch_gemm_tc_bn<32>(g, nsplit, st);
     return launch_gemm_tc_bn<64>(g, nsplit, st);
 }
@@ -271,6 +296,7 @@ template <class T> int panel_factor(int M, int N, T *A, size_t lda, T *tau, T *T
     p.A = A; p.lda = lda; p.M = M; p.N = N; p.tau = tau; p.Tm = Tm; p.ldt = ldt;
     p.rec = ws.rec;
     p.counter = ws.sync; p.err = (int *)(ws.sync + 1);
+    p.status = device_status_ptr();
     p.rows_per_cta = (M + G - 1) / G;
     RNPGPU_CHECK(cudaMemsetAsync(ws.sync, 0, 2 * sizeof(unsigned), st));
     void *args[] = {&p};
@@ -484,6 +510,7 @@ template <class T> int multq_thin(bool notran, size_t m, size_t n, size_t k, con
     unsigned *sync = cv.take<unsigned>(2);
     p.counter = sync;
     p.err = (int *)(sync + 1);
+    p.status = device_status_ptr();
     p.rows_per_cta = tp.rows;
     RNPGPU_CHECK(cudaMemsetAsync(sync, 0, 2 * sizeof(unsigned), st));
     void *args[] = {&p};

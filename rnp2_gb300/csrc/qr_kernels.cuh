@@ -161,67 +161,29 @@ __device__ __forceinline__ cf32 scale_x(cf32 x, const ReflScalars<cf32> &s) {
     return s.sh < 0 ? cf32(shift_f32(re, s.sh), shift_f32(im, s.sh)) : cf32(re, im);
 }
 
-// FP32 data: the reflector scalars from alpha and the squared norm n2 of x
-// (FP64).  Squares of FP32 magnitudes neither overflow nor underflow in FP64,
-// so beta = -sign(Re alpha) sqrt(|alpha|^2 + n2) needs no scaling, and
-// 1/beta and 1/(alpha - beta) come from one FP64 division:
-//   inv = 1/(beta |alpha - beta|^2),  1/beta = |alpha - beta|^2 inv,
-//   1/(alpha - beta) = conj(alpha - beta) beta inv.
-template <class T> __device__ ReflScalars<T> reflector_scalars_sq(T alpha, double n2) {
-    typedef typename Tr<T>::R R;
-    ReflScalars<T> s;
-    const double ar = (double)Tr<T>::re(alpha), ai = (double)Tr<T>::im(alpha);
-    s.knt = 0;
-    if (n2 == 0.0 && ai == 0.0) {
-        s.identity = true;
-        s.tau = T(0);
-        s.scal = T(1);
-        s.sr = 1.0;
-        s.si = 0.0;
-        s.sr_hi = 1.0f; s.sr_lo = 0.0f; s.si_hi = 0.0f; s.si_lo = 0.0f;
-        s.sh = 0;
-        s.beta = ar;
-        return s;
-    }
-    s.identity = false;
-    double beta = sqrt(fma(ar, ar, fma(ai, ai, n2)));
-    if (ar > 0.0) beta = -beta;
-    const double dr = ar - beta;
-    const double z2 = fma(dr, dr, ai * ai);
-    const double inv = 1.0 / (beta * z2);
-    const double rb = z2 * inv, rz = beta * inv;
-    const double tr = (beta - ar) * rb, ti = -ai * rb;
-    const double sr = dr * rz, si = -ai * rz;
-    s.tau = Tr<T>::make((R)tr, (R)ti);
-    s.scal = Tr<T>::make((R)sr, (R)si);
-    s.sr = sr;
-    s.si = si;
-    set_f32_scale(s, sr, si);
-    s.beta = beta;
-    return s;
-}
-
 // ---------------------------------------------------------------------------
 // Panel factorization across a cooperative grid.
 // Rows [b*R, min(M,(b+1)*R)) of the panel belong to block b.  One grid
 // barrier per column j: after it every block holds the combined partial sums
 // of the previous phase and
-//   1. (thread 0) forms ||x|| of column j below the diagonal by downdating
+//   1. (one thread) forms ||x|| of column j below the diagonal by downdating
 //      ||a - c v||^2 = s1 - 2 Re(c conj(s2)) + |c|^2 s3  (c = conj(tau) w_j)
 //      from the sums gathered in the previous phase, and from it beta, tau
-//      and 1/(alpha-beta) (FP64, identical in every block); when the
-//      downdating would cancel (result < delta * s1) or the column holds
-//      magnitudes outside the safe squaring range, an extra barrier
-//      recomputes the norm exactly with the three-accumulator scheme;
+//      and 1/(alpha-beta) (identical in every block); when the downdating
+//      would cancel (result < s1 / 2) or the column holds magnitudes outside
+//      the safe squaring range, an extra barrier recomputes the norm exactly
+//      with the three-accumulator scheme (FP64);
 //   2. (all threads, meanwhile) applies H[j-1]^H (tau[j-1], v[j-1],
 //      w[j-1] = v^H A) to its rows of the panel columns right of j-1;
 //   3. scales its rows of x into v;
 //   4. accumulates over its rows w_c = v^H A[:,c] (c > j), the Gram column
 //      g_c = V[:,c]^H v (c < j) and the downdating sums of column j+1, and
-//      writes them into the partial record of the next phase; after the
-//      barrier block 0 extends T by column j from the Gram column.
+//      writes them into the partial record of the next phase; while the
+//      following barrier settles, one warp of block 0 extends T by column j
+//      from the Gram column.
 // FP32 panels accumulate the downdating sums error-free in FP32 (hi + lo
-// pairs, about 2^-48 relative) and keep the FP64 pipe to thread 0.
+// pairs, about 2^-48 relative), downdate and form the reflector scalars in
+// FP32 pair arithmetic, and use FP64 only on the exact path.
 // Records are double-buffered by phase parity and combined by all threads in
 // a fixed order with all loads of a thread in flight at once: the result is
 // deterministic for a given grid size.
@@ -245,6 +207,7 @@ template <class T> struct PanelArgs {
     PanelRec<T> *rec;    // [2][gridDim.x]
     unsigned *counter;   // zeroed before launch
     int *err;            // zeroed before launch
+    int *status;         // library-wide status word
     int rows_per_cta;
 };
 
@@ -270,6 +233,54 @@ template <class U, int N> __device__ __forceinline__ U tree_sum(U (&v)[N]) {
     return v[0];
 }
 
+// FP32 data whose downdated squared norm n2 is an FP32 pair and whose
+// magnitudes lie in the safe range [2^-40, 2^48] (squares and their sums stay
+// normal FP32 numbers): beta = -sign(Re alpha) sqrt(|alpha|^2 + n2) rounded
+// once from the pair, tau = (beta - alpha)/beta and 1/(alpha - beta) in FP32
+template <class T> __device__ ReflScalars<T> reflector_scalars_f32(T alpha, F2 n2) {
+    typedef typename Tr<T>::R R;
+    ReflScalars<T> s;
+    const float ar = re_f(alpha), ai = im_f(alpha);
+    s.knt = 0;
+    s.sh = 0;
+    s.sr_lo = 0.0f;
+    s.si_lo = 0.0f;
+    if (n2.h == 0.0f && n2.l == 0.0f && ai == 0.0f) {
+        s.identity = true;
+        s.tau = T(0);
+        s.scal = T(1);
+        s.sr = 1.0;
+        s.si = 0.0;
+        s.sr_hi = 1.0f;
+        s.si_hi = 0.0f;
+        s.beta = ar;
+        return s;
+    }
+    s.identity = false;
+    const F2 q = f2_add(f2_add(f2_sq(ar), f2_sq(ai)), n2);
+    float beta = sqrtf(q.h + q.l);
+    if (ar > 0.0f) beta = -beta;
+    const float d = ar - beta;  // |d| = |ar| + |beta|: no cancellation
+    const float tr = (beta - ar) / beta, ti = -ai / beta;
+    float sr, si;
+    if (Tr<T>::is_complex) {
+        const float z2 = fmaf(d, d, ai * ai);
+        sr = d / z2;
+        si = -ai / z2;
+    } else {
+        sr = 1.0f / d;
+        si = 0.0f;
+    }
+    s.tau = Tr<T>::make((R)tr, (R)ti);
+    s.scal = Tr<T>::make((R)sr, (R)si);
+    s.sr = sr;
+    s.si = si;
+    s.sr_hi = sr;
+    s.si_hi = si;
+    s.beta = beta;
+    return s;
+}
+
 // SMEM = true: the block's rows of the panel live in dynamic shared memory
 // for the whole launch (loaded once, written back at the end); SMEM = false:
 // they are read and written in place in global memory (panels too tall for
@@ -281,13 +292,13 @@ template <class T, bool SMEM> __global__ void __launch_bounds__(kPanelThreads) k
     constexpr int kSlots = kRecT + kRecD;            // one thread per record entry ...
     constexpr int kGroups = kPanelThreads / kSlots;  // ... and kGroups subsets of the records
     constexpr int UNR = (sizeof(T) <= 4) ? 32 : (sizeof(T) <= 8 ? 16 : 8);
-    const double delta = is64 ? 0.5 : 1e-4;
     const int G = gridDim.x, b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int r0 = b * p.rows_per_cta;
     const int r1 = min(p.M, r0 + p.rows_per_cta);
     const size_t lda = p.lda;
     T *A = p.A;
     GridBarrier bar{p.counter, p.err, (unsigned)G, 0u};
+    bar.status = p.status;
 
     __shared__ T s_T[kPanelMaxCols][kPanelMaxCols + 1];
     __shared__ T s_cv[kRecT];          // combined record
@@ -300,6 +311,9 @@ template <class T, bool SMEM> __global__ void __launch_bounds__(kPanelThreads) k
     __shared__ float s_rh[nwarps][6], s_rl[nwarps][6];
     __shared__ ReflScalars<T> s_refl;
     __shared__ int s_exact;
+    __shared__ T s_g[kPanelMaxCols];   // block 0: Gram column of the last reflector
+    __shared__ T s_gtau;
+    __shared__ int s_gid, s_gcol;
     extern __shared__ __align__(16) unsigned char s_dyn[];
     T *sP = reinterpret_cast<T *>(s_dyn);
     const int ldp = p.rows_per_cta;
@@ -424,6 +438,22 @@ template <class T, bool SMEM> __global__ void __launch_bounds__(kPanelThreads) k
         __syncthreads();
     };
 
+    // block 0, one warp: T(0:jc, jc) = -tau_jc T(0:jc, 0:jc) g(0:jc),
+    // T(jc, jc) = tau_jc, for the column jc saved after the last combine
+    // (GenerateBlockTr "F","C", Reflector.hpp:588-622)
+    auto t_column = [&]() {
+        const int jc = s_gcol;
+        if (jc < 0) return;
+        if (lane < jc) {
+            T acc = T(0);
+            for (int l = lane; l < jc; ++l) acc = fmac(s_T[lane][l], s_g[l], acc);
+            s_T[lane][jc] = s_gid ? T(0) : (-s_gtau) * acc;
+        }
+        if (lane == 0) s_T[jc][jc] = s_gtau;
+        __syncwarp();
+    };
+    if (tid == 0) s_gcol = -1;
+
     // prologue: exact norm of column 0
     exact_record(0);
     if (!bar.sync()) return;
@@ -435,41 +465,49 @@ template <class T, bool SMEM> __global__ void __launch_bounds__(kPanelThreads) k
 
     for (int j = 0; j < p.N; ++j) {
         if (j > 0) {
-            // 1. thread 0: downdated norm of column j and its reflector scalars
-            if (tid == 0) {
-                double s1, s3, unsafe, s2r, s2i;
-                if (is64) {
-                    s1 = s_cd[0]; s3 = s_cd[1]; unsafe = s_cd[2]; s2r = s_cd[3]; s2i = s_cd[4];
-                } else {
-                    s1 = (double)s_ch[0] + (double)s_cl[0];
-                    s3 = (double)s_ch[1] + (double)s_cl[1];
-                    unsafe = (double)s_ch[2];
-                    s2r = (double)s_ch[3] + (double)s_cl[3];
-                    s2i = (double)s_ch[4] + (double)s_cl[4];
-                }
+            // 1. one thread of the last warp (which owns no rows to update
+            //    when the block holds fewer rows than threads) forms the
+            //    downdated norm of column j and its reflector scalars
+            if (tid == kPanelThreads - 1) {
                 const T a_pre = s_cv[kPanelMaxCols], vn = s_cv[kPanelMaxCols + 1];
-                double n2 = s1;
-                T alpha = a_pre;
+                T alpha = a_pre, c = T(0);
                 if (!prev.identity) {
                     const T ctau = Tr<T>::conj(prev.tau);
                     const T wj = s_cv[j];
                     alpha = fmac(-(ctau * vn), wj, a_pre);
-                    const T c = ctau * wj;
-                    const double cr = re_of(c), ci = im_of(c);
-                    // Re(c * conj(s2)) = cr*s2r + ci*s2i
-                    n2 = s1 - 2.0 * (cr * s2r + ci * s2i) + (cr * cr + ci * ci) * s3;
+                    c = ctau * wj;
                 }
-                const int exact = (unsafe != 0.0 || !(n2 >= delta * s1) || !(n2 < 1e300)) ? 1 : 0;
-                s_exact = exact;
-                if (!exact) {
-                    if (is64) {
+                if (is64) {
+                    const double s1 = s_cd[0], s3 = s_cd[1], unsafe = s_cd[2], s2r = s_cd[3], s2i = s_cd[4];
+                    double n2 = s1;
+                    if (!prev.identity) {
+                        const double cr = re_of(c), ci = im_of(c);
+                        // Re(c * conj(s2)) = cr*s2r + ci*s2i
+                        n2 = s1 - 2.0 * (cr * s2r + ci * s2i) + (cr * cr + ci * ci) * s3;
+                    }
+                    const int exact = (unsafe != 0.0 || !(n2 >= 0.5 * s1) || !(n2 < 1e300)) ? 1 : 0;
+                    s_exact = exact;
+                    if (!exact) {
                         NormAcc nacc;
                         nacc.zero();
                         nacc.med = n2;
                         s_refl = reflector_scalars<T>(alpha, nacc);
-                    } else {
-                        s_refl = reflector_scalars_sq<T>(alpha, n2);
                     }
+                } else {
+                    // FP32 data: the same downdating in FP32 pair arithmetic
+                    const F2 s1{s_ch[0], s_cl[0]}, s3{s_ch[1], s_cl[1]}, s2r{s_ch[3], s_cl[3]}, s2i{s_ch[4], s_cl[4]};
+                    F2 n2 = s1;
+                    if (!prev.identity) {
+                        const float cr = re_f(c), ci = im_f(c);
+                        const F2 u = f2_add(f2_mul(s2r, cr), f2_mul(s2i, ci));
+                        const F2 cc = f2_add(f2_sq(cr), f2_sq(ci));
+                        n2 = f2_add(f2_add(s1, f2_mul(u, -2.0f)), f2_mul(cc, s3));
+                    }
+                    const float ma = fmaxf(fabsf(re_f(alpha)), fabsf(im_f(alpha)));
+                    const bool bad_alpha = ma > 0x1p48f || (ma < 0x1p-40f && ma != 0.0f);
+                    const int exact = (s_ch[2] != 0.0f || bad_alpha || !(n2.h >= 0.5f * s1.h) || !(n2.h < 0x1p120f)) ? 1 : 0;
+                    s_exact = exact;
+                    if (!exact) s_refl = reflector_scalars_f32<T>(alpha, n2);
                 }
             }
             // 2. apply H[j-1]^H to own rows r >= j-1 of columns j..N-1
@@ -500,17 +538,34 @@ template <class T, bool SMEM> __global__ void __launch_bounds__(kPanelThreads) k
         // 4. partial record of this phase
         ++phase;
         PanelRec<T> &rc = my_rec();
-        for (int c = warp; c < p.N; c += nwarps) {
-            T acc = T(0);
-            if (c != j) {
-                for (int r = max(r0, j) + lane; r < r1; r += 32) {
-                    const T v = (r == j) ? T(1) : at(r, j);
-                    const T a = at(r, c);
-                    acc = (c > j) ? fmac(Tr<T>::conj(v), a, acc) : fmac(Tr<T>::conj(a), v, acc);
+        // two columns per warp at a time, two rows per step (four
+        // independent chains)
+        for (int c0 = warp; c0 < p.N; c0 += 2 * nwarps) {
+            const int c1 = c0 + nwarps;
+            const bool u0 = (c0 != j), u1 = (c1 < p.N && c1 != j);
+            T a00 = T(0), a01 = T(0), a10 = T(0), a11 = T(0);
+            auto step = [&](int r, T &x0, T &x1) {
+                const T v = (r == j) ? T(1) : at(r, j);
+                if (u0) {
+                    const T a = at(r, c0);
+                    x0 = (c0 > j) ? fmac(Tr<T>::conj(v), a, x0) : fmac(Tr<T>::conj(a), v, x0);
                 }
-                acc = warp_sum(acc);
+                if (u1) {
+                    const T a = at(r, c1);
+                    x1 = (c1 > j) ? fmac(Tr<T>::conj(v), a, x1) : fmac(Tr<T>::conj(a), v, x1);
+                }
+            };
+            int r = max(r0, j) + lane;
+            for (; r + 32 < r1; r += 64) {
+                step(r, a00, a10);
+                step(r + 32, a01, a11);
             }
-            if (lane == 0) rc.v[c] = acc;
+            if (r < r1) step(r, a00, a10);
+            const T acc0 = warp_sum(a00 + a01), acc1 = warp_sum(a10 + a11);
+            if (lane == 0) {
+                rc.v[c0] = acc0;
+                if (c1 < p.N) rc.v[c1] = acc1;
+            }
         }
         for (int c = p.N + tid; c < kPanelMaxCols; c += kPanelThreads) rc.v[c] = T(0);
         T anext = T(0), vnext = T(0);
@@ -607,20 +662,23 @@ template <class T, bool SMEM> __global__ void __launch_bounds__(kPanelThreads) k
             rc.v[kPanelMaxCols] = anext;
             rc.v[kPanelMaxCols + 1] = vnext;
         }
-        if (!bar.sync()) return;
+        // block 0 extends T by the previous column while the barrier settles
+        bar.arrive();
+        if (b == 0 && warp == 1) t_column();
+        if (!bar.wait()) return;
         combine(!is64);
-        // T column j from the Gram column (block 0):
-        // T(0:j, j) = -tau_j * T(0:j, 0:j) * g(0:j);  T(j, j) = tau_j
         if (b == 0) {
-            if (tid < j) {
-                T acc = T(0);
-                for (int l = tid; l < j; ++l) acc = fmac(s_T[tid][l], s_cv[l], acc);
-                s_T[tid][j] = rs.identity ? T(0) : (-rs.tau) * acc;
+            if (tid < kPanelMaxCols) s_g[tid] = s_cv[tid];
+            if (tid == 0) {
+                s_gtau = rs.tau;
+                s_gid = rs.identity ? 1 : 0;
+                s_gcol = j;
             }
-            if (tid == 0) s_T[j][j] = rs.tau;
         }
         prev = rs;
     }
+    __syncthreads();
+    if (b == 0 && warp == 1) t_column();
     __syncthreads();
     if (SMEM) {
         for (int c = 0; c < p.N; ++c)

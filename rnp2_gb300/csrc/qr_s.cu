@@ -4,18 +4,6 @@
 #define RNPGPU_P s
 #include "qr_type.inc"
 
-// Error word of the tensor-core kernels' bounded waits (they run in this
-// unit only): returns it and, if reset is nonzero, clears it; synchronous.
-extern "C" int rnpgpu_device_status(int reset) {
-    int v = 0;
-    if (cudaMemcpyFromSymbol(&v, rnpgpu::g_tc_status, sizeof(int)) != cudaSuccess) return -1;
-    if (reset) {
-        const int z = 0;
-        cudaMemcpyToSymbol(rnpgpu::g_tc_status, &z, sizeof(int));
-    }
-    return v;
-}
-
 // C = alpha op(A) op(B) + beta C for FP32 on the tensor cores (three-term
 // BF16 split, FP32 accumulation); op "N" or "T", beta 0 or 1.  No reference
 // counterpart: the contraction the FP32 trailing updates use, exported so it

@@ -196,6 +196,35 @@ __device__ __forceinline__ void df_add_prod(float &hi, float &lo, float a, float
     df_add(hi, lo, p);
     lo += e;
 }
+// FP32 hi + lo pairs (double-float arithmetic after Dekker, "A floating-point
+// technique for extending the available precision", 1971): about 2^-44
+// relative, on the FP32 pipe
+struct F2 {
+    float h, l;
+};
+__device__ __forceinline__ F2 f2_norm(float h, float l) {
+    const float s = h + l;
+    return F2{s, l - (s - h)};
+}
+__device__ __forceinline__ F2 f2_add(F2 a, F2 b) {
+    const float s = a.h + b.h, bp = s - a.h;
+    const float e = ((a.h - (s - bp)) + (b.h - bp)) + (a.l + b.l);
+    return f2_norm(s, e);
+}
+__device__ __forceinline__ F2 f2_neg(F2 a) { return F2{-a.h, -a.l}; }
+__device__ __forceinline__ F2 f2_mul(F2 a, float c) {
+    const float p = a.h * c;
+    return f2_norm(p, fmaf(a.l, c, fmaf(a.h, c, -p)));
+}
+__device__ __forceinline__ F2 f2_mul(F2 a, F2 b) {
+    const float p = a.h * b.h;
+    return f2_norm(p, fmaf(a.h, b.l, fmaf(a.l, b.h, fmaf(a.h, b.h, -p))));
+}
+__device__ __forceinline__ F2 f2_sq(float a) {
+    const float p = a * a;
+    return F2{p, fmaf(a, a, -p)};
+}
+
 __device__ __forceinline__ void df_warp_sum(float &hi, float &lo) {
     for (int o = 16; o > 0; o >>= 1) {
         const float oh = __shfl_xor_sync(0xffffffffu, hi, o), ol = __shfl_xor_sync(0xffffffffu, lo, o);
@@ -256,26 +285,38 @@ struct GridBarrier {
     unsigned nblocks;
     unsigned gen;
     long long spin_limit = kSpinLimit;
-    // returns false when this launch must stop (timeout or an error elsewhere)
+    int *status = nullptr;  // library-wide status word, also set on a timeout
+    // arrive + wait; returns false when this launch must stop (timeout or an
+    // error elsewhere)
     __device__ bool sync() {
-        __shared__ int s_ok;
+        arrive();
+        return wait();
+    }
+    // split form: work between arrive() and wait() overlaps the barrier;
+    // it must not touch what other blocks read after the barrier
+    __device__ void arrive() {
         __syncthreads();
+        if (nblocks > 1 && threadIdx.x == 0) {
+            ++gen;
+            __threadfence();
+            red_release_add(counter, 1u);
+        }
+    }
+    __device__ bool wait() {
+        __shared__ int s_ok;
         if (nblocks > 1) {
             if (threadIdx.x == 0) {
-                ++gen;
                 const unsigned target = gen * nblocks;
-                __threadfence();
-                red_release_add(counter, 1u);
                 int ok = 1;
                 const long long t0 = clock64();
                 while (ld_acquire(counter) < target) {
                     if (ld_volatile(err) != 0) { ok = 0; break; }
                     if (clock64() - t0 > spin_limit) {
                         atomicExch(err, (int)kStatusBarrierTimeout);
+                        if (status) atomicExch(status, (int)kStatusBarrierTimeout);
                         ok = 0;
                         break;
                     }
-                    __nanosleep(32);
                 }
                 __threadfence();
                 s_ok = ok;
@@ -283,6 +324,7 @@ struct GridBarrier {
             __syncthreads();
             return s_ok != 0;
         }
+        __syncthreads();
         return true;
     }
 };

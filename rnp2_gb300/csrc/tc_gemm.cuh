@@ -310,5 +310,164 @@ template <int BN> __global__ void __launch_bounds__(kThreads) k_gemm_tc(GemmArgs
     if (warp == 0) tmem_dealloc(tmem_d, kCols);
 }
 
+
+// ---------------------------------------------------------------------------
+// Persistent rank-K update (K <= 32), the FP32 trailing update of the
+// blocked factorization:  C(M x N) -= V(M x K) W(N x K)^T, V unit-lower
+// trapezoidal in stored form (vunit), N <= kUpdMaxN.
+// W's three BF16 slices are split once per CTA and stay in shared memory;
+// the CTA then walks 128-row tiles (t = blockIdx.x, += gridDim.x): it splits
+// the tile's V into its slices, and streams the tile's C in 64-column chunks
+// through two TMEM accumulator sets (the MMAs of chunk c+1 run while the
+// epilogue of chunk c reads C, subtracts and writes it back).
+// ---------------------------------------------------------------------------
+constexpr int kUpdChunk = 64;
+constexpr int kUpdMaxN = 512;
+
+struct UpdArgs {
+    const float *V;  // M x K (ldv), unit-lower in stored form
+    size_t ldv;
+    const float *W;  // N x K (ldw)
+    size_t ldw;
+    float *C;        // M x N (ldc)
+    size_t ldc;
+    int M, N, K;
+};
+
+__host__ __device__ constexpr int upd_npad(int N) { return (N + kUpdChunk - 1) / kUpdChunk * kUpdChunk; }
+__host__ __device__ constexpr size_t upd_smem_bytes(int N) {
+    return (size_t)3 * kBM * kBK * 2 + (size_t)3 * upd_npad(N) * kBK * 2 + 64;
+}
+
+template <int CH> __global__ void __launch_bounds__(kThreads) k_update_tc(UpdArgs g, int *err) {
+    static_assert(CH == kUpdChunk, "chunk width");
+    extern __shared__ __align__(1024) unsigned char smem[];
+    const int npad = upd_npad(g.N);
+    constexpr int kSliceA = kBM * kBK * 2;
+    const int sliceB = npad * kBK * 2;
+    unsigned char *sA = smem;                    // 3 slices of the V tile
+    unsigned char *sB = smem + 3 * kSliceA;      // 3 slices of W (all N rows)
+    uint64_t *bars = reinterpret_cast<uint64_t *>(sB + 3 * sliceB);
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    constexpr uint32_t kCols = 512;              // 2 sets x 3 classes x 64 columns
+    if (tid == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        fence_barrier_init();
+    }
+    if (warp == 0) {
+        tmem_alloc(tmem_slot, kCols);
+        tmem_relinquish();
+    }
+    // W -> B slices: element (n, k) of the N x K operand is W(n, k)
+    for (int idx = tid; idx < npad * kBK; idx += kThreads) {
+        const int n = idx % npad, k = idx / npad;
+        const float w = (n < g.N && k < g.K) ? g.W[n + (size_t)k * g.ldw] : 0.f;
+        __nv_bfloat16 h0, h1, h2;
+        split3(w, h0, h1, h2);
+        const uint32_t o = tile_off(n, k);
+        *reinterpret_cast<__nv_bfloat16 *>(sB + o) = h0;
+        *reinterpret_cast<__nv_bfloat16 *>(sB + sliceB + o) = h1;
+        *reinterpret_cast<__nv_bfloat16 *>(sB + 2 * sliceB + o) = h2;
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem_base = *tmem_slot;
+    constexpr uint32_t idesc = idesc_bf16(kBM, kUpdChunk);
+    const int nchunks = npad / kUpdChunk;
+    const int ntiles = (g.M + kBM - 1) / kBM;
+    uint32_t phase[2] = {0u, 0u};
+    bool ok = true;
+    // MMAs of chunk c into accumulator set s (one elected thread)
+    auto issue = [&](int c, int s) {
+        tc_fence_after();
+        const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB) + (uint32_t)(c * kUpdChunk / 8) * (kBK / 8) * 128;
+        const uint32_t d0 = tmem_base + (uint32_t)(s * 3 * kUpdChunk);
+        const int pa[6] = {0, 0, 1, 0, 1, 2};
+        const int pb[6] = {0, 1, 0, 2, 1, 0};
+        const int pc[6] = {0, 1, 1, 2, 2, 2};
+        const bool first_in_class[6] = {true, true, false, true, false, false};
+#pragma unroll
+        for (int kk = 0; kk < kBK / 16; ++kk) {
+#pragma unroll
+            for (int q = 0; q < 6; ++q) {
+                const uint64_t ad = smem_desc(a0 + pa[q] * kSliceA + kk * 256, 128, (kBK / 8) * 128);
+                const uint64_t bd = smem_desc(b0 + pb[q] * sliceB + kk * 256, 128, (kBK / 8) * 128);
+                umma_bf16(d0 + (uint32_t)(pc[q] * kUpdChunk), ad, bd, idesc, (kk == 0 && first_in_class[q]) ? 0u : 1u);
+            }
+        }
+        umma_commit(&bars[s]);
+    };
+    for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+        const int m0 = t * kBM;
+        // V tile -> A slices (rows m0.., unit-lower in stored form)
+        for (int idx = tid; idx < kBM * kBK; idx += kThreads) {
+            const int mi = idx % kBM, k = idx / kBM, gm = m0 + mi;
+            float v = 0.f;
+            if (gm < g.M && k < g.K) v = (gm > k) ? g.V[gm + (size_t)k * g.ldv] : (gm == k ? 1.f : 0.f);
+            __nv_bfloat16 h0, h1, h2;
+            split3(v, h0, h1, h2);
+            const uint32_t o = tile_off(mi, k);
+            *reinterpret_cast<__nv_bfloat16 *>(sA + o) = h0;
+            *reinterpret_cast<__nv_bfloat16 *>(sA + kSliceA + o) = h1;
+            *reinterpret_cast<__nv_bfloat16 *>(sA + 2 * kSliceA + o) = h2;
+        }
+        fence_proxy_async();
+        __syncthreads();
+        if (tid == 0) issue(0, 0);
+        // epilogue mapping: warp w reads TMEM lanes 32*(w%4).. (tile rows) and
+        // the column half w/4 of each chunk; its C values for the next chunk
+        // are loaded while the current chunk is finished
+        const int q = warp & 3, half = warp >> 2;
+        const int row = m0 + q * 32 + lane;
+        constexpr int kHalf = kUpdChunk / 2;
+        auto load_c = [&](int c, float (&buf)[kHalf]) {
+            const int col0 = c * kUpdChunk + half * kHalf;
+            const float *cp = g.C + row + (size_t)col0 * g.ldc;
+#pragma unroll
+            for (int i = 0; i < kHalf; ++i) buf[i] = (row < g.M && col0 + i < g.N) ? cp[(size_t)i * g.ldc] : 0.f;
+        };
+        float cur[kHalf], nxt[kHalf];
+        load_c(0, cur);
+        for (int c = 0; c < nchunks; ++c) {
+            const int s = c & 1;
+            if (tid == 0 && c + 1 < nchunks) issue(c + 1, s ^ 1);
+            if (c + 1 < nchunks) load_c(c + 1, nxt);
+            if (!mbar_wait(&bars[s], phase[s])) ok = false;
+            phase[s] ^= 1u;
+            tc_fence_after();
+            if (!__syncthreads_and(ok ? 1 : 0)) {
+                ok = false;
+                break;
+            }
+            const uint32_t lane_base = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(s * 3 * kUpdChunk);
+            const int col0 = c * kUpdChunk + half * kHalf;
+            float *cp = g.C + row + (size_t)col0 * g.ldc;
+#pragma unroll
+            for (int c0 = 0; c0 < kHalf; c0 += 16) {
+                float big[16], mid[16], small[16];
+                tmem_ld16(lane_base + (uint32_t)(half * kHalf + c0), big);
+                tmem_ld16(lane_base + (uint32_t)(kUpdChunk + half * kHalf + c0), mid);
+                tmem_ld16(lane_base + (uint32_t)(2 * kUpdChunk + half * kHalf + c0), small);
+                if (row < g.M) {
+#pragma unroll
+                    for (int i = 0; i < 16; ++i)
+                        if (col0 + c0 + i < g.N) cp[(size_t)(c0 + i) * g.ldc] = cur[c0 + i] - (big[i] + fmaf(small[i], 0x1p-16f, mid[i] * 0x1p-8f));
+                }
+            }
+#pragma unroll
+            for (int i = 0; i < kHalf; ++i) cur[i] = nxt[i];
+            tc_fence_before();
+            __syncthreads();
+        }
+    }
+    if (!ok && tid == 0) atomicExch(err, (int)kStatusBarrierTimeout);
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tmem_base, kCols);
+}
+
 } // namespace tc
 } // namespace rnpgpu
