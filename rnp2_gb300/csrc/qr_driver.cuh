@@ -114,10 +114,12 @@ template <int BN> int launch_gemm_tc_bn(const GemmArgs<float> &g, int nsplit, cu
 
 // FP32 updates with a short contraction (the rank-32 trailing and MultQ
 // updates C -= V W^H, K <= 64) and at least one full 128-row tile run on the
-// tensor cores (three-term BF16 split); long reductions (W = C^H V over all
-// rows) stay on FP32 FMA, whose round-to-nearest accumulation is more
-// accurate over long K than the tensor-core accumulator and, for these
-// skinny shapes, faster.
+// tensor cores (three-term BF16 split).  The long reduction W = C^H V of the
+// trailing update goes to the persistent tensor-core kernel below, which
+// accumulates at most a few hundred rows per block in TMEM and sums the
+// per-block partials in FP32 afterwards; other long reductions stay on FP32
+// FMA, whose round-to-nearest accumulation over long K is more accurate than
+// one tensor-core accumulator.
 inline bool use_tensor_cores(const GemmArgs<float> &g) { return g.M >= 128 && g.K >= 16 && g.K <= 64; }
 template <class T> bool use_tensor_cores(const GemmArgs<T> &) { return false; }
 
@@ -146,6 +148,31 @@ inline int launch_update_tc(const GemmArgs<float> &g, cudaStream_t st) {
     RNPGPU_CHECK_LAUNCH();
     return kOk;
 }
+
+// W partials P_g = C^T V (g < nsplit, leading dimension N, stride N*K) on the
+// tensor cores, one partial per persistent block; nsplit <= maxsplit.
+inline bool w_tc_ok(int M, int N, int K) { return M >= 1024 && N <= tc::kUpdMaxN && K <= 32; }
+inline int launch_w_tc(const float *C, size_t ldc, const float *V, size_t ldv, float *P, int M, int N, int K, int maxsplit, int &nsplit, cudaStream_t st) {
+    static std::once_flag once;
+    static cudaError_t attr = cudaSuccess;
+    std::call_once(once, []() {
+        attr = cudaFuncSetAttribute((const void *)tc::k_w_tc<tc::kWCols, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::kWSmem);
+        if (attr == cudaSuccess) attr = cudaFuncSetAttribute((const void *)tc::k_w_tc<tc::kWCols, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::kWSmem);
+    });
+    RNPGPU_CHECK(attr);
+    int *err = device_status_ptr();
+    if (err == nullptr) return kErrCuda;
+    const int nkb = (M + tc::kWRows - 1) / tc::kWRows;
+    nsplit = std::max(1, std::min(std::min(nkb, maxsplit), device_facts().sm_count));
+    tc::WArgs w;
+    w.C = C; w.ldc = ldc; w.V = V; w.ldv = ldv; w.P = P; w.M = M; w.N = N; w.K = K;
+    const bool vec = ((uintptr_t)C % 16 == 0) && (ldc % 4 == 0);
+    if (vec) tc::k_w_tc<tc::kWCols, true><<<nsplit, tc::kWThreads, tc::kWSmem, st>>>(w, err);
+    else tc::k_w_tc<tc::kWCols, false><<<nsplit, tc::kWThreads, tc::kWSmem, st>>>(w, err);
+    RNPGPU_CHECK_LAUNCH();
+    return kOk;
+}
+template <class T> int launch_w_tc(const T *, size_t, const T *, size_t, T *, int, int, int, int, int &, cudaStream_t) { return kErrDevice; }
 
 inline int launch_gemm_tc(const GemmArgs<float> &g, int nsplit, cudaStream_t st) {
     if (is_trailing_update(g, nsplit)) return launch_update_tc(g, st);
@@ -211,6 +238,18 @@ template <class T> int apply_block(bool left, bool notran, int M, int N, int ib,
     if (M <= 0 || N <= 0 || ib <= 0) return kOk;
     int rc;
     if (left) {
+        if (std::is_same<T, float>::value && w_tc_ok(M, N, ib)) {
+            // FP32: W partials on the tensor cores, one per persistent block
+            int nsplit = 1;
+            {
+                KScope ks("larfb_w", st);
+                if ((rc = launch_w_tc(C, ldc, V, ldv, ws.P, M, N, ib, ws.smax, nsplit, st))) return rc;
+            }
+            k_sum_times_t<T><<<(N + 7) / 8, 256, 0, st>>>(ws.P, (size_t)N, (size_t)N * ib, nsplit, N, ib, Tm, ldt, notran ? kOpC : kOpN, ws.W, (size_t)N);
+            RNPGPU_CHECK_LAUNCH();
+            GemmArgs<T> u = gemm_args<T>(V, ldv, kOpN, 1, ws.W, (size_t)N, kOpC, 0, C, ldc, M, N, ib, T(-1), kBetaOne);
+            return launch_gemm(u, 1, st, "larfb_update");
+        }
         // W = C^H V  (N x ib), reduction over the M rows
         const int tiles = (N + 63) / 64;
         const int S = choose_splits(M, tiles, ws.smax);
@@ -339,7 +378,9 @@ template <class T> BlockWs<T> carve_block(Carver &cv, int rows_w, int smax) {
     w.smax = smax;
     return w;
 }
-inline int smax_for(size_t K) { return (int)std::max<size_t>(1, std::min<size_t>(64, K / 256)); }
+// split-K slots of the W partials: up to one per SM (the tensor-core W
+// reduction writes one partial per persistent block)
+inline int smax_for(size_t K) { return (int)std::max<size_t>(1, std::min<size_t>((size_t)std::max(64, device_facts().sm_count), K / 256)); }
 template <class T> size_t t_bytes() { return ((size_t)kPanelMaxCols * kPanelMaxCols * sizeof(T) + 255) / 256 * 256; }
 
 // ---------------------------------------------------------------------------
