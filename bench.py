@@ -437,6 +437,67 @@ def other_configs(torch, dev, gq, lib, peak64):
     return out
 
 
+# DRAM bytes per launch from the ncu captures summarised under profiles/
+# (dram__bytes_read.sum + dram__bytes_write.sum, one capture each; None where
+# no capture of the current kernel exists)
+NCU_TRAFFIC = {}
+
+
+def measured_hbm_gbs():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "MEASURED_PEAKS.json hbm_gbs (measured copy bandwidth)"
+    except Exception:
+        return 6800.0, "fallback 6.8 TB/s (no MEASURED_PEAKS.json)"
+
+
+def kernel_rooflines(prof, tot_ms, top_name, peak64, steps):
+    """Roofline of every main kernel class of the mixed step from its
+    algorithmic work per launch (exact for this workload's shapes: 16 panels of
+    32 columns on 65536 - 32 i rows, 15 trailing updates of the remaining
+    columns) and its average CUDA-event duration per launch."""
+    nb = 32
+    panels = [(M - nb * i, nb) for i in range(N // nb)]
+    updates = [(M - nb * i, N - nb * (i + 1)) for i in range(N // nb - 1)]
+    mean = lambda xs: sum(xs) / len(xs)
+    hbm, hbm_src = measured_hbm_gbs()
+    work = {
+        "panel": ("hbm", mean([2.0 * m * c * 4 for m, c in panels]),
+                  "k_panel<float>: FP32 panel, rows read and written once (2 m 32 x 4 B)"),
+        "larfb_update": ("hbm", mean([2.0 * m * c * 4 + m * nb * 4.0 for m, c in updates]),
+                         "tc::k_update_tc: C -= V W^T, C read and written once, V read once"),
+        "larfb_w": ("hbm", mean([m * c * 4.0 + m * nb * 4.0 for m, c in updates]),
+                    "tc::k_w_tc: W = C^T V partials, C and V read once"),
+        "residual_fp64": ("fp64", 2.0 * M * N * NRHS, "k_gemm<double,128,16>: r = b - A x (2 m n nrhs flops)"),
+        "normal_eq_fp64": ("fp64", 2.0 * M * N * NRHS, "k_gemm<double,128,16>: A^T r, split-K (2 m n nrhs flops)"),
+    }
+    out = {}
+    for name, (kind, per_launch, desc) in work.items():
+        cnt, ms = prof.get(name, (0, 0.0))
+        if cnt <= 0:
+            continue
+        avg_s = ms / cnt * 1e-3
+        if kind == "hbm":
+            ach = per_launch / avg_s / 1e9
+            r = {"kernel": desc, "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+                 "peak_source": hbm_src, "algorithmic_bytes_per_launch": per_launch}
+        else:
+            ach = per_launch / avg_s / 1e12
+            r = {"kernel": desc, "bound": "tensor", "pipe": "fp64 (DFMA; FP64 MMA is slower on this GPU)", "achieved": ach,
+                 "peak": peak64, "unit": "TFLOP/s", "frac": ach / peak64 if peak64 else None,
+                 "peak_source": "FP64 FMA throughput measured in this run (rnpgpu_probe_peak); MEASURED_PEAKS.json has no FP64 figure",
+                 "algorithmic_flops_per_launch": per_launch}
+        r["traffic"] = NCU_TRAFFIC.get(name)
+        r["launches_per_step"] = cnt / float(steps)
+        r["avg_launch_us"] = avg_s * 1e6
+        r["share_of_step"] = ms / tot_ms if tot_ms else None
+        out[name] = r
+    main = out.pop(top_name, None)
+    if main is not None:
+        main["class"] = top_name
+    return main, out
+
+
 def gpu_arm(args, rank, world, local):
     import torch
 
@@ -573,20 +634,7 @@ def gpu_arm(args, rank, world, local):
     lib.rnpgpu_probe_peak(0, C.c_void_p(scratch.data_ptr()), scratch.numel() * 8, C.byref(peak64))
     tot_ms = sum(v[1] for v in prof.values())
     top = max(prof.items(), key=lambda kv: kv[1][1]) if prof else ("none", (0, 0.0))
-    res = prof.get("residual_fp64", (0, 0.0))
-    roofline = None
-    if res[0] > 0:
-        per_launch_flops = 2.0 * M * N * NRHS
-        avg_s = res[1] / res[0] * 1e-3
-        achieved = per_launch_flops / avg_s / 1e12
-        roofline = {
-            "kernel": "residual_fp64 (k_gemm<double,128,16>: r = b - A x)",
-            "bound": "tensor", "pipe": "fp64 (DFMA)", "achieved": achieved, "peak": peak64.value, "unit": "TFLOP/s",
-            "frac": achieved / peak64.value if peak64.value else None, "traffic": None,
-            "peak_source": "FP64 FMA throughput measured in this run (rnpgpu_probe_peak); MEASURED_PEAKS.json has no FP64 figure",
-            "algorithmic_flops_per_launch": per_launch_flops,
-            "share_of_step": res[1] / tot_ms if tot_ms else None,
-        }
+    roofline, roofline_others = kernel_rooflines(prof, tot_ms, top[0], peak64.value, prof_steps)
 
     # ---------------- the other plain configurations ------------------------
     others = {} if args.no_configs else other_configs(torch, dev, gq, lib, peak64.value)
@@ -630,6 +678,7 @@ def gpu_arm(args, rank, world, local):
         "profile_ms_per_step": {k: v[1] / prof_steps for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])},
         "top_kernel": top[0],
         "roofline": roofline,
+        "roofline_other_kernels": roofline_others,
         "configs": others,
         "cpu_baseline": cpu,
         "clocks": clk.summary(),
