@@ -218,7 +218,7 @@ def batched_config(torch, dev, gq, lib, peak64, count=20000, loop_sample=200, ch
     a0 = torch.randn(b.a.numel(), generator=g, dtype=torch.float64, device=dev)
     b.a.copy_(a0)
     tune_ms = b.tune()
-    cfg = [b.config(c) for c in range(3)]
+    cfg = [b.config(c) for c in range(4)]
     # capture one run in a CUDA graph
     s = torch.cuda.Stream()
     s.wait_stream(torch.cuda.current_stream())
@@ -326,7 +326,7 @@ def batched_ls_config(torch, dev, count=4096, check_sample=32):
 
     ls, ms, ns = batched_ls_problems(torch, dev, count, 5)
     tune_ms = ls.tune_mixed()
-    cfg = [ls.config(c) for c in range(3)]
+    cfg = [ls.config(c) for c in range(4)]
 
     def graph_time(fn, reps=4):
         s = torch.cuda.Stream()

@@ -7,8 +7,9 @@
  * a_offset[i], is m[i] x n[i] column-major with leading dimension lda[i]
  * (m[i] <= 512); its tau (min(m[i], n[i]) entries) starts at tau_offset[i]
  * of the tau buffer.  On exit each matrix holds R and its reflectors exactly
- * as after RNP::LA::QR::Factor.  The plan splits the batch into three size
- * classes by rows (<= 64, <= 256, <= 512).
+ * as after RNP::LA::QR::Factor.  The plan splits the batch into four size
+ * classes: m, n <= 32 (one warp per matrix, or a small block, as the
+ * autotuner finds faster) and m <= 64, <= 256, <= 512 (one block per matrix).
  *
  *   1. rnpgpu_geqrf_batched_plan(type, batch, m, n, lda, a_offset,
  *      tau_offset, work, &lwork_bytes, &plan): HOST arrays; query the device
@@ -61,8 +62,14 @@ typedef struct rnpgpu_batch_plan rnpgpu_batch_plan;
 int rnpgpu_geqrf_batched_plan(int type, int batch, const int *m, const int *n, const int *lda, const long long *a_offset, const long long *tau_offset, void *work, size_t *lwork_bytes, rnpgpu_batch_plan **plan);
 int rnpgpu_gels_batched_plan(int type, int batch, const int *m, const int *n, const int *lda, const long long *a_offset, const long long *tau_offset, const long long *b_offset, const long long *x_offset, void *work, size_t *lwork_bytes, rnpgpu_batch_plan **plan);
 int rnpgpu_batch_plan_destroy(rnpgpu_batch_plan *plan);
-/* block shape (threads, panel width) and matrix count of size class cls (0, 1, 2) */
+/* block shape (threads, panel width; threads == 32: one warp per matrix) and
+   matrix count of size class cls (0 .. 3) */
 int rnpgpu_batch_plan_config(const rnpgpu_batch_plan *plan, int cls, int *threads, int *nb, int *count);
+/* set the block shape of class cls to one of the autotuner's candidates
+   (class 0: (32, 0) one warp per matrix, or (64, 8); class 1: (64|128, 8),
+   (128, 16); class 2: (128, 8|16), (256, 16|32); class 3: (256, 8|16),
+   (512, 16)); -3 for any other shape */
+int rnpgpu_batch_plan_set_config(rnpgpu_batch_plan *plan, int cls, int threads, int nb);
 
 int rnpgpu_sgeqrf_batched(const rnpgpu_batch_plan *plan, float *a, float *tau);
 int rnpgpu_dgeqrf_batched(const rnpgpu_batch_plan *plan, double *a, double *tau);

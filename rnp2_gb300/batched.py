@@ -21,6 +21,8 @@ def _setup(L):
     L.rnpgpu_gels_batched_plan.restype = C.c_int
     L.rnpgpu_batch_plan_destroy.argtypes = [P]
     L.rnpgpu_batch_plan_config.argtypes = [P, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    L.rnpgpu_batch_plan_set_config.argtypes = [P, C.c_int, C.c_int, C.c_int]
+    L.rnpgpu_batch_plan_set_config.restype = C.c_int
     for p in "sdcz":
         f = getattr(L, "rnpgpu_%sgeqrf_batched" % p)
         f.argtypes = [P, P, P]
@@ -109,6 +111,12 @@ class BatchedQR:
         t, nb, cnt = C.c_int(), C.c_int(), C.c_int()
         self._L.rnpgpu_batch_plan_config(self.plan, cls, C.byref(t), C.byref(nb), C.byref(cnt))
         return {"threads": t.value, "nb": nb.value, "count": cnt.value}
+
+    def force_config(self, cls, threads, nb):
+        """Pin the block shape of a size class (one of the autotuner's candidates)."""
+        rc = self._L.rnpgpu_batch_plan_set_config(self.plan, cls, threads, nb)
+        if rc:
+            raise RNPGPUError("batch_plan_set_config", rc)
 
     def __del__(self):
         try:
@@ -236,6 +244,12 @@ class BatchedLS:
         t, nb, cnt = C.c_int(), C.c_int(), C.c_int()
         self._L.rnpgpu_batch_plan_config(self.plan, cls, C.byref(t), C.byref(nb), C.byref(cnt))
         return {"threads": t.value, "nb": nb.value, "count": cnt.value}
+
+    def force_config(self, cls, threads, nb):
+        """Pin the block shape of a size class (one of the autotuner's candidates)."""
+        rc = self._L.rnpgpu_batch_plan_set_config(self.plan, cls, threads, nb)
+        if rc:
+            raise RNPGPUError("batch_plan_set_config", rc)
 
     def __del__(self):
         try:

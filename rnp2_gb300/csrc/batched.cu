@@ -2,7 +2,8 @@
 // the C ABI (include/rnp_gpu/batched_gb300.h).
 //
 // A plan is built once per batch shape: the host splits the matrices into
-// size classes by rows (<= 64, <= 256, <= 512: the rows a block stages),
+// size classes (m, n <= 32: a warp per matrix; m <= 64, <= 256, <= 512: a
+// block per matrix staging that many rows),
 // sorts each class by decreasing cost (2mn^2 - 2n^3/3), uploads the sorted
 // descriptors into the caller's workspace and keeps, per class, the block
 // shape (threads, panel width) chosen by the autotuner.  A run resets the
@@ -56,8 +57,7 @@ int plan_create(int type, int batch, const int *m, const int *n, const int *lda,
         d.index = i;
         aext = std::max(aext, d.a_off + (long long)d.lda * d.n);
         text = std::max(text, d.tau_off + (long long)std::min(d.m, d.n));
-        int c = 0;
-        while (m[i] > kClassRows[c]) ++c;
+        const int c = class_of(m[i], n[i]);
         cls[c].push_back(d);
     }
     auto cost = [](const BatchDesc &d) {
@@ -123,6 +123,16 @@ int rnpgpu_gels_batched_plan(int type, int batch, const int *m, const int *n, co
 int rnpgpu_batch_plan_destroy(rnpgpu_batch_plan *plan) {
     plan_free(plan);
     return 0;
+}
+
+int rnpgpu_batch_plan_set_config(rnpgpu_batch_plan *plan, int cls, int threads, int nb) {
+    if (plan == nullptr || cls < 0 || cls >= rnpgpu::kClasses) return -1;
+    for (const rnpgpu::BatchConfig &c : rnpgpu::kCandidates[cls])
+        if (c.threads != 0 && c.threads == threads && c.nb == nb) {
+            plan->cfg[cls] = c;
+            return 0;
+        }
+    return -3;
 }
 
 int rnpgpu_batch_plan_config(const rnpgpu_batch_plan *plan, int cls, int *threads, int *nb, int *count) {

@@ -182,4 +182,66 @@ __global__ void __launch_bounds__(NT) k_geqrf_batched(const BatchDesc *__restric
     }
 }
 
+// ---------------------------------------------------------------------------
+// Warp per matrix, for the smallest size class (m <= 32, n <= 32): each warp
+// of the block takes matrices from the work queue, keeps one in its slice of
+// shared memory (column-major, leading dimension 33) and factors it column by
+// column (Factor_unblocked, RNP/LA/QR.hpp:78-102): lanes over rows for the
+// norm and the scaling of x, lanes over columns for w = v^H A and the update.
+// No block-wide barrier is involved; lanes beyond m or n idle.
+// ---------------------------------------------------------------------------
+constexpr int kWarpRows = 32;
+constexpr int kWarpLd = 33;
+
+template <class T, int WPB> __global__ void __launch_bounds__(WPB * 32) k_geqrf_warp(const BatchDesc *__restrict__ desc, int count, T *A, T *tau, unsigned *queue) {
+    typedef typename Tr<T>::R R;
+    extern __shared__ __align__(16) unsigned char s_raw[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    T *sM = reinterpret_cast<T *>(s_raw) + (size_t)wib * kWarpRows * kWarpLd;
+    __shared__ ReflScalars<T> s_refl[WPB];
+    for (;;) {
+        unsigned idx = 0;
+        if (lane == 0) idx = atomicAdd(queue, 1u);
+        idx = __shfl_sync(0xffffffffu, idx, 0);
+        if (idx >= (unsigned)count) break;
+        const BatchDesc d = desc[idx];
+        T *a = A + d.a_off;
+        T *tp = tau + d.tau_off;
+        const int m = d.m, n = d.n, lda = d.lda, k = min(m, n);
+        for (int c = 0; c < n; ++c)
+            if (lane < m) sM[c * kWarpLd + lane] = a[lane + (size_t)c * lda];
+        __syncwarp();
+        for (int j = 0; j < k; ++j) {
+            T *col = sM + j * kWarpLd;
+            NormAcc acc;
+            acc.zero();
+            if (lane > j && lane < m) acc.add(col[lane]);
+            acc.warp_reduce();
+            if (lane == 0) s_refl[wib] = reflector_scalars<T>(col[j], acc);
+            __syncwarp();
+            const ReflScalars<T> rs = s_refl[wib];
+            if (!rs.identity && lane > j && lane < m) col[lane] = scale_x(col[lane], rs);
+            __syncwarp();
+            // H^H on the columns right of j: lane c forms w_c = v^H a_c and updates a_c
+            const int c = lane;
+            if (!rs.identity && c > j && c < n) {
+                T *ac = sM + c * kWarpLd;
+                T w = ac[j];
+                for (int r = j + 1; r < m; ++r) w = fmac(Tr<T>::conj(col[r]), ac[r], w);
+                const T cw = Tr<T>::conj(rs.tau) * w;
+                ac[j] = ac[j] - cw;
+                for (int r = j + 1; r < m; ++r) ac[r] = fmac(-col[r], cw, ac[r]);
+            }
+            if (lane == 0) {
+                tp[j] = rs.tau;
+                if (!rs.identity) col[j] = Tr<T>::make((R)rs.beta, 0);
+            }
+            __syncwarp();
+        }
+        for (int c = 0; c < n; ++c)
+            if (lane < m) a[lane + (size_t)c * lda] = sM[c * kWarpLd + lane];
+        __syncwarp();
+    }
+}
+
 } // namespace rnpgpu

@@ -11,21 +11,30 @@
 
 namespace rnpgpu {
 
-// size classes by rows: matrices of class c have m <= kClassRows[c]; each
-// class stages kClassRows[c] rows per block
-constexpr int kClasses = 3;
-constexpr int kClassRows[kClasses] = {64, 256, 512};
+// size classes: class 0 holds matrices with m, n <= 32 (a warp per matrix,
+// or a small block), classes 1..3 those with m <= 64, 256, 512 (a block per
+// matrix staging kClassMR[c] rows)
+constexpr int kClasses = 4;
+constexpr int kClassRows[kClasses] = {32, 64, 256, 512};
+constexpr int kClassMR[kClasses] = {64, 64, 256, 512};
+inline int class_of(int m, int n) {
+    if (m <= kWarpRows && n <= kWarpRows) return 0;
+    if (m <= 64) return 1;
+    return m <= 256 ? 2 : 3;
+}
 
 struct BatchConfig {
-    int threads, nb;
+    int threads, nb;  // threads == 32: one warp per matrix (k_geqrf_warp)
 };
 // candidate block shapes (threads, panel width) per class
 static const BatchConfig kCandidates[kClasses][4] = {
+    {{32, 0}, {64, 8}, {0, 0}, {0, 0}},
     {{64, 8}, {128, 8}, {128, 16}, {0, 0}},
     {{128, 8}, {128, 16}, {256, 16}, {256, 32}},
     {{256, 8}, {256, 16}, {512, 16}, {0, 0}},
 };
-static const BatchConfig kDefaults[kClasses] = {{64, 8}, {256, 16}, {256, 8}};
+static const BatchConfig kDefaults[kClasses] = {{32, 0}, {64, 8}, {256, 16}, {256, 8}};
+constexpr int kWarpsPerBlock = 4;
 
 template <int MR> constexpr int tile_for() { return MR >= 512 ? 16 : 32; }
 
@@ -47,8 +56,28 @@ template <class T, int NT, int NB, int MR> int launch_batched_cfg(const BatchDes
     return kOk;
 }
 
+template <class T> int launch_batched_warp(const BatchDesc *desc, int count, T *A, T *tau, unsigned *queue, cudaStream_t st) {
+    constexpr size_t smem = (size_t)kWarpsPerBlock * kWarpRows * kWarpLd * sizeof(T);
+    static std::once_flag once;
+    static cudaError_t attr = cudaSuccess;
+    static int per_sm = 1;
+    std::call_once(once, []() {
+        attr = cudaFuncSetAttribute((const void *)k_geqrf_warp<T, kWarpsPerBlock>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (attr == cudaSuccess) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_geqrf_warp<T, kWarpsPerBlock>, kWarpsPerBlock * 32, smem);
+        if (per_sm < 1) per_sm = 1;
+    });
+    RNPGPU_CHECK(attr);
+    const int blocks = (count + kWarpsPerBlock - 1) / kWarpsPerBlock;
+    const int grid = std::max(1, std::min(blocks, device_facts().sm_count * per_sm));
+    KScope ks("geqrf_batched", st);
+    k_geqrf_warp<T, kWarpsPerBlock><<<grid, kWarpsPerBlock * 32, smem, st>>>(desc, count, A, tau, queue);
+    RNPGPU_CHECK_LAUNCH();
+    return kOk;
+}
+
 template <class T> size_t batched_smem(int cls, BatchConfig cfg) {
-    const int mr = kClassRows[cls], tile = mr >= 512 ? 16 : 32;
+    if (cfg.threads == 32) return (size_t)kWarpsPerBlock * kWarpRows * kWarpLd * sizeof(T);
+    const int mr = kClassMR[cls], tile = mr >= 512 ? 16 : 32;
     return ((size_t)mr * cfg.nb + (size_t)mr * tile + (size_t)tile * cfg.nb + (size_t)cfg.nb * cfg.nb + 2 * (size_t)cfg.nb) * sizeof(T);
 }
 inline bool fits_smem(size_t bytes) {
@@ -63,14 +92,15 @@ inline bool fits_smem(size_t bytes) {
 
 template <class T> int launch_batched(int cls, BatchConfig cfg, const BatchDesc *desc, int count, T *A, T *tau, unsigned *queue, cudaStream_t st) {
     if (count <= 0) return kOk;
+    if (cls == 0 && cfg.threads == 32) return launch_batched_warp<T>(desc, count, A, tau, queue, st);
     if (!fits_smem(batched_smem<T>(cls, cfg))) cfg = BatchConfig{cfg.threads, 8};
     const int t = cfg.threads, nb = cfg.nb;
-    if (cls == 0) {
+    if (cls <= 1) {
         if (t == 128 && nb == 8) return launch_batched_cfg<T, 128, 8, 64>(desc, count, A, tau, queue, st);
         if (t == 128 && nb == 16) return launch_batched_cfg<T, 128, 16, 64>(desc, count, A, tau, queue, st);
         return launch_batched_cfg<T, 64, 8, 64>(desc, count, A, tau, queue, st);
     }
-    if (cls == 1) {
+    if (cls == 2) {
         if (t == 128 && nb == 8) return launch_batched_cfg<T, 128, 8, 256>(desc, count, A, tau, queue, st);
         if (t == 128 && nb == 16) return launch_batched_cfg<T, 128, 16, 256>(desc, count, A, tau, queue, st);
         if (t == 256 && nb == 32) return launch_batched_cfg<T, 256, 32, 256>(desc, count, A, tau, queue, st);
@@ -99,8 +129,9 @@ template <class TH, class TL, int MT> int launch_ls_cls(LsBatchArgs<TH, TL> q, c
 }
 template <class TH, class TL> int launch_ls(int cls, const LsBatchArgs<TH, TL> &q, cudaStream_t st) {
     if (q.count <= 0) return kOk;
-    if (cls == 0) return launch_ls_cls<TH, TL, 2>(q, st);
-    if (cls == 1) return launch_ls_cls<TH, TL, 8>(q, st);
+    if (cls == 0) return launch_ls_cls<TH, TL, 1>(q, st);
+    if (cls == 1) return launch_ls_cls<TH, TL, 2>(q, st);
+    if (cls == 2) return launch_ls_cls<TH, TL, 8>(q, st);
     return launch_ls_cls<TH, TL, 16>(q, st);
 }
 

@@ -60,12 +60,39 @@ def test_batched_matches_oracle(oracle, dtype):
     check(b, vals, oracle, dtype)
 
 
+@pytest.mark.parametrize("dtype", [torch.float64, torch.complex64])
+@pytest.mark.parametrize("warp", [True, False])
+def test_batched_small_class_warp_and_block(oracle, dtype, warp):
+    """Matrices with m, n <= 32 (tall, square and fat) go to the smallest
+    class, factored by one warp per matrix or by a small block; both must
+    match the oracle."""
+    rng = np.random.default_rng(7)
+    count = 300
+    ms = rng.integers(1, 33, count)
+    ns = rng.integers(1, 33, count)
+    b = BatchedQR(ms, ns, dtype)
+    vals = []
+    for i in range(count):
+        x = rng.standard_normal((ms[i], ns[i]))
+        if dtype.is_complex:
+            x = x + 1j * rng.standard_normal((ms[i], ns[i]))
+        vals.append(np.asfortranarray(x.astype(NP[dtype])))
+        b.matrix(i).copy_(torch.from_numpy(vals[-1]))
+    assert b.config(0)["count"] == count
+    if not warp:
+        b.force_config(0, 64, 8)
+    b.factor()
+    torch.cuda.synchronize()
+    assert b.config(0)["threads"] == (32 if warp else 64)
+    check(b, vals, oracle, dtype)
+
+
 def test_batched_autotuned_and_graph_replayed(oracle):
     dtype = torch.float64
     b, vals = make_batch(200, dtype, seed=2)
     a0 = b.a.clone()
     b.tune()
-    cfg = [b.config(c) for c in range(3)]
+    cfg = [b.config(c) for c in range(4)]
     assert sum(c["count"] for c in cfg) == 200 and all(c["count"] > 0 for c in cfg)
     # capture one run into a CUDA graph, replay it twice on fresh inputs
     s = torch.cuda.Stream()
