@@ -156,6 +156,10 @@ __global__ void __launch_bounds__(NT) k_geqrf_batched(const BatchDesc *__restric
                         for (int q = 0; q <= l; ++q) s = fmac(w[q], sT[q + l * NB], s);
                         sW[c + l * TILE] = s;
                     }
+                    // columns past a narrow last panel are read (times a zero
+                    // coefficient) by the update below: they must hold zeros,
+                    // not whatever the shared memory held before
+                    for (int l = jb; l < NB; ++l) sW[c + l * TILE] = T(0);
                 }
                 __syncthreads();
                 // C(r, c) -= sum_l V(r, l) conj(W(c, l))
