@@ -237,6 +237,104 @@ template <class T, bool CSMEM, int VBUF> __global__ void __launch_bounds__(kThin
 }
 
 // ---------------------------------------------------------------------------
+// The same product when the reflectors cover most of C's rows (k close to m):
+// a fixed row range per block would leave the blocks above the current
+// reflector block idle, so here every reflector block's active rows
+// [i_b, m) are split evenly over all blocks (C stays in global memory, read
+// through L2 after the barrier that makes the previous block's updates
+// visible).  The block stages its rows of V_b and C in shared memory and
+// forms V_b^H C and the update with one output per thread and no warp
+// reductions (the shuffle reductions of the tiled form cost more FP64 work
+// than the products when a block holds few rows).  Shared memory holds the
+// largest such row range (rows_per_cta = ceil(m / gridDim.x)) of V and C.
+// ---------------------------------------------------------------------------
+template <class T> inline size_t thin_dyn_smem_bytes(int rmax, int n) {
+    return ((size_t)2 * kPanelMaxCols * n + (size_t)kPanelMaxCols * (kPanelMaxCols + 1) + (size_t)rmax * (kPanelMaxCols + 1) + (size_t)rmax * n) * sizeof(T);
+}
+
+template <class T> __global__ void __launch_bounds__(kThinThreads) k_multq_thin_dyn(ThinArgs<T> p) {
+    extern __shared__ __align__(16) unsigned char s_dyn[];
+    const int n = p.n, RMAX = p.rows_per_cta;
+    T *sW = reinterpret_cast<T *>(s_dyn);                   // 32 x n (ld 32)
+    T *sY = sW + kPanelMaxCols * n;                         // 32 x n (ld 32)
+    T *sT = sY + kPanelMaxCols * n;                         // 32 x 33
+    T *sV = sT + kPanelMaxCols * (kPanelMaxCols + 1);       // 32 x RMAX+1 ... stored [l][r], ld RMAX + 1
+    T *sC = sV + (size_t)kPanelMaxCols * (RMAX + 1);        // n x RMAX, stored [c][r], ld RMAX
+    const int G = gridDim.x, g = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int ldv = RMAX + 1;
+    GridBarrier bar{p.counter, p.err, (unsigned)G, 0u};
+    bar.status = p.status;
+    const int nw = kPanelMaxCols * n;
+    const int slice = (nw + G - 1) / G;
+    for (int s = 0; s < p.nblk; ++s) {
+        const int b = p.forward ? s : p.nblk - 1 - s;
+        const int i = b * kPanelMaxCols;
+        const int ib = min(kPanelMaxCols, p.k - i);
+        const int rb = (p.m - i + G - 1) / G;                  // rows per block for this reflector block
+        const int r0 = min(p.m, i + g * rb), r1 = min(p.m, r0 + rb), nr = r1 - r0;
+        // the previous reflector block's updates (by other blocks) are visible
+        if (s > 0 && !bar.sync()) return;
+        // stage V_b (stored form) and C for rows [r0, r1)
+        for (int e = tid; e < nr * kPanelMaxCols; e += kThinThreads) {
+            const int rr = e % nr, l = e / nr, r = r0 + rr;
+            sV[l * ldv + rr] = (l < ib) ? vload(p.A, p.lda, i, r, l) : T(0);
+        }
+        for (int e = tid; e < nr * n; e += kThinThreads) {
+            const int rr = e % nr, c = e / nr;
+            sC[(size_t)c * RMAX + rr] = ldcg(&p.C[(r0 + rr) + (size_t)c * p.ldc]);
+        }
+        __syncthreads();
+        // 1. partial V^H C: one (reflector, column) entry per thread and step
+        T *mine = p.part + (size_t)g * nw;
+        for (int e = tid; e < nw; e += kThinThreads) {
+            const int l = e % kPanelMaxCols, c = e / kPanelMaxCols;
+            T acc = T(0);
+            if (l < ib)
+                for (int rr = 0; rr < nr; ++rr) acc = fmac(Tr<T>::conj(sV[l * ldv + rr]), sC[(size_t)c * RMAX + rr], acc);
+            mine[e] = acc;
+        }
+        if (!bar.sync()) return;
+        // 2. this block's slice of the reduction, fixed order over blocks
+        for (int e = g * slice + warp; e < min(nw, (g + 1) * slice); e += kThinWarps) {
+            T a = T(0);
+            for (int q = lane; q < G; q += 32) a = a + ldcg(&p.part[(size_t)q * nw + e]);
+            a = warp_sum(a);
+            if (lane == 0) p.wred[e] = a;
+        }
+        if (!bar.sync()) return;
+        // 3. Y = op(T) (V^H C)
+        for (int e = tid; e < nw; e += kThinThreads) sW[e] = ldcg(&p.wred[e]);
+        const T *Tb = p.Tf + (size_t)b * kPanelMaxCols * kPanelMaxCols;
+        for (int e = tid; e < kPanelMaxCols * kPanelMaxCols; e += kThinThreads) {
+            const int r = e % kPanelMaxCols, c = e / kPanelMaxCols;
+            sT[r * (kPanelMaxCols + 1) + c] = (r <= c && c < ib) ? Tb[r + (size_t)c * kPanelMaxCols] : T(0);
+        }
+        __syncthreads();
+        for (int e = tid; e < nw; e += kThinThreads) {
+            const int l = e % kPanelMaxCols, c = e / kPanelMaxCols;
+            T acc = T(0);
+            if (l < ib) {
+                if (p.forward) {
+                    for (int j = 0; j <= l; ++j) acc = fmac(Tr<T>::conj(sT[j * (kPanelMaxCols + 1) + l]), sW[j + c * kPanelMaxCols], acc);
+                } else {
+                    for (int j = l; j < ib; ++j) acc = fmac(sT[l * (kPanelMaxCols + 1) + j], sW[j + c * kPanelMaxCols], acc);
+                }
+            }
+            sY[e] = acc;
+        }
+        __syncthreads();
+        // 4. C(r, c) -= sum_l V(r, l) Y(l, c): one entry per thread and step
+        for (int e = tid; e < nr * n; e += kThinThreads) {
+            const int rr = e % nr, c = e / nr;
+            T acc = sC[(size_t)c * RMAX + rr];
+            for (int l = 0; l < ib; ++l) acc = fmac(-sV[l * ldv + rr], sY[l + c * kPanelMaxCols], acc);
+            p.C[(r0 + rr) + (size_t)c * p.ldc] = acc;
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Gram matrices V_b^H V_b of all reflector blocks, split over row chunks:
 // block (s, b) sums rows [i_b + s*chunk, i_b + (s+1)*chunk) of block b and
 // writes the 32 x 32 partial at P + (b * S + s) * 32 * 32 (leading dimension

@@ -502,6 +502,7 @@ template <class T> int build_all_t(size_t rows, size_t k, const T *a, size_t lda
 // Thin left MultQ in one cooperative launch (multq_thin.cuh)
 // ---------------------------------------------------------------------------
 struct ThinPlan {
+    bool dyn;
     bool csmem;
     int vbuf;
     int grid, rows;
@@ -515,9 +516,26 @@ template <class T> size_t thin_ws_bytes(size_t n) {
 }
 // C's rows and two V staging buffers in shared memory when they fit, then one
 // buffer, then C alone, then neither
-template <class T> ThinPlan thin_plan(size_t m, size_t n) {
+template <class T> ThinPlan thin_plan(size_t m, size_t n, size_t k) {
     ThinPlan tp;
     const int sms = std::max(1, device_facts().sm_count);
+    // reflectors covering a quarter of the rows or more: re-split the active
+    // rows over all blocks for every reflector block (k_multq_thin_dyn)
+    tp.dyn = false;
+    if (k * 4 >= m && k > (size_t)kPanelMaxCols) {
+        const int grid = (int)std::max<size_t>(1, std::min<size_t>((size_t)sms, m / 4));
+        const int rows = (int)((m + grid - 1) / grid);
+        const size_t smem = thin_dyn_smem_bytes<T>(rows, (int)n);
+        if (smem <= kThinSmemMax) {
+            tp.dyn = true;
+            tp.grid = grid;
+            tp.rows = rows;
+            tp.csmem = false;
+            tp.vbuf = 0;
+            tp.smem = smem;
+            return tp;
+        }
+    }
     tp.grid = (int)std::max<size_t>(1, std::min<size_t>((size_t)sms, (m + 31) / 32));
     tp.rows = (int)((m + tp.grid - 1) / tp.grid);
     static const int modes[4][2] = {{1, 2}, {1, 1}, {1, 0}, {0, 0}};
@@ -531,13 +549,14 @@ template <class T> ThinPlan thin_plan(size_t m, size_t n) {
 }
 template <class T, bool CS, int VB> const void *thin_kernel() { return (const void *)k_multq_thin<T, CS, VB>; }
 template <class T> int multq_thin(bool notran, size_t m, size_t n, size_t k, const T *a, size_t lda, const T *Tf, T *c, size_t ldc, void *ws, cudaStream_t st) {
-    const ThinPlan tp = thin_plan<T>(m, n);
-    const void *kern = tp.csmem ? (tp.vbuf == 2 ? thin_kernel<T, true, 2>() : tp.vbuf == 1 ? thin_kernel<T, true, 1>() : thin_kernel<T, true, 0>()) : thin_kernel<T, false, 0>();
+    const ThinPlan tp = thin_plan<T>(m, n, k);
+    const void *kern = tp.dyn ? (const void *)k_multq_thin_dyn<T>
+                              : tp.csmem ? (tp.vbuf == 2 ? thin_kernel<T, true, 2>() : tp.vbuf == 1 ? thin_kernel<T, true, 1>() : thin_kernel<T, true, 0>()) : thin_kernel<T, false, 0>();
     static std::once_flag once;
     static cudaError_t attr = cudaSuccess;
     std::call_once(once, []() {
-        const void *ks[4] = {thin_kernel<T, true, 2>(), thin_kernel<T, true, 1>(), thin_kernel<T, true, 0>(), thin_kernel<T, false, 0>()};
-        for (int q = 0; q < 4 && attr == cudaSuccess; ++q) attr = cudaFuncSetAttribute(ks[q], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kThinSmemMax);
+        const void *ks[5] = {thin_kernel<T, true, 2>(), thin_kernel<T, true, 1>(), thin_kernel<T, true, 0>(), thin_kernel<T, false, 0>(), (const void *)k_multq_thin_dyn<T>};
+        for (int q = 0; q < 5 && attr == cudaSuccess; ++q) attr = cudaFuncSetAttribute(ks[q], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kThinSmemMax);
     });
     RNPGPU_CHECK(attr);
     Carver cv(ws);

@@ -194,7 +194,10 @@ def test_empty_inputs_are_quick_returns():
 
 # MultQ on the left with a thin C goes through the one-launch kernel; C's
 # rows are held in shared memory or, when they do not fit, in place.
-THIN = [("d", 3000, 1, 70), ("d", 2000, 16, 256), ("s", 5000, 33, 100), ("z", 40000, 64, 64), ("c", 700, 64, 45), ("z", 129, 7, 129)]
+# (k >= m / 4 takes the variant that re-splits the active rows per reflector
+# block: the last three and the 129-row case)
+THIN = [("d", 3000, 1, 70), ("d", 2000, 16, 256), ("s", 5000, 33, 100), ("z", 40000, 64, 64), ("c", 700, 64, 45), ("z", 129, 7, 129),
+        ("z", 600, 48, 600), ("d", 1000, 64, 999), ("s", 2000, 5, 1500)]
 
 
 @pytest.mark.parametrize("p,m,nrhs,k", THIN)
