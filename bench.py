@@ -437,10 +437,16 @@ def other_configs(torch, dev, gq, lib, peak64):
     return out
 
 
-# DRAM bytes per launch from the ncu captures summarised under profiles/
-# (dram__bytes_read.sum + dram__bytes_write.sum, one capture each; None where
-# no capture of the current kernel exists)
-NCU_TRAFFIC = {}
+# DRAM traffic of one captured launch per kernel class, from the ncu captures
+# summarised under profiles/ (dram__bytes_read.sum + dram__bytes_write.sum,
+# captured launch's algorithmic bytes): the reported traffic is scaled to the
+# average launch by the algorithmic bytes (traffic grows with the columns and
+# rows processed)
+NCU_TRAFFIC = {
+    "panel": (8.494080e6 + 0.003072e6, 2.0 * 65408 * 32 * 4),              # profiles/k_panel_f32_65536x32.md
+    "larfb_update": (100.570368e6 + 31.947008e6, 2.0 * 65408 * 352 * 4 + 65408 * 32 * 4.0),  # profiles/k_update_tc_65536.md
+    "larfb_w": (100.706048e6 + 3.111424e6, 65408 * 352 * 4.0 + 65408 * 32 * 4.0),             # profiles/k_w_tc_65536.md
+}
 
 
 def measured_hbm_gbs():
@@ -487,7 +493,8 @@ def kernel_rooflines(prof, tot_ms, top_name, peak64, steps):
                  "peak": peak64, "unit": "TFLOP/s", "frac": ach / peak64 if peak64 else None,
                  "peak_source": "FP64 FMA throughput measured in this run (rnpgpu_probe_peak); MEASURED_PEAKS.json has no FP64 figure",
                  "algorithmic_flops_per_launch": per_launch}
-        r["traffic"] = NCU_TRAFFIC.get(name)
+        cap = NCU_TRAFFIC.get(name)
+        r["traffic"] = cap[0] * per_launch / cap[1] if cap else None
         r["launches_per_step"] = cnt / float(steps)
         r["avg_launch_us"] = avg_s * 1e6
         r["share_of_step"] = ms / tot_ms if tot_ms else None
