@@ -220,6 +220,22 @@ inline int choose_splits(int K, int tiles, int smax) {
     return std::max(s, 1);
 }
 
+// W = (sum of nsplit partials) * op(T); many partials are first summed by the
+// parallel reduction, then W is multiplied by op(T) in place
+template <class T> int sum_times_t(const T *P, size_t ldp, size_t pstride, int nsplit, int rows, int k, const T *Tm, int ldt, int opT, T *W, size_t ldw, cudaStream_t st) {
+    if (nsplit > 8) {
+        k_reduce_splits<T><<<dim3((unsigned)((rows + 63) / 64), (unsigned)k), 256, 0, st>>>(P, ldp, pstride, nsplit, rows, W, ldw);
+        RNPGPU_CHECK_LAUNCH();
+        P = W;
+        ldp = ldw;
+        pstride = 0;
+        nsplit = 1;
+    }
+    k_sum_times_t<T><<<(rows + 7) / 8, 256, 0, st>>>(P, ldp, pstride, nsplit, rows, k, Tm, ldt, opT, W, ldw);
+    RNPGPU_CHECK_LAUNCH();
+    return kOk;
+}
+
 // ---------------------------------------------------------------------------
 // Block reflector application (ApplyBlock, storev "C", dir "F",
 // RNP/LA/Reflector.hpp:725-815).  V is the ib-column reflector block in its
@@ -245,8 +261,7 @@ template <class T> int apply_block(bool left, bool notran, int M, int N, int ib,
                 KScope ks("larfb_w", st);
                 if ((rc = launch_w_tc(C, ldc, V, ldv, ws.P, M, N, ib, ws.smax, nsplit, st))) return rc;
             }
-            k_sum_times_t<T><<<(N + 7) / 8, 256, 0, st>>>(ws.P, (size_t)N, (size_t)N * ib, nsplit, N, ib, Tm, ldt, notran ? kOpC : kOpN, ws.W, (size_t)N);
-            RNPGPU_CHECK_LAUNCH();
+            if ((rc = sum_times_t<T>(ws.P, (size_t)N, (size_t)N * ib, nsplit, N, ib, Tm, ldt, notran ? kOpC : kOpN, ws.W, (size_t)N, st))) return rc;
             GemmArgs<T> u = gemm_args<T>(V, ldv, kOpN, 1, ws.W, (size_t)N, kOpC, 0, C, ldc, M, N, ib, T(-1), kBetaOne);
             return launch_gemm(u, 1, st, "larfb_update");
         }
@@ -266,8 +281,7 @@ template <class T> int apply_block(bool left, bool notran, int M, int N, int ib,
         g.dstride = (size_t)N * ib;
         if ((rc = launch_gemm(g, nsplit, st, "larfb_w"))) return rc;
         // W := W T (H^H) or W T^H (H)
-        k_sum_times_t<T><<<(N + 7) / 8, 256, 0, st>>>(ws.P, (size_t)N, (size_t)N * ib, nsplit, N, ib, Tm, ldt, notran ? kOpC : kOpN, ws.W, (size_t)N);
-        RNPGPU_CHECK_LAUNCH();
+        if ((rc = sum_times_t<T>(ws.P, (size_t)N, (size_t)N * ib, nsplit, N, ib, Tm, ldt, notran ? kOpC : kOpN, ws.W, (size_t)N, st))) return rc;
         // C -= V W^H
         GemmArgs<T> u = gemm_args<T>(V, ldv, kOpN, 1, ws.W, (size_t)N, kOpC, 0, C, ldc, M, N, ib, T(-1), kBetaOne);
         return launch_gemm(u, 1, st, "larfb_update");
@@ -281,8 +295,7 @@ template <class T> int apply_block(bool left, bool notran, int M, int N, int ib,
         g.kchunk = kchunk;
         g.dstride = (size_t)M * ib;
         if ((rc = launch_gemm(g, nsplit, st, "larfb_w"))) return rc;
-        k_sum_times_t<T><<<(M + 7) / 8, 256, 0, st>>>(ws.P, (size_t)M, (size_t)M * ib, nsplit, M, ib, Tm, ldt, notran ? kOpN : kOpC, ws.W, (size_t)M);
-        RNPGPU_CHECK_LAUNCH();
+        if ((rc = sum_times_t<T>(ws.P, (size_t)M, (size_t)M * ib, nsplit, M, ib, Tm, ldt, notran ? kOpN : kOpC, ws.W, (size_t)M, st))) return rc;
         // C -= W V^H
         GemmArgs<T> u = gemm_args<T>(ws.W, (size_t)M, kOpN, 0, V, ldv, kOpC, 1, C, ldc, M, N, ib, T(-1), kBetaOne);
         return launch_gemm(u, 1, st, "larfb_update");

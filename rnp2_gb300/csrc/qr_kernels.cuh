@@ -869,6 +869,36 @@ __global__ void __launch_bounds__(256) k_sum_times_t(const T *P, size_t ldp, siz
 }
 
 // ---------------------------------------------------------------------------
+// out(r, c) = sum over s < nsplit of P_s(r, c): four threads per entry, each
+// over every fourth partial in independent batches of eight loads, then the
+// four sums in a fixed order (one long chain of dependent loads per entry
+// would leave the sum latency bound).  Grid: ((rows + 63) / 64, cols).
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void __launch_bounds__(256) k_reduce_splits(const T *P, size_t ldp, size_t pstride, int nsplit, int rows, T *out, size_t ldo) {
+    __shared__ T s_part[4][64];
+    const int tid = threadIdx.x, rl = tid % 64, q = tid / 64;
+    const int r = blockIdx.x * 64 + rl, c = blockIdx.y;
+    T a[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) a[u] = T(0);
+    if (r < rows) {
+        const T *base = P + r + (size_t)c * ldp;
+        int sp = q;
+        for (; sp + 28 < nsplit; sp += 32) {
+#pragma unroll
+            for (int u = 0; u < 8; ++u) a[u] = a[u] + base[(size_t)(sp + 4 * u) * pstride];
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+            if (sp + 4 * u < nsplit) a[u] = a[u] + base[(size_t)(sp + 4 * u) * pstride];
+    }
+    s_part[q][rl] = ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7]));
+    __syncthreads();
+    if (q == 0 && r < rows) out[r + (size_t)c * ldo] = (s_part[0][rl] + s_part[1][rl]) + (s_part[2][rl] + s_part[3][rl]);
+}
+
+// ---------------------------------------------------------------------------
 // T factors from Gram matrices (GenerateBlockTr "F","C" recurrence,
 // RNP/LA/Reflector.hpp:588-622):  for i = 0..k-1,
 //   T(0:i, i) = -tau_i * T(0:i,0:i) * G(0:i, i),  T(i,i) = tau_i

@@ -124,6 +124,16 @@ __device__ __forceinline__ void split3(float x, __nv_bfloat16 &h0, __nv_bfloat16
     h2 = __float2bfloat16_rn(r);
 }
 
+// eight consecutive-K values of one row, split, as one 16-byte store per
+// slice at byte offset o of slice 0 (slices slice_bytes apart)
+__device__ __forceinline__ void put8_slices(unsigned char *slice0, size_t slice_bytes, uint32_t o, const float (&x)[8]) {
+    __align__(16) __nv_bfloat16 h[3][8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) split3(x[e], h[0][e], h[1][e], h[2][e]);
+#pragma unroll
+    for (int q = 0; q < 3; ++q) *reinterpret_cast<uint4 *>(slice0 + q * slice_bytes + o) = *reinterpret_cast<const uint4 *>(h[q]);
+}
+
 template <int BN> struct SmemLayout {
     static constexpr int kSliceA = kBM * kBK * 2;          // bytes of one bf16 slice of the A tile
     static constexpr int kSliceB = BN * kBK * 2;
@@ -360,16 +370,15 @@ template <int CH> __global__ void __launch_bounds__(kThreads) k_update_tc(UpdArg
         tmem_alloc(tmem_slot, kCols);
         tmem_relinquish();
     }
-    // W -> B slices: element (n, k) of the N x K operand is W(n, k)
-    for (int idx = tid; idx < npad * kBK; idx += kThreads) {
-        const int n = idx % npad, k = idx / npad;
-        const float w = (n < g.N && k < g.K) ? g.W[n + (size_t)k * g.ldw] : 0.f;
-        __nv_bfloat16 h0, h1, h2;
-        split3(w, h0, h1, h2);
-        const uint32_t o = tile_off(n, k);
-        *reinterpret_cast<__nv_bfloat16 *>(sB + o) = h0;
-        *reinterpret_cast<__nv_bfloat16 *>(sB + sliceB + o) = h1;
-        *reinterpret_cast<__nv_bfloat16 *>(sB + 2 * sliceB + o) = h2;
+    // W -> B slices: element (n, k) of the N x K operand is W(n, k); a thread
+    // takes 8 consecutive k of one row (consecutive threads, consecutive
+    // rows: the 16-byte stores of a warp fall into distinct banks)
+    for (int idx = tid; idx < npad * (kBK / 8); idx += kThreads) {
+        const int n = idx % npad, k0 = (idx / npad) * 8;
+        float x[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) x[e] = (n < g.N && k0 + e < g.K) ? g.W[n + (size_t)(k0 + e) * g.ldw] : 0.f;
+        put8_slices(sB, sliceB, tile_off(n, k0), x);
     }
     tc_fence_before();
     __syncthreads();
@@ -402,17 +411,19 @@ template <int CH> __global__ void __launch_bounds__(kThreads) k_update_tc(UpdArg
     };
     for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
         const int m0 = t * kBM;
-        // V tile -> A slices (rows m0.., unit-lower in stored form)
-        for (int idx = tid; idx < kBM * kBK; idx += kThreads) {
-            const int mi = idx % kBM, k = idx / kBM, gm = m0 + mi;
-            float v = 0.f;
-            if (gm < g.M && k < g.K) v = (gm > k) ? g.V[gm + (size_t)k * g.ldv] : (gm == k ? 1.f : 0.f);
-            __nv_bfloat16 h0, h1, h2;
-            split3(v, h0, h1, h2);
-            const uint32_t o = tile_off(mi, k);
-            *reinterpret_cast<__nv_bfloat16 *>(sA + o) = h0;
-            *reinterpret_cast<__nv_bfloat16 *>(sA + kSliceA + o) = h1;
-            *reinterpret_cast<__nv_bfloat16 *>(sA + 2 * kSliceA + o) = h2;
+        // V tile -> A slices (rows m0.., unit-lower in stored form), 8
+        // consecutive k of one row per thread as for W
+        for (int idx = tid; idx < kBM * (kBK / 8); idx += kThreads) {
+            const int mi = idx % kBM, k0 = (idx / kBM) * 8, gm = m0 + mi;
+            float x[8];
+#pragma unroll
+            for (int e = 0; e < 8; ++e) {
+                const int k = k0 + e;
+                float v = 0.f;
+                if (gm < g.M && k < g.K) v = (gm > k) ? g.V[gm + (size_t)k * g.ldv] : (gm == k ? 1.f : 0.f);
+                x[e] = v;
+            }
+            put8_slices(sA, kSliceA, tile_off(mi, k0), x);
         }
         fence_proxy_async();
         __syncthreads();
