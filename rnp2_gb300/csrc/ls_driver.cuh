@@ -31,11 +31,6 @@ struct RefineInfo {
 template <class T> int trsm_upper(size_t n, size_t nrhs, const T *a, size_t lda, T *b, size_t ldb, cudaStream_t st) {
     if (n == 0 || nrhs == 0) return kOk;
     KScope ks("trsm", st);
-    if (nrhs <= 32) {
-        k_trsm_multi<T, false><<<1, 1024, 0, st>>>((int)n, (int)nrhs, a, lda, b, ldb);
-        RNPGPU_CHECK_LAUNCH();
-        return kOk;
-    }
     k_trsm_upper<T><<<(unsigned)std::min<size_t>(nrhs, 65535), 512, 0, st>>>((int)n, (int)nrhs, a, lda, b, ldb);
     RNPGPU_CHECK_LAUNCH();
     return kOk;
@@ -44,11 +39,6 @@ template <class T> int trsm_upper(size_t n, size_t nrhs, const T *a, size_t lda,
 template <class T> int trsm_upper_ct(size_t n, size_t nrhs, const T *a, size_t lda, T *b, size_t ldb, cudaStream_t st) {
     if (n == 0 || nrhs == 0) return kOk;
     KScope ks("trsm", st);
-    if (nrhs <= 32) {
-        k_trsm_multi<T, true><<<1, 1024, 0, st>>>((int)n, (int)nrhs, a, lda, b, ldb);
-        RNPGPU_CHECK_LAUNCH();
-        return kOk;
-    }
     k_trsm_upper_ct<T><<<(unsigned)std::min<size_t>(nrhs, 65535), 512, 0, st>>>((int)n, (int)nrhs, a, lda, b, ldb);
     RNPGPU_CHECK_LAUNCH();
     return kOk;

@@ -97,77 +97,6 @@ template <class T> __global__ void __launch_bounds__(512) k_trsm_upper_ct(int n,
     }
 }
 
-// Up to 32 right-hand sides in one block of 1024 threads: R is read once for
-// all of them.  Per 32 x 32 diagonal block, warp w solves right-hand side w
-// with shuffles (the block staged in shared memory), then all threads update
-// the remaining rows of every right-hand side (one (row, rhs) entry per
-// thread and step, 32 independent loads of R in flight).
-//   CT = false: X = R^{-1} Y (backward, rows above each block)
-//   CT = true : X = R^{-H} Y (forward, rows below each block)
-template <class T, bool CT> __global__ void __launch_bounds__(1024) k_trsm_multi(int n, int nrhs, const T *R, size_t ldr, T *B, size_t ldb) {
-    __shared__ T sD[32][33];
-    __shared__ T sX[32][33];
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int nblk = (n + 31) / 32;
-    for (int bi = 0; bi < nblk; ++bi) {
-        // block of rows [i0, i1): from the bottom for R, from the top for R^H
-        const int i0 = CT ? bi * 32 : max(0, n - (bi + 1) * 32);
-        const int i1 = CT ? min(n, i0 + 32) : n - bi * 32;
-        const int nbk = i1 - i0;
-        for (int idx = tid; idx < 32 * 32; idx += 1024) {
-            const int r = idx % 32, c = idx / 32;
-            sD[r][c] = (r < nbk && c < nbk && r <= c) ? R[(i0 + r) + (size_t)(i0 + c) * ldr] : T(0);
-        }
-        __syncthreads();
-        if (warp < nrhs) {
-            T *y = B + (size_t)warp * ldb;
-            T yv = (lane < nbk) ? y[i0 + lane] : T(0);
-            if (!CT) {
-                for (int i = nbk - 1; i >= 0; --i) {
-                    if (lane == i) yv = yv / sD[i][i];
-                    const T xi = shfl(yv, i);
-                    if (lane < i) yv = yv - sD[lane][i] * xi;
-                }
-            } else {
-                for (int i = 0; i < nbk; ++i) {
-                    if (lane == i) yv = yv / Tr<T>::conj(sD[i][i]);
-                    const T xi = shfl(yv, i);
-                    if (lane > i && lane < nbk) yv = yv - Tr<T>::conj(sD[i][lane]) * xi;
-                }
-            }
-            if (lane < nbk) y[i0 + lane] = yv;
-            sX[warp][lane] = (lane < nbk) ? yv : T(0);
-        }
-        __syncthreads();
-        // remaining rows: above the block (R) or below it (R^H)
-        const int rbeg = CT ? i1 : 0, rcount = CT ? n - i1 : i0;
-        for (int item = tid; item < rcount * nrhs; item += 1024) {
-            const int r = rbeg + item % rcount, w = item / rcount;
-            T a[4] = {T(0), T(0), T(0), T(0)};
-            if (!CT) {
-                const T *rc = R + r + (size_t)i0 * ldr;
-                if (nbk == 32 && sizeof(T) <= 8) {
-#pragma unroll
-                    for (int c = 0; c < 32; ++c) a[c & 3] = fmac(rc[(size_t)c * ldr], sX[w][c], a[c & 3]);
-                } else {
-                    for (int c = 0; c < nbk; ++c) a[0] = fmac(rc[(size_t)c * ldr], sX[w][c], a[0]);
-                }
-            } else {
-                const T *rc = R + i0 + (size_t)r * ldr;
-                if (nbk == 32 && sizeof(T) <= 8) {
-#pragma unroll
-                    for (int c = 0; c < 32; ++c) a[c & 3] = fmac(Tr<T>::conj(rc[c]), sX[w][c], a[c & 3]);
-                } else {
-                    for (int c = 0; c < nbk; ++c) a[0] = fmac(Tr<T>::conj(rc[c]), sX[w][c], a[0]);
-                }
-            }
-            T *yp = B + r + (size_t)w * ldb;
-            *yp = *yp - ((a[0] + a[1]) + (a[2] + a[3]));
-        }
-        __syncthreads();
-    }
-}
-
 template <class Tin, class Tout> __device__ __forceinline__ Tout convert_scalar(Tin v);
 template <> __device__ __forceinline__ float convert_scalar<double, float>(double v) { return (float)v; }
 template <> __device__ __forceinline__ double convert_scalar<float, double>(float v) { return (double)v; }

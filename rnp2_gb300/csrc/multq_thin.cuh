@@ -97,13 +97,15 @@ template <class T, bool CSMEM, int VBUF> __global__ void __launch_bounds__(kThin
     // the block and columns beyond its width as zeros, the diagonal as ones
     auto stage_v = [&](int bb, T *buf) {
         const int i = bb * kPanelMaxCols, ib = min(kPanelMaxCols, p.k - i), rs = max(r0, i);
-        const int nr = r1 - rs;
-        for (int e = tid; e < nr * kPanelMaxCols; e += kThinThreads) {
-            const int rr = e % nr, l = e / nr, r = rs + rr;
-            T *dst = buf + (size_t)l * R + (r - r0);
-            if (l >= ib || r < i + l) *dst = T(0);
-            else if (r == i + l) *dst = T(1);
-            else stage_elem(dst, p.A + r + (size_t)(i + l) * p.lda);
+        // columns outer, rows inner: no index division per element
+        for (int l = 0; l < kPanelMaxCols; ++l) {
+            const T *src = p.A + (size_t)(i + l) * p.lda;
+            T *dcol = buf + (size_t)l * R - r0;
+            for (int r = rs + tid; r < r1; r += kThinThreads) {
+                if (l >= ib || r < i + l) dcol[r] = T(0);
+                else if (r == i + l) dcol[r] = T(1);
+                else stage_elem(dcol + r, src + r);
+            }
         }
         cp_async_commit();
     };
