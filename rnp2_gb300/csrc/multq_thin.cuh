@@ -100,11 +100,12 @@ template <class T, bool CSMEM, int VBUF> __global__ void __launch_bounds__(kThin
         // columns outer, rows inner: no index division per element
         for (int l = 0; l < kPanelMaxCols; ++l) {
             const T *src = p.A + (size_t)(i + l) * p.lda;
-            T *dcol = buf + (size_t)l * R - r0;
+            T *dcol = buf + (size_t)l * R;
             for (int r = rs + tid; r < r1; r += kThinThreads) {
-                if (l >= ib || r < i + l) dcol[r] = T(0);
-                else if (r == i + l) dcol[r] = T(1);
-                else stage_elem(dcol + r, src + r);
+                T *dst = dcol + (r - r0);
+                if (l >= ib || r < i + l) *dst = T(0);
+                else if (r == i + l) *dst = T(1);
+                else stage_elem(dst, src + r);
             }
         }
         cp_async_commit();
