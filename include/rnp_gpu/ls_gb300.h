@@ -61,6 +61,18 @@ typedef struct {
 int rnpgpu_dsgels(size_t m, size_t n, size_t nrhs, const double *a, size_t lda, const double *b, size_t ldb, double *x, size_t ldx, int max_iter, int flags, rnpgpu_refine_info *info, size_t *lwork, double *work);
 int rnpgpu_zcgels(size_t m, size_t n, size_t nrhs, const rnpgpu_complex_double *a, size_t lda, const rnpgpu_complex_double *b, size_t ldb, rnpgpu_complex_double *x, size_t ldx, int max_iter, int flags, rnpgpu_refine_info *info, size_t *lwork, rnpgpu_complex_double *work);
 
+/* ---- FP64-accurate residual of a real least-squares problem (no reference
+ *      counterpart; the product a refinement loop needs): r = b - A x
+ *      (m x nrhs) and, when g != NULL, g = A^T r (n x nrhs).  The products run
+ *      on the BF16 tensor cores from exact fixed-point slices of A, x and r
+ *      (eight 7-bit digits each, relative to per-column / per-right-hand-side
+ *      powers of two), so the error is that of an FP64 dot product, about
+ *      2^-50 of sum_k |a_ik| |x_kj| scaled to the column maxima; Inf or NaN in
+ *      A or x makes the affected results NaN.  r may be b (in place).
+ *      work: device workspace of *lwork_bytes bytes (query with work == NULL
+ *      or *lwork_bytes == 0). ---- */
+int rnpgpu_dls_residual(size_t m, size_t n, size_t nrhs, const double *a, size_t lda, const double *x, size_t ldx, const double *b, size_t ldb, double *r, size_t ldr, double *g, size_t ldg, void *work, size_t *lwork_bytes);
+
 #ifdef __cplusplus
 }
 #endif

@@ -50,6 +50,7 @@ def _signatures():
         sig["rnpgpu_%sgels" % p] = [SZ, SZ, SZ, P, SZ, P, P, SZ, PSZ, P]
     for name in ("rnpgpu_dsgels", "rnpgpu_zcgels"):
         sig[name] = [SZ, SZ, SZ, P, SZ, P, SZ, P, SZ, C.c_int, C.c_int, C.POINTER(RefineInfo), PSZ, P]
+    sig["rnpgpu_dls_residual"] = [SZ, SZ, SZ, P, SZ, P, SZ, P, SZ, P, SZ, P, SZ, P, PSZ]
     sig["rnpgpu_set_stream"] = [P]
     sig["rnpgpu_get_stream"] = []
     sig["rnpgpu_get_last_error"] = []

@@ -14,6 +14,7 @@
 #pragma once
 #include "ls_kernels.cuh"
 #include "qr_driver.cuh"
+#include "oz_gemm.cuh"
 #include <cmath>
 #include <vector>
 
@@ -98,8 +99,11 @@ template <class T> int gels(size_t m, size_t n, size_t nrhs, T *a, size_t lda, T
 // mixed precision least squares with iterative refinement
 // ---------------------------------------------------------------------------
 template <class TH, class TL> struct RefinePlan {
-    size_t af, tauf, ts, wq, r, rf, p, g, norms, total;
+    size_t af, tauf, ts, wq, r, rf, p, g, norms, cexp, rexp, total;
     int split;
+    // the FP64 products r = b - A x and A^T r on the tensor cores (exact
+    // integer slices) for real FP64 data; other types use FP64 FMA
+    static constexpr bool kOz = std::is_same<TH, double>::value;
     RefinePlan(size_t m, size_t n, size_t nrhs) {
         auto al = [](size_t b) { return (b + 255) / 256 * 256; };
         af = al(m * n * sizeof(TL));
@@ -113,7 +117,10 @@ template <class TH, class TL> struct RefinePlan {
         g = al(n * nrhs * sizeof(TH));
         norms = al((n + 6 * nrhs) * sizeof(double));
         rf = std::max(rf, al(n * nrhs * sizeof(TL)));
-        total = af + tauf + ts + wq + r + rf + p + g + norms;
+        cexp = kOz ? oz_colexp_bytes(n) : 0;
+        rexp = kOz ? oz_rexp_bytes(nrhs) : 0;
+        if (kOz) p = std::max(p, oz_partial_bytes(n));
+        total = af + tauf + ts + wq + r + rf + p + g + norms + cexp + rexp;
     }
 };
 
@@ -149,6 +156,9 @@ int gels_refine(size_t m, size_t n, size_t nrhs, const TH *a, size_t lda, const 
     TH *P = cv.take<TH>(plan.p / sizeof(TH));
     TH *g = cv.take<TH>(plan.g / sizeof(TH));
     double *dn = cv.take<double>(plan.norms / sizeof(double));
+    int *cexp = cv.take<int>(plan.cexp / sizeof(int));
+    int *rexp = cv.take<int>(plan.rexp / sizeof(int));
+    constexpr bool oz = RefinePlan<TH, TL>::kOz;
     const size_t lwq = plan.wq / sizeof(TL);
     const dim3 gmn((unsigned)std::min<size_t>((m + 255) / 256, 2048), (unsigned)std::min<size_t>(n, 65535));
     const dim3 gmr((unsigned)std::min<size_t>((m + 255) / 256, 2048), (unsigned)std::min<size_t>(nrhs, 65535));
@@ -164,8 +174,12 @@ int gels_refine(size_t m, size_t n, size_t nrhs, const TH *a, size_t lda, const 
 
     // ||A||_F and ||b_j|| in FP64
     std::vector<double> h(n + 6 * nrhs);
-    k_col_sumsq<TH><<<cb, 256, 0, st>>>((int)m, (int)n, a, lda, dn);
-    RNPGPU_CHECK_LAUNCH();
+    if constexpr (oz) {
+        if ((rc = oz_column_scales((int)m, (int)n, a, lda, cexp, dn, st))) return rc;
+    } else {
+        k_col_sumsq<TH><<<cb, 256, 0, st>>>((int)m, (int)n, a, lda, dn);
+        RNPGPU_CHECK_LAUNCH();
+    }
     k_col_sumsq<TH><<<cb, 256, 0, st>>>((int)m, (int)nrhs, b, ldb, dn + n);
     RNPGPU_CHECK_LAUNCH();
     RNPGPU_CHECK(cudaMemcpyAsync(h.data(), dn, (n + nrhs) * sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -199,16 +213,20 @@ int gels_refine(size_t m, size_t n, size_t nrhs, const TH *a, size_t lda, const 
     //                                   estimate of the LS backward error)
     double eta = HUGE_VAL, mu = HUGE_VAL;
     auto check = [&]() -> int {
-        const int S = choose_splits((int)m, ((int)n + 127) / 128, plan.split);
-        const int kchunk = (((int)m + S - 1) / S + 15) / 16 * 16;
-        const int nsplit = ((int)m + kchunk - 1) / kchunk;
-        GemmArgs<TH> ga = gemm_args<TH>(a, lda, kOpC, 0, r, m, kOpN, 0, P, n, (int)n, (int)nrhs, (int)m, TH(1), kBetaZero);
-        ga.kchunk = kchunk;
-        ga.dstride = n * nrhs;
-        int rc2 = launch_gemm(ga, nsplit, st, "normal_eq_fp64");
-        if (rc2) return rc2;
-        k_sum_partials<TH><<<gnr, 256, 0, st>>>(P, n, n * nrhs, nsplit, (int)n, (int)nrhs, g, n);
-        RNPGPU_CHECK_LAUNCH();
+        int rc2;
+        if constexpr (oz) {
+            if ((rc2 = oz_normal((int)m, (int)n, (int)nrhs, a, lda, r, m, g, n, cexp, rexp, P, st))) return rc2;
+        } else {
+            const int S = choose_splits((int)m, ((int)n + 127) / 128, plan.split);
+            const int kchunk = (((int)m + S - 1) / S + 15) / 16 * 16;
+            const int nsplit = ((int)m + kchunk - 1) / kchunk;
+            GemmArgs<TH> ga = gemm_args<TH>(a, lda, kOpC, 0, r, m, kOpN, 0, P, n, (int)n, (int)nrhs, (int)m, TH(1), kBetaZero);
+            ga.kchunk = kchunk;
+            ga.dstride = n * nrhs;
+            if ((rc2 = launch_gemm(ga, nsplit, st, "normal_eq_fp64"))) return rc2;
+            k_sum_partials<TH><<<gnr, 256, 0, st>>>(P, n, n * nrhs, nsplit, (int)n, (int)nrhs, g, n);
+            RNPGPU_CHECK_LAUNCH();
+        }
         k_col_sumsq<TH><<<(unsigned)std::min<size_t>(nrhs, 4096), 256, 0, st>>>((int)n, (int)nrhs, g, n, dn + n + 3 * nrhs);
         RNPGPU_CHECK_LAUNCH();
         k_convert<TH, TL><<<gnr, 256, 0, st>>>((int)n, (int)nrhs, g, n, gf, n);
@@ -255,9 +273,13 @@ int gels_refine(size_t m, size_t n, size_t nrhs, const TH *a, size_t lda, const 
         k_col_sumsq<TH><<<(unsigned)std::min<size_t>(nrhs, 4096), 256, 0, st>>>((int)n, (int)nrhs, x, ldx, dn + n + 2 * nrhs);
         RNPGPU_CHECK_LAUNCH();
         // r = b - A x in FP64
-        RNPGPU_CHECK(cudaMemcpy2DAsync(r, m * sizeof(TH), b, ldb * sizeof(TH), m * sizeof(TH), nrhs, cudaMemcpyDeviceToDevice, st));
-        GemmArgs<TH> gr = gemm_args<TH>(a, lda, kOpN, 0, x, ldx, kOpN, 0, r, m, (int)m, (int)nrhs, (int)n, TH(-1), kBetaOne);
-        if ((rc = launch_gemm(gr, 1, st, "residual_fp64"))) return rc;
+        if constexpr (oz) {
+            if ((rc = oz_residual((int)m, (int)n, (int)nrhs, a, lda, x, ldx, b, ldb, r, m, cexp, rexp, st))) return rc;
+        } else {
+            RNPGPU_CHECK(cudaMemcpy2DAsync(r, m * sizeof(TH), b, ldb * sizeof(TH), m * sizeof(TH), nrhs, cudaMemcpyDeviceToDevice, st));
+            GemmArgs<TH> gr = gemm_args<TH>(a, lda, kOpN, 0, x, ldx, kOpN, 0, r, m, (int)m, (int)nrhs, (int)n, TH(-1), kBetaOne);
+            if ((rc = launch_gemm(gr, 1, st, "residual_fp64"))) return rc;
+        }
         ++it;
         if ((rc = correction_size(corr))) return rc;
         // Q steps contract fast, so failing to halve means they have stalled;

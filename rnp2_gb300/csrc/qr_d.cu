@@ -5,3 +5,8 @@
 #define RNPGPU_LOW_T float
 #define RNPGPU_MIXED_FN rnpgpu_dsgels
 #include "qr_type.inc"
+
+extern "C" int rnpgpu_dls_residual(size_t m, size_t n, size_t nrhs, const double *a, size_t lda, const double *x, size_t ldx, const double *b, size_t ldb, double *r, size_t ldr,
+                                   double *g, size_t ldg, void *work, size_t *lwork_bytes) {
+    return rnpgpu::ls_residual(m, n, nrhs, a, lda, x, ldx, b, ldb, r, ldr, g, ldg, work, lwork_bytes);
+}

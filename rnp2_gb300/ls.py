@@ -4,6 +4,8 @@ tensors in column-major layout (see rnp2_gb300.qr).
   gels(A, B)            plain: Factor, MultQ("L","C"), triangular solve; in place
   gels_refine(A, B)     mixed: FP32 factor + FP64 iterative refinement
   trsm_upper(R, B)      B <- R^{-1} B, R upper triangular (SolveTrM "L","U","N","N")
+  residual(A, X, B)     R = B - A X and optionally G = A^T R, FP64-accurate on
+                        the tensor cores (FP64 real data)
 """
 import ctypes as C
 
@@ -75,3 +77,28 @@ def gels_refine(A, B, X=None, max_iter=0, work=None, forward=False):
     lw = C.c_size_t(work.numel())
     _check("gels_refine", fn(m, n, nrhs, a, lda, b, ldb, x, ldx, int(max_iter), 1 if forward else 0, C.byref(info), C.byref(lw), work.data_ptr()))
     return X, info.as_dict()
+
+
+def residual(A, X, B, R=None, normal=False, work=None):
+    """R = B - A X (and G = A^T R when normal=True) for FP64 A (m x n), X
+    (n x nrhs), B (m x nrhs), computed from exact fixed-point slices on the
+    tensor cores.  Returns R, or (R, G)."""
+    m, n = A.shape
+    nrhs = B.shape[1]
+    if R is None:
+        R = empty_colmajor(m, nrhs, torch.float64, A.device)
+    G = empty_colmajor(n, nrhs, torch.float64, A.device) if normal else None
+    a, lda = colmajor(A)
+    x, ldx = colmajor(X)
+    b, ldb = colmajor(B)
+    r, ldr = colmajor(R)
+    g, ldg = colmajor(G) if normal else (None, max(n, 1))
+    fn = lib().rnpgpu_dls_residual
+    _bind_stream()
+    if work is None:
+        lw = C.c_size_t(0)
+        _check("dls_residual", fn(m, n, nrhs, a, lda, x, ldx, b, ldb, r, ldr, g, ldg, None, C.byref(lw)))
+        work = torch.empty(max(lw.value, 1), dtype=torch.uint8, device=A.device)
+    lw = C.c_size_t(work.numel())
+    _check("dls_residual", fn(m, n, nrhs, a, lda, x, ldx, b, ldb, r, ldr, g, ldg, work.data_ptr(), C.byref(lw)))
+    return (R, G) if normal else R
