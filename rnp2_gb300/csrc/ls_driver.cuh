@@ -99,7 +99,7 @@ template <class T> int gels(size_t m, size_t n, size_t nrhs, T *a, size_t lda, T
 // mixed precision least squares with iterative refinement
 // ---------------------------------------------------------------------------
 template <class TH, class TL> struct RefinePlan {
-    size_t af, tauf, ts, wq, r, rf, p, g, norms, cexp, rexp, total;
+    size_t af, tauf, ts, wq, r, rf, p, g, norms, ozw, total;
     int split;
     // the FP64 products r = b - A x and A^T r on the tensor cores (exact
     // integer slices) for real FP64 data; other types use FP64 FMA
@@ -117,10 +117,8 @@ template <class TH, class TL> struct RefinePlan {
         g = al(n * nrhs * sizeof(TH));
         norms = al((n + 6 * nrhs) * sizeof(double));
         rf = std::max(rf, al(n * nrhs * sizeof(TL)));
-        cexp = kOz ? oz_colexp_bytes(n) : 0;
-        rexp = kOz ? oz_rexp_bytes(nrhs) : 0;
-        if (kOz) p = std::max(p, oz_partial_bytes(n));
-        total = af + tauf + ts + wq + r + rf + p + g + norms + cexp + rexp;
+        ozw = kOz ? OzWork::bytes(m, n, nrhs) : 0;
+        total = af + tauf + ts + wq + r + rf + p + g + norms + ozw;
     }
 };
 
@@ -156,9 +154,9 @@ int gels_refine(size_t m, size_t n, size_t nrhs, const TH *a, size_t lda, const 
     TH *P = cv.take<TH>(plan.p / sizeof(TH));
     TH *g = cv.take<TH>(plan.g / sizeof(TH));
     double *dn = cv.take<double>(plan.norms / sizeof(double));
-    int *cexp = cv.take<int>(plan.cexp / sizeof(int));
-    int *rexp = cv.take<int>(plan.rexp / sizeof(int));
-    constexpr bool oz = RefinePlan<TH, TL>::kOz;
+    constexpr bool use_oz = RefinePlan<TH, TL>::kOz;
+    OzWork ow{};
+    if (use_oz) ow.carve(cv, m, n, nrhs);
     const size_t lwq = plan.wq / sizeof(TL);
     const dim3 gmn((unsigned)std::min<size_t>((m + 255) / 256, 2048), (unsigned)std::min<size_t>(n, 65535));
     const dim3 gmr((unsigned)std::min<size_t>((m + 255) / 256, 2048), (unsigned)std::min<size_t>(nrhs, 65535));
@@ -166,17 +164,20 @@ int gels_refine(size_t m, size_t n, size_t nrhs, const TH *a, size_t lda, const 
     const unsigned cb = (unsigned)std::min<size_t>(std::max(n, nrhs), 4096);
     int rc;
 
-    // low-precision working copy and its factorization
-    k_convert<TH, TL><<<gmn, 256, 0, st>>>((int)m, (int)n, a, lda, Af, m);
-    RNPGPU_CHECK_LAUNCH();
+    // low-precision working copy and its factorization (for real FP64 data the
+    // same pass writes the packed digits of A for the residual products)
+    if constexpr (use_oz) {
+        if ((rc = oz_prepare_a((int)m, (int)n, a, lda, ow, dn, Af, m, st))) return rc;
+    } else {
+        k_convert<TH, TL><<<gmn, 256, 0, st>>>((int)m, (int)n, a, lda, Af, m);
+        RNPGPU_CHECK_LAUNCH();
+    }
     size_t lw = lwq;
     if ((rc = geqrf<TL>(m, n, Af, m, tauf, &lw, wq, Tf))) return rc < 0 ? -13 : rc;
 
     // ||A||_F and ||b_j|| in FP64
     std::vector<double> h(n + 6 * nrhs);
-    if constexpr (oz) {
-        if ((rc = oz_column_scales((int)m, (int)n, a, lda, cexp, dn, st))) return rc;
-    } else {
+    if constexpr (!use_oz) {
         k_col_sumsq<TH><<<cb, 256, 0, st>>>((int)m, (int)n, a, lda, dn);
         RNPGPU_CHECK_LAUNCH();
     }
@@ -214,8 +215,8 @@ int gels_refine(size_t m, size_t n, size_t nrhs, const TH *a, size_t lda, const 
     double eta = HUGE_VAL, mu = HUGE_VAL;
     auto check = [&]() -> int {
         int rc2;
-        if constexpr (oz) {
-            if ((rc2 = oz_normal((int)m, (int)n, (int)nrhs, a, lda, r, m, g, n, cexp, rexp, P, st))) return rc2;
+        if constexpr (use_oz) {
+            if ((rc2 = oz_normal((int)m, (int)n, (int)nrhs, ow, r, m, g, n, st))) return rc2;
         } else {
             const int S = choose_splits((int)m, ((int)n + 127) / 128, plan.split);
             const int kchunk = (((int)m + S - 1) / S + 15) / 16 * 16;
@@ -273,8 +274,8 @@ int gels_refine(size_t m, size_t n, size_t nrhs, const TH *a, size_t lda, const 
         k_col_sumsq<TH><<<(unsigned)std::min<size_t>(nrhs, 4096), 256, 0, st>>>((int)n, (int)nrhs, x, ldx, dn + n + 2 * nrhs);
         RNPGPU_CHECK_LAUNCH();
         // r = b - A x in FP64
-        if constexpr (oz) {
-            if ((rc = oz_residual((int)m, (int)n, (int)nrhs, a, lda, x, ldx, b, ldb, r, m, cexp, rexp, st))) return rc;
+        if constexpr (use_oz) {
+            if ((rc = oz_residual((int)m, (int)n, (int)nrhs, ow, x, ldx, b, ldb, r, m, st))) return rc;
         } else {
             RNPGPU_CHECK(cudaMemcpy2DAsync(r, m * sizeof(TH), b, ldb * sizeof(TH), m * sizeof(TH), nrhs, cudaMemcpyDeviceToDevice, st));
             GemmArgs<TH> gr = gemm_args<TH>(a, lda, kOpN, 0, x, ldx, kOpN, 0, r, m, (int)m, (int)nrhs, (int)n, TH(-1), kBetaOne);
