@@ -167,6 +167,7 @@ int gels_refine(size_t m, size_t n, size_t nrhs, const TH *a, size_t lda, const 
     // low-precision working copy and its factorization (for real FP64 data the
     // same pass writes the packed digits of A for the residual products)
     if constexpr (use_oz) {
+        KScope ks("prepare_digits", st);
         if ((rc = oz_prepare_a((int)m, (int)n, a, lda, ow, dn, Af, m, st))) return rc;
     } else {
         k_convert<TH, TL><<<gmn, 256, 0, st>>>((int)m, (int)n, a, lda, Af, m);
@@ -175,7 +176,8 @@ int gels_refine(size_t m, size_t n, size_t nrhs, const TH *a, size_t lda, const 
     size_t lw = lwq;
     if ((rc = geqrf<TL>(m, n, Af, m, tauf, &lw, wq, Tf))) return rc < 0 ? -13 : rc;
 
-    // ||A||_F and ||b_j|| in FP64
+    // ||A||_F (real FP64 data: from the FP32 working copy, which only scales
+    // the stopping test) and ||b_j|| in FP64
     std::vector<double> h(n + 6 * nrhs);
     if constexpr (!use_oz) {
         k_col_sumsq<TH><<<cb, 256, 0, st>>>((int)m, (int)n, a, lda, dn);

@@ -1,5 +1,5 @@
 // oz_gemm.cuh — the FP64 products of the mixed least-squares refinement,
-// r = b - A x and g = A^T r, on the BF16 tensor cores by exact integer
+// r = b - A x and g = A^T r, on the FP16 tensor cores by exact integer
 // slicing.
 //
 // On this GPU the FP64 pipe runs at about 1.2 TFLOP/s: as FP64 FMAs each of
@@ -17,14 +17,15 @@
 //   scale 2^f_j chosen the same way for the scaled values;
 // * a scaled value v in (-1/2, 1/2) is rounded to the integer N = round(v 2^56)
 //   and written as eight balanced base-128 digits, v ~ sum_p d_p 2^(-7(p+1)),
-//   d_p an integer in [-64, 64] (exact in BF16);
+//   d_p an integer in [-64, 64] (exact in FP16);
 // * a digit product d_p D_q is an integer of magnitude <= 2^12; the products
 //   of one level L = p + q go into one FP32 tensor-memory accumulator.  Over
 //   512 K values a level L <= 4 stays below 5 * 2^12 * 2^9 < 2^24, so those
 //   sums are exact integers; levels 5..7 weigh less than 2^-35 relative, where
 //   FP32 rounding of their sums no longer matters; levels >= 8 are dropped;
-// * the levels are combined in FP64 every 512 K values and at the end,
-//   result = 2^scale * 2^-14 * sum_L 2^(-7L) S_L.
+// * every 512 K values the exact levels are combined exactly in 64-bit
+//   integers, sum_{L<=4} S_L 2^(7(4-L)) (< 2^53), the others in FP32, and at
+//   the end result = 2^scale * 2^-14 * sum_L 2^(-7L) S_L in FP64.
 //
 // The error is that of representing both operands to 2^-56 of their scales
 // plus the dropped levels: about 2^-50 of sum_k 2^e_k |x_kj| 2^(f_j - e_k) —
@@ -33,7 +34,10 @@
 // Tensor-core layout.  One accumulation D (128 TMEM lanes x 128 FP32 columns)
 // per 128 rows of A (residual) or 128 columns of A (A^T r): lane = that row or
 // column, column c = 16 b + j holds level 7 - b of right-hand side j.  The
-// A tile's digits are eight K-major planes (the UMMA A operand, M = 128); the
+// A tile's digits are eight planes in tensor memory (the UMMA A operand,
+// M = 128: row i in lane i, K packed two FP16 per column), written by the
+// converter warps with tcgen05.st so that shared memory only carries the
+// packed bytes and the stacks; the
 // other operand's digits are one stack of eight 16-row blocks, block b = digit
 // 7 - b (the UMMA B operand).  Digit plane p multiplies the window of blocks
 // p..7 (N = 16 (8 - p)) into columns 0 .. 16 (8 - p): column block b' then
@@ -44,21 +48,38 @@
 // Operand preparation.  A does not change during a solve, so its digits are
 // extracted once (k_adigits, fused with the FP32 copy the factorization
 // needs) into a packed form of the same size as the FP64 matrix: eight bytes
-// per element, byte p = (d_p + 64) xor 64, so that zero bytes mean zero
-// digits (the padding to whole 128 x 128 tiles is zero).  The other operand
-// (x, or r for A^T r) is small; k_xstack / k_rstack compute its scales f_j and
-// write its digits directly as the BF16 digit-stack image of every 16-K step.
+// per element, byte p = (d_p + 64) xor 64 (zero bytes are zero digits),
+// stored in 16 x 16 element blocks (2 KB: row-major, the 16-byte chunks of
+// row r rotated by xor with r mod 8) so that one 16-K step of either product
+// is eight whole blocks: contiguous for the residual (block column), eight
+// 2 KB pieces for A^T r (block row).  A is padded with zero blocks to whole
+// 128 x 128 tiles.  The other operand (x, or r for A^T r) is small;
+// k_xstack / k_rstack compute its scales f_j and write its digits directly as
+// the FP16 digit-stack image of every 16-K step (the UMMA B operand, read by
+// the tensor core straight from the staging buffer).
 //
-// CTA of k_oz: 8 producer warps (cp.async of the packed digits and the stack
-// images NR - 1 steps ahead, byte -> BF16 expansion, 16-byte stores into the
-// digit stage; one thread issues the eight tcgen05.mma per 16-K step and
-// commits them to the stage's mbarrier) and 4 drain warps (tcgen05.ld of a
-// finished accumulator, FP64 level combination, output), two accumulator sets
-// so that the drain of one chunk overlaps the MMAs of the next.  Every wait is
-// bounded.
+// CTA of k_oz (warp-specialised, all hand-offs on mbarriers):
+//   warp 16       one thread issues the bulk copies (cp.async.bulk) of each
+//                 step's A blocks into a ring of kNA buffers (freed by the
+//                 converters); warp 22 the same for the stack images (ring of
+//                 kNT, freed by the MMAs), so that neither waits on the other
+//                 and the A copies run up to kNA steps ahead;
+//   warps 0..15   two groups of eight warps, for even and odd steps (so that
+//                 one group's waits overlap the other's work), expand the
+//                 packed bytes of a step into the eight FP16 digit planes of
+//                 one of kNS tensor-memory stages (tcgen05.st);
+//   warp 17       issues the eight tcgen05.mma of a step from one elected
+//                 lane and commits them to the stage's and the stack buffer's
+//                 mbarriers (and to the accumulator's at a chunk end);
+//   warps 18..21  drain a finished accumulator (tcgen05.ld), combine the
+//                 levels exactly in integer arithmetic (running sums in shared
+//                 memory), write the outputs.
+// Two accumulator sets let the drain of one chunk overlap the MMAs of the
+// next.  Every wait is bounded.
 #pragma once
 #include "ls_kernels.cuh"
 #include "qr_driver.cuh"
+#include <cuda_fp16.h>
 
 namespace rnpgpu {
 namespace oz {
@@ -67,19 +88,29 @@ constexpr int kDig = 8;                          // digits per operand
 constexpr int kKst = 16;                         // K values per step (one UMMA K)
 constexpr int kChunkSteps = 32;                  // steps per exact accumulation chunk (512 K)
 constexpr int kRhs = 16;                         // right-hand sides per launch
-constexpr int kProd = 256;                       // producer threads (warps 0..7)
-constexpr int kThreads = kProd + 128;            // + drain warps 8..11
-constexpr int kNR = 6;                           // FP64 staging buffers (kNR - 1 steps ahead)
-constexpr int kPlane = 128 * kKst * 2;           // one digit plane of the A tile (4 KB)
-constexpr int kStack = kDig * kRhs * kKst * 2;   // digit stack of the other operand (4 KB)
-constexpr int kStage = kDig * kPlane + kStack;   // 36 KB
-constexpr int kRawA = kProd * 64;                // 8 packed elements per producer thread (16 KB)
-constexpr int kRawX = kStack;                    // one stack image (16 bytes per producer thread)
-constexpr int kSmemStages = 2 * kStage;
-constexpr int kSmemRawA = kSmemStages;
-constexpr int kSmemRawX = kSmemRawA + kNR * kRawA;
-constexpr int kSmemCtl = kSmemRawX + kNR * kRawX;
-constexpr int kSmem = kSmemCtl + 256;
+constexpr int kConvWarps = 16;                   // converter warps 0..15
+constexpr int kLoadWarp = 16, kMmaWarp = 17;      // then the drain warps 18..21
+constexpr int kStackWarp = 22;
+constexpr int kThreads = 23 * 32;
+constexpr int kNA = 8;                           // staging ring of A blocks (bulk copies up to kNA steps ahead)
+constexpr int kNT = 8;                           // staging ring of stack images
+constexpr int kNS = 4;                           // digit-plane stages in TMEM
+constexpr int kBlock = 16 * 16 * 8;              // one 16 x 16 block of packed A (2 KB)
+constexpr int kRawA = 8 * kBlock;                // a step's A blocks (16 KB)
+constexpr int kStack = kDig * kRhs * kKst * 2;   // a step's stack image of the other operand (4 KB)
+constexpr int kPlaneCols = kKst / 2;            // one digit plane of the A tile in TMEM: 128 lanes x 8 columns
+constexpr int kStageCols = kDig * kPlaneCols;    // 64 columns per stage
+constexpr int kAccCols = 128;                    // one accumulator set
+constexpr int kTmemCols = 512;                   // 2 accumulator sets + kNS stages
+static_assert(2 * kAccCols + kNS * kStageCols <= kTmemCols, "tensor memory");
+constexpr int kSmemA = 0;
+constexpr int kSmemT = kSmemA + kNA * kRawA;
+constexpr int kSmemAcc = kSmemT + kNT * kStack;  // the drain's running sums: 128 rows x 16 x (8 + 4) bytes
+constexpr int kSmemCtl = kSmemAcc + 128 * kRhs * 12;
+constexpr int kCtlBytes = (2 * kNA + 2 * kNT + 2 * kNS + 4) * 8 + 8 + 3 * kRhs * 4;  // mbarriers, TMEM slot, flags
+constexpr int kSmem = kSmemCtl + (kCtlBytes + 255) / 256 * 256;
+// one CTA per SM: each allocates all of tensor memory
+static_assert(kSmem > 114 * 1024, "the shared-memory request must keep a second CTA off the SM");
 constexpr int kZeroExp = -(1 << 20);             // scale of an all-zero column / vector
 constexpr int kNonFinite = 1 << 20;              // an Inf or NaN was seen
 constexpr unsigned long long kBias = 0x81020408102040ull;  // 64 * sum_q 128^q, q = 0..7
@@ -89,8 +120,8 @@ enum Mode : int { kResidual = 0, kNormal = 1 };
 struct Args {
     int mode;
     int m, n, nrhs;             // nrhs <= 16
-    const uint2 *Ad;            // packed digits of A, padded to whole 128 x 128 tiles
-    size_t ldd;
+    const unsigned char *Ad;    // packed digits of A in 16 x 16 blocks, nbr block rows per block column
+    int nbr;
     const uint4 *XS;            // stack images of the other operand, one per 16-K step (256 x 16 bytes)
     const int *fexp;            // f_j of the other operand (16)
     const double *B;            // residual: b (m x nrhs)
@@ -147,8 +178,8 @@ __device__ __forceinline__ void oz_fields(double v, int se, uint32_t (&u)[kDig])
 // FP32; subtracting 2^23 + 64 leaves u - 64)
 __device__ __forceinline__ float oz_digit_value(uint32_t u) { return __uint_as_float(0x4B000000u | u) - 8388672.0f; }
 
-// BF16 bits of a digit: an exact FP32 integer of magnitude <= 64 is its own top 16 bits
-__device__ __forceinline__ uint16_t oz_digit_bf16(uint32_t u) { return (uint16_t)(__float_as_uint(oz_digit_value(u)) >> 16); }
+// FP16 bits of a digit (an integer of magnitude <= 64: exact)
+__device__ __forceinline__ uint16_t oz_digit_f16(uint32_t u) { return __half_as_ushort(__float2half_rn(oz_digit_value(u))); }
 
 // packed form of one element: byte p = u_p xor 64 (zero bytes = zero digits)
 __device__ __forceinline__ uint2 oz_pack(const uint32_t (&u)[kDig]) {
@@ -158,20 +189,31 @@ __device__ __forceinline__ uint2 oz_pack(const uint32_t (&u)[kDig]) {
     return w;
 }
 
-// byte offset of (row, k) in a K-major, no-swizzle BF16 tile with kKst = 16
+// byte offset of (row, k) in a K-major, no-swizzle 16-bit tile with kKst = 16
 // columns: core matrix (row/8, k/8) is 128 contiguous bytes
 __device__ __forceinline__ uint32_t toff(int row, int k) { return (uint32_t)(((row >> 3) * 2 + (k >> 3)) * 128 + (row & 7) * 16 + (k & 7) * 2); }
 
-template <int BYTES> __device__ __forceinline__ void cp_zfill(void *dst, const void *src, bool valid) {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src), "n"(BYTES), "r"(valid ? BYTES : 0) : "memory");
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(tc::smem_u32(bar)), "r"(bytes) : "memory");
 }
-template <int N> __device__ __forceinline__ void cp_wait_group() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+// bulk global -> shared copy completing on an mbarrier (16-byte aligned, size a multiple of 16)
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(tc::smem_u32(dst)), "l"(src), "r"(bytes), "r"(tc::smem_u32(bar))
+                 : "memory");
+}
 __device__ __forceinline__ void mbar_arrive(uint64_t *bar) { asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc::smem_u32(bar)) : "memory"); }
-// barrier 1 over the producer warps, and-reduction of a flag
-__device__ __forceinline__ int producers_and(int pred) {
-    int r;
-    asm volatile("{\n.reg .pred p, q;\nsetp.ne.s32 p, %1, 0;\nbar.red.and.pred q, 1, %2, p;\nselp.s32 %0, 1, 0, q;\n}\n" : "=r"(r) : "r"(pred), "n"(kProd) : "memory");
-    return r;
+// 32 lanes x 4 consecutive 32-bit TMEM columns from registers
+__device__ __forceinline__ void tmem_st4(uint32_t taddr, uint32_t r0, uint32_t r1, uint32_t r2, uint32_t r3) {
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1, %2, %3, %4};" ::"r"(taddr), "r"(r0), "r"(r1), "r"(r2), "r"(r3) : "memory");
+}
+__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+// instruction descriptor: FP16 x FP16 -> FP32, both operands K-major, M x N
+__host__ __device__ constexpr uint32_t idesc_f16(int M, int N) { return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24); }
+// D (TMEM) += A (TMEM) * B (shared memory descriptor), kind::f16 -> FP32
+__device__ __forceinline__ void umma_f16_ta(uint32_t tmem_d, uint32_t tmem_a, uint64_t bdesc, uint32_t idesc, uint32_t accumulate) {
+    asm volatile("{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n}\n" ::"r"(tmem_d), "r"(tmem_a), "l"(bdesc), "r"(idesc),
+                 "r"(accumulate)
+                 : "memory");
 }
 // 32 lanes x 8 consecutive 32-bit TMEM columns
 __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
@@ -188,74 +230,130 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
 // Operand preparation
 // ---------------------------------------------------------------------------
 // e_k = max_i floor(log2 |a_ik|) + 2 (kZeroExp for a zero column, kNonFinite
-// when the column holds an Inf or NaN) and, when sumsq != nullptr,
-// ||A(:,k)||_2^2 in FP64 (the same order of summation as k_col_sumsq); one
-// block per column
-template <int kTag> __global__ void __launch_bounds__(256) k_col_exp_sumsq(int m, int n, const double *A, size_t lda, int *colexp, double *sumsq) {
-    __shared__ double s[8];
+// when the column holds an Inf or NaN), from the exponent bits alone (no
+// floating-point work: the FP64 pipe of this GPU is slow); one block per column
+template <int kTag> __global__ void __launch_bounds__(256) k_col_exp(int m, int n, const double *A, size_t lda, int *colexp) {
     __shared__ int sx[8];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     for (int c = blockIdx.x; c < n; c += gridDim.x) {
-        double acc = 0.0;
         int ex = kZeroExp;
-        for (int r = tid; r < m; r += 256) {
-            const double v = A[r + (size_t)c * lda];
-            acc += v * v;
-            ex = max(ex, oz_exp(v));
+        const double *col = A + (size_t)c * lda;
+        int r = tid;
+        for (; r + 3 * 256 < m; r += 4 * 256) {
+            const int e0 = oz_exp(col[r]), e1 = oz_exp(col[r + 256]), e2 = oz_exp(col[r + 512]), e3 = oz_exp(col[r + 768]);
+            ex = max(ex, max(max(e0, e1), max(e2, e3)));
         }
-        acc = warp_sum(acc);
+        for (; r < m; r += 256) ex = max(ex, oz_exp(col[r]));
         ex = __reduce_max_sync(0xFFFFFFFFu, ex);
-        if (lane == 0) {
-            s[warp] = acc;
-            sx[warp] = ex;
-        }
+        if (lane == 0) sx[warp] = ex;
         __syncthreads();
         if (tid == 0) {
-            double t = 0.0;
             int e = kZeroExp;
-            for (int w = 0; w < 8; ++w) {
-                t += s[w];
-                e = max(e, sx[w]);
-            }
+            for (int w = 0; w < 8; ++w) e = max(e, sx[w]);
             colexp[c] = (e >= kNonFinite) ? kNonFinite : (e == kZeroExp ? kZeroExp : e + 2);
-            if (sumsq) sumsq[c] = t;
         }
         __syncthreads();
     }
 }
 
-// Ad(0:m, 0:n) = packed digits of A relative to 2^e_k; Af(0:m, 0:n) =
-// (float) A when Af != nullptr (the working copy of the FP32 factorization)
-template <int kTag> __global__ void __launch_bounds__(256) k_adigits(int m, int n, const double *A, size_t lda, const int *colexp, uint2 *Ad, size_t ldd, float *Af, size_t ldf) {
-    for (int c = blockIdx.y; c < n; c += gridDim.y) {
-        const int ek = colexp[c];
-        const bool live = ek > kZeroExp && ek < kNonFinite;
-        for (int r = blockIdx.x * 256 + threadIdx.x; r < m; r += gridDim.x * 256) {
-            const double v = A[r + (size_t)c * lda];
-            if (Af) Af[r + (size_t)c * ldf] = (float)v;
-            uint2 w = make_uint2(0u, 0u);
-            if (live) {
-                uint32_t u[kDig];
-                oz_fields(v, -ek, u);
-                w = oz_pack(u);
+// out[j] = ||Af(0:m, j)||_2^2 of the FP32 working copy, accumulated in FP32
+// with eight partial sums per thread and combined in FP64 (relative error
+// below 1e-6: the norm only scales the stopping test); one block per column
+template <int kTag> __global__ void __launch_bounds__(256) k_col_sumsq_f32(int m, int n, const float *Af, size_t ldf, double *out) {
+    __shared__ double s[8];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int c = blockIdx.x; c < n; c += gridDim.x) {
+        const float *col = Af + (size_t)c * ldf;
+        float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        int r = tid;
+        for (; r + 7 * 256 < m; r += 8 * 256) {
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const float v = col[r + u * 256];
+                acc[u] = fmaf(v, v, acc[u]);
             }
-            Ad[r + (size_t)c * ldd] = w;
+        }
+        for (; r < m; r += 256) acc[0] = fmaf(col[r], col[r], acc[0]);
+        double t = 0.0;
+#pragma unroll
+        for (int u = 0; u < 8; ++u) t += (double)acc[u];
+        t = warp_sum(t);
+        if (lane == 0) s[warp] = t;
+        __syncthreads();
+        if (tid == 0) {
+            double v = 0.0;
+            for (int w = 0; w < 8; ++w) v += s[w];
+            out[c] = v;
+        }
+        __syncthreads();
+    }
+}
+
+// byte offset of element (r, c) inside a 16 x 16 block of packed A: row-major
+// 128-byte rows whose 16-byte chunks (two elements) are rotated by r mod 8, so
+// that eight threads reading one chunk each of eight rows hit distinct banks
+__device__ __forceinline__ uint32_t blk_off(int r, int c) { return (uint32_t)(r * 128 + (((c >> 1) ^ (r & 7)) << 4) + ((c & 1) << 3)); }
+
+// Packed digits of A relative to 2^e_k in 16 x 16 blocks: block (bi, bk) at
+// byte (bk * nbr + bi) * 2048 of Ad, zero outside m x n (the grid covers
+// whole 128-row tiles and 16-column blocks: nbr = 8 * ceil(m / 128), and the
+// caller sizes the column blocks to 8 * ceil(n / 128)).  Af(0:m, 0:n) =
+// (float) A when Af != nullptr (the working copy of the FP32 factorization).
+// Thread (ml, g) of a block handles row ml of a 128-row tile and columns
+// 8g..8g+7 of a 16-column block: coalesced reads along each column, one
+// 16-byte chunk write per column pair.
+template <int kTag> __global__ void __launch_bounds__(256) k_adigits(int m, int n, int nbr, int nbc, const double *A, size_t lda, const int *colexp, unsigned char *Ad, float *Af, size_t ldf) {
+    const int ml = threadIdx.x & 127, g = threadIdx.x >> 7;
+    const int ntile = nbr / 8;
+    for (int bk = blockIdx.y; bk < nbc; bk += gridDim.y) {
+        for (int rt = blockIdx.x; rt < ntile; rt += gridDim.x) {
+            const int i = rt * 128 + ml;
+            uint2 w[8];
+#pragma unroll
+            for (int e = 0; e < 8; ++e) {
+                const int k = bk * 16 + 8 * g + e;
+                w[e] = make_uint2(0u, 0u);
+                if (i < m && k < n) {
+                    const double v = A[i + (size_t)k * lda];
+                    if (Af) Af[i + (size_t)k * ldf] = (float)v;
+                    const int ek = colexp[k];
+                    if (ek > kZeroExp && ek < kNonFinite) {
+                        uint32_t u[kDig];
+                        oz_fields(v, -ek, u);
+                        w[e] = oz_pack(u);
+                    }
+                }
+            }
+            unsigned char *blk = Ad + ((size_t)bk * nbr + (size_t)(rt * 8 + (ml >> 4))) * kBlock;
+            const int r = ml & 15;
+#pragma unroll
+            for (int e = 0; e < 8; e += 2) *reinterpret_cast<uint4 *>(blk + blk_off(r, 8 * g + e)) = make_uint4(w[e].x, w[e].y, w[e + 1].x, w[e + 1].y);
         }
     }
 }
 
-// the digit stack image of one element of the other operand: digit q of
-// right-hand side j at K offset kk goes to block 7 - q of the image
-__device__ __forceinline__ void oz_stack_put(unsigned char *img, int kk, int j, double v, int se) {
-    uint32_t u[kDig];
-    oz_fields(v, se, u);
+// Eight consecutive K values (kk = 8h .. 8h + 7) of right-hand side j of the
+// other operand, scaled by 2^se[e], into the stack image img: digit q goes to
+// block 7 - q, row 16 (7 - q) + j, as one 16-byte chunk per digit.
+__device__ __forceinline__ void oz_stack_put8(unsigned char *img, int h, int j, const double (&v)[8], const int (&se)[8]) {
+    uint32_t w[kDig][4];
 #pragma unroll
-    for (int q = 0; q < kDig; ++q) *reinterpret_cast<uint16_t *>(img + toff(16 * (7 - q) + j, kk)) = oz_digit_bf16(u[q]);
+    for (int e = 0; e < 8; e += 2) {
+        uint32_t ua[kDig], ub[kDig];
+        oz_fields(v[e], se[e], ua);
+        oz_fields(v[e + 1], se[e + 1], ub);
+#pragma unroll
+        for (int q = 0; q < kDig; ++q) w[q][e >> 1] = (uint32_t)oz_digit_f16(ua[q]) | ((uint32_t)oz_digit_f16(ub[q]) << 16);
+    }
+#pragma unroll
+    for (int q = 0; q < kDig; ++q) *reinterpret_cast<uint4 *>(img + toff(16 * (7 - q) + j, 8 * h)) = make_uint4(w[q][0], w[q][1], w[q][2], w[q][3]);
 }
 
 // x (n x nrhs, nrhs <= 16) for the residual: f_j = max_k (floor(log2 |x_kj|) + e_k) + 2,
-// then the stack image of every 16-row step of x scaled by 2^(e_k - f_j)
-template <int kTag> __global__ void __launch_bounds__(1024) k_xstack(int n, int nrhs, const double *X, size_t ldx, const int *colexp, int *fexp, uint4 *XS) {
+// then the stack image of every 16-row step of x scaled by 2^(e_k - f_j).
+// Every block computes f_j (x is small), then writes the images of its steps;
+// block 0 stores f_j.  Thread (j, h) of a 32-thread group handles K half h.
+template <int kTag> __global__ void __launch_bounds__(256) k_xstack(int n, int nrhs, const double *X, size_t ldx, const int *colexp, int *fexp, uint4 *XS) {
     __shared__ int sf[kRhs];
     const int tid = threadIdx.x, lane = tid & 31;
     if (tid < kRhs) sf[tid] = kZeroExp;
@@ -265,13 +363,14 @@ template <int kTag> __global__ void __launch_bounds__(1024) k_xstack(int n, int 
     for (int j = 0; j < kRhs; ++j) mx[j] = kZeroExp;
     for (int k = tid; k < n; k += blockDim.x) {
         const int ek = colexp[k];
+        double v[kRhs];
+#pragma unroll
+        for (int j = 0; j < kRhs; ++j) v[j] = (j < nrhs) ? X[k + ldx * (size_t)j] : 0.0;
 #pragma unroll
         for (int j = 0; j < kRhs; ++j) {
-            if (j < nrhs) {
-                const int ex = oz_exp(X[k + ldx * (size_t)j]);
-                if (ex >= kNonFinite) mx[j] = kNonFinite;
-                else if (ex > kZeroExp && ek > kZeroExp && ek < kNonFinite) mx[j] = max(mx[j], ex + ek + 2);
-            }
+            const int ex = oz_exp(v[j]);
+            if (ex >= kNonFinite) mx[j] = kNonFinite;
+            else if (ex > kZeroExp && ek > kZeroExp && ek < kNonFinite) mx[j] = max(mx[j], ex + ek + 2);
         }
     }
 #pragma unroll
@@ -280,26 +379,32 @@ template <int kTag> __global__ void __launch_bounds__(1024) k_xstack(int n, int 
         if (lane == 0 && r > kZeroExp) atomicMax(&sf[j], r);
     }
     __syncthreads();
-    if (tid < kRhs) fexp[tid] = sf[tid];
+    if (blockIdx.x == 0 && tid < kRhs) fexp[tid] = sf[tid];
     const int nsteps = (n + kKst - 1) / kKst;
-    for (int idx = tid; idx < nsteps * 256; idx += blockDim.x) {
-        const int s = idx >> 8, kk = idx & 15, j = (idx >> 4) & 15, k = s * kKst + kk;
-        double v = 0.0;
-        int se = 0;
-        if (k < n && j < nrhs && sf[j] < kNonFinite) {
-            const int ek = colexp[k];
-            if (ek > kZeroExp && ek < kNonFinite) {
-                v = X[k + ldx * (size_t)j];
-                se = ek - sf[j];
+    for (int idx = blockIdx.x * blockDim.x + tid; idx < nsteps * 32; idx += gridDim.x * blockDim.x) {
+        const int s = idx >> 5, j = (idx >> 1) & 15, h = idx & 1;
+        double v[8];
+        int se[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+            const int k = s * kKst + 8 * h + e;
+            v[e] = 0.0;
+            se[e] = 0;
+            if (k < n && j < nrhs && sf[j] < kNonFinite) {
+                const int ek = colexp[k];
+                if (ek > kZeroExp && ek < kNonFinite) {
+                    v[e] = X[k + ldx * (size_t)j];
+                    se[e] = ek - sf[j];
+                }
             }
         }
-        oz_stack_put(reinterpret_cast<unsigned char *>(XS + (size_t)s * 256), kk, j, v, se);
+        oz_stack_put8(reinterpret_cast<unsigned char *>(XS + (size_t)s * 256), h, j, v, se);
     }
 }
 
 // r (m x nrhs, nrhs <= 16) for A^T r: f_j = max over the residual's CTAs of
 // max_i floor(log2 |r_ij|), plus 2; then the stack image of every 16-row step
-// of r scaled by 2^-f_j.  CTA 0 writes f_j.
+// of r scaled by 2^-f_j.  Block 0 stores f_j.
 template <int kTag> __global__ void __launch_bounds__(256) k_rstack(int m, int nrhs, const double *R, size_t ldr, const int *rexp, int rexp_n, int *fexp, uint4 *RS) {
     __shared__ int sf[kRhs];
     const int tid = threadIdx.x;
@@ -315,16 +420,19 @@ template <int kTag> __global__ void __launch_bounds__(256) k_rstack(int m, int n
     }
     __syncthreads();
     if (blockIdx.x == 0 && tid < kRhs) fexp[tid] = sf[tid];
-    const int nsteps = (m + kKst - 1) / kKst, kk = tid & 15, j = tid >> 4;
-    for (int s = blockIdx.x; s < nsteps; s += gridDim.x) {
-        const int i = s * kKst + kk;
-        double v = 0.0;
-        int se = 0;
-        if (i < m && j < nrhs && sf[j] > kZeroExp && sf[j] < kNonFinite) {
-            v = R[i + ldr * (size_t)j];
-            se = -sf[j];
+    const int nsteps = (m + kKst - 1) / kKst;
+    for (int idx = blockIdx.x * blockDim.x + tid; idx < nsteps * 32; idx += gridDim.x * blockDim.x) {
+        const int s = idx >> 5, j = (idx >> 1) & 15, h = idx & 1;
+        const bool live = j < nrhs && sf[j] > kZeroExp && sf[j] < kNonFinite;
+        double v[8];
+        int se[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+            const int i = s * kKst + 8 * h + e;
+            v[e] = (live && i < m) ? R[i + ldr * (size_t)j] : 0.0;
+            se[e] = live ? -sf[j] : 0;
         }
-        oz_stack_put(reinterpret_cast<unsigned char *>(RS + (size_t)s * 256), kk, j, v, se);
+        oz_stack_put8(reinterpret_cast<unsigned char *>(RS + (size_t)s * 256), h, j, v, se);
     }
 }
 
@@ -374,38 +482,34 @@ __device__ __forceinline__ bool oz_next_item(const Args &a, Cursor &c, int nitem
 }
 __device__ __forceinline__ bool oz_next(const Args &a, Cursor &c, int nitems) { return (++c.s < c.nsteps) ? true : oz_next_item(a, c, nitems); }
 
-// issue the cp.async copies of one step owned by producer tid: eight packed
-// elements of A (zero-filled outside A: zero bytes are zero digits) and 16
-// bytes of the step's stack image
-__device__ __forceinline__ void oz_prefetch(const Args &a, const Cursor &c, unsigned char *rawA, unsigned char *rawX, int tid) {
-    const int kb = c.k0 + c.s * kKst;
+// the bulk copies of one step: its eight A blocks (residual: one contiguous
+// block column piece; A^T r: eight blocks of a block row), completion counted
+// on abar, and its stack image, counted on tbar
+__device__ __forceinline__ void oz_load_a(const Args &a, const Cursor &c, unsigned char *dst, uint64_t *abar) {
+    const int sb = (c.k0 + c.s * kKst) / kKst;
+    mbar_expect_tx(abar, (uint32_t)kRawA);
     if (a.mode == kResidual) {
-        const int ml = tid & 127, g = tid >> 7, i = c.mt * 128 + ml;
-#pragma unroll
-        for (int e = 0; e < 8; ++e) {
-            const int k = kb + 8 * g + e;
-            const bool ok = i < a.m && k < c.k1;
-            cp_zfill<8>(rawA + ((e >> 1) * kProd + tid) * 16 + (e & 1) * 8, ok ? a.Ad + i + a.ldd * (size_t)k : a.Ad, ok);
-        }
+        bulk_g2s(dst, a.Ad + ((size_t)sb * a.nbr + (size_t)c.mt * 8) * kBlock, (uint32_t)kRawA, abar);
     } else {
-        const int ml = tid >> 1, g = tid & 1, col = c.mt * 128 + ml;
 #pragma unroll
-        for (int e = 0; e < 8; ++e) {
-            const int i = kb + 8 * g + e;
-            const bool ok = col < a.n && i < c.k1;
-            cp_zfill<8>(rawA + ((e >> 1) * kProd + tid) * 16 + (e & 1) * 8, ok ? a.Ad + i + a.ldd * (size_t)col : a.Ad, ok);
-        }
+        for (int j = 0; j < 8; ++j) bulk_g2s(dst + j * kBlock, a.Ad + ((size_t)(c.mt * 8 + j) * a.nbr + (size_t)sb) * kBlock, (uint32_t)kBlock, abar);
     }
-    cp_zfill<16>(rawX + tid * 16, a.XS + (size_t)(kb / kKst) * 256 + tid, true);
+}
+__device__ __forceinline__ void oz_load_t(const Args &a, const Cursor &c, unsigned char *dst, uint64_t *tbar) {
+    const int sb = (c.k0 + c.s * kKst) / kKst;
+    mbar_expect_tx(tbar, (uint32_t)kStack);
+    bulk_g2s(dst, a.XS + (size_t)sb * 256, (uint32_t)kStack, tbar);
 }
 
 // (a template only so that every translation unit may include it)
 template <int kTag> __global__ void __launch_bounds__(kThreads, 1) k_oz(Args a) {
     extern __shared__ __align__(1024) unsigned char smem[];
-    unsigned char *rawA0 = smem + kSmemRawA;
-    unsigned char *rawX0 = smem + kSmemRawX;
-    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kSmemCtl);  // 0,1 stage; 2,3 acc full; 4,5 acc empty
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 6);
+    unsigned char *ra0 = smem + kSmemA, *rt0 = smem + kSmemT;
+    uint64_t *a_full = reinterpret_cast<uint64_t *>(smem + kSmemCtl);
+    uint64_t *a_empty = a_full + kNA, *t_full = a_empty + kNA, *t_empty = t_full + kNT;
+    uint64_t *stg_full = t_empty + kNT, *stg_empty = stg_full + kNS;
+    uint64_t *acc_full = stg_empty + kNS, *acc_empty = acc_full + 2;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(acc_empty + 2);
     int *snf = reinterpret_cast<int *>(tmem_slot + 1);
     int *sexp = snf + 1;     // [16] f_j
     int *snan = sexp + 16;   // [16] right-hand side j produces NaN
@@ -419,120 +523,170 @@ template <int kTag> __global__ void __launch_bounds__(kThreads, 1) k_oz(Args a) 
     }
     if (tid == 0) {
         *snf = 0;
-        for (int i = 0; i < 4; ++i) tc::mbar_init(&bars[i], 1);
-        tc::mbar_init(&bars[4], 4);
-        tc::mbar_init(&bars[5], 4);
+        for (int i = 0; i < kNA; ++i) {
+            tc::mbar_init(&a_full[i], 1);
+            tc::mbar_init(&a_empty[i], kConvWarps / 2);  // the converter group of the step
+        }
+        for (int i = 0; i < kNT; ++i) {
+            tc::mbar_init(&t_full[i], 1);
+            tc::mbar_init(&t_empty[i], 1);  // the MMA commit
+        }
+        for (int i = 0; i < kNS; ++i) {
+            tc::mbar_init(&stg_full[i], kConvWarps / 2);  // the converter group of the step
+            tc::mbar_init(&stg_empty[i], 1);              // the MMA commit
+        }
+        for (int i = 0; i < 2; ++i) {
+            tc::mbar_init(&acc_full[i], 1);
+            tc::mbar_init(&acc_empty[i], 4);
+        }
         tc::fence_barrier_init();
     }
     if (warp == 0) {
-        tc::tmem_alloc(tmem_slot, 256);
+        tc::tmem_alloc(tmem_slot, kTmemCols);
         tc::tmem_relinquish();
-    }
-    tc::tc_fence_before();
-    __syncthreads();
-    tc::tc_fence_after();
-    const uint32_t tmem = *tmem_slot;
-
-    // producers: start the copies of the first kNR - 1 steps
-    Cursor cv, pf;
-    bool has_cv = false, has_pf = false;
-    if (tid < kProd) {
-        has_cv = oz_first(a, cv, nitems);
-        pf = cv;
-        has_pf = has_cv;
-        for (int u = 0; u < kNR - 1; ++u) {
-            if (has_pf) {
-                oz_prefetch(a, pf, rawA0 + u * kRawA, rawX0 + u * kRawX, tid);
-                has_pf = oz_next(a, pf, nitems);
-            }
-            cp_async_commit();
-        }
     }
     // an Inf or NaN in A makes every result NaN, one in the other operand its column
     for (int k = tid; k < a.n; k += kThreads)
         if (a.colexp[k] >= kNonFinite) *snf = 1;
+    tc::tc_fence_before();
     __syncthreads();
+    tc::tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
     if (tid < kRhs) snan[tid] = (*snf != 0 || sexp[tid] >= kNonFinite) ? 1 : 0;
     __syncthreads();
 
-    if (tid < kProd) {
-        // ------------------------------ producers ------------------------------
-        bool ok = true;
-        int t = 0, cc = 0, last_commit = -1;
-        const int ml = (a.mode == kResidual) ? (tid & 127) : (tid >> 1);
-        const int g = (a.mode == kResidual) ? (tid >> 7) : (tid & 1);
-        while (has_cv) {
-            // keep kNR - 1 steps of copies in flight
-            if (has_pf) {
-                const int b = (t + kNR - 1) % kNR;
-                oz_prefetch(a, pf, rawA0 + b * kRawA, rawX0 + b * kRawX, tid);
-                has_pf = oz_next(a, pf, nitems);
-            }
-            cp_async_commit();
-            cp_wait_group<kNR - 1>();
-            const int rb = t % kNR;
-            const unsigned char *ra = rawA0 + rb * kRawA;
-            uint32_t wd[8][2];  // packed digits of the eight elements, bytes decoded to u = d + 64
-#pragma unroll
-            for (int pr = 0; pr < 4; ++pr) {
-                const uint4 q4 = *reinterpret_cast<const uint4 *>(ra + (pr * kProd + tid) * 16);
-                wd[2 * pr][0] = q4.x ^ 0x40404040u;
-                wd[2 * pr][1] = q4.y ^ 0x40404040u;
-                wd[2 * pr + 1][0] = q4.z ^ 0x40404040u;
-                wd[2 * pr + 1][1] = q4.w ^ 0x40404040u;
-            }
-            const uint4 xs = *reinterpret_cast<const uint4 *>(rawX0 + rb * kRawX + tid * 16);
-            // plane p, element pair (e, e + 1): two BF16 digits in one word
-            uint32_t w[kDig][4];
-#pragma unroll
-            for (int p = 0; p < kDig; ++p) {
-                const uint32_t sel = 0x7440u | (uint32_t)(p & 3);
-#pragma unroll
-                for (int e = 0; e < 8; e += 2) {
-                    const float fa = __uint_as_float(__byte_perm(wd[e][p >> 2], 0x4B000000u, sel)) - 8388672.0f;
-                    const float fb = __uint_as_float(__byte_perm(wd[e + 1][p >> 2], 0x4B000000u, sel)) - 8388672.0f;
-                    w[p][e >> 1] = __byte_perm(__float_as_uint(fa), __float_as_uint(fb), 0x7632);
+    if (warp == kLoadWarp || warp == kStackWarp) {
+        // ------------------------------ the two loaders ------------------------------
+        if (lane == 0) {
+            const bool isA = (warp == kLoadWarp);
+            const int nbuf = isA ? kNA : kNT;
+            uint64_t *full = isA ? a_full : t_full, *empty = isA ? a_empty : t_empty;
+            Cursor c;
+            bool have = oz_first(a, c, nitems), ok = true;
+            int t = 0;
+            while (have) {
+                const int b = t % nbuf;
+                if (t >= nbuf && !tc::mbar_wait(&empty[b], (uint32_t)(((t / nbuf) - 1) & 1))) {
+                    ok = false;
+                    break;
                 }
+                if (isA) oz_load_a(a, c, ra0 + b * kRawA, &full[b]);
+                else oz_load_t(a, c, rt0 + b * kStack, &full[b]);
+                ++t;
+                have = oz_next(a, c, nitems);
             }
-            // the MMAs of step t - 2 read this stage
-            if (t >= 2 && ok) ok = tc::mbar_wait(&bars[t & 1], (uint32_t)(((t >> 1) - 1) & 1));
-            unsigned char *stg = smem + (t & 1) * kStage;
-#pragma unroll
-            for (int p = 0; p < kDig; ++p)
-                *reinterpret_cast<uint4 *>(stg + p * kPlane + toff(ml, 8 * g)) = make_uint4(w[p][0], w[p][1], w[p][2], w[p][3]);
-            *reinterpret_cast<uint4 *>(stg + kDig * kPlane + tid * 16) = xs;
-            tc::fence_proxy_async();
-            if (!producers_and(ok ? 1 : 0)) {
+            // no copy may still be in flight when the CTA exits
+            for (int u = max(0, t - nbuf); u < t; ++u) tc::mbar_wait(&full[u % nbuf], (uint32_t)((u / nbuf) & 1));
+            if (!ok) atomicExch(a.err, (int)kStatusBarrierTimeout);
+        }
+    } else if (warp < kConvWarps) {
+        // ------------------------------- converters ------------------------------
+        // group grp takes the steps t = grp, grp + 2, ...; thread (ml, g): row /
+        // column ml of the 128-tile, K values 8g .. 8g + 7
+        const int grp = warp >> 3, ml = tid & 127, g = (tid >> 7) & 1, r = ml & 15, blk = ml >> 4;
+        Cursor c;
+        bool have = oz_first(a, c, nitems), ok = true;
+        if (have && grp == 1) have = oz_next(a, c, nitems);
+        int t = grp;
+        while (have) {
+            const int b = t % kNA, st = t % kNS;
+            if (!tc::mbar_wait(&a_full[b], (uint32_t)((t / kNA) & 1))) {
                 ok = false;
                 break;
             }
-            const bool first = (cv.s % kChunkSteps) == 0;
-            const bool last = (cv.s % kChunkSteps) == kChunkSteps - 1 || cv.s == cv.nsteps - 1;
-            if (tid == 0) {
-                const int set = cc & 1;
-                if (first && cc >= 2) ok = tc::mbar_wait(&bars[4 + set], (uint32_t)(((cc >> 1) - 1) & 1));
-                if (ok) {
-                    tc::tc_fence_after();
-                    const uint32_t sb = tc::smem_u32(stg), d = tmem + (uint32_t)(set * 128);
+            const unsigned char *rb = ra0 + b * kRawA + blk * kBlock;
+            uint32_t wd[8][2];  // the eight elements' packed digits (byte p = u_p xor 64)
+            if (a.mode == kResidual) {
+                // row r of the block, columns 8g .. 8g + 7
 #pragma unroll
-                    for (int p = 0; p < kDig; ++p) {
-                        const uint64_t ad = tc::smem_desc(sb + p * kPlane, 128, 256);
-                        const uint64_t bd = tc::smem_desc(sb + kDig * kPlane + p * 512, 128, 256);
-                        tc::umma_bf16(d, ad, bd, tc::idesc_bf16(128, 16 * (kDig - p)), (first && p == 0) ? 0u : 1u);
-                    }
-                    tc::umma_commit(&bars[t & 1]);
-                    last_commit = t;
-                    if (last) tc::umma_commit(&bars[2 + set]);
+                for (int pr = 0; pr < 4; ++pr) {
+                    const uint4 q4 = *reinterpret_cast<const uint4 *>(rb + blk_off(r, 8 * g + 2 * pr));
+                    wd[2 * pr][0] = q4.x;
+                    wd[2 * pr][1] = q4.y;
+                    wd[2 * pr + 1][0] = q4.z;
+                    wd[2 * pr + 1][1] = q4.w;
+                }
+            } else {
+                // column r of the block, rows 8g .. 8g + 7
+#pragma unroll
+                for (int e = 0; e < 8; ++e) {
+                    const uint2 q2 = *reinterpret_cast<const uint2 *>(rb + blk_off(8 * g + e, r));
+                    wd[e][0] = q2.x;
+                    wd[e][1] = q2.y;
                 }
             }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&a_empty[b]);
+            // plane p, element pair (e, e + 1): the two bytes side by side in the
+            // low bytes of two halves, 0x64 above them with the xor undone gives
+            // the FP16 numbers 1024 + u; subtracting 1088 leaves d = u - 64 exactly
+            uint32_t w[kDig][4];
+            const __half2 k1088 = __floats2half2_rn(1088.0f, 1088.0f);
+#pragma unroll
+            for (int p = 0; p < kDig; ++p) {
+                const uint32_t bp = (uint32_t)(p & 3), sel = bp | (bp << 4) | ((4u + bp) << 8) | ((4u + bp) << 12);
+#pragma unroll
+                for (int e = 0; e < 8; e += 2) {
+                    const uint32_t x = (__byte_perm(wd[e][p >> 2], wd[e + 1][p >> 2], sel) & 0x00FF00FFu) ^ 0x64406440u;
+                    const __half2 h = __hsub2(*reinterpret_cast<const __half2 *>(&x), k1088);
+                    w[p][e >> 1] = *reinterpret_cast<const uint32_t *>(&h);
+                }
+            }
+            if (t >= kNS && !tc::mbar_wait(&stg_empty[st], (uint32_t)(((t / kNS) - 1) & 1))) {
+                ok = false;
+                break;
+            }
+            tc::tc_fence_after();
+            // plane p of stage st: columns stage + 8p .. 8p + 7 (K pairs); this
+            // thread's K values 8g .. 8g + 7 are columns 4g .. 4g + 3 of its lane
+            const uint32_t tcol = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(2 * kAccCols + st * kStageCols + 4 * g);
+#pragma unroll
+            for (int p = 0; p < kDig; ++p) tmem_st4(tcol + (uint32_t)(p * kPlaneCols), w[p][0], w[p][1], w[p][2], w[p][3]);
+            tmem_wait_st();
+            tc::tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&stg_full[st]);
+            t += 2;
+            have = oz_next(a, c, nitems) && oz_next(a, c, nitems);
+        }
+        if (!ok && lane == 0) atomicExch(a.err, (int)kStatusBarrierTimeout);
+    } else if (warp == kMmaWarp) {
+        // ------------------------------- MMA issue -------------------------------
+        // the whole warp runs the loop (so that the descriptors are warp-uniform
+        // values) and one elected lane issues the tcgen05 instructions
+        Cursor c;
+        bool have = oz_first(a, c, nitems), ok = true;
+        int t = 0, cc = 0;
+        while (have) {
+            const int st = t % kNS, bt = t % kNT, set = cc & 1;
+            const bool first = (c.s % kChunkSteps) == 0;
+            const bool last = (c.s % kChunkSteps) == kChunkSteps - 1 || c.s == c.nsteps - 1;
+            bool w_ok = tc::mbar_wait(&stg_full[st], (uint32_t)((t / kNS) & 1)) && tc::mbar_wait(&t_full[bt], (uint32_t)((t / kNT) & 1));
+            if (w_ok && first && cc >= 2) w_ok = tc::mbar_wait(&acc_empty[set], (uint32_t)(((cc >> 1) - 1) & 1));
+            if (!__all_sync(0xFFFFFFFFu, w_ok)) {
+                ok = false;
+                break;
+            }
+            tc::tc_fence_after();
+            const uint32_t ta = tmem + (uint32_t)(2 * kAccCols + st * kStageCols), sbk = tc::smem_u32(rt0 + bt * kStack), d = tmem + (uint32_t)(set * kAccCols);
+            if (tc::elect_one()) {
+#pragma unroll
+                for (int p = 0; p < kDig; ++p) {
+                    const uint64_t bd = tc::smem_desc(sbk + p * 512, 128, 256);
+                    umma_f16_ta(d, ta + (uint32_t)(p * kPlaneCols), bd, idesc_f16(128, 16 * (kDig - p)), (first && p == 0) ? 0u : 1u);
+                }
+                tc::umma_commit(&stg_empty[st]);
+                tc::umma_commit(&t_empty[bt]);
+                if (last) tc::umma_commit(&acc_full[set]);
+            }
+            __syncwarp();
             if (last) ++cc;
             ++t;
-            has_cv = oz_next(a, cv, nitems);
+            have = oz_next(a, c, nitems);
         }
-        cp_async_wait_all();
         // every MMA issued has finished before the accumulators are released
-        if (tid == 0 && last_commit >= 0) tc::mbar_wait(&bars[last_commit & 1], (uint32_t)((last_commit >> 1) & 1));
-        if (!ok && tid == 0) atomicExch(a.err, (int)kStatusBarrierTimeout);
+        if (t > 0) tc::mbar_wait(&stg_empty[(t - 1) % kNS], (uint32_t)(((t - 1) / kNS) & 1));
+        if (!ok && lane == 0) atomicExch(a.err, (int)kStatusBarrierTimeout);
     } else {
         // -------------------------------- drain --------------------------------
         const int qd = warp & 3, ml = qd * 32 + lane;
@@ -540,25 +694,30 @@ template <int kTag> __global__ void __launch_bounds__(kThreads, 1) k_oz(Args a) 
         bool ok = true;
         Cursor c;
         bool have = oz_first(a, c, nitems);
+        long long *acc_i = reinterpret_cast<long long *>(smem + kSmemAcc);  // [16][128]: sum_{L<=4} S_L 2^(7(4-L))
+        float *acc_t = reinterpret_cast<float *>(smem + kSmemAcc + 128 * kRhs * 8);  // [16][128]: S_5 + 2^-7 S_6 + 2^-14 S_7
         while (have) {
-            double acc[kRhs];
 #pragma unroll
-            for (int j = 0; j < kRhs; ++j) acc[j] = 0.0;
+            for (int j = 0; j < kRhs; ++j) {
+                acc_i[j * 128 + ml] = 0;
+                acc_t[j * 128 + ml] = 0.0f;
+            }
             const int nch = (c.nsteps + kChunkSteps - 1) / kChunkSteps;
             for (int ch = 0; ch < nch; ++ch) {
                 const int set = cc & 1;
-                if (!tc::mbar_wait(&bars[2 + set], (uint32_t)((cc >> 1) & 1))) {
+                if (!tc::mbar_wait(&acc_full[set], (uint32_t)((cc >> 1) & 1))) {
                     ok = false;
                     break;
                 }
                 tc::tc_fence_after();
-                const uint32_t tb = tmem + ((uint32_t)(qd * 32) << 16) + (uint32_t)(set * 128);
+                const uint32_t tb = tmem + ((uint32_t)(qd * 32) << 16) + (uint32_t)(set * kAccCols);
 #pragma unroll
                 for (int jh = 0; jh < 2; ++jh) {
-                    // Horner over the levels, 7 (column block 0) down to 0 (block 7):
-                    // levels 7..5 in FP32, then FP64
+                    // column block b holds level 7 - b.  Levels 7..5 by Horner in FP32;
+                    // levels 0..4 are exact integers below 2^24: Horner in 64-bit
+                    // integers from level 0
                     float S[8], tl[8];
-                    double h[8];
+                    long long I[8];
                     tmem_ld8(tb + 8 * jh, S);
 #pragma unroll
                     for (int u = 0; u < 8; ++u) tl[u] = S[u];
@@ -568,23 +727,30 @@ template <int kTag> __global__ void __launch_bounds__(kThreads, 1) k_oz(Args a) 
 #pragma unroll
                         for (int u = 0; u < 8; ++u) tl[u] = fmaf(tl[u], 0x1p-7f, S[u]);
                     }
-                    tmem_ld8(tb + 48 + 8 * jh, S);
+                    tmem_ld8(tb + 112 + 8 * jh, S);
 #pragma unroll
-                    for (int u = 0; u < 8; ++u) h[u] = fma((double)tl[u], 0x1p-7, (double)S[u]);
+                    for (int u = 0; u < 8; ++u) I[u] = (long long)__float2int_rn(S[u]);
 #pragma unroll
-                    for (int b = 4; b < 8; ++b) {
+                    for (int b = 6; b >= 3; --b) {
                         tmem_ld8(tb + 16 * b + 8 * jh, S);
 #pragma unroll
-                        for (int u = 0; u < 8; ++u) h[u] = fma(h[u], 0x1p-7, (double)S[u]);
+                        for (int u = 0; u < 8; ++u) I[u] = I[u] * 128 + (long long)__float2int_rn(S[u]);
                     }
 #pragma unroll
-                    for (int u = 0; u < 8; ++u) acc[8 * jh + u] += h[u];
+                    for (int u = 0; u < 8; ++u) {
+                        acc_i[(8 * jh + u) * 128 + ml] += I[u];
+                        acc_t[(8 * jh + u) * 128 + ml] += tl[u];
+                    }
                 }
                 tc::tc_fence_before();
                 __syncwarp();
-                if (lane == 0) mbar_arrive(&bars[4 + set]);
+                if (lane == 0) mbar_arrive(&acc_empty[set]);
                 ++cc;
             }
+            // sum_L 2^(-7L) S_L = 2^-28 acc_i + 2^-35 acc_t
+            double acc[kRhs];
+#pragma unroll
+            for (int j = 0; j < kRhs; ++j) acc[j] = fma((double)acc_t[j * 128 + ml], 0x1p-35, (double)acc_i[j * 128 + ml] * 0x1p-28);
             if (!ok) break;
             if (a.mode == kResidual) {
                 const int i = c.mt * 128 + ml;
@@ -618,7 +784,7 @@ template <int kTag> __global__ void __launch_bounds__(kThreads, 1) k_oz(Args a) 
     if (a.mode == kResidual && tid < kRhs) a.rexp_out[blockIdx.x * kRhs + tid] = srmax[tid];
     if (warp == 0) {
         tc::tc_fence_after();
-        tc::tmem_dealloc(tmem, 256);
+        tc::tmem_dealloc(tmem, kTmemCols);
     }
 }
 
@@ -644,21 +810,23 @@ inline int oz_nranges(int m, int n) { return (m + oz_range_rows(m, n) - 1) / oz_
 
 // Device workspace of the FP64-accurate products (regions 256-byte aligned)
 struct OzWork {
-    int *colexp;  // n
-    uint2 *Ad;    // m x n packed digits of A (leading dimension m)
-    uint4 *XS;    // stack images of x: ceil(n/16) x 256
-    uint4 *RS;    // stack images of r: ceil(m/16) x 256
-    int *fexp;    // 16
-    int *rexp;    // groups x kOzMaxGrid x 16
-    double *P;    // kOzMaxGrid x n x 16 partials of A^T r
+    int *colexp;        // n
+    unsigned char *Ad;  // packed digits of A: nbr x nbc blocks of 16 x 16 elements (2 KB)
+    uint4 *XS;          // stack images of x: ceil(n/16) x 256
+    uint4 *RS;          // stack images of r: ceil(m/16) x 256
+    int *fexp;          // 16
+    int *rexp;          // groups x kOzMaxGrid x 16
+    double *P;          // kOzMaxGrid x n x 16 partials of A^T r
     static size_t al(size_t b) { return (b + 255) / 256 * 256; }
+    static int nbr(size_t m) { return (int)(8 * ((m + 127) / 128)); }
+    static int nbc(size_t n) { return (int)(8 * ((n + 127) / 128)); }
     static size_t bytes(size_t m, size_t n, size_t nrhs) {
-        return al(n * sizeof(int)) + al(m * n * sizeof(uint2)) + al((n + 15) / 16 * 4096) + al((m + 15) / 16 * 4096) + al(oz::kRhs * sizeof(int)) +
+        return al(n * sizeof(int)) + al((size_t)nbr(m) * nbc(n) * oz::kBlock) + al((n + 15) / 16 * 4096) + al((m + 15) / 16 * 4096) + al(oz::kRhs * sizeof(int)) +
                al((size_t)oz_groups(nrhs) * kOzMaxGrid * oz::kRhs * sizeof(int)) + al((size_t)kOzMaxGrid * n * oz::kRhs * sizeof(double)) + 256;
     }
     void carve(Carver &cv, size_t m, size_t n, size_t nrhs) {
         colexp = cv.take<int>(n);
-        Ad = cv.take<uint2>(m * n);
+        Ad = cv.take<unsigned char>((size_t)nbr(m) * nbc(n) * oz::kBlock);
         XS = cv.take<uint4>((n + 15) / 16 * 256);
         RS = cv.take<uint4>((m + 15) / 16 * 256);
         fexp = cv.take<int>(oz::kRhs);
@@ -675,14 +843,19 @@ inline int oz_attr() {
     return kOk;
 }
 
-// once per A: column scales (and ||A(:,k)||^2 into sumsq when given), the
-// packed digits, and the FP32 copy Af when given
+// once per A: column scales, the packed digits, and the FP32 copy Af when
+// given (with ||Af(:,k)||^2 into sumsq when both are given)
 inline int oz_prepare_a(int m, int n, const double *A, size_t lda, const OzWork &w, double *sumsq, float *Af, size_t ldf, cudaStream_t st) {
-    oz::k_col_exp_sumsq<0><<<(unsigned)std::min(n, 4096), 256, 0, st>>>(m, n, A, lda, w.colexp, sumsq);
+    oz::k_col_exp<0><<<(unsigned)std::min(n, 8192), 256, 0, st>>>(m, n, A, lda, w.colexp);
     RNPGPU_CHECK_LAUNCH();
-    const dim3 grid((unsigned)std::min((m + 255) / 256, 2048), (unsigned)std::min(n, 65535));
-    oz::k_adigits<0><<<grid, 256, 0, st>>>(m, n, A, lda, w.colexp, w.Ad, (size_t)m, Af, ldf);
+    const int nbr = OzWork::nbr((size_t)m), nbc = OzWork::nbc((size_t)n);
+    const dim3 grid((unsigned)std::min(nbr / 8, 65535), (unsigned)std::min(nbc, 65535));
+    oz::k_adigits<0><<<grid, 256, 0, st>>>(m, n, nbr, nbc, A, lda, w.colexp, w.Ad, Af, ldf);
     RNPGPU_CHECK_LAUNCH();
+    if (sumsq && Af) {
+        oz::k_col_sumsq_f32<0><<<(unsigned)std::min(n, 8192), 256, 0, st>>>(m, n, Af, ldf, sumsq);
+        RNPGPU_CHECK_LAUNCH();
+    }
     return kOk;
 }
 
@@ -695,7 +868,8 @@ inline int oz_residual(int m, int n, int nrhs, const OzWork &w, const double *x,
     KScope ks("residual_fp64", st);
     for (int g0 = 0, grp = 0; g0 < nrhs; g0 += oz::kRhs, ++grp) {
         const int ng = std::min(oz::kRhs, nrhs - g0);
-        oz::k_xstack<0><<<1, 1024, 0, st>>>(n, ng, x + ldx * (size_t)g0, ldx, w.colexp, w.fexp, w.XS);
+        const unsigned xgrid = (unsigned)std::max(1, std::min((n + 15) / 16 * 32 / 256, 64));
+        oz::k_xstack<0><<<xgrid, 256, 0, st>>>(n, ng, x + ldx * (size_t)g0, ldx, w.colexp, w.fexp, w.XS);
         RNPGPU_CHECK_LAUNCH();
         oz::Args a{};
         a.mode = oz::kResidual;
@@ -703,7 +877,7 @@ inline int oz_residual(int m, int n, int nrhs, const OzWork &w, const double *x,
         a.n = n;
         a.nrhs = ng;
         a.Ad = w.Ad;
-        a.ldd = (size_t)m;
+        a.nbr = OzWork::nbr((size_t)m);
         a.XS = w.XS;
         a.fexp = w.fexp;
         a.B = b + ldb * (size_t)g0;
@@ -728,7 +902,7 @@ inline int oz_normal(int m, int n, int nrhs, const OzWork &w, const double *r, s
     const int rgrid = oz_grid((m + 127) / 128);
     const int rr = oz_range_rows(m, n), nr = oz_nranges(m, n);
     const int grid = oz_grid(((n + 127) / 128) * nr);
-    const unsigned sgrid = (unsigned)std::min((m + 15) / 16, 2 * std::max(1, device_facts().sm_count));
+    const unsigned sgrid = (unsigned)std::max(1, std::min((m + 15) / 16 * 32 / 256, 2 * std::max(1, device_facts().sm_count)));
     KScope ks("normal_eq_fp64", st);
     for (int g0 = 0, grp = 0; g0 < nrhs; g0 += oz::kRhs, ++grp) {
         const int ng = std::min(oz::kRhs, nrhs - g0);
@@ -740,7 +914,7 @@ inline int oz_normal(int m, int n, int nrhs, const OzWork &w, const double *r, s
         a.n = n;
         a.nrhs = ng;
         a.Ad = w.Ad;
-        a.ldd = (size_t)m;
+        a.nbr = OzWork::nbr((size_t)m);
         a.XS = w.RS;
         a.fexp = w.fexp;
         a.out = w.P;
@@ -752,8 +926,8 @@ inline int oz_normal(int m, int n, int nrhs, const OzWork &w, const double *r, s
         a.err = err;
         oz::k_oz<0><<<grid, oz::kThreads, oz::kSmem, st>>>(a);
         RNPGPU_CHECK_LAUNCH();
-        const dim3 gs((unsigned)std::min((n + 255) / 256, 2048), (unsigned)ng);
-        k_sum_partials<double><<<gs, 256, 0, st>>>(w.P, (size_t)n, (size_t)n * oz::kRhs, nr, n, ng, g + ldg * (size_t)g0, ldg);
+        const dim3 gs((unsigned)((n + 63) / 64), (unsigned)ng);
+        k_reduce_splits<double><<<gs, 256, 0, st>>>(w.P, (size_t)n, (size_t)n * oz::kRhs, nr, n, g + ldg * (size_t)g0, ldg);
         RNPGPU_CHECK_LAUNCH();
     }
     return kOk;
