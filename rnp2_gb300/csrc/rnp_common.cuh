@@ -293,12 +293,14 @@ struct GridBarrier {
         return wait();
     }
     // split form: work between arrive() and wait() overlaps the barrier;
-    // it must not touch what other blocks read after the barrier
+    // it must not touch what other blocks read after the barrier.  The
+    // block's writes are ordered before thread 0's release by the block
+    // barrier, and the release/acquire pair carries them to the waiting
+    // blocks (no separate fence).
     __device__ void arrive() {
         __syncthreads();
         if (nblocks > 1 && threadIdx.x == 0) {
             ++gen;
-            __threadfence();
             red_release_add(counter, 1u);
         }
     }
@@ -309,16 +311,17 @@ struct GridBarrier {
                 const unsigned target = gen * nblocks;
                 int ok = 1;
                 const long long t0 = clock64();
-                while (ld_acquire(counter) < target) {
-                    if (ld_volatile(err) != 0) { ok = 0; break; }
-                    if (clock64() - t0 > spin_limit) {
-                        atomicExch(err, (int)kStatusBarrierTimeout);
-                        if (status) atomicExch(status, (int)kStatusBarrierTimeout);
-                        ok = 0;
-                        break;
+                for (unsigned it = 1; ld_acquire(counter) < target; ++it) {
+                    if ((it & 63u) == 0) {  // the error word and the time limit, now and then
+                        if (ld_volatile(err) != 0) { ok = 0; break; }
+                        if (clock64() - t0 > spin_limit) {
+                            atomicExch(err, (int)kStatusBarrierTimeout);
+                            if (status) atomicExch(status, (int)kStatusBarrierTimeout);
+                            ok = 0;
+                            break;
+                        }
                     }
                 }
-                __threadfence();
                 s_ok = ok;
             }
             __syncthreads();
