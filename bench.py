@@ -446,6 +446,8 @@ NCU_TRAFFIC = {
     "panel": (8.494080e6 + 0.003072e6, 2.0 * 65408 * 32 * 4),              # profiles/k_panel_f32_65536x32.md
     "larfb_update": (100.570368e6 + 31.947008e6, 2.0 * 65408 * 352 * 4 + 65408 * 32 * 4.0),  # profiles/k_update_tc_65536.md
     "larfb_w": (100.706048e6 + 3.111424e6, 65408 * 352 * 4.0 + 65408 * 32 * 4.0),             # profiles/k_w_tc_65536.md
+    "residual_fp64": (277.589248e6 + 5.319424e6, 65536 * 512 * 8.0 + 2.0 * 65536 * 16 * 8),    # profiles/k_oz_residual_65536x512x16.md
+    "normal_eq_fp64": (285.316352e6 + 3.713280e6, 65536 * 512 * 8.0 + 65536 * 16 * 8.0 + 65536 * 256.0),
 }
 
 
@@ -474,8 +476,12 @@ def kernel_rooflines(prof, tot_ms, top_name, peak64, steps):
                          "tc::k_update_tc: C -= V W^T, C read and written once, V read once"),
         "larfb_w": ("hbm", mean([m * c * 4.0 + m * nb * 4.0 for m, c in updates]),
                     "tc::k_w_tc: W = C^T V partials, C and V read once"),
-        "residual_fp64": ("fp64", 2.0 * M * N * NRHS, "k_gemm<double,128,16>: r = b - A x (2 m n nrhs flops)"),
-        "normal_eq_fp64": ("fp64", 2.0 * M * N * NRHS, "k_gemm<double,128,16>: A^T r, split-K (2 m n nrhs flops)"),
+        "residual_fp64": ("hbm", M * N * 8.0 + 2.0 * M * NRHS * 8,
+                          "k_xstack + oz::k_oz (residual): r = b - A x FP64-accurate from the packed digits of A (m n x 8 B read) on the FP16 tensor cores, b read, r written"),
+        "normal_eq_fp64": ("hbm", M * N * 8.0 + M * NRHS * 8.0 + M * 256.0,
+                           "k_rstack + oz::k_oz (A^T r) + k_reduce_splits: packed digits of A read once, r read once, its stack images written and read"),
+        "prepare_digits": ("hbm", 2 * M * N * 8.0 + M * N * 8.0 + 2 * M * N * 4.0 + M * N * 4.0,
+                           "k_col_exp + k_adigits + k_col_sumsq_f32 (once per solve): A read twice, packed digits and the FP32 copy written, the copy read"),
     }
     out = {}
     for name, (kind, per_launch, desc) in work.items():
