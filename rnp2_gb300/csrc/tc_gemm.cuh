@@ -250,7 +250,7 @@ template <int BN> __global__ void __launch_bounds__(kThreads) k_gemm_tc(GemmArgs
         fence_proxy_async();
         __syncthreads();
         if (t + 1 < nsteps) fetch(kbeg + (t + 1) * kBK);
-        if (tid == 0) {
+        if (warp == 0) {  // warp-uniform descriptors, one elected issuing lane
             tc_fence_after();
             const uint32_t base = smem_u32(smem + s * L::kStage);
             const uint32_t a0 = base, b0 = base + 3 * L::kSliceA;
@@ -260,17 +260,20 @@ template <int BN> __global__ void __launch_bounds__(kThreads) k_gemm_tc(GemmArgs
             const int pb[6] = {0, 1, 0, 2, 1, 0};
             const int pc[6] = {0, 1, 1, 2, 2, 2};
             const bool first_in_class[6] = {true, true, false, true, false, false};
+            if (elect_one()) {
 #pragma unroll
-            for (int kk = 0; kk < kBK / 16; ++kk) {
+                for (int kk = 0; kk < kBK / 16; ++kk) {
 #pragma unroll
-                for (int q = 0; q < 6; ++q) {
-                    const uint64_t ad = smem_desc(a0 + pa[q] * L::kSliceA + kk * 256, 128, (kBK / 8) * 128);
-                    const uint64_t bd = smem_desc(b0 + pb[q] * L::kSliceB + kk * 256, 128, (kBK / 8) * 128);
-                    const bool fresh = (t == 0 && kk == 0 && first_in_class[q]);
-                    umma_bf16(tmem_d + (uint32_t)(pc[q] * BN), ad, bd, idesc, fresh ? 0u : 1u);
+                    for (int q = 0; q < 6; ++q) {
+                        const uint64_t ad = smem_desc(a0 + pa[q] * L::kSliceA + kk * 256, 128, (kBK / 8) * 128);
+                        const uint64_t bd = smem_desc(b0 + pb[q] * L::kSliceB + kk * 256, 128, (kBK / 8) * 128);
+                        const bool fresh = (t == 0 && kk == 0 && first_in_class[q]);
+                        umma_bf16(tmem_d + (uint32_t)(pc[q] * BN), ad, bd, idesc, fresh ? 0u : 1u);
+                    }
                 }
+                umma_commit(&bars[s]);
             }
-            umma_commit(&bars[s]);
+            __syncwarp();
         }
     }
     // wait for the last MMAs (both stages' outstanding commits)
@@ -395,7 +398,8 @@ template <int CH> __global__ void __launch_bounds__(kThreads) k_update_tc(UpdArg
     const int ntiles = (g.M + kBM - 1) / kBM;
     uint32_t phase[2] = {0u, 0u};
     bool ok = true;
-    // MMAs of chunk c into accumulator set s (one elected thread)
+    // MMAs of chunk c into accumulator set s: called by all of warp 0 (the
+    // descriptors are warp-uniform values), issued by one elected lane
     auto issue = [&](int c, int s) {
         tc_fence_after();
         const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB) + (uint32_t)(c * kUpdChunk / 8) * (kBK / 8) * 128;
@@ -404,16 +408,19 @@ template <int CH> __global__ void __launch_bounds__(kThreads) k_update_tc(UpdArg
         const int pb[6] = {0, 1, 0, 2, 1, 0};
         const int pc[6] = {0, 1, 1, 2, 2, 2};
         const bool first_in_class[6] = {true, true, false, true, false, false};
+        if (elect_one()) {
 #pragma unroll
-        for (int kk = 0; kk < kBK / 16; ++kk) {
+            for (int kk = 0; kk < kBK / 16; ++kk) {
 #pragma unroll
-            for (int q = 0; q < 6; ++q) {
-                const uint64_t ad = smem_desc(a0 + pa[q] * kSliceA + kk * 256, 128, (kBK / 8) * 128);
-                const uint64_t bd = smem_desc(b0 + pb[q] * sliceB + kk * 256, 128, (kBK / 8) * 128);
-                umma_bf16(d0 + (uint32_t)(pc[q] * kUpdChunk), ad, bd, idesc, (kk == 0 && first_in_class[q]) ? 0u : 1u);
+                for (int q = 0; q < 6; ++q) {
+                    const uint64_t ad = smem_desc(a0 + pa[q] * kSliceA + kk * 256, 128, (kBK / 8) * 128);
+                    const uint64_t bd = smem_desc(b0 + pb[q] * sliceB + kk * 256, 128, (kBK / 8) * 128);
+                    umma_bf16(d0 + (uint32_t)(pc[q] * kUpdChunk), ad, bd, idesc, (kk == 0 && first_in_class[q]) ? 0u : 1u);
+                }
             }
+            umma_commit(&bars[s]);
         }
-        umma_commit(&bars[s]);
+        __syncwarp();
     };
     for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
         const int m0 = t * kBM;
@@ -433,7 +440,7 @@ template <int CH> __global__ void __launch_bounds__(kThreads) k_update_tc(UpdArg
         }
         fence_proxy_async();
         __syncthreads();
-        if (tid == 0) issue(0, 0);
+        if (warp == 0) issue(0, 0);
         // epilogue mapping: warp w reads TMEM lanes 32*(w%4).. (tile rows) and
         // the column half w/4 of each chunk; its C values for the next chunk
         // are loaded while the current chunk is finished
@@ -450,7 +457,7 @@ template <int CH> __global__ void __launch_bounds__(kThreads) k_update_tc(UpdArg
         load_c(0, cur);
         for (int c = 0; c < nchunks; ++c) {
             const int s = c & 1;
-            if (tid == 0 && c + 1 < nchunks) issue(c + 1, s ^ 1);
+            if (warp == 0 && c + 1 < nchunks) issue(c + 1, s ^ 1);
             if (c + 1 < nchunks) load_c(c + 1, nxt);
             if (!mbar_wait(&bars[s], phase[s])) ok = false;
             phase[s] ^= 1u;
@@ -633,7 +640,7 @@ template <int CH, bool VEC> __global__ void __launch_bounds__(kWThreads) k_w_tc(
         fence_proxy_async();
         __syncthreads();
         if (t + 1 < nsteps) fetch(t + 1);
-        if (tid == 0) {
+        if (warp == 0) {  // warp-uniform descriptors, one elected issuing lane
             tc_fence_after();
             const uint32_t a0 = smem_u32(sA + st * 3 * kWSliceA), b0 = smem_u32(sB);
             const uint32_t d0 = tmem_base + (uint32_t)(cc * 96);
@@ -641,17 +648,20 @@ template <int CH, bool VEC> __global__ void __launch_bounds__(kWThreads) k_w_tc(
             const int pb[6] = {0, 1, 0, 2, 1, 0};
             const int pc[6] = {0, 1, 1, 2, 2, 2};
             const bool first_in_class[6] = {true, true, false, true, false, false};
+            if (elect_one()) {
 #pragma unroll
-            for (int kk = 0; kk < kWRows / 16; ++kk) {
+                for (int kk = 0; kk < kWRows / 16; ++kk) {
 #pragma unroll
-                for (int q = 0; q < 6; ++q) {
-                    const uint64_t ad = smem_desc(a0 + pa[q] * kWSliceA + kk * 256, 128, (kWRows / 8) * 128);
-                    const uint64_t bd = smem_desc(b0 + pb[q] * kWSliceB + kk * 256, 128, (kWRows / 8) * 128);
-                    const bool fresh = (kbl == 0 && kk == 0 && first_in_class[q]);
-                    umma_bf16(d0 + (uint32_t)(pc[q] * 32), ad, bd, idesc, fresh ? 0u : 1u);
+                    for (int q = 0; q < 6; ++q) {
+                        const uint64_t ad = smem_desc(a0 + pa[q] * kWSliceA + kk * 256, 128, (kWRows / 8) * 128);
+                        const uint64_t bd = smem_desc(b0 + pb[q] * kWSliceB + kk * 256, 128, (kWRows / 8) * 128);
+                        const bool fresh = (kbl == 0 && kk == 0 && first_in_class[q]);
+                        umma_bf16(d0 + (uint32_t)(pc[q] * 32), ad, bd, idesc, fresh ? 0u : 1u);
+                    }
                 }
+                umma_commit(&bars[st]);
             }
-            umma_commit(&bars[st]);
+            __syncwarp();
         }
         pending[st] = true;
     }
