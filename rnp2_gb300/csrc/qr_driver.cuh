@@ -401,12 +401,54 @@ template <class T> size_t t_bytes() { return ((size_t)kPanelMaxCols * kPanelMaxC
 // ---------------------------------------------------------------------------
 template <class T> int geqr2(size_t m, size_t n, T *a, size_t lda, T *tau, T *work);
 
-template <class T> size_t geqrf_bytes(size_t m, size_t n, int smax) {
+// serial blocked form: panel workspace, one T, one update workspace
+template <class T> size_t geqrf_serial_bytes(size_t m, size_t n, int smax) {
     return panel_ws_bytes<T>(panel_gmax<T>()) + t_bytes<T>() + block_ws_bytes<T>((int)n, smax);
+}
+// Look-ahead (below) pays for FP64 and complex data, whose trailing updates
+// are FMA-bound and long against the panel (square 4096 complex: 513 -> 451
+// ms); FP32 trailing updates on the tensor cores are short and latency bound,
+// and running the next panel beside them made the 65536 x 512 FP32 factor
+// slower (8.8 -> 9.6 ms per mixed solve), so FP32 keeps the serial order.
+template <class T> constexpr bool geqrf_lookahead() { return !std::is_same<T, float>::value; }
+// look-ahead form: a second T and a second update workspace
+template <class T> size_t geqrf_bytes(size_t m, size_t n, int smax) {
+    return geqrf_serial_bytes<T>(m, n, smax) + (geqrf_lookahead<T>() ? t_bytes<T>() + block_ws_bytes<T>((int)n, smax) : 0);
+}
+
+// Per host thread and device: the side stream and two events of the
+// look-ahead factorization (created on first use, outside stream capture).
+struct LookAhead {
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_panel = nullptr, ev_big = nullptr;
+};
+inline LookAhead *lookahead_ctx() {
+    constexpr int kMaxDev = 16;
+    static thread_local LookAhead la[kMaxDev];
+    static thread_local int state[kMaxDev] = {};  // 0 untried, 1 ready, 2 failed
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDev) return nullptr;
+    if (state[dev] == 0) {
+        LookAhead &l = la[dev];
+        const bool ok = cudaStreamCreateWithFlags(&l.side, cudaStreamNonBlocking) == cudaSuccess &&
+                        cudaEventCreateWithFlags(&l.ev_panel, cudaEventDisableTiming) == cudaSuccess &&
+                        cudaEventCreateWithFlags(&l.ev_big, cudaEventDisableTiming) == cudaSuccess;
+        state[dev] = ok ? 1 : 2;
+        if (!ok) cudaGetLastError();
+    }
+    return state[dev] == 1 ? &la[dev] : nullptr;
 }
 
 // Tstore (optional): receives the 32 x 32 T factor of every column block
 // (block b at Tstore + b*32*32, leading dimension 32) for later MultQ calls.
+//
+// Look-ahead: after panel i only the next panel's columns are updated on the
+// caller's stream; the rest of the trailing matrix is updated on a side
+// stream while panel i + 1 (latency bound: one grid barrier per column) is
+// factored, and the caller's stream waits for that update before it touches
+// those columns again.  The results are the same as in the serial order (the
+// same operations on the same data).  Without the larger workspace, inside
+// stream capture, or for a single trailing block the serial order is used.
 template <class T> int geqrf(size_t m, size_t n, T *a, size_t lda, T *tau, size_t *lwork, T *work, T *Tstore = nullptr) {
     if (lwork == nullptr) return -6;
     const size_t k = std::min(m, n);
@@ -420,30 +462,69 @@ template <class T> int geqrf(size_t m, size_t n, T *a, size_t lda, T *tau, size_
     }
     if (a == nullptr) return -3;
     if (tau == nullptr) return -5;
-    while (smax > 1 && elems_for<T>(geqrf_bytes<T>(m, n, smax)) > *lwork) smax /= 2;
-    if (elems_for<T>(geqrf_bytes<T>(m, n, smax)) > *lwork) {
-        // not enough workspace for the blocked code: level-2 code needs n
-        if (*lwork < n) return -6;
-        return geqr2<T>(m, n, a, lda, tau, work);
-    }
+    const size_t nb = GpuTuning::nb;
     cudaStream_t st = current_stream();
+    bool ahead = geqrf_lookahead<T>() && n > 2 * nb && k > nb && elems_for<T>(geqrf_bytes<T>(m, n, smax)) <= *lwork;
+    if (ahead) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) ahead = false;
+    }
+    LookAhead *la = ahead ? lookahead_ctx() : nullptr;
+    if (la == nullptr) {
+        ahead = false;
+        while (smax > 1 && elems_for<T>(geqrf_serial_bytes<T>(m, n, smax)) > *lwork) smax /= 2;
+        if (elems_for<T>(geqrf_serial_bytes<T>(m, n, smax)) > *lwork) {
+            // not enough workspace for the blocked code: level-2 code needs n
+            if (*lwork < n) return -6;
+            return geqr2<T>(m, n, a, lda, tau, work);
+        }
+    }
     Carver cv(work);
     const int gmax = panel_gmax<T>();
     PanelWs<T> pw = carve_panel<T>(cv, gmax);
-    T *Tm = cv.take<T>((size_t)kPanelMaxCols * kPanelMaxCols);
+    T *Tm[2];
+    Tm[0] = cv.take<T>((size_t)kPanelMaxCols * kPanelMaxCols);
     BlockWs<T> bw = carve_block<T>(cv, (int)n, smax);
-    const size_t nb = GpuTuning::nb;
+    BlockWs<T> bw2 = bw;
+    Tm[1] = Tm[0];
+    if (ahead) {
+        Tm[1] = cv.take<T>((size_t)kPanelMaxCols * kPanelMaxCols);
+        bw2 = carve_block<T>(cv, (int)n, smax);
+    }
+    bool big_pending = false;
     for (size_t i = 0; i < k; i += nb) {
         const int ib = (int)std::min(nb, k - i);
         T *Ai = a + i + i * lda;
-        T *Tb = Tstore ? Tstore + (i / nb) * kPanelMaxCols * kPanelMaxCols : Tm;
+        T *Tb = Tstore ? Tstore + (i / nb) * kPanelMaxCols * kPanelMaxCols : Tm[(i / nb) & 1];
         int rc = panel_factor<T>((int)(m - i), ib, Ai, lda, tau + i, Tb, kPanelMaxCols, pw, st);
         if (rc) return rc;
-        if (i + ib < n) {
-            rc = apply_block<T>(true, false, (int)(m - i), (int)(n - i - ib), ib, Ai, lda, Tb, kPanelMaxCols, a + i + (i + ib) * lda, lda, bw, st);
+        const size_t c1 = i + ib;  // first trailing column
+        if (c1 >= n) continue;
+        if (!ahead) {
+            rc = apply_block<T>(true, false, (int)(m - i), (int)(n - c1), ib, Ai, lda, Tb, kPanelMaxCols, a + i + c1 * lda, lda, bw, st);
             if (rc) return rc;
+            continue;
+        }
+        const size_t w1 = std::min(nb, n - c1);  // the next panel's columns
+        if (c1 + w1 < n) {
+            // the rest of the trailing matrix, on the side stream (after the
+            // previous side update, in stream order)
+            RNPGPU_CHECK(cudaEventRecord(la->ev_panel, st));
+            RNPGPU_CHECK(cudaStreamWaitEvent(la->side, la->ev_panel, 0));
+        }
+        // the next panel's columns were last written by the previous side update
+        if (big_pending) RNPGPU_CHECK(cudaStreamWaitEvent(st, la->ev_big, 0));
+        big_pending = false;
+        rc = apply_block<T>(true, false, (int)(m - i), (int)w1, ib, Ai, lda, Tb, kPanelMaxCols, a + i + c1 * lda, lda, bw, st);
+        if (rc) return rc;
+        if (c1 + w1 < n) {
+            rc = apply_block<T>(true, false, (int)(m - i), (int)(n - c1 - w1), ib, Ai, lda, Tb, kPanelMaxCols, a + i + (c1 + w1) * lda, lda, bw2, la->side);
+            if (rc) return rc;
+            RNPGPU_CHECK(cudaEventRecord(la->ev_big, la->side));
+            big_pending = true;
         }
     }
+    if (big_pending) RNPGPU_CHECK(cudaStreamWaitEvent(st, la->ev_big, 0));
     return kOk;
 }
 
