@@ -472,6 +472,8 @@ def kernel_rooflines(prof, tot_ms, top_name, peak64, steps):
     work = {
         "panel": ("hbm", mean([2.0 * m * c * 4 for m, c in panels]),
                   "k_panel<float>: FP32 panel, rows read and written once (2 m 32 x 4 B)"),
+        "panel_cqr": ("hbm", mean([2.0 * m * c * 4 for m, c in panels]),
+                      "k_panel_cqr: FP32 CholeskyQR2 panel with Householder reconstruction, rows read and written once (2 m 32 x 4 B)"),
         "larfb_update": ("hbm", mean([2.0 * m * c * 4 + m * nb * 4.0 for m, c in updates]),
                          "tc::k_update_tc: C -= V W^T, C read and written once, V read once"),
         "larfb_w": ("hbm", mean([m * c * 4.0 + m * nb * 4.0 for m, c in updates]),

@@ -99,7 +99,7 @@ template <class T> int gels(size_t m, size_t n, size_t nrhs, T *a, size_t lda, T
 // mixed precision least squares with iterative refinement
 // ---------------------------------------------------------------------------
 template <class TH, class TL> struct RefinePlan {
-    size_t af, tauf, ts, wq, r, rf, p, g, norms, ozw, total;
+    size_t af, tauf, ts, wq, r, rf, p, g, norms, ozw, cqrw, total;
     int split;
     // the FP64 products r = b - A x and A^T r on the tensor cores (exact
     // integer slices) for real FP64 data; other types use FP64 FMA
@@ -118,7 +118,8 @@ template <class TH, class TL> struct RefinePlan {
         norms = al((n + 6 * nrhs) * sizeof(double));
         rf = std::max(rf, al(n * nrhs * sizeof(TL)));
         ozw = kOz ? OzWork::bytes(m, n, nrhs) : 0;
-        total = af + tauf + ts + wq + r + rf + p + g + norms + ozw;
+        cqrw = std::is_same<TL, float>::value ? cqr_ws_bytes() : 0;
+        total = af + tauf + ts + wq + r + rf + p + g + norms + ozw + cqrw;
     }
 };
 
@@ -157,6 +158,8 @@ int gels_refine(size_t m, size_t n, size_t nrhs, const TH *a, size_t lda, const 
     constexpr bool use_oz = RefinePlan<TH, TL>::kOz;
     OzWork ow{};
     if (use_oz) ow.carve(cv, m, n, nrhs);
+    CqrWs cw;
+    if (std::is_same<TL, float>::value) cw = carve_cqr(cv);
     const size_t lwq = plan.wq / sizeof(TL);
     const dim3 gmn((unsigned)std::min<size_t>((m + 255) / 256, 2048), (unsigned)std::min<size_t>(n, 65535));
     const dim3 gmr((unsigned)std::min<size_t>((m + 255) / 256, 2048), (unsigned)std::min<size_t>(nrhs, 65535));
@@ -174,7 +177,24 @@ int gels_refine(size_t m, size_t n, size_t nrhs, const TH *a, size_t lda, const 
         RNPGPU_CHECK_LAUNCH();
     }
     size_t lw = lwq;
-    if ((rc = geqrf<TL>(m, n, Af, m, tauf, &lw, wq, Tf))) return rc < 0 ? -13 : rc;
+    if constexpr (std::is_same<TL, float>::value) {
+        // FP32 factor with CholeskyQR2 panels; a panel whose Gram matrix is
+        // too ill-conditioned for them sends the whole factorization back to
+        // Householder panels
+        RNPGPU_CHECK(cudaMemsetAsync(cw.fail, 0, sizeof(int), st));
+        if ((rc = geqrf<TL>(m, n, Af, m, tauf, &lw, wq, Tf, &cw))) return rc < 0 ? -13 : rc;
+        int failed = 0;
+        RNPGPU_CHECK(cudaMemcpyAsync(&failed, cw.fail, sizeof(int), cudaMemcpyDeviceToHost, st));
+        RNPGPU_CHECK(cudaStreamSynchronize(st));
+        if (failed) {
+            k_convert<TH, TL><<<gmn, 256, 0, st>>>((int)m, (int)n, a, lda, Af, m);
+            RNPGPU_CHECK_LAUNCH();
+            lw = lwq;
+            if ((rc = geqrf<TL>(m, n, Af, m, tauf, &lw, wq, Tf))) return rc < 0 ? -13 : rc;
+        }
+    } else {
+        if ((rc = geqrf<TL>(m, n, Af, m, tauf, &lw, wq, Tf))) return rc < 0 ? -13 : rc;
+    }
 
     // ||A||_F (real FP64 data: from the FP32 working copy, which only scales
     // the stopping test) and ||b_j|| in FP64

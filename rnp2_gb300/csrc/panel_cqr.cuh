@@ -1,0 +1,469 @@
+// panel_cqr.cuh — FP32 panel factorization for the internal FP32 factor of
+// the mixed least-squares solver (not the drop-in Factor, whose output must
+// be the reference's Householder QR): CholeskyQR2 with a double-float first
+// Gram matrix, then Householder reconstruction of the orthonormal factor.
+//
+//   G1 = A^T A (double-float sums), R1 = chol(G1) (double-float), Q1 = A R1^-1;
+//   G2 = Q1^T Q1, R2 = chol(G2), Q = Q1 R2^-1, R = R2 R1   (both in FP32)
+//   (Yamamoto, Nakatsukasa, Yanagisawa and Fukaya, "Roundoff error analysis
+//   of the CholeskyQR2 algorithm", ETNA 44, 2015: the second pass restores
+//   orthogonality to working precision when kappa(Q1) is modest; the
+//   double-float first pass keeps kappa(Q1) modest for kappa(A) up to about
+//   10^5 — Yamazaki, Tomov and Dongarra, "Mixed-precision Cholesky QR
+//   factorization and its case studies on multicore CPU with multiple GPUs",
+//   SIAM J. Sci. Comput. 37(3), 2015);
+//   then the Householder form of Q (Ballard, Demmel, Grigori, Jacquelin,
+//   Knight and Nguyen, "Reconstructing Householder vectors from tall-skinny
+//   QR", J. Parallel Distrib. Comput. 85, 2015): the LU factorization
+//   Q - S = L U without pivoting, with s_j = -sign of the j-th pivot of Q's
+//   top block (so that |u_jj| >= 1), gives V = L (unit lower trapezoidal),
+//   T = -U S L1^-T and the R of the Householder QR, S R.  Below the top block
+//   V = Q U^-1 = Q1 (U R2)^-1: one triangular solve per row.
+//
+// Every block keeps its rows in shared memory (row-major, 36 floats a row).
+// A Gram matrix is formed as 36 upper-triangle tiles of 4 x 4 entries, one
+// warp per tile with the rows split across its lanes, summed across the lanes
+// by a butterfly; the per-block partials are then summed across blocks by
+// all blocks at once (one warp per entry), and every block reads the total
+// back and factors it itself, identically — four grid barriers in all.
+// Panels narrower than 32 columns are padded with zero columns and a unit
+// Gram diagonal, which carries an identity through every step.
+//
+// A first-pass pivot that is not positive or below 2^-38 of its column's
+// squared norm, or a second-pass pivot below 2^-14 of its diagonal (Q1 far
+// from orthonormal), marks the panel as failed before anything is written;
+// the caller then refactors it with Householder panels.  That happens for
+// panels with condition numbers near 10^5 and above, zero columns and
+// non-finite data.
+#pragma once
+#include "qr_kernels.cuh"
+
+namespace rnpgpu {
+
+constexpr int kCqrThreads = 512;
+constexpr int kPanelMaxBlocksCqr = 256;
+constexpr int kCqrLd = 36;                     // floats per row of a block's rows in shared memory
+constexpr int kCqrTiles = 36;                  // 4 x 4 tiles of a 32 x 32 upper triangle
+constexpr int kCqrEntries = kCqrTiles * 16;    // entries of a Gram partial (tile-major)
+constexpr int kCqrStaticSmem = 40 * 1024;      // bound on the kernel's static shared memory
+constexpr int kCqrMaxDynSmem = 227 * 1024 - kCqrStaticSmem;
+
+struct CqrArgs {
+    float *A;
+    size_t lda;
+    int M, N;             // N <= 32, every block holds >= 32 rows
+    float *tau;           // N
+    float *Tm;            // N x N upper triangular T (ldt), may be null
+    int ldt;
+    float2 *gpart;        // [gridDim.x][kCqrEntries] per-block Gram partials (hi, lo)
+    float2 *gfin;         // [kCqrEntries] the summed Gram matrix
+    float *qtop;          // 32 x 32 row-major: the top rows of Q1
+    unsigned *counter;    // zeroed before the launch
+    int *err;             // zeroed before the launch
+    int *status;          // library-wide status word
+    int *fail;            // set when a Cholesky factorization fails
+    int rows_per_cta;
+};
+
+// double-float helpers beyond rnp_common.cuh: a - b c with the sum left
+// unnormalized; square root and reciprocal with one correction step each
+// (Karp and Markstein, "High-precision division and square root", ACM TOMS
+// 23(4), 1997)
+__device__ __forceinline__ F2 f2_fms(F2 a, F2 b, F2 c) {
+    const float p = b.h * c.h;
+    const float e = fmaf(b.h, c.l, fmaf(b.l, c.h, fmaf(b.h, c.h, -p)));
+    const float s = a.h - p, bp = s - a.h;
+    const float err = (a.h - (s - bp)) + (-p - bp);
+    return F2{s, (a.l + err) - e};
+}
+__device__ __forceinline__ F2 f2_sqrt(F2 a) {
+    const float s = sqrtf(a.h);
+    const float r = fmaf(-s, s, a.h) + a.l;
+    return f2_norm(s, r * (0.5f / s));
+}
+__device__ __forceinline__ F2 f2_rcp(F2 a) {
+    const float q = 1.0f / a.h;
+    const float r = fmaf(-a.h, q, 1.0f) - a.l * q;
+    return f2_norm(q, r * q);
+}
+// tile t of the 8 x 8 grid of 4 x 4 tiles over the upper triangle, row-major
+__device__ __forceinline__ void cqr_tile(int t, int &ti, int &tj) {
+    int i = 0;
+    while (t >= 8 - i) {
+        t -= 8 - i;
+        ++i;
+    }
+    ti = i;
+    tj = i + t;
+}
+// a warp's 16 sums (h, l per lane) -> each even lane holds the total of one
+// entry, whose index it returns (a butterfly that halves the entries at each
+// of four steps, then adds lane pairs)
+__device__ __forceinline__ int cqr_warp_reduce16(float (&h)[16], float (&l)[16], int lane) {
+#pragma unroll
+    for (int lvl = 0; lvl < 4; ++lvl) {
+        const int o = 16 >> lvl, n = 8 >> lvl;
+        const bool up = (lane & o) != 0;
+#pragma unroll
+        for (int i = 0; i < n; ++i) {
+            const F2 a{h[i], l[i]}, c{h[i + n], l[i + n]};
+            const F2 send = up ? a : c, keep = up ? c : a;
+            const F2 recv{__shfl_xor_sync(0xFFFFFFFFu, send.h, o), __shfl_xor_sync(0xFFFFFFFFu, send.l, o)};
+            const F2 s = f2_add(keep, recv);
+            h[i] = s.h;
+            l[i] = s.l;
+        }
+    }
+    const F2 recv{__shfl_xor_sync(0xFFFFFFFFu, h[0], 1), __shfl_xor_sync(0xFFFFFFFFu, l[0], 1)};
+    const F2 s = f2_add(F2{h[0], l[0]}, recv);
+    h[0] = s.h;
+    l[0] = s.l;
+    return ((lane >> 4) & 1) * 8 + ((lane >> 3) & 1) * 4 + ((lane >> 2) & 1) * 2 + ((lane >> 1) & 1);
+}
+
+// packed FP32x2 arithmetic (two independent lanes per instruction)
+__device__ __forceinline__ float2 cqr_neg2(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 cqr_dup(float a) { return make_float2(a, a); }
+// (h, l) += a c for two entries at once: TwoProduct by FMA and TwoSum, as
+// df_add_prod, on packed pairs
+__device__ __forceinline__ void df_add_prod2(float2 &h, float2 &l, float2 a, float2 c) {
+    const float2 p = __fmul2_rn(a, c);
+    const float2 e = __ffma2_rn(a, c, cqr_neg2(p));
+    const float2 s = __fadd2_rn(h, p);
+    const float2 bp = __fadd2_rn(s, cqr_neg2(h));
+    const float2 err = __fadd2_rn(__fadd2_rn(h, cqr_neg2(__fadd2_rn(s, cqr_neg2(bp)))), __fadd2_rn(p, cqr_neg2(bp)));
+    l = __fadd2_rn(l, __fadd2_rn(err, e));
+    h = s;
+}
+
+// x (one row, 32 entries as 16 pairs) <- x Rf^-1 for Rf upper triangular in
+// shared memory (rows of kCqrLd floats, 16-byte aligned) with reciprocal
+// diagonal rinv
+__device__ __forceinline__ void cqr_row_solve(float2 (&x)[16], const float (*Rf)[kCqrLd], const float *rinv) {
+    // opaque to the compiler, so that it does not hoist the factor's loads out
+    // of a caller's loop over rows (they would not fit in registers)
+    asm volatile("" : "+l"(Rf), "+l"(rinv));
+#pragma unroll
+    for (int l = 0; l < 32; ++l) {
+        float xl = ((l & 1) ? x[l >> 1].y : x[l >> 1].x) * rinv[l];
+        if (l & 1) x[l >> 1].y = xl;
+        else x[l >> 1].x = xl;
+        const float2 nx = cqr_dup(-xl);
+#pragma unroll
+        for (int q = (l + 1) / 4; q < 8; ++q) {
+            const float4 r = *reinterpret_cast<const float4 *>(&Rf[l][4 * q]);
+            if (4 * q > l) x[2 * q] = __ffma2_rn(nx, make_float2(r.x, r.y), x[2 * q]);
+            else if (4 * q + 1 > l) x[2 * q].y = fmaf(-xl, r.y, x[2 * q].y);
+            if (4 * q + 2 > l) x[2 * q + 1] = __ffma2_rn(nx, make_float2(r.z, r.w), x[2 * q + 1]);
+            else if (4 * q + 3 > l) x[2 * q + 1].y = fmaf(-xl, r.w, x[2 * q + 1].y);
+        }
+    }
+}
+__device__ __forceinline__ void cqr_row_load(float2 (&x)[16], const float *row) {
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const float4 v = *reinterpret_cast<const float4 *>(row + 4 * q);
+        x[2 * q] = make_float2(v.x, v.y);
+        x[2 * q + 1] = make_float2(v.z, v.w);
+    }
+}
+__device__ __forceinline__ void cqr_row_store(float *row, const float2 (&x)[16]) {
+#pragma unroll
+    for (int q = 0; q < 8; ++q) *reinterpret_cast<float4 *>(row + 4 * q) = make_float4(x[2 * q].x, x[2 * q].y, x[2 * q + 1].x, x[2 * q + 1].y);
+}
+
+// Cholesky of the 32 x 32 Gram matrix in sG (upper triangle; hi, lo pairs) by
+// all 16 warps of the block: thread (w, j) holds entries (w, j) and (w + 16,
+// j); row k of R is finished by the warp that holds it and published in sG's
+// row k, then every thread updates its entries below — one block barrier a
+// step.  Double-float (kDF) or FP32 arithmetic.  R in FP32 -> Rf (upper,
+// zero below), its reciprocal diagonal -> rinv; a pivot not above thr times
+// its column's original diagonal (or not finite) sets *fail.
+template <bool kDF> __device__ __forceinline__ void cqr_cholesky(float2 (*sG)[kPanelMaxCols + 1], float (*Rf)[kCqrLd], float *rinv, float thr, int *fail) {
+    constexpr unsigned FULL = 0xFFFFFFFFu;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const float2 v0 = sG[w][lane], v1 = sG[w + 16][lane];
+    F2 g0 = kDF ? F2{v0.x, v0.y} : F2{v0.x + v0.y, 0.f};
+    F2 g1 = kDF ? F2{v1.x, v1.y} : F2{v1.x + v1.y, 0.f};
+    const float d0 = (lane == w) ? g0.h : g1.h;  // the diagonal held by lane w (row w) or lane w + 16 (row w + 16)
+    __syncthreads();
+    for (int k = 0; k < kPanelMaxCols; ++k) {
+        if (w == (k & 15)) {
+            const F2 gk = (k < 16) ? g0 : g1;
+            F2 piv{__shfl_sync(FULL, gk.h, k), __shfl_sync(FULL, gk.l, k)};
+            if (kDF) piv = f2_norm(piv.h, piv.l);
+            const float dk = __shfl_sync(FULL, d0, k);
+            bool bad = false;
+            if (!(piv.h > thr * dk) || !(piv.h <= 3.0e38f)) {
+                bad = true;
+                piv = F2{1.f, 0.f};
+            }
+            F2 r{0.f, 0.f};
+            if (kDF) {
+                const F2 sq = f2_sqrt(piv), rs = f2_rcp(sq);
+                if (lane == k) r = sq;
+                else if (lane > k) r = f2_mul(f2_norm(gk.h, gk.l), rs);
+            } else {
+                const float sq = sqrtf(piv.h);
+                if (lane == k) r.h = sq;
+                else if (lane > k) r.h = gk.h * (1.0f / sq);
+            }
+            sG[k][lane] = make_float2(r.h, r.l);
+            if (lane == 0 && bad) *fail = 1;
+        }
+        __syncthreads();
+        const float2 rkj = sG[k][lane];
+        if (w > k && lane >= w) {
+            const float2 rki = sG[k][w];
+            g0 = kDF ? f2_fms(g0, F2{rki.x, rki.y}, F2{rkj.x, rkj.y}) : F2{fmaf(-rki.x, rkj.x, g0.h), 0.f};
+        }
+        if (w + 16 > k && lane >= w + 16) {
+            const float2 rki = sG[k][w + 16];
+            g1 = kDF ? f2_fms(g1, F2{rki.x, rki.y}, F2{rkj.x, rkj.y}) : F2{fmaf(-rki.x, rkj.x, g1.h), 0.f};
+        }
+    }
+    for (int idx = threadIdx.x; idx < kPanelMaxCols * kPanelMaxCols; idx += blockDim.x) {
+        const int i = idx >> 5, j = idx & 31;
+        const float v = sG[i][j].x;
+        Rf[i][j] = (i <= j) ? v : 0.f;
+        if (i == j) rinv[i] = 1.0f / v;
+    }
+    __syncthreads();
+}
+
+// LU without pivoting of Q1_top - S R2 = L M by all 16 warps (thread (w, c):
+// rows w and w + 16, column c), s_j = -sign of the j-th eliminated pivot of
+// Q1_top (the sign of Q_top's, R2's diagonal being positive).  M = U R2 ->
+// Mt (upper), its reciprocal diagonal -> minv, L transposed -> Lt (Lt[c][i] =
+// L(i, c) for c < i, zero elsewhere), the signs -> S.
+__device__ __forceinline__ void cqr_top_lu(const float *qtop, const float (*R2)[kCqrLd], float (*Mt)[kCqrLd], float *minv, float (*Lt)[kCqrLd], float *S) {
+    constexpr unsigned FULL = 0xFFFFFFFFu;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    float e0 = __ldcg(qtop + w * 32 + lane), e1 = __ldcg(qtop + (w + 16) * 32 + lane);
+    for (int j = 0; j < kPanelMaxCols; ++j) {
+        if (w == (j & 15)) {
+            const float ej = (j < 16) ? e0 : e1;
+            const float piv = __shfl_sync(FULL, ej, j);
+            const float s = (piv >= 0.f) ? -1.f : 1.f;
+            Mt[j][lane] = (lane >= j) ? fmaf(-s, R2[j][lane], ej) : 0.f;
+            if (lane == 0) S[j] = s;
+        }
+        __syncthreads();
+        const float mjc = Mt[j][lane], rm = 1.0f / Mt[j][j];
+        if (w > j) {
+            const float l = __shfl_sync(FULL, e0, j) * rm;
+            if (lane > j) e0 = fmaf(-l, mjc, e0);
+            else if (lane == j) e0 = l;
+        }
+        if (w + 16 > j) {
+            const float l = __shfl_sync(FULL, e1, j) * rm;
+            if (lane > j) e1 = fmaf(-l, mjc, e1);
+            else if (lane == j) e1 = l;
+        }
+    }
+    Lt[lane][w] = (lane < w) ? e0 : 0.f;
+    Lt[lane][w + 16] = (lane < w + 16) ? e1 : 0.f;
+    if (threadIdx.x < kPanelMaxCols) minv[threadIdx.x] = 1.0f / Mt[threadIdx.x][threadIdx.x];
+    __syncthreads();
+}
+
+template <int kTag> __global__ void __launch_bounds__(kCqrThreads, 1) k_panel_cqr(CqrArgs p) {
+    constexpr int NB = kPanelMaxCols, LD = kCqrLd;
+    const int G = gridDim.x, b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int r0 = b * p.rows_per_cta, r1 = min(p.M, r0 + p.rows_per_cta), R = max(r1 - r0, 0);
+    const int N = p.N;
+    GridBarrier bar{p.counter, p.err, (unsigned)G, 0u};
+    bar.status = p.status;
+
+    extern __shared__ __align__(16) unsigned char s_dyn[];
+    float *sQ = reinterpret_cast<float *>(s_dyn);  // the block's rows, row-major (LD)
+    __shared__ __align__(16) float sR1[NB][LD];    // R1 in FP32 (upper)
+    __shared__ __align__(16) float sR2[NB][LD];    // R2 (upper)
+    __shared__ __align__(16) float sMt[NB][LD];    // M = U R2 (upper)
+    __shared__ __align__(16) float sLt[NB][LD];    // L of the top block, transposed: sLt[k][j] = L(j, k), j > k
+    __shared__ float2 sGram[NB][NB + 1];           // a summed Gram matrix (upper triangle), then R
+    __shared__ float sR1inv[NB], sR2inv[NB], sMinv[NB], sS[NB];
+    __shared__ int s_fail;
+
+    // the block's Gram partial of sQ into gpart[b]: double-float or FP32 sums,
+    // entries of a tile row in packed pairs
+    auto gram_partial = [&](bool df) {
+        for (int t = warp; t < kCqrTiles; t += kCqrThreads / 32) {
+            int ti, tj;
+            cqr_tile(t, ti, tj);
+            float2 h2[8], l2[8];
+#pragma unroll
+            for (int e = 0; e < 8; ++e) h2[e] = l2[e] = make_float2(0.f, 0.f);
+            if (df) {
+                for (int r = lane; r < R; r += 32) {
+                    const float4 a = *reinterpret_cast<const float4 *>(sQ + (size_t)r * LD + 4 * ti);
+                    const float4 c = *reinterpret_cast<const float4 *>(sQ + (size_t)r * LD + 4 * tj);
+                    const float av[4] = {a.x, a.y, a.z, a.w};
+                    const float2 c01 = make_float2(c.x, c.y), c23 = make_float2(c.z, c.w);
+#pragma unroll
+                    for (int x = 0; x < 4; ++x) {
+                        df_add_prod2(h2[2 * x], l2[2 * x], cqr_dup(av[x]), c01);
+                        df_add_prod2(h2[2 * x + 1], l2[2 * x + 1], cqr_dup(av[x]), c23);
+                    }
+                }
+            } else {
+                for (int r = lane; r < R; r += 32) {
+                    const float4 a = *reinterpret_cast<const float4 *>(sQ + (size_t)r * LD + 4 * ti);
+                    const float4 c = *reinterpret_cast<const float4 *>(sQ + (size_t)r * LD + 4 * tj);
+                    const float av[4] = {a.x, a.y, a.z, a.w};
+                    const float2 c01 = make_float2(c.x, c.y), c23 = make_float2(c.z, c.w);
+#pragma unroll
+                    for (int x = 0; x < 4; ++x) {
+                        h2[2 * x] = __ffma2_rn(cqr_dup(av[x]), c01, h2[2 * x]);
+                        h2[2 * x + 1] = __ffma2_rn(cqr_dup(av[x]), c23, h2[2 * x + 1]);
+                    }
+                }
+            }
+            float h[16], l[16];
+#pragma unroll
+            for (int e = 0; e < 8; ++e) {
+                h[2 * e] = h2[e].x;
+                h[2 * e + 1] = h2[e].y;
+                l[2 * e] = l2[e].x;
+                l[2 * e + 1] = l2[e].y;
+            }
+            const int e = cqr_warp_reduce16(h, l, lane);
+            if ((lane & 1) == 0) p.gpart[(size_t)b * kCqrEntries + t * 16 + e] = make_float2(h[0], l[0]);
+        }
+    };
+    // the partials summed across blocks, one warp per entry, into gfin
+    auto gram_sum = [&]() {
+        for (int e = b + G * warp; e < kCqrEntries; e += G * (kCqrThreads / 32)) {
+            F2 s{0.f, 0.f};
+            for (int q = lane; q < G; q += 32) {
+                const float2 v = __ldcg(&p.gpart[(size_t)q * kCqrEntries + e]);
+                s = f2_add(s, F2{v.x, v.y});
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) s = f2_add(s, F2{__shfl_xor_sync(0xFFFFFFFFu, s.h, o), __shfl_xor_sync(0xFFFFFFFFu, s.l, o)});
+            if (lane == 0) __stcg(&p.gfin[e], make_float2(s.h, s.l));
+        }
+    };
+    // every block: the summed Gram matrix into sGram (upper triangle), unit
+    // diagonal on the padding columns
+    auto gram_load = [&]() {
+        for (int idx = tid; idx < kCqrEntries; idx += kCqrThreads) {
+            int ti, tj;
+            cqr_tile(idx >> 4, ti, tj);
+            const int i = 4 * ti + ((idx >> 2) & 3), j = 4 * tj + (idx & 3);
+            if (i <= j) sGram[i][j] = (i == j && i >= N) ? make_float2(1.f, 0.f) : __ldcg(&p.gfin[idx]);
+        }
+        __syncthreads();
+    };
+    auto failed = [&]() {
+        if (s_fail && b == 0 && tid == 0) atomicExch(p.fail, 1);
+        return s_fail != 0;
+    };
+
+    // ---- the block's rows, row-major, zero padding columns ----
+    if (tid == 0) s_fail = 0;
+    for (int r = tid; r < R; r += kCqrThreads) {
+        const float *src = p.A + (size_t)(r0 + r);
+        float v[NB];
+#pragma unroll
+        for (int c = 0; c < NB; ++c) v[c] = (c < N) ? src[(size_t)c * p.lda] : 0.f;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) *reinterpret_cast<float4 *>(sQ + (size_t)r * LD + 4 * q) = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+    }
+    __syncthreads();
+
+    // ---- first pass: G1 = A^T A, R1 = chol(G1) (double-float), Q1 = A R1^-1 ----
+    gram_partial(true);
+    if (!bar.sync()) return;
+    gram_sum();
+    if (!bar.sync()) return;
+    gram_load();
+    cqr_cholesky<true>(sGram, sR1, sR1inv, 0x1p-38f, &s_fail);
+    if (failed()) return;
+    for (int r = tid; r < R; r += kCqrThreads) {
+        float2 x[NB / 2];
+        cqr_row_load(x, sQ + (size_t)r * LD);
+        cqr_row_solve(x, sR1, sR1inv);
+        cqr_row_store(sQ + (size_t)r * LD, x);
+    }
+    __syncthreads();
+    // the top 32 rows of Q1 for every block's reconstruction
+    if (b == 0)
+        for (int idx = tid; idx < NB * NB; idx += kCqrThreads) __stcg(&p.qtop[idx], sQ[(size_t)(idx >> 5) * LD + (idx & 31)]);
+
+    // ---- second pass: G2 = Q1^T Q1, R2 = chol(G2) (FP32) ----
+    gram_partial(false);
+    if (!bar.sync()) return;
+    gram_sum();
+    if (!bar.sync()) return;
+    gram_load();
+    cqr_cholesky<false>(sGram, sR2, sR2inv, 0x1p-14f, &s_fail);
+    if (failed()) return;
+
+    // ---- Householder reconstruction: Q1_top - S R2 = L M (M = U R2) ----
+    cqr_top_lu(p.qtop, sR2, sMt, sMinv, sLt, sS);
+    // V below the top block: x M = q1 for every row (block 0: warps 1..15,
+    // while warp 0 forms T)
+    const int t0 = (b == 0) ? 32 : 0;
+    if (tid >= t0) {
+        for (int r = tid - t0; r < R; r += kCqrThreads - t0) {
+            const int gr = r0 + r;
+            if (gr < N) continue;
+            float2 x[NB / 2];
+            cqr_row_load(x, sQ + (size_t)r * LD);
+            cqr_row_solve(x, sMt, sMinv);
+#pragma unroll
+            for (int c = 0; c < NB; ++c)
+                if (c < N) p.A[(size_t)gr + (size_t)c * p.lda] = (c & 1) ? x[c >> 1].y : x[c >> 1].x;
+        }
+    }
+    if (b != 0) return;
+    if (warp == 0) {
+        // T = -U S L1^-T by rows (lane i): U = M R2^-1, then t L1^T = -(U S)_i;
+        // tau = diag(T)
+        float2 u[NB / 2];
+        cqr_row_load(u, &sMt[lane][0]);
+        cqr_row_solve(u, sR2, sR2inv);
+        float t[NB];
+#pragma unroll
+        for (int j = 0; j < NB; ++j) t[j] = (j >= lane) ? -((j & 1) ? u[j >> 1].y : u[j >> 1].x) * sS[j] : 0.f;
+#pragma unroll
+        for (int k = 0; k < NB; ++k) {
+#pragma unroll
+            for (int q = (k + 1) / 4; q < 8; ++q) {
+                const float4 lk = *reinterpret_cast<const float4 *>(&sLt[k][4 * q]);
+                if (4 * q + 0 > k) t[4 * q + 0] = fmaf(-t[k], lk.x, t[4 * q + 0]);
+                if (4 * q + 1 > k) t[4 * q + 1] = fmaf(-t[k], lk.y, t[4 * q + 1]);
+                if (4 * q + 2 > k) t[4 * q + 2] = fmaf(-t[k], lk.z, t[4 * q + 2]);
+                if (4 * q + 3 > k) t[4 * q + 3] = fmaf(-t[k], lk.w, t[4 * q + 3]);
+            }
+        }
+        if (lane < N) {
+            if (p.Tm) {
+#pragma unroll
+                for (int j = 0; j < NB; ++j)
+                    if (j >= lane && j < N) p.Tm[lane + (size_t)j * p.ldt] = t[j];
+            }
+#pragma unroll
+            for (int j = 0; j < NB; ++j)
+                if (j == lane) p.tau[lane] = t[j];
+        }
+    } else {
+        // the top N x N block: L below the diagonal, R = S R2 R1 on and above it
+        for (int idx = tid - 32; idx < NB * NB; idx += kCqrThreads - 32) {
+            const int i = idx & 31, j = idx >> 5;
+            if (i >= N || j >= N) continue;
+            float v;
+            if (i > j) {
+                v = sLt[j][i];
+            } else {
+                float s = 0.f;
+                for (int k = i; k <= j; ++k) s = fmaf(sR2[i][k], sR1[k][j], s);
+                v = sS[i] * s;
+            }
+            p.A[(size_t)i + (size_t)j * p.lda] = v;
+        }
+    }
+}
+
+} // namespace rnpgpu

@@ -8,6 +8,7 @@
 // synchronizing.
 #pragma once
 #include "qr_kernels.cuh"
+#include "panel_cqr.cuh"
 #include "multq_thin.cuh"
 #include "tc_gemm.cuh"
 #include <algorithm>
@@ -401,6 +402,59 @@ template <class T> size_t t_bytes() { return ((size_t)kPanelMaxCols * kPanelMaxC
 // ---------------------------------------------------------------------------
 template <class T> int geqr2(size_t m, size_t n, T *a, size_t lda, T *tau, T *work);
 
+// CholeskyQR2 panels of the mixed solver's FP32 factor (panel_cqr.cuh):
+// Gram partials, the top rows of Q1, the failure flag
+struct CqrWs {
+    float2 *gpart = nullptr;
+    float2 *gfin = nullptr;
+    float *qtop = nullptr;
+    int *fail = nullptr;
+};
+inline size_t cqr_ws_bytes() {
+    const auto r = [](size_t b) { return (b + 255) / 256 * 256; };
+    return r((size_t)kPanelMaxBlocksCqr * kCqrEntries * sizeof(float2)) + r(kCqrEntries * sizeof(float2)) +
+           r((size_t)kPanelMaxCols * kPanelMaxCols * sizeof(float)) + 256;
+}
+inline CqrWs carve_cqr(Carver &cv) {
+    CqrWs w;
+    w.gpart = cv.take<float2>((size_t)kPanelMaxBlocksCqr * kCqrEntries);
+    w.gfin = cv.take<float2>(kCqrEntries);
+    w.qtop = cv.take<float>((size_t)kPanelMaxCols * kPanelMaxCols);
+    w.fail = cv.take<int>(1);
+    return w;
+}
+// grid of a CholeskyQR2 panel: every block at least 32 rows (block 0 holds
+// the top block), all of a block's rows in shared memory; 0 when the panel
+// does not qualify
+inline int cqr_grid(int M, int N) {
+    if (N < 1 || N > kPanelMaxCols) return 0;
+    const int g = std::min({M / kPanelMaxCols, device_facts().sm_count, kPanelMaxBlocksCqr});
+    if (g < 1) return 0;
+    const int rpc = (M + g - 1) / g;
+    if ((size_t)rpc * kCqrLd * sizeof(float) > (size_t)kCqrMaxDynSmem) return 0;
+    return g;
+}
+inline int panel_factor_cqr(int M, int N, float *A, size_t lda, float *tau, float *Tm, int ldt, const PanelWs<float> &pw, const CqrWs &cw, cudaStream_t st) {
+    const int G = cqr_grid(M, N);
+    if (G == 0) return kErrDevice;
+    static std::once_flag once;
+    static cudaError_t attr = cudaSuccess;
+    std::call_once(once, []() { attr = cudaFuncSetAttribute((const void *)k_panel_cqr<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, kCqrMaxDynSmem); });
+    RNPGPU_CHECK(attr);
+    CqrArgs p;
+    p.A = A; p.lda = lda; p.M = M; p.N = N; p.tau = tau; p.Tm = Tm; p.ldt = ldt;
+    p.gpart = cw.gpart; p.gfin = cw.gfin; p.qtop = cw.qtop; p.fail = cw.fail;
+    p.counter = pw.sync; p.err = (int *)(pw.sync + 1); p.status = device_status_ptr();
+    p.rows_per_cta = (M + G - 1) / G;
+    RNPGPU_CHECK(cudaMemsetAsync(pw.sync, 0, 2 * sizeof(unsigned), st));
+    void *args[] = {&p};
+    KScope ks("panel_cqr", st);
+    const size_t smem = (size_t)p.rows_per_cta * kCqrLd * sizeof(float);
+    RNPGPU_CHECK(cudaLaunchCooperativeKernel((const void *)k_panel_cqr<0>, dim3(G), dim3(kCqrThreads), args, smem, st));
+    note_launch();
+    return kOk;
+}
+
 // serial blocked form: panel workspace, one T, one update workspace
 template <class T> size_t geqrf_serial_bytes(size_t m, size_t n, int smax) {
     return panel_ws_bytes<T>(panel_gmax<T>()) + t_bytes<T>() + block_ws_bytes<T>((int)n, smax);
@@ -449,7 +503,7 @@ inline LookAhead *lookahead_ctx() {
 // those columns again.  The results are the same as in the serial order (the
 // same operations on the same data).  Without the larger workspace, inside
 // stream capture, or for a single trailing block the serial order is used.
-template <class T> int geqrf(size_t m, size_t n, T *a, size_t lda, T *tau, size_t *lwork, T *work, T *Tstore = nullptr) {
+template <class T> int geqrf(size_t m, size_t n, T *a, size_t lda, T *tau, size_t *lwork, T *work, T *Tstore = nullptr, const CqrWs *cqr = nullptr) {
     if (lwork == nullptr) return -6;
     const size_t k = std::min(m, n);
     if (k == 0) return kOk;
@@ -496,7 +550,15 @@ template <class T> int geqrf(size_t m, size_t n, T *a, size_t lda, T *tau, size_
         const int ib = (int)std::min(nb, k - i);
         T *Ai = a + i + i * lda;
         T *Tb = Tstore ? Tstore + (i / nb) * kPanelMaxCols * kPanelMaxCols : Tm[(i / nb) & 1];
-        int rc = panel_factor<T>((int)(m - i), ib, Ai, lda, tau + i, Tb, kPanelMaxCols, pw, st);
+        int rc;
+        if constexpr (std::is_same<T, float>::value) {
+            if (cqr != nullptr && cqr_grid((int)(m - i), ib) > 0)
+                rc = panel_factor_cqr((int)(m - i), ib, Ai, lda, tau + i, Tb, kPanelMaxCols, pw, *cqr, st);
+            else
+                rc = panel_factor<T>((int)(m - i), ib, Ai, lda, tau + i, Tb, kPanelMaxCols, pw, st);
+        } else {
+            rc = panel_factor<T>((int)(m - i), ib, Ai, lda, tau + i, Tb, kPanelMaxCols, pw, st);
+        }
         if (rc) return rc;
         const size_t c1 = i + ib;  // first trailing column
         if (c1 >= n) continue;

@@ -131,3 +131,63 @@ def test_mixed_refinement_reaches_fp64(oracle, cplx, forward):
         assert ferr <= 1e-5, ferr
     # A and b untouched
     assert np.array_equal(from_dev(dA), A) and np.array_equal(from_dev(db), b)
+
+
+def panel_kinds(fn):
+    """Run fn with kernel-class timing on; {class: launches} of its panels."""
+    from rnp2_gb300 import _capi
+
+    lib = _capi.lib()
+    lib.rnpgpu_timing_enable(1)
+    _capi.timing_report()
+    try:
+        out = fn()
+        torch.cuda.synchronize()
+        rep = _capi.timing_report()
+    finally:
+        lib.rnpgpu_timing_enable(0)
+    return out, {k: v[0] for k, v in rep.items() if k.startswith("panel")}
+
+
+def check_refined(A, b, X, info):
+    n = A.shape[1]
+    bound = 10 * n * np.finfo(np.float64).eps
+    assert info["converged"] == 1, info
+    assert info["backward_error"] <= bound and info["normal_residual"] <= bound
+    assert ls_backward_error(A, b, X.cpu().numpy()) <= bound
+
+
+@pytest.mark.parametrize("mn", [(4096, 100), (3000, 64), (1000, 33)])
+def test_mixed_fp32_factor_uses_cholesky_qr2_panels(mn):
+    # the mixed solver's FP32 factor takes CholeskyQR2 panels on real data;
+    # widths that are not a multiple of 32 pad the last panel
+    m, n = mn
+    rng = np.random.default_rng(m + n)
+    A = rng.standard_normal((m, n))
+    b = A @ rng.standard_normal((n, 3)) + 1e-8 * rng.standard_normal((m, 3))
+    (X, info), kinds = panel_kinds(lambda: gls.gels_refine(to_dev(A), to_dev(b)))
+    assert kinds == {"panel_cqr": (n + 31) // 32}, kinds
+    check_refined(A, b, X, info)
+
+
+def test_mixed_fp32_factor_falls_back_to_householder_panels():
+    # two columns 1e-6 apart in angle: the first Cholesky pivot of their panel
+    # keeps 1e-12 of the column's squared norm, below the CholeskyQR2 limit, so
+    # the factor is redone with Householder panels.  Any panel that fails has a
+    # condition number near 10^6 or more, where the refinement contracts slowly:
+    # the check is that it refines far below FP32 accuracy from the redone
+    # factor (a stale or damaged factor would not), and that the error it
+    # reports is the true one
+    m, n = 4096, 96
+    rng = np.random.default_rng(21)
+    A = rng.standard_normal((m, n))
+    u = rng.standard_normal(m)
+    u -= A[:, 40] * (u @ A[:, 40]) / (A[:, 40] @ A[:, 40])
+    A[:, 41] = A[:, 40] + 1e-6 * np.linalg.norm(A[:, 40]) * u / np.linalg.norm(u)
+    b = A @ rng.standard_normal((n, 2)) + 1e-8 * rng.standard_normal((m, 2))
+    (X, info), kinds = panel_kinds(lambda: gls.gels_refine(to_dev(A), to_dev(b)))
+    assert kinds.get("panel") == 3 and kinds.get("panel_cqr", 0) >= 2, kinds
+    be = ls_backward_error(A, b, X.cpu().numpy())
+    assert info["backward_error"] <= 1e-10 and be <= 1e-10, (info, be)
+    if info["converged"] == 1:
+        assert be <= 10 * n * np.finfo(np.float64).eps
