@@ -140,9 +140,6 @@ __device__ __forceinline__ void df_add_prod2(float2 &h, float2 &l, float2 a, flo
 // shared memory (rows of kCqrLd floats, 16-byte aligned) with reciprocal
 // diagonal rinv
 __device__ __forceinline__ void cqr_row_solve(float2 (&x)[16], const float (*Rf)[kCqrLd], const float *rinv) {
-    // opaque to the compiler, so that it does not hoist the factor's loads out
-    // of a caller's loop over rows (they would not fit in registers)
-    asm volatile("" : "+l"(Rf), "+l"(rinv));
 #pragma unroll
     for (int l = 0; l < 32; ++l) {
         float xl = ((l & 1) ? x[l >> 1].y : x[l >> 1].x) * rinv[l];
@@ -172,105 +169,228 @@ __device__ __forceinline__ void cqr_row_store(float *row, const float2 (&x)[16])
     for (int q = 0; q < 8; ++q) *reinterpret_cast<float4 *>(row + 4 * q) = make_float4(x[2 * q].x, x[2 * q].y, x[2 * q + 1].x, x[2 * q + 1].y);
 }
 
+// 1 / sqrt(a) for a > 0: the hardware approximation and one Newton step
+// y + y (1 - a y^2) / 2, the residual formed with the exact product a.h y
+// (about 2^-43 relative in double-float; FP32 to about an ulp)
+__device__ __forceinline__ F2 f2_rsqrt(F2 a) {
+    const float y = rsqrtf(a.h);
+    const float p = a.h * y, pe = fmaf(a.h, y, -p);
+    const float r = fmaf(-p, y, 1.0f) - fmaf(pe, y, a.l * y * y);
+    return f2_norm(y, 0.5f * y * r);
+}
+__device__ __forceinline__ float f32_rsqrt(float a) {
+    const float y = rsqrtf(a);
+    return fmaf(0.5f * y, fmaf(-a * y, y, 1.0f), y);
+}
+
+// arithmetic of the blocked Cholesky: double-float (kDF) or FP32 in the
+// same F2 carrier (lo stays zero)
+template <bool kDF> struct CqrArith {
+    static __device__ __forceinline__ F2 from(float2 v) { return kDF ? F2{v.x, v.y} : F2{v.x + v.y, 0.f}; }
+    static __device__ __forceinline__ F2 fms(F2 a, F2 b, F2 c) { return kDF ? f2_fms(a, b, c) : F2{fmaf(-b.h, c.h, a.h), 0.f}; }
+    static __device__ __forceinline__ F2 mul(F2 a, F2 b) { return kDF ? f2_mul(f2_norm(a.h, a.l), b) : F2{a.h * b.h, 0.f}; }
+    static __device__ __forceinline__ F2 norm(F2 a) { return kDF ? f2_norm(a.h, a.l) : a; }
+    static __device__ __forceinline__ F2 rsqrt(F2 a) { return kDF ? f2_rsqrt(a) : F2{f32_rsqrt(a.h), 0.f}; }
+};
+
 // Cholesky of the 32 x 32 Gram matrix in sG (upper triangle; hi, lo pairs) by
-// all 16 warps of the block: thread (w, j) holds entries (w, j) and (w + 16,
-// j); row k of R is finished by the warp that holds it and published in sG's
-// row k, then every thread updates its entries below — one block barrier a
-// step.  Double-float (kDF) or FP32 arithmetic.  R in FP32 -> Rf (upper,
-// zero below), its reciprocal diagonal -> rinv; a pivot not above thr times
-// its column's original diagonal (or not finite) sets *fail.
-template <bool kDF> __device__ __forceinline__ void cqr_cholesky(float2 (*sG)[kPanelMaxCols + 1], float (*Rf)[kCqrLd], float *rinv, float thr, int *fail) {
-    constexpr unsigned FULL = 0xFFFFFFFFu;
+// the whole block, four columns a step: thread (w, j) holds entries (w, j)
+// and (w + 16, j).  At step b warp 0 factors the 4 x 4 diagonal block
+// D = R_BB^T R_BB, forms the block's four rows of R (lane x: R_B,x =
+// R_BB^-T G_B,x) and writes them over sG's rows; after a block barrier every
+// thread updates its entries below, and the holders of the next four rows
+// publish them in sG — two block barriers a step.  Double-float (kDF) or
+// FP32.  R in FP32 -> Rf (upper, zero below), its reciprocal diagonal ->
+// rinv; a pivot not above thr times its column's original diagonal (or not
+// finite) sets *fail.
+template <bool kDF> __device__ __forceinline__ void cqr_cholesky(float2 (*sG)[kPanelMaxCols + 1], float (*Rf)[kCqrLd], float *rinv, float *sD0, float thr, int *fail) {
+    using A = CqrArith<kDF>;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const float2 v0 = sG[w][lane], v1 = sG[w + 16][lane];
-    F2 g0 = kDF ? F2{v0.x, v0.y} : F2{v0.x + v0.y, 0.f};
-    F2 g1 = kDF ? F2{v1.x, v1.y} : F2{v1.x + v1.y, 0.f};
-    const float d0 = (lane == w) ? g0.h : g1.h;  // the diagonal held by lane w (row w) or lane w + 16 (row w + 16)
+    F2 g0 = A::from(sG[w][lane]), g1 = A::from(sG[w + 16][lane]);
+    if (threadIdx.x < kPanelMaxCols) sD0[threadIdx.x] = sG[threadIdx.x][threadIdx.x].x;
     __syncthreads();
-    for (int k = 0; k < kPanelMaxCols; ++k) {
-        if (w == (k & 15)) {
-            const F2 gk = (k < 16) ? g0 : g1;
-            F2 piv{__shfl_sync(FULL, gk.h, k), __shfl_sync(FULL, gk.l, k)};
-            if (kDF) piv = f2_norm(piv.h, piv.l);
-            const float dk = __shfl_sync(FULL, d0, k);
+    for (int k0 = 0; k0 < kPanelMaxCols; k0 += 4) {
+        if (w == 0) {
+            // the diagonal block's factor (upper, r[a][c] for a <= c) and the
+            // reciprocals of its diagonal
+            F2 r[4][4], ri[4];
             bool bad = false;
-            if (!(piv.h > thr * dk) || !(piv.h <= 3.0e38f)) {
-                bad = true;
-                piv = F2{1.f, 0.f};
+#pragma unroll
+            for (int a = 0; a < 4; ++a)
+#pragma unroll
+                for (int c = a; c < 4; ++c) r[a][c] = A::from(sG[k0 + a][k0 + c]);
+#pragma unroll
+            for (int a = 0; a < 4; ++a) {
+#pragma unroll
+                for (int m = 0; m < a; ++m)
+#pragma unroll
+                    for (int c = a; c < 4; ++c) r[a][c] = A::fms(r[a][c], r[m][a], r[m][c]);
+                F2 piv = A::norm(r[a][a]);
+                if (!(piv.h > thr * sD0[k0 + a]) || !(piv.h <= 3.0e38f)) {
+                    bad = true;
+                    piv = F2{1.f, 0.f};
+                }
+                ri[a] = A::rsqrt(piv);
+                r[a][a] = A::mul(piv, ri[a]);
+#pragma unroll
+                for (int c = a + 1; c < 4; ++c) r[a][c] = A::mul(r[a][c], ri[a]);
             }
-            F2 r{0.f, 0.f};
-            if (kDF) {
-                const F2 sq = f2_sqrt(piv), rs = f2_rcp(sq);
-                if (lane == k) r = sq;
-                else if (lane > k) r = f2_mul(f2_norm(gk.h, gk.l), rs);
+            // the block's rows of R in column `lane`
+            F2 rj[4];
+            if (lane > k0 + 3) {
+#pragma unroll
+                for (int a = 0; a < 4; ++a) {
+                    rj[a] = A::from(sG[k0 + a][lane]);
+#pragma unroll
+                    for (int m = 0; m < a; ++m) rj[a] = A::fms(rj[a], r[m][a], rj[m]);
+                    rj[a] = A::mul(rj[a], ri[a]);
+                }
             } else {
-                const float sq = sqrtf(piv.h);
-                if (lane == k) r.h = sq;
-                else if (lane > k) r.h = gk.h * (1.0f / sq);
+#pragma unroll
+                for (int a = 0; a < 4; ++a) {
+                    rj[a] = F2{0.f, 0.f};
+#pragma unroll
+                    for (int c = a; c < 4; ++c)
+                        if (lane == k0 + c) rj[a] = r[a][c];
+                }
             }
-            sG[k][lane] = make_float2(r.h, r.l);
+            __syncwarp();
+#pragma unroll
+            for (int a = 0; a < 4; ++a) {
+                if (lane >= k0) sG[k0 + a][lane] = make_float2(rj[a].h, rj[a].l);
+                Rf[k0 + a][lane] = (lane >= k0 + a) ? rj[a].h : 0.f;
+            }
             if (lane == 0 && bad) *fail = 1;
         }
         __syncthreads();
-        const float2 rkj = sG[k][lane];
-        if (w > k && lane >= w) {
-            const float2 rki = sG[k][w];
-            g0 = kDF ? f2_fms(g0, F2{rki.x, rki.y}, F2{rkj.x, rkj.y}) : F2{fmaf(-rki.x, rkj.x, g0.h), 0.f};
+        // this thread's entries (i, lane), i > k0 + 3, lane >= i
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            const F2 rj = A::from(sG[k0 + a][lane]);
+            if (w > k0 + 3 && lane >= w) g0 = A::fms(g0, A::from(sG[k0 + a][w]), rj);
+            if (w + 16 > k0 + 3 && lane >= w + 16) g1 = A::fms(g1, A::from(sG[k0 + a][w + 16]), rj);
         }
-        if (w + 16 > k && lane >= w + 16) {
-            const float2 rki = sG[k][w + 16];
-            g1 = kDF ? f2_fms(g1, F2{rki.x, rki.y}, F2{rkj.x, rkj.y}) : F2{fmaf(-rki.x, rkj.x, g1.h), 0.f};
-        }
+        if (w >= k0 + 4 && w < k0 + 8) sG[w][lane] = make_float2(g0.h, g0.l);
+        if (w + 16 >= k0 + 4 && w + 16 < k0 + 8) sG[w + 16][lane] = make_float2(g1.h, g1.l);
+        __syncthreads();
     }
-    for (int idx = threadIdx.x; idx < kPanelMaxCols * kPanelMaxCols; idx += blockDim.x) {
-        const int i = idx >> 5, j = idx & 31;
-        const float v = sG[i][j].x;
-        Rf[i][j] = (i <= j) ? v : 0.f;
-        if (i == j) rinv[i] = 1.0f / v;
-    }
+    if (threadIdx.x < kPanelMaxCols) rinv[threadIdx.x] = 1.0f / Rf[threadIdx.x][threadIdx.x];
     __syncthreads();
 }
 
-// LU without pivoting of Q1_top - S R2 = L M by all 16 warps (thread (w, c):
-// rows w and w + 16, column c), s_j = -sign of the j-th eliminated pivot of
-// Q1_top (the sign of Q_top's, R2's diagonal being positive).  M = U R2 ->
-// Mt (upper), its reciprocal diagonal -> minv, L transposed -> Lt (Lt[c][i] =
+// LU without pivoting of Q1_top - S R2 = L M by the whole block, four rows a
+// step (thread (w, c): rows w and w + 16, column c; the current rows are
+// staged in sE), s_j = -sign of the j-th eliminated pivot of Q1_top (the sign
+// of Q_top's, R2's diagonal being positive).  Warp 0 factors the 4 x 4
+// diagonal block and writes the block's rows of M, their reciprocal pivots
+// and the block's own multipliers; after a block barrier every thread forms
+// the multipliers of its rows below and updates its entries.  M = U R2 -> Mt
+// (upper), its reciprocal diagonal -> minv, L transposed -> Lt (Lt[c][i] =
 // L(i, c) for c < i, zero elsewhere), the signs -> S.
-__device__ __forceinline__ void cqr_top_lu(const float *qtop, const float (*R2)[kCqrLd], float (*Mt)[kCqrLd], float *minv, float (*Lt)[kCqrLd], float *S) {
+__device__ __forceinline__ void cqr_top_lu(const float *qtop, const float (*R2)[kCqrLd], float (*Mt)[kCqrLd], float *minv, float (*Lt)[kCqrLd], float *S, float (*sE)[kCqrLd]) {
     constexpr unsigned FULL = 0xFFFFFFFFu;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     float e0 = __ldcg(qtop + w * 32 + lane), e1 = __ldcg(qtop + (w + 16) * 32 + lane);
-    for (int j = 0; j < kPanelMaxCols; ++j) {
-        if (w == (j & 15)) {
-            const float ej = (j < 16) ? e0 : e1;
-            const float piv = __shfl_sync(FULL, ej, j);
-            const float s = (piv >= 0.f) ? -1.f : 1.f;
-            Mt[j][lane] = (lane >= j) ? fmaf(-s, R2[j][lane], ej) : 0.f;
-            if (lane == 0) S[j] = s;
+    if (w < 4) sE[w][lane] = e0;
+    __syncthreads();
+    for (int j0 = 0; j0 < kPanelMaxCols; j0 += 4) {
+        if (w == 0) {
+            // the diagonal block: m[a][c] (c >= a) rows of M, l[a][c] (c < a) multipliers
+            float m[4][4], l[4][4], mi[4], sg[4];
+#pragma unroll
+            for (int a = 0; a < 4; ++a)
+#pragma unroll
+                for (int c = 0; c < 4; ++c) m[a][c] = sE[j0 + a][j0 + c];
+#pragma unroll
+            for (int a = 0; a < 4; ++a) {
+                sg[a] = (m[a][a] >= 0.f) ? -1.f : 1.f;
+#pragma unroll
+                for (int c = a; c < 4; ++c) m[a][c] = fmaf(-sg[a], R2[j0 + a][j0 + c], m[a][c]);
+                mi[a] = 1.0f / m[a][a];
+#pragma unroll
+                for (int b = a + 1; b < 4; ++b) {
+                    l[b][a] = m[b][a] * mi[a];
+#pragma unroll
+                    for (int c = a + 1; c < 4; ++c) m[b][c] = fmaf(-l[b][a], m[a][c], m[b][c]);
+                }
+            }
+            // the block's rows of M in column `lane`
+            float mc[4];
+            if (lane > j0 + 3) {
+#pragma unroll
+                for (int a = 0; a < 4; ++a) {
+                    float v = fmaf(-sg[a], R2[j0 + a][lane], sE[j0 + a][lane]);
+#pragma unroll
+                    for (int b = 0; b < a; ++b) v = fmaf(-l[a][b], mc[b], v);
+                    mc[a] = v;
+                }
+            } else {
+#pragma unroll
+                for (int a = 0; a < 4; ++a) {
+                    mc[a] = 0.f;
+#pragma unroll
+                    for (int c = a; c < 4; ++c)
+                        if (lane == j0 + c) mc[a] = m[a][c];
+                }
+            }
+#pragma unroll
+            for (int a = 0; a < 4; ++a) Mt[j0 + a][lane] = mc[a];
+            if (lane < 4) {
+#pragma unroll
+                for (int a = 0; a < 4; ++a)
+                    if (lane == a) {
+                        S[j0 + a] = sg[a];
+                        minv[j0 + a] = mi[a];
+                    }
+            }
+            if (lane == 0) {
+#pragma unroll
+                for (int a = 1; a < 4; ++a)
+#pragma unroll
+                    for (int c = 0; c < a; ++c) Lt[j0 + c][j0 + a] = l[a][c];
+            }
         }
         __syncthreads();
-        const float mjc = Mt[j][lane], rm = 1.0f / Mt[j][j];
-        if (w > j) {
-            const float l = __shfl_sync(FULL, e0, j) * rm;
-            if (lane > j) e0 = fmaf(-l, mjc, e0);
-            else if (lane == j) e0 = l;
-        }
-        if (w + 16 > j) {
-            const float l = __shfl_sync(FULL, e1, j) * rm;
-            if (lane > j) e1 = fmaf(-l, mjc, e1);
-            else if (lane == j) e1 = l;
-        }
+        // multipliers of this thread's rows i > j0 + 3 and their update
+        auto eliminate = [&](float &e) {
+            float li[4];
+#pragma unroll
+            for (int a = 0; a < 4; ++a) {
+                float v = __shfl_sync(FULL, e, j0 + a);
+#pragma unroll
+                for (int b = 0; b < a; ++b) v = fmaf(-li[b], Mt[j0 + b][j0 + a], v);
+                li[a] = v * minv[j0 + a];
+            }
+            if (lane > j0 + 3) {
+#pragma unroll
+                for (int a = 0; a < 4; ++a) e = fmaf(-li[a], Mt[j0 + a][lane], e);
+            } else {
+#pragma unroll
+                for (int a = 0; a < 4; ++a)
+                    if (lane == j0 + a) e = li[a];
+            }
+        };
+        if (w > j0 + 3) eliminate(e0);
+        if (w + 16 > j0 + 3) eliminate(e1);
+        if (w >= j0 + 4 && w < j0 + 8) sE[w][lane] = e0;
+        if (w + 16 >= j0 + 4 && w + 16 < j0 + 8) sE[w + 16][lane] = e1;
+        __syncthreads();
     }
-    Lt[lane][w] = (lane < w) ? e0 : 0.f;
-    Lt[lane][w + 16] = (lane < w + 16) ? e1 : 0.f;
-    if (threadIdx.x < kPanelMaxCols) minv[threadIdx.x] = 1.0f / Mt[threadIdx.x][threadIdx.x];
+    // multipliers from earlier blocks (the block's own ones are in Lt already)
+    if (lane < (w & ~3)) Lt[lane][w] = e0;
+    else if (lane >= w) Lt[lane][w] = 0.f;
+    if (lane < ((w + 16) & ~3)) Lt[lane][w + 16] = e1;
+    else if (lane >= w + 16) Lt[lane][w + 16] = 0.f;
     __syncthreads();
 }
 
 template <int kTag> __global__ void __launch_bounds__(kCqrThreads, 1) k_panel_cqr(CqrArgs p) {
     constexpr int NB = kPanelMaxCols, LD = kCqrLd;
     const int G = gridDim.x, b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int r0 = b * p.rows_per_cta, r1 = min(p.M, r0 + p.rows_per_cta), R = max(r1 - r0, 0);
+    // block 0 holds the top 32 rows (it also forms T and the top block at the
+    // end); the other blocks share the rest, rows_per_cta each
+    const int r0 = (b == 0) ? 0 : (G == 1 ? 0 : NB + (b - 1) * p.rows_per_cta);
+    const int r1 = (G == 1) ? p.M : (b == 0 ? NB : min(p.M, r0 + p.rows_per_cta)), R = max(r1 - r0, 0);
     const int N = p.N;
     GridBarrier bar{p.counter, p.err, (unsigned)G, 0u};
     bar.status = p.status;
@@ -282,7 +402,8 @@ template <int kTag> __global__ void __launch_bounds__(kCqrThreads, 1) k_panel_cq
     __shared__ __align__(16) float sMt[NB][LD];    // M = U R2 (upper)
     __shared__ __align__(16) float sLt[NB][LD];    // L of the top block, transposed: sLt[k][j] = L(j, k), j > k
     __shared__ float2 sGram[NB][NB + 1];           // a summed Gram matrix (upper triangle), then R
-    __shared__ float sR1inv[NB], sR2inv[NB], sMinv[NB], sS[NB];
+    __shared__ __align__(16) float sE[NB][LD];     // rows of the top block's LU, staged
+    __shared__ float sR1inv[NB], sR2inv[NB], sMinv[NB], sS[NB], sD0[NB];
     __shared__ int s_fail;
 
     // the block's Gram partial of sQ into gpart[b]: double-float or FP32 sums,
@@ -378,12 +499,16 @@ template <int kTag> __global__ void __launch_bounds__(kCqrThreads, 1) k_panel_cq
     gram_sum();
     if (!bar.sync()) return;
     gram_load();
-    cqr_cholesky<true>(sGram, sR1, sR1inv, 0x1p-38f, &s_fail);
+    cqr_cholesky<true>(sGram, sR1, sR1inv, sD0, 0x1p-38f, &s_fail);
     if (failed()) return;
     for (int r = tid; r < R; r += kCqrThreads) {
         float2 x[NB / 2];
         cqr_row_load(x, sQ + (size_t)r * LD);
-        cqr_row_solve(x, sR1, sR1inv);
+        // z = 0 (r < 2^30), but the compiler cannot tell: the factor's loads
+        // stay in the loop instead of being hoisted out of it (they would
+        // not fit in registers)
+        const int z = r & 0x40000000;
+        cqr_row_solve(x, sR1 + z, sR1inv + z);
         cqr_row_store(sQ + (size_t)r * LD, x);
     }
     __syncthreads();
@@ -397,60 +522,56 @@ template <int kTag> __global__ void __launch_bounds__(kCqrThreads, 1) k_panel_cq
     gram_sum();
     if (!bar.sync()) return;
     gram_load();
-    cqr_cholesky<false>(sGram, sR2, sR2inv, 0x1p-14f, &s_fail);
+    cqr_cholesky<false>(sGram, sR2, sR2inv, sD0, 0x1p-14f, &s_fail);
     if (failed()) return;
 
     // ---- Householder reconstruction: Q1_top - S R2 = L M (M = U R2) ----
-    cqr_top_lu(p.qtop, sR2, sMt, sMinv, sLt, sS);
-    // V below the top block: x M = q1 for every row (block 0: warps 1..15,
-    // while warp 0 forms T)
-    const int t0 = (b == 0) ? 32 : 0;
-    if (tid >= t0) {
-        for (int r = tid - t0; r < R; r += kCqrThreads - t0) {
-            const int gr = r0 + r;
-            if (gr < N) continue;
-            float2 x[NB / 2];
-            cqr_row_load(x, sQ + (size_t)r * LD);
-            cqr_row_solve(x, sMt, sMinv);
+    cqr_top_lu(p.qtop, sR2, sMt, sMinv, sLt, sS, sE);
+    // V below the top block: x M = q1 for every row
+    for (int r = tid; r < R; r += kCqrThreads) {
+        const int gr = r0 + r;
+        if (gr < N) continue;
+        float2 x[NB / 2];
+        cqr_row_load(x, sQ + (size_t)r * LD);
+        const int z = r & 0x40000000;  // zero, opaque: as in the first row solve
+        cqr_row_solve(x, sMt + z, sMinv + z);
 #pragma unroll
-            for (int c = 0; c < NB; ++c)
-                if (c < N) p.A[(size_t)gr + (size_t)c * p.lda] = (c & 1) ? x[c >> 1].y : x[c >> 1].x;
-        }
+        for (int c = 0; c < NB; ++c)
+            if (c < N) p.A[(size_t)gr + (size_t)c * p.lda] = (c & 1) ? x[c >> 1].y : x[c >> 1].x;
     }
     if (b != 0) return;
+
+    // block 0: T = -U S L1^-T = -M P with P = R2^-1 S L1^-T (U = M R2^-1),
+    // from the two triangular inverses (warp 0: R2^-1, warp 1: L1^-1, lane =
+    // column); the top N x N block: L below the diagonal, R = S R2 R1 on and
+    // above it
+    float (*sInvR)[LD] = sE;                                     // R2^-1 (the LU's staging is free)
+    float (*sInvL)[LD] = reinterpret_cast<float (*)[LD]>(&sGram[0][0]);  // L1^-1 (sGram is free)
     if (warp == 0) {
-        // T = -U S L1^-T by rows (lane i): U = M R2^-1, then t L1^T = -(U S)_i;
-        // tau = diag(T)
-        float2 u[NB / 2];
-        cqr_row_load(u, &sMt[lane][0]);
-        cqr_row_solve(u, sR2, sR2inv);
-        float t[NB];
+        float x[NB];
 #pragma unroll
-        for (int j = 0; j < NB; ++j) t[j] = (j >= lane) ? -((j & 1) ? u[j >> 1].y : u[j >> 1].x) * sS[j] : 0.f;
+        for (int i = 0; i < NB; ++i) x[i] = (i == lane) ? 1.f : 0.f;
+#pragma unroll
+        for (int i = NB - 1; i >= 0; --i) {
+            x[i] *= sR2inv[i];
+#pragma unroll
+            for (int k = 0; k < i; ++k) x[k] = fmaf(-sR2[k][i], x[i], x[k]);
+        }
+#pragma unroll
+        for (int i = 0; i < NB; ++i) sInvR[i][lane] = x[i];
+    } else if (warp == 1) {
+        float x[NB];
+#pragma unroll
+        for (int i = 0; i < NB; ++i) x[i] = (i == lane) ? 1.f : 0.f;
 #pragma unroll
         for (int k = 0; k < NB; ++k) {
 #pragma unroll
-            for (int q = (k + 1) / 4; q < 8; ++q) {
-                const float4 lk = *reinterpret_cast<const float4 *>(&sLt[k][4 * q]);
-                if (4 * q + 0 > k) t[4 * q + 0] = fmaf(-t[k], lk.x, t[4 * q + 0]);
-                if (4 * q + 1 > k) t[4 * q + 1] = fmaf(-t[k], lk.y, t[4 * q + 1]);
-                if (4 * q + 2 > k) t[4 * q + 2] = fmaf(-t[k], lk.z, t[4 * q + 2]);
-                if (4 * q + 3 > k) t[4 * q + 3] = fmaf(-t[k], lk.w, t[4 * q + 3]);
-            }
+            for (int j = k + 1; j < NB; ++j) x[j] = fmaf(-sLt[k][j], x[k], x[j]);
         }
-        if (lane < N) {
-            if (p.Tm) {
 #pragma unroll
-                for (int j = 0; j < NB; ++j)
-                    if (j >= lane && j < N) p.Tm[lane + (size_t)j * p.ldt] = t[j];
-            }
-#pragma unroll
-            for (int j = 0; j < NB; ++j)
-                if (j == lane) p.tau[lane] = t[j];
-        }
+        for (int i = 0; i < NB; ++i) sInvL[i][lane] = x[i];
     } else {
-        // the top N x N block: L below the diagonal, R = S R2 R1 on and above it
-        for (int idx = tid - 32; idx < NB * NB; idx += kCqrThreads - 32) {
+        for (int idx = tid - 64; idx < NB * NB; idx += kCqrThreads - 64) {
             const int i = idx & 31, j = idx >> 5;
             if (i >= N || j >= N) continue;
             float v;
@@ -463,6 +584,24 @@ template <int kTag> __global__ void __launch_bounds__(kCqrThreads, 1) k_panel_cq
             }
             p.A[(size_t)i + (size_t)j * p.lda] = v;
         }
+    }
+    __syncthreads();
+    // P(i, j) = sum_{i <= k <= j} R2^-1(i, k) s_k L1^-1(j, k) into sR1 (R1 is done with)
+    for (int idx = tid; idx < NB * NB; idx += kCqrThreads) {
+        const int i = idx >> 5, j = idx & 31;
+        float s = 0.f;
+        for (int k = i; k <= j; ++k) s = fmaf(sInvR[i][k] * sS[k], sInvL[j][k], s);
+        sR1[i][j] = (i <= j) ? s : 0.f;
+    }
+    __syncthreads();
+    // T(i, j) = -sum_{i <= k <= j} M(i, k) P(k, j); tau = diag(T)
+    for (int idx = tid; idx < NB * NB; idx += kCqrThreads) {
+        const int i = idx & 31, j = idx >> 5;
+        if (i >= N || j >= N || i > j) continue;
+        float s = 0.f;
+        for (int k = i; k <= j; ++k) s = fmaf(sMt[i][k], sR1[k][j], s);
+        if (p.Tm) p.Tm[i + (size_t)j * p.ldt] = -s;
+        if (i == j) p.tau[i] = -s;
     }
 }
 

@@ -423,15 +423,18 @@ inline CqrWs carve_cqr(Carver &cv) {
     w.fail = cv.take<int>(1);
     return w;
 }
-// grid of a CholeskyQR2 panel: every block at least 32 rows (block 0 holds
-// the top block), all of a block's rows in shared memory; 0 when the panel
-// does not qualify
+// rows of a CholeskyQR2 panel per block: block 0 holds the top 32 rows, the
+// other blocks share the rest (one block: all rows)
+inline int cqr_rows_per_block(int M, int g) { return g == 1 ? M : (M - kPanelMaxCols + g - 2) / (g - 1); }
+inline int cqr_rows_held(int M, int g) { return std::max(kPanelMaxCols, cqr_rows_per_block(M, g)); }
+// grid of a CholeskyQR2 panel: M / 32 blocks at most (every block at least
+// 32 rows), all of a block's rows in shared memory; 0 when the panel does not
+// qualify
 inline int cqr_grid(int M, int N) {
     if (N < 1 || N > kPanelMaxCols) return 0;
     const int g = std::min({M / kPanelMaxCols, device_facts().sm_count, kPanelMaxBlocksCqr});
     if (g < 1) return 0;
-    const int rpc = (M + g - 1) / g;
-    if ((size_t)rpc * kCqrLd * sizeof(float) > (size_t)kCqrMaxDynSmem) return 0;
+    if ((size_t)cqr_rows_held(M, g) * kCqrLd * sizeof(float) > (size_t)kCqrMaxDynSmem) return 0;
     return g;
 }
 inline int panel_factor_cqr(int M, int N, float *A, size_t lda, float *tau, float *Tm, int ldt, const PanelWs<float> &pw, const CqrWs &cw, cudaStream_t st) {
@@ -445,11 +448,11 @@ inline int panel_factor_cqr(int M, int N, float *A, size_t lda, float *tau, floa
     p.A = A; p.lda = lda; p.M = M; p.N = N; p.tau = tau; p.Tm = Tm; p.ldt = ldt;
     p.gpart = cw.gpart; p.gfin = cw.gfin; p.qtop = cw.qtop; p.fail = cw.fail;
     p.counter = pw.sync; p.err = (int *)(pw.sync + 1); p.status = device_status_ptr();
-    p.rows_per_cta = (M + G - 1) / G;
+    p.rows_per_cta = cqr_rows_per_block(M, G);
     RNPGPU_CHECK(cudaMemsetAsync(pw.sync, 0, 2 * sizeof(unsigned), st));
     void *args[] = {&p};
     KScope ks("panel_cqr", st);
-    const size_t smem = (size_t)p.rows_per_cta * kCqrLd * sizeof(float);
+    const size_t smem = (size_t)cqr_rows_held(M, G) * kCqrLd * sizeof(float);
     RNPGPU_CHECK(cudaLaunchCooperativeKernel((const void *)k_panel_cqr<0>, dim3(G), dim3(kCqrThreads), args, smem, st));
     note_launch();
     return kOk;
