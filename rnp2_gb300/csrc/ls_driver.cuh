@@ -32,7 +32,14 @@ struct RefineInfo {
 template <class T> int trsm_upper(size_t n, size_t nrhs, const T *a, size_t lda, T *b, size_t ldb, cudaStream_t st) {
     if (n == 0 || nrhs == 0) return kOk;
     KScope ks("trsm", st);
-    k_trsm_upper<T><<<(unsigned)std::min<size_t>(nrhs, 65535), 512, 0, st>>>((int)n, (int)nrhs, a, lda, b, ldb);
+    bool small = false;
+    if constexpr (sizeof(T) <= 8) {
+        if (n <= (size_t)kTrsmSmallMax) {
+            k_trsm_small<T, false><<<(unsigned)std::min<size_t>(nrhs, 65535), 512, 0, st>>>((int)n, (int)nrhs, a, lda, b, ldb);
+            small = true;
+        }
+    }
+    if (!small) k_trsm_upper<T><<<(unsigned)std::min<size_t>(nrhs, 65535), 512, 0, st>>>((int)n, (int)nrhs, a, lda, b, ldb);
     RNPGPU_CHECK_LAUNCH();
     return kOk;
 }
@@ -40,7 +47,14 @@ template <class T> int trsm_upper(size_t n, size_t nrhs, const T *a, size_t lda,
 template <class T> int trsm_upper_ct(size_t n, size_t nrhs, const T *a, size_t lda, T *b, size_t ldb, cudaStream_t st) {
     if (n == 0 || nrhs == 0) return kOk;
     KScope ks("trsm", st);
-    k_trsm_upper_ct<T><<<(unsigned)std::min<size_t>(nrhs, 65535), 512, 0, st>>>((int)n, (int)nrhs, a, lda, b, ldb);
+    bool small = false;
+    if constexpr (sizeof(T) <= 8) {
+        if (n <= (size_t)kTrsmSmallMax) {
+            k_trsm_small<T, true><<<(unsigned)std::min<size_t>(nrhs, 65535), 512, 0, st>>>((int)n, (int)nrhs, a, lda, b, ldb);
+            small = true;
+        }
+    }
+    if (!small) k_trsm_upper_ct<T><<<(unsigned)std::min<size_t>(nrhs, 65535), 512, 0, st>>>((int)n, (int)nrhs, a, lda, b, ldb);
     RNPGPU_CHECK_LAUNCH();
     return kOk;
 }

@@ -97,6 +97,77 @@ template <class T> __global__ void __launch_bounds__(512) k_trsm_upper_ct(int n,
     }
 }
 
+// The same solves for n <= 512 and elements of at most 8 bytes, with the
+// latencies hidden: R y = b by back substitution (CT = false) or R^H y = b by
+// forward substitution (CT = true), one block per right-hand side, 32 rows a
+// step.  The right-hand side stays in shared memory; the next diagonal block
+// is loaded by warps 1..15 while warp 0 solves the current one (two buffers),
+// the reciprocals of the diagonal are formed by all lanes at once, and every
+// thread loads the 32 coefficients of its row's update before the barrier
+// that waits for the block solve.
+constexpr int kTrsmSmallMax = 512;
+template <class T, bool CT> __global__ void __launch_bounds__(512) k_trsm_small(int n, int nrhs, const T *R, size_t ldr, T *B, size_t ldb) {
+    __shared__ T sy[kTrsmSmallMax];
+    __shared__ T sD[2][32][33];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nblk = (n + 31) / 32;
+    auto first_row = [&](int s) { return 32 * (CT ? s : nblk - 1 - s); };
+    auto load_diag = [&](int s, int buf, int t0, int nt) {
+        const int i0 = first_row(s), nbk = min(32, n - i0);
+        for (int idx = t0; idx < 32 * 32; idx += nt) {
+            const int r = idx & 31, c = idx >> 5;
+            sD[buf][r][c] = (r < nbk && c < nbk && r <= c) ? R[(i0 + r) + (size_t)(i0 + c) * ldr] : T(0);
+        }
+    };
+    for (int col = blockIdx.x; col < nrhs; col += gridDim.x) {
+        T *y = B + (size_t)col * ldb;
+        for (int i = tid; i < n; i += blockDim.x) sy[i] = y[i];
+        load_diag(0, 0, tid, blockDim.x);
+        __syncthreads();
+        for (int s = 0; s < nblk; ++s) {
+            const int i0 = first_row(s), nbk = min(32, n - i0), buf = s & 1;
+            const int r = tid;
+            const bool upd = CT ? (r >= i0 + nbk && r < n) : (r < i0);
+            T coef[32];
+            if (upd) {
+#pragma unroll
+                for (int c = 0; c < 32; ++c) coef[c] = (c < nbk) ? (CT ? Tr<T>::conj(R[(i0 + c) + (size_t)r * ldr]) : R[r + (size_t)(i0 + c) * ldr]) : T(0);
+            }
+            if (warp == 0) {
+                T yv = (lane < nbk) ? sy[i0 + lane] : T(0);
+                const T d = (lane < nbk) ? (CT ? Tr<T>::conj(sD[buf][lane][lane]) : sD[buf][lane][lane]) : T(1);
+                const T dinv = T(1) / d;
+                if (!CT) {
+                    for (int i = nbk - 1; i >= 0; --i) {
+                        if (lane == i) yv = yv * dinv;
+                        const T xi = shfl(yv, i);
+                        if (lane < i) yv = yv - sD[buf][lane][i] * xi;
+                    }
+                } else {
+                    for (int i = 0; i < nbk; ++i) {
+                        if (lane == i) yv = yv * dinv;
+                        const T xi = shfl(yv, i);
+                        if (lane > i && lane < nbk) yv = yv - Tr<T>::conj(sD[buf][i][lane]) * xi;
+                    }
+                }
+                if (lane < nbk) sy[i0 + lane] = yv;
+            } else if (s + 1 < nblk) {
+                load_diag(s + 1, buf ^ 1, tid - 32, blockDim.x - 32);
+            }
+            __syncthreads();
+            if (upd) {
+                T a[4] = {T(0), T(0), T(0), T(0)};
+#pragma unroll
+                for (int c = 0; c < 32; ++c) a[c & 3] = fmac(coef[c], sy[i0 + c], a[c & 3]);
+                sy[r] = sy[r] - ((a[0] + a[1]) + (a[2] + a[3]));
+            }
+            __syncthreads();
+        }
+        for (int i = tid; i < n; i += blockDim.x) y[i] = sy[i];
+        __syncthreads();
+    }
+}
+
 template <class Tin, class Tout> __device__ __forceinline__ Tout convert_scalar(Tin v);
 template <> __device__ __forceinline__ float convert_scalar<double, float>(double v) { return (float)v; }
 template <> __device__ __forceinline__ double convert_scalar<float, double>(float v) { return (double)v; }

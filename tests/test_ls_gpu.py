@@ -59,16 +59,20 @@ def test_gels_against_oracle(oracle, p, mnr):
     assert rel(X.cpu().numpy(), Bo[:n]) <= tol
 
 
-@pytest.mark.parametrize("p", ["d", "z"])
-def test_trsm_upper(oracle, p):
-    n, nrhs = 300, 5
+@pytest.mark.parametrize("p", ["s", "d", "c", "z"])
+@pytest.mark.parametrize("n", [300, 17, 512, 600])
+def test_trsm_upper(oracle, p, n):
+    # n <= 512 with 4- and 8-byte elements: the latency-hiding kernel (ragged
+    # last block at 300 and 17); 600 and complex FP64: the general one
+    nrhs = 5
     # well conditioned: unit diagonal plus a small strictly upper part
-    R = np.asfortranarray(np.eye(n) + np.triu(mat(oracle, p, n, n, [5, 5, 5, 5]), 1) / n)
+    R = np.asfortranarray((np.eye(n) + np.triu(mat(oracle, p, n, n, [5, 5, 5, 5]), 1) / n).astype(NP[p]))
     B = mat(oracle, p, n, nrhs, [6, 6, 6, 7])
     dB = to_dev(B)
     gls.trsm_upper(to_dev(R), dB)
     torch.cuda.synchronize()
-    assert rel(R @ from_dev(dB), B) <= 1e-14
+    tol = 1e-14 if p in "dz" else 2e-6
+    assert rel(R.astype(np.complex128) @ from_dev(dB), B) <= tol
 
 
 def conditioned(m, n, nrhs, cond, cplx, seed=0):
@@ -158,14 +162,16 @@ def check_refined(A, b, X, info):
 
 
 @pytest.mark.parametrize("mn", [(4096, 100), (3000, 64), (1000, 33)])
-def test_mixed_fp32_factor_uses_cholesky_qr2_panels(mn):
+@pytest.mark.parametrize("forward", [False, True])
+def test_mixed_fp32_factor_uses_cholesky_qr2_panels(mn, forward):
     # the mixed solver's FP32 factor takes CholeskyQR2 panels on real data;
-    # widths that are not a multiple of 32 pad the last panel
+    # widths that are not a multiple of 32 pad the last panel (forward mode
+    # also runs the R^-T solves of the seminormal steps on ragged blocks)
     m, n = mn
     rng = np.random.default_rng(m + n)
     A = rng.standard_normal((m, n))
     b = A @ rng.standard_normal((n, 3)) + 1e-8 * rng.standard_normal((m, 3))
-    (X, info), kinds = panel_kinds(lambda: gls.gels_refine(to_dev(A), to_dev(b)))
+    (X, info), kinds = panel_kinds(lambda: gls.gels_refine(to_dev(A), to_dev(b), forward=forward))
     assert kinds == {"panel_cqr": (n + 31) // 32}, kinds
     check_refined(A, b, X, info)
 
