@@ -445,8 +445,6 @@ def other_configs(torch, dev, gq, lib, peak64):
 NCU_TRAFFIC = {
     "panel": (8.494080e6 + 0.003072e6, 2.0 * 65408 * 32 * 4),              # profiles/k_panel_f32_65536x32.md
     "panel_cqr": (8.482304e6 + 0.0, 2.0 * 65408 * 32 * 4),                 # profiles/k_panel_cqr_65536x32.md
-    "larfb_update": (100.570368e6 + 31.947008e6, 2.0 * 65408 * 352 * 4 + 65408 * 32 * 4.0),  # profiles/k_update_tc_65536.md
-    "larfb_w": (100.706048e6 + 3.111424e6, 65408 * 352 * 4.0 + 65408 * 32 * 4.0),             # profiles/k_w_tc_65536.md
     "residual_fp64": (277.589248e6 + 5.319424e6, 65536 * 512 * 8.0 + 2.0 * 65536 * 16 * 8),    # profiles/k_oz_residual_65536x512x16.md
     "normal_eq_fp64": (285.316352e6 + 3.713280e6, 65536 * 512 * 8.0 + 65536 * 16 * 8.0 + 65536 * 256.0),
 }
@@ -476,9 +474,9 @@ def kernel_rooflines(prof, tot_ms, top_name, peak64, steps):
         "panel_cqr": ("hbm", mean([2.0 * m * c * 4 for m, c in panels]),
                       "k_panel_cqr: FP32 CholeskyQR2 panel with Householder reconstruction, rows read and written once (2 m 32 x 4 B)"),
         "larfb_update": ("hbm", mean([2.0 * m * c * 4 + m * nb * 4.0 for m, c in updates]),
-                         "tc::k_update_tc: C -= V W^T, C read and written once, V read once"),
+                         "k_update_f32: C -= V (W T)^T on the FP32 pipe, C read and written once, V read once"),
         "larfb_w": ("hbm", mean([m * c * 4.0 + m * nb * 4.0 for m, c in updates]),
-                    "tc::k_w_tc: W = C^T V partials, C and V read once"),
+                    "k_w_f32: W = C^T V partials on the FP32 pipe, C and V read once"),
         "residual_fp64": ("hbm", M * N * 8.0 + 2.0 * M * NRHS * 8,
                           "k_xstack + oz::k_oz (residual): r = b - A x FP64-accurate from the packed digits of A (m n x 8 B read) on the FP16 tensor cores, b read, r written"),
         "normal_eq_fp64": ("hbm", M * N * 8.0 + M * NRHS * 8.0 + M * 256.0,

@@ -9,6 +9,7 @@
 #pragma once
 #include "qr_kernels.cuh"
 #include "panel_cqr.cuh"
+#include "update_f32.cuh"
 #include "multq_thin.cuh"
 #include "tc_gemm.cuh"
 #include <algorithm>
@@ -125,58 +126,68 @@ inline bool use_tensor_cores(const GemmArgs<float> &g) { return g.M >= 128 && g.
 template <class T> bool use_tensor_cores(const GemmArgs<T> &) { return false; }
 
 // The trailing update C -= V W^T (V unit-lower, K <= 32, N <= 512) goes to
-// the persistent kernel that keeps W's slices resident (one CTA per SM: the
-// request for more than half an SM's shared memory keeps a second CTA, and
-// its TMEM allocation, off the SM).
+// the FP32 rank-32 update kernel (update_f32.cuh).
 inline bool is_trailing_update(const GemmArgs<float> &g, int nsplit) {
     return nsplit == 1 && g.opA == kOpN && g.vunitA && (g.opB == kOpC || g.opB == kOpT) && !g.vunitB && g.beta_mode == kBetaOne && g.alpha == -1.0f && g.K <= 32 &&
-           g.N <= tc::kUpdMaxN && g.M >= 128;
+           g.N <= kUpdMaxN && g.M >= 128;
 }
-inline int launch_update_tc(const GemmArgs<float> &g, cudaStream_t st) {
-    const size_t smem = std::max<size_t>(tc::upd_smem_bytes(g.N), 116 * 1024);
+// two blocks of the update kernel per SM (96 KB of shared memory each: the
+// largest carveout), as many blocks as SMs hold: each walks its row tiles
+inline int launch_update_f32(const GemmArgs<float> &g, cudaStream_t st) {
     static std::once_flag once;
     static cudaError_t attr = cudaSuccess;
-    std::call_once(once, []() { attr = cudaFuncSetAttribute((const void *)tc::k_update_tc<tc::kUpdChunk>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); });
+    std::call_once(once, []() {
+        const void *ks[2] = {(const void *)k_update_f32<true>, (const void *)k_update_f32<false>};
+        for (const void *k : ks) {
+            if (attr == cudaSuccess) attr = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kUfSmem);
+            if (attr == cudaSuccess) attr = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
+        }
+    });
     RNPGPU_CHECK(attr);
-    int *err = device_status_ptr();
-    if (err == nullptr) return kErrCuda;
-    tc::UpdArgs u;
+    UpdArgs u;
     u.V = g.A; u.ldv = g.lda; u.W = g.B; u.ldw = g.ldb; u.C = g.D; u.ldc = g.ldd;
     u.M = g.M; u.N = g.N; u.K = g.K;
-    const int ntiles = (g.M + tc::kBM - 1) / tc::kBM;
-    const int grid = std::max(1, std::min(ntiles, device_facts().sm_count));
-    tc::k_update_tc<tc::kUpdChunk><<<grid, tc::kThreads, smem, st>>>(u, err);
+    const int ntiles = (g.M + kUfRows - 1) / kUfRows, gy = (g.N + kUfCols - 1) / kUfCols;
+    const int gx = std::max(1, std::min(ntiles, device_facts().sm_count * 2 / gy));
+    const bool vec = ((uintptr_t)g.D % 16 == 0) && (g.ldd % 4 == 0);
+    if (vec) k_update_f32<true><<<dim3(gx, gy), kUfThreads, kUfSmem, st>>>(u);
+    else k_update_f32<false><<<dim3(gx, gy), kUfThreads, kUfSmem, st>>>(u);
     RNPGPU_CHECK_LAUNCH();
     return kOk;
 }
 
 // W partials P_g = C^T V (g < nsplit, leading dimension N, stride N*K) on the
-// tensor cores, one partial per persistent block; nsplit <= maxsplit.
-inline bool w_tc_ok(int M, int N, int K) { return M >= 1024 && N <= tc::kUpdMaxN && K <= 32; }
+// FP32 pipe (update_f32.cuh), one partial per split of the rows; nsplit <=
+// maxsplit.
+inline bool w_tc_ok(int M, int N, int K) { return M >= 1024 && N <= kUpdMaxN && K <= 32; }
 inline int launch_w_tc(const float *C, size_t ldc, const float *V, size_t ldv, float *P, int M, int N, int K, int maxsplit, int &nsplit, cudaStream_t st) {
     static std::once_flag once;
     static cudaError_t attr = cudaSuccess;
     std::call_once(once, []() {
-        attr = cudaFuncSetAttribute((const void *)tc::k_w_tc<tc::kWCols, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::kWSmem);
-        if (attr == cudaSuccess) attr = cudaFuncSetAttribute((const void *)tc::k_w_tc<tc::kWCols, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::kWSmem);
+        const void *ks[2] = {(const void *)k_w_f32<true>, (const void *)k_w_f32<false>};
+        for (const void *k : ks) {
+            if (attr == cudaSuccess) attr = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kWfSmem);
+            if (attr == cudaSuccess) attr = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
+        }
     });
     RNPGPU_CHECK(attr);
-    int *err = device_status_ptr();
-    if (err == nullptr) return kErrCuda;
-    const int nkb = (M + tc::kWRows - 1) / tc::kWRows;
+    const int nkb = (M + 127) / 128;
     nsplit = std::max(1, std::min(std::min(nkb, maxsplit), device_facts().sm_count));
-    tc::WArgs w;
-    w.C = C; w.ldc = ldc; w.V = V; w.ldv = ldv; w.P = P; w.M = M; w.N = N; w.K = K;
+    UpdArgs u;
+    u.V = V; u.ldv = ldv; u.W = nullptr; u.ldw = 0; u.C = const_cast<float *>(C); u.ldc = ldc; u.M = M; u.N = N; u.K = K;
+    const int rps = ((M + nsplit - 1) / nsplit + 3) / 4 * 4;  // a multiple of 4: aligned row quads
+    nsplit = (M + rps - 1) / rps;
+    const dim3 grid(nsplit, (N + kWfCols - 1) / kWfCols);
     const bool vec = ((uintptr_t)C % 16 == 0) && (ldc % 4 == 0);
-    if (vec) tc::k_w_tc<tc::kWCols, true><<<nsplit, tc::kWThreads, tc::kWSmem, st>>>(w, err);
-    else tc::k_w_tc<tc::kWCols, false><<<nsplit, tc::kWThreads, tc::kWSmem, st>>>(w, err);
+    if (vec) k_w_f32<true><<<grid, kUfThreads, kWfSmem, st>>>(u, P, rps);
+    else k_w_f32<false><<<grid, kUfThreads, kWfSmem, st>>>(u, P, rps);
     RNPGPU_CHECK_LAUNCH();
     return kOk;
 }
 template <class T> int launch_w_tc(const T *, size_t, const T *, size_t, T *, int, int, int, int, int &, cudaStream_t) { return kErrDevice; }
 
 inline int launch_gemm_tc(const GemmArgs<float> &g, int nsplit, cudaStream_t st) {
-    if (is_trailing_update(g, nsplit)) return launch_update_tc(g, st);
+    if (is_trailing_update(g, nsplit)) return launch_update_f32(g, st);
     if (g.N <= 32) return launch_gemm_tc_bn<32>(g, nsplit, st);
     return launch_gemm_tc_bn<64>(g, nsplit, st);
 }

@@ -330,376 +330,5 @@ template <int BN> __global__ void __launch_bounds__(kThreads) k_gemm_tc(GemmArgs
 }
 
 
-// ---------------------------------------------------------------------------
-// Persistent rank-K update (K <= 32), the FP32 trailing update of the
-// blocked factorization:  C(M x N) -= V(M x K) W(N x K)^T, V unit-lower
-// trapezoidal in stored form (vunit), N <= kUpdMaxN.
-// W's three BF16 slices are split once per CTA and stay in shared memory;
-// the CTA then walks 128-row tiles (t = blockIdx.x, += gridDim.x): it splits
-// the tile's V into its slices, and streams the tile's C in 64-column chunks
-// through two TMEM accumulator sets (the MMAs of chunk c+1 run while the
-// epilogue of chunk c reads C, subtracts and writes it back).
-// ---------------------------------------------------------------------------
-constexpr int kUpdChunk = 64;
-constexpr int kUpdMaxN = 512;
-
-struct UpdArgs {
-    const float *V;  // M x K (ldv), unit-lower in stored form
-    size_t ldv;
-    const float *W;  // N x K (ldw)
-    size_t ldw;
-    float *C;        // M x N (ldc)
-    size_t ldc;
-    int M, N, K;
-};
-
-__host__ __device__ constexpr int upd_npad(int N) { return (N + kUpdChunk - 1) / kUpdChunk * kUpdChunk; }
-__host__ __device__ constexpr size_t upd_smem_bytes(int N) {
-    return (size_t)3 * kBM * kBK * 2 + (size_t)3 * upd_npad(N) * kBK * 2 + 64;
-}
-
-template <int CH> __global__ void __launch_bounds__(kThreads) k_update_tc(UpdArgs g, int *err) {
-    static_assert(CH == kUpdChunk, "chunk width");
-    extern __shared__ __align__(1024) unsigned char smem[];
-    const int npad = upd_npad(g.N);
-    constexpr int kSliceA = kBM * kBK * 2;
-    const int sliceB = npad * kBK * 2;
-    unsigned char *sA = smem;                    // 3 slices of the V tile
-    unsigned char *sB = smem + 3 * kSliceA;      // 3 slices of W (all N rows)
-    uint64_t *bars = reinterpret_cast<uint64_t *>(sB + 3 * sliceB);
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2);
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    constexpr uint32_t kCols = 512;              // 2 sets x 3 classes x 64 columns
-    if (tid == 0) {
-        mbar_init(&bars[0], 1);
-        mbar_init(&bars[1], 1);
-        fence_barrier_init();
-    }
-    if (warp == 0) {
-        tmem_alloc(tmem_slot, kCols);
-        tmem_relinquish();
-    }
-    // W -> B slices: element (n, k) of the N x K operand is W(n, k); a thread
-    // takes 8 consecutive k of one row (consecutive threads, consecutive
-    // rows: the 16-byte stores of a warp fall into distinct banks)
-    for (int idx = tid; idx < npad * (kBK / 8); idx += kThreads) {
-        const int n = idx % npad, k0 = (idx / npad) * 8;
-        float x[8];
-#pragma unroll
-        for (int e = 0; e < 8; ++e) x[e] = (n < g.N && k0 + e < g.K) ? g.W[n + (size_t)(k0 + e) * g.ldw] : 0.f;
-        put8_slices(sB, sliceB, tile_off(n, k0), x);
-    }
-    tc_fence_before();
-    __syncthreads();
-    tc_fence_after();
-    const uint32_t tmem_base = *tmem_slot;
-    constexpr uint32_t idesc = idesc_bf16(kBM, kUpdChunk);
-    const int nchunks = npad / kUpdChunk;
-    const int ntiles = (g.M + kBM - 1) / kBM;
-    uint32_t phase[2] = {0u, 0u};
-    bool ok = true;
-    // MMAs of chunk c into accumulator set s: called by all of warp 0 (the
-    // descriptors are warp-uniform values), issued by one elected lane
-    auto issue = [&](int c, int s) {
-        tc_fence_after();
-        const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB) + (uint32_t)(c * kUpdChunk / 8) * (kBK / 8) * 128;
-        const uint32_t d0 = tmem_base + (uint32_t)(s * 3 * kUpdChunk);
-        const int pa[6] = {0, 0, 1, 0, 1, 2};
-        const int pb[6] = {0, 1, 0, 2, 1, 0};
-        const int pc[6] = {0, 1, 1, 2, 2, 2};
-        const bool first_in_class[6] = {true, true, false, true, false, false};
-        if (elect_one()) {
-#pragma unroll
-            for (int kk = 0; kk < kBK / 16; ++kk) {
-#pragma unroll
-                for (int q = 0; q < 6; ++q) {
-                    const uint64_t ad = smem_desc(a0 + pa[q] * kSliceA + kk * 256, 128, (kBK / 8) * 128);
-                    const uint64_t bd = smem_desc(b0 + pb[q] * sliceB + kk * 256, 128, (kBK / 8) * 128);
-                    umma_bf16(d0 + (uint32_t)(pc[q] * kUpdChunk), ad, bd, idesc, (kk == 0 && first_in_class[q]) ? 0u : 1u);
-                }
-            }
-            umma_commit(&bars[s]);
-        }
-        __syncwarp();
-    };
-    for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
-        const int m0 = t * kBM;
-        // V tile -> A slices (rows m0.., unit-lower in stored form), 8
-        // consecutive k of one row per thread as for W
-        for (int idx = tid; idx < kBM * (kBK / 8); idx += kThreads) {
-            const int mi = idx % kBM, k0 = (idx / kBM) * 8, gm = m0 + mi;
-            float x[8];
-#pragma unroll
-            for (int e = 0; e < 8; ++e) {
-                const int k = k0 + e;
-                float v = 0.f;
-                if (gm < g.M && k < g.K) v = (gm > k) ? g.V[gm + (size_t)k * g.ldv] : (gm == k ? 1.f : 0.f);
-                x[e] = v;
-            }
-            put8_slices(sA, kSliceA, tile_off(mi, k0), x);
-        }
-        fence_proxy_async();
-        __syncthreads();
-        if (warp == 0) issue(0, 0);
-        // epilogue mapping: warp w reads TMEM lanes 32*(w%4).. (tile rows) and
-        // the column half w/4 of each chunk; its C values for the next chunk
-        // are loaded while the current chunk is finished
-        const int q = warp & 3, half = warp >> 2;
-        const int row = m0 + q * 32 + lane;
-        constexpr int kHalf = kUpdChunk / 2;
-        auto load_c = [&](int c, float (&buf)[kHalf]) {
-            const int col0 = c * kUpdChunk + half * kHalf;
-            const float *cp = g.C + row + (size_t)col0 * g.ldc;
-#pragma unroll
-            for (int i = 0; i < kHalf; ++i) buf[i] = (row < g.M && col0 + i < g.N) ? cp[(size_t)i * g.ldc] : 0.f;
-        };
-        float cur[kHalf], nxt[kHalf];
-        load_c(0, cur);
-        for (int c = 0; c < nchunks; ++c) {
-            const int s = c & 1;
-            if (warp == 0 && c + 1 < nchunks) issue(c + 1, s ^ 1);
-            if (c + 1 < nchunks) load_c(c + 1, nxt);
-            if (!mbar_wait(&bars[s], phase[s])) ok = false;
-            phase[s] ^= 1u;
-            tc_fence_after();
-            if (!__syncthreads_and(ok ? 1 : 0)) {
-                ok = false;
-                break;
-            }
-            const uint32_t lane_base = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(s * 3 * kUpdChunk);
-            const int col0 = c * kUpdChunk + half * kHalf;
-            float *cp = g.C + row + (size_t)col0 * g.ldc;
-#pragma unroll
-            for (int c0 = 0; c0 < kHalf; c0 += 16) {
-                float big[16], mid[16], small[16];
-                tmem_ld16(lane_base + (uint32_t)(half * kHalf + c0), big);
-                tmem_ld16(lane_base + (uint32_t)(kUpdChunk + half * kHalf + c0), mid);
-                tmem_ld16(lane_base + (uint32_t)(2 * kUpdChunk + half * kHalf + c0), small);
-                if (row < g.M) {
-#pragma unroll
-                    for (int i = 0; i < 16; ++i)
-                        if (col0 + c0 + i < g.N) cp[(size_t)(c0 + i) * g.ldc] = cur[c0 + i] - (big[i] + fmaf(small[i], 0x1p-16f, mid[i] * 0x1p-8f));
-                }
-            }
-#pragma unroll
-            for (int i = 0; i < kHalf; ++i) cur[i] = nxt[i];
-            tc_fence_before();
-            __syncthreads();
-        }
-    }
-    if (!ok && tid == 0) atomicExch(err, (int)kStatusBarrierTimeout);
-    tc_fence_before();
-    __syncthreads();
-    if (warp == 0) tmem_dealloc(tmem_base, kCols);
-}
-
-
-// ---------------------------------------------------------------------------
-// Persistent reduction W_g = C^T V over row blocks (the first half of the
-// trailing update, W = C^H V for FP32 data), N <= kUpdMaxN, K <= 32.
-// The MMA's M dimension runs over C's columns (128 per chunk), N over V's
-// columns, K over rows: both operands are K-major straight from column-major
-// storage.  Block g takes 128-row blocks kb = g, g + gridDim.x, ...; for each
-// it splits V's rows once, then streams the block's C in 128-column chunks
-// through two shared-memory stages (the next chunk's loads are in flight
-// while the current chunk's MMAs run) into per-chunk TMEM accumulators that
-// persist across the block's row blocks.  The epilogue writes block g's
-// partial W (N x K, leading dimension N) at P + g * N * K; the partials are
-// summed afterwards in a fixed order.
-// ---------------------------------------------------------------------------
-constexpr int kWRows = 128;   // K per row block
-constexpr int kWCols = 128;   // C columns per chunk (MMA M)
-constexpr int kWThreads = 256;
-
-template <int KB> __device__ __forceinline__ uint32_t tile_off_k(int row, int k) {
-    return (uint32_t)(((row >> 3) * (KB / 8) + (k >> 3)) * 128 + (row & 7) * 16 + (k & 7) * 2);
-}
-
-struct WArgs {
-    const float *C;  // M x N (ldc)
-    size_t ldc;
-    const float *V;  // M x K (ldv), unit-lower in stored form
-    size_t ldv;
-    float *P;        // [gridDim.x][N x K], leading dimension N
-    int M, N, K;
-};
-
-constexpr int kWSliceA = kWCols * kWRows * 2;  // 32 KB: one BF16 slice of a C chunk
-constexpr int kWSliceB = 32 * kWRows * 2;      // 8 KB: one BF16 slice of V's rows
-constexpr size_t kWSmem = (size_t)2 * 3 * kWSliceA + 3 * kWSliceB + 64;
-
-// VEC: C's base is 16-byte aligned and ldc a multiple of 4, so a thread's
-// 8 rows come in two 16-byte loads (8 scalar loads of one column would each
-// touch another cache line of the chunk, and the L1 left beside this shared
-// memory cannot hold them between the loads)
-template <int CH, bool VEC> __global__ void __launch_bounds__(kWThreads) k_w_tc(WArgs g, int *err) {
-    static_assert(CH == kWCols, "chunk width");
-    extern __shared__ __align__(1024) unsigned char smem[];
-    unsigned char *sA = smem;                         // 2 stages x 3 slices
-    unsigned char *sB = smem + 2 * 3 * kWSliceA;      // 3 slices of V's rows
-    uint64_t *bars = reinterpret_cast<uint64_t *>(sB + 3 * kWSliceB);
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2);
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    constexpr uint32_t kCols = 512;                   // up to 4 chunks x 3 classes x 32
-    if (tid == 0) {
-        mbar_init(&bars[0], 1);
-        mbar_init(&bars[1], 1);
-        fence_barrier_init();
-    }
-    if (warp == 0) {
-        tmem_alloc(tmem_slot, kCols);
-        tmem_relinquish();
-    }
-    tc_fence_before();
-    __syncthreads();
-    tc_fence_after();
-    const uint32_t tmem_base = *tmem_slot;
-    const int nkb = (g.M + kWRows - 1) / kWRows;
-    const int nch = (g.N + kWCols - 1) / kWCols;
-    const int my_kb = ((int)blockIdx.x < nkb) ? (nkb - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
-    const int nsteps = my_kb * nch;
-    constexpr uint32_t idesc = idesc_bf16(kWCols, 32);
-    // a thread moves 8 consecutive rows of one column at a time: consecutive
-    // threads take consecutive columns, so the 16-byte slice stores of a
-    // warp fall into distinct banks (core-matrix rows are 16 bytes apart)
-    constexpr int LU = kWCols * (kWRows / 8) / kWThreads;  // 8-row pieces per thread per step
-    float cr[LU][8];
-    auto fetch = [&](int t) {
-        const int kb = blockIdx.x + (t / nch) * gridDim.x, cc = t % nch;
-#pragma unroll
-        for (int u = 0; u < LU; ++u) {
-            const int idx = tid + u * kWThreads;
-            const int c = idx % kWCols, r0 = (idx / kWCols) * 8;
-            const int gr = kb * kWRows + r0, gc = cc * kWCols + c;
-            const float *src = g.C + gr + (size_t)gc * g.ldc;
-            if (VEC && gc < g.N && gr + 8 <= g.M) {
-                const float4 lo = *reinterpret_cast<const float4 *>(src), hi = *reinterpret_cast<const float4 *>(src + 4);
-                cr[u][0] = lo.x; cr[u][1] = lo.y; cr[u][2] = lo.z; cr[u][3] = lo.w;
-                cr[u][4] = hi.x; cr[u][5] = hi.y; cr[u][6] = hi.z; cr[u][7] = hi.w;
-            } else {
-#pragma unroll
-                for (int e = 0; e < 8; ++e) cr[u][e] = (gc < g.N && gr + e < g.M) ? src[e] : 0.f;
-            }
-        }
-    };
-    auto put8 = [&](unsigned char *slice0, size_t slice_bytes, uint32_t o, const float (&x)[8]) {
-        __align__(16) __nv_bfloat16 h[3][8];
-#pragma unroll
-        for (int e = 0; e < 8; ++e) split3(x[e], h[0][e], h[1][e], h[2][e]);
-#pragma unroll
-        for (int q = 0; q < 3; ++q) *reinterpret_cast<uint4 *>(slice0 + q * slice_bytes + o) = *reinterpret_cast<const uint4 *>(h[q]);
-    };
-    auto stash = [&](int st) {
-        unsigned char *a = sA + st * 3 * kWSliceA;
-#pragma unroll
-        for (int u = 0; u < LU; ++u) {
-            const int idx = tid + u * kWThreads;
-            const int c = idx % kWCols, r0 = (idx / kWCols) * 8;
-            put8(a, kWSliceA, tile_off_k<kWRows>(c, r0), cr[u]);
-        }
-    };
-    auto split_v = [&](int kb) {
-        for (int idx = tid; idx < 32 * (kWRows / 8); idx += kWThreads) {
-            const int n = idx % 32, r0 = (idx / 32) * 8;
-            float x[8];
-#pragma unroll
-            for (int e = 0; e < 8; ++e) {
-                const int gr = kb * kWRows + r0 + e;
-                float v = 0.f;
-                if (gr < g.M && n < g.K) v = (gr > n) ? g.V[gr + (size_t)n * g.ldv] : (gr == n ? 1.f : 0.f);
-                x[e] = v;
-            }
-            put8(sB, kWSliceB, tile_off_k<kWRows>(n, r0), x);
-        }
-    };
-    uint32_t phase[2] = {0u, 0u};
-    bool pending[2] = {false, false};
-    bool ok = true;
-    auto wait_stage = [&](int st) {
-        if (pending[st]) {
-            if (!mbar_wait(&bars[st], phase[st])) ok = false;
-            phase[st] ^= 1u;
-            pending[st] = false;
-        }
-    };
-    if (nsteps > 0) fetch(0);
-    for (int t = 0; t < nsteps; ++t) {
-        const int st = t & 1, cc = t % nch, kbl = t / nch;
-        if (cc == 0) {
-            // V's rows of the next row block: every MMA still reading them is done
-            wait_stage(0);
-            wait_stage(1);
-            split_v(blockIdx.x + kbl * gridDim.x);
-        }
-        wait_stage(st);
-        if (!__syncthreads_and(ok ? 1 : 0)) {
-            ok = false;
-            break;
-        }
-        stash(st);
-        fence_proxy_async();
-        __syncthreads();
-        if (t + 1 < nsteps) fetch(t + 1);
-        if (warp == 0) {  // warp-uniform descriptors, one elected issuing lane
-            tc_fence_after();
-            const uint32_t a0 = smem_u32(sA + st * 3 * kWSliceA), b0 = smem_u32(sB);
-            const uint32_t d0 = tmem_base + (uint32_t)(cc * 96);
-            const int pa[6] = {0, 0, 1, 0, 1, 2};
-            const int pb[6] = {0, 1, 0, 2, 1, 0};
-            const int pc[6] = {0, 1, 1, 2, 2, 2};
-            const bool first_in_class[6] = {true, true, false, true, false, false};
-            if (elect_one()) {
-#pragma unroll
-                for (int kk = 0; kk < kWRows / 16; ++kk) {
-#pragma unroll
-                    for (int q = 0; q < 6; ++q) {
-                        const uint64_t ad = smem_desc(a0 + pa[q] * kWSliceA + kk * 256, 128, (kWRows / 8) * 128);
-                        const uint64_t bd = smem_desc(b0 + pb[q] * kWSliceB + kk * 256, 128, (kWRows / 8) * 128);
-                        const bool fresh = (kbl == 0 && kk == 0 && first_in_class[q]);
-                        umma_bf16(d0 + (uint32_t)(pc[q] * 32), ad, bd, idesc, fresh ? 0u : 1u);
-                    }
-                }
-                umma_commit(&bars[st]);
-            }
-            __syncwarp();
-        }
-        pending[st] = true;
-    }
-    wait_stage(0);
-    wait_stage(1);
-    tc_fence_after();
-    ok = __syncthreads_and(ok ? 1 : 0) != 0;
-    if (!ok && tid == 0) atomicExch(err, (int)kStatusBarrierTimeout);
-    // epilogue: warp w reads TMEM lanes 32*(w%4).. (C columns), V columns 16*(w/4)..
-    if (ok) {
-        float *P = g.P + (size_t)blockIdx.x * g.N * g.K;
-        const int q = warp & 3, half = warp >> 2;
-        for (int cc = 0; cc < nch; ++cc) {
-            const int n = cc * kWCols + q * 32 + lane;
-            float v[16];
-            if (nsteps > 0) {
-                const uint32_t base = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(cc * 96 + half * 16);
-                float big[16], mid[16], small[16];
-                tmem_ld16(base, big);
-                tmem_ld16(base + 32, mid);
-                tmem_ld16(base + 64, small);
-#pragma unroll
-                for (int i = 0; i < 16; ++i) v[i] = big[i] + fmaf(small[i], 0x1p-16f, mid[i] * 0x1p-8f);
-            } else {
-#pragma unroll
-                for (int i = 0; i < 16; ++i) v[i] = 0.f;
-            }
-            if (n < g.N) {
-#pragma unroll
-                for (int i = 0; i < 16; ++i)
-                    if (half * 16 + i < g.K) P[n + (size_t)(half * 16 + i) * g.N] = v[i];
-            }
-        }
-    }
-    tc_fence_before();
-    __syncthreads();
-    if (warp == 0) tmem_dealloc(tmem_base, kCols);
-}
-
 } // namespace tc
 } // namespace rnpgpu
