@@ -194,6 +194,9 @@ def test_mixed_fp32_factor_falls_back_to_householder_panels():
     (X, info), kinds = panel_kinds(lambda: gls.gels_refine(to_dev(A), to_dev(b)))
     assert kinds.get("panel") == 3 and kinds.get("panel_cqr", 0) >= 2, kinds
     be = ls_backward_error(A, b, X.cpu().numpy())
-    assert info["backward_error"] <= 1e-10 and be <= 1e-10, (info, be)
+    # far below FP32 accuracy (a stale or damaged factor leaves ~1e-3); at
+    # this condition number ten steps end between 1e-12 and 1e-9 depending on
+    # the rounding of the FP32 factor
+    assert info["backward_error"] <= 1e-9 and be <= 1e-9, (info, be)
     if info["converged"] == 1:
         assert be <= 10 * n * np.finfo(np.float64).eps
