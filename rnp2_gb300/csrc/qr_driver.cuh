@@ -232,16 +232,13 @@ inline int choose_splits(int K, int tiles, int smax) {
     return std::max(s, 1);
 }
 
-// W = (sum of nsplit partials) * op(T); many partials are first summed by the
-// parallel reduction, then W is multiplied by op(T) in place
+// W = (sum of nsplit partials) * op(T) in one launch (many partials: four
+// split lanes per entry)
 template <class T> int sum_times_t(const T *P, size_t ldp, size_t pstride, int nsplit, int rows, int k, const T *Tm, int ldt, int opT, T *W, size_t ldw, cudaStream_t st) {
     if (nsplit > 8) {
-        k_reduce_splits<T><<<dim3((unsigned)((rows + 63) / 64), (unsigned)k), 256, 0, st>>>(P, ldp, pstride, nsplit, rows, W, ldw);
+        k_reduce_times_t<T><<<(rows + 1) / 2, 256, 0, st>>>(P, ldp, pstride, nsplit, rows, k, Tm, ldt, opT, W, ldw);
         RNPGPU_CHECK_LAUNCH();
-        P = W;
-        ldp = ldw;
-        pstride = 0;
-        nsplit = 1;
+        return kOk;
     }
     k_sum_times_t<T><<<(rows + 7) / 8, 256, 0, st>>>(P, ldp, pstride, nsplit, rows, k, Tm, ldt, opT, W, ldw);
     RNPGPU_CHECK_LAUNCH();
