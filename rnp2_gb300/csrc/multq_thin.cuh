@@ -46,11 +46,11 @@ template <class T> struct ThinArgs {
 
 // shared memory of the thin kernel: W, Y, T, VBUF staging buffers for the
 // block's rows of V_b (column-major, leading dimension rows) and, when CSMEM,
-// the block's rows of C (row-major, leading dimension n + 1)
+// the block's rows of C (column-major, leading dimension rows + 4)
 template <class T> inline size_t thin_smem_bytes(int rows, int n, bool csmem, int vbuf) {
     size_t e = (size_t)2 * kPanelMaxCols * n + (size_t)kPanelMaxCols * (kPanelMaxCols + 1);
     e += (size_t)vbuf * kPanelMaxCols * rows;
-    if (csmem) e += (size_t)rows * (n + 1);
+    if (csmem) e += (size_t)(rows + 4) * n;
     return e * sizeof(T);
 }
 
@@ -76,20 +76,20 @@ template <class T> __device__ __forceinline__ void stage_elem(T *dst, const T *s
 // its use, 2 = V_{b+1} staged during block b's barriers (double buffer)
 template <class T, bool CSMEM, int VBUF> __global__ void __launch_bounds__(kThinThreads) k_multq_thin(ThinArgs<T> p) {
     extern __shared__ __align__(16) unsigned char s_dyn[];
-    const int n = p.n, ldsc = n + 1, R = p.rows_per_cta;
+    const int n = p.n, R = p.rows_per_cta, ldcs = R + 4;
     T *sW = reinterpret_cast<T *>(s_dyn);                   // 32 x n (ld 32): V^H C
     T *sY = sW + kPanelMaxCols * n;                         // 32 x n (ld 32): op(T) V^H C
     T *sT = sY + kPanelMaxCols * n;                         // 32 x 33
     T *sV0 = sT + kPanelMaxCols * (kPanelMaxCols + 1);      // 32 x R (ld R)
     T *sV1 = sV0 + (VBUF >= 1 ? (size_t)kPanelMaxCols * R : 0);
-    T *sC = sV0 + (size_t)VBUF * kPanelMaxCols * R;         // R x (n+1), row-major
+    T *sC = sV0 + (size_t)VBUF * kPanelMaxCols * R;         // R x n, column-major (ldcs)
     const int G = gridDim.x, g = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int r0 = g * R;
     const int r1 = min(p.m, r0 + R);
     GridBarrier bar{p.counter, p.err, (unsigned)G, 0u};
     bar.status = p.status;
     auto cref = [&](int r, int c) -> T & {
-        if (CSMEM) return sC[(size_t)(r - r0) * ldsc + c];
+        if (CSMEM) return sC[(size_t)c * ldcs + (r - r0)];
         return p.C[r + (size_t)c * p.ldc];
     };
     auto block_of = [&](int s) { return p.forward ? s : p.nblk - 1 - s; };
@@ -97,6 +97,32 @@ template <class T, bool CSMEM, int VBUF> __global__ void __launch_bounds__(kThin
     // the block and columns beyond its width as zeros, the diagonal as ones
     auto stage_v = [&](int bb, T *buf) {
         const int i = bb * kPanelMaxCols, ib = min(kPanelMaxCols, p.k - i), rs = max(r0, i);
+        if constexpr (std::is_same<T, float>::value) {
+            // FP32: 16-byte copies of row quads strictly below the diagonal
+            // (block rows start at multiples of 4: rows_per_cta is one), the
+            // quads that meet the diagonal or the end element by element
+            if (((uintptr_t)p.A % 16 == 0) && (p.lda % 4 == 0) && (R % 4 == 0) && (r0 % 4 == 0)) {
+                const int q0 = (rs - r0) / 4, nq = (r1 - r0 + 3) / 4;
+                for (int idx = tid; idx < kPanelMaxCols * (nq - q0); idx += kThinThreads) {
+                    const int l = idx / (nq - q0), r = r0 + 4 * (q0 + idx % (nq - q0));
+                    const T *src = p.A + (size_t)(i + l) * p.lda;
+                    T *dst = buf + (size_t)l * R + (r - r0);
+                    if (l < ib && r > i + l && r + 4 <= r1) {
+                        cp_async_cg16(dst, src + r);
+                    } else {
+#pragma unroll
+                        for (int e = 0; e < 4; ++e) {
+                            const int rr = r + e;
+                            if (rr >= r1 || rr < rs || l >= ib || rr < i + l) dst[e] = T(0);
+                            else if (rr == i + l) dst[e] = T(1);
+                            else dst[e] = src[rr];
+                        }
+                    }
+                }
+                cp_async_commit();
+                return;
+            }
+        }
         // columns outer, rows inner: no index division per element
         for (int l = 0; l < kPanelMaxCols; ++l) {
             const T *src = p.A + (size_t)(i + l) * p.lda;
@@ -116,10 +142,14 @@ template <class T, bool CSMEM, int VBUF> __global__ void __launch_bounds__(kThin
     };
     if (CSMEM) {
         for (int c = 0; c < n; ++c)
-            for (int r = r0 + tid; r < r1; r += kThinThreads) sC[(size_t)(r - r0) * ldsc + c] = p.C[r + (size_t)c * p.ldc];
+            for (int r = r0 + tid; r < r0 + R; r += kThinThreads) sC[(size_t)c * ldcs + (r - r0)] = (r < r1) ? p.C[r + (size_t)c * p.ldc] : T(0);
     }
     if (VBUF > 0 && p.nblk > 0) stage_v(block_of(0), sV0);
 
+    // FP32 with C and V in shared memory: 4-row quads as float4 (rows past the
+    // block's end are zeros in both), 4 x 4 register tiles
+    constexpr bool kQuads = std::is_same<T, float>::value && CSMEM && VBUF > 0;
+    const bool quads = kQuads && (n % 4 == 0) && (R % 4 == 0) && (r0 % 4 == 0);
     const int nw = kPanelMaxCols * n;          // entries of V^H C
     const int ctiles = (n + 3) / 4;
     const int ntiles = (kPanelMaxCols / 4) * ctiles;
@@ -134,7 +164,50 @@ template <class T, bool CSMEM, int VBUF> __global__ void __launch_bounds__(kThin
         __syncthreads();
         // 1. partial V^H C over own rows; tile t = (reflectors 4*(t % 8) .., columns 4*(t / 8) ..)
         T *mine = p.part + (size_t)g * nw;
-        for (int t = warp; t < ntiles; t += kThinWarps) {
+        if constexpr (kQuads) {
+            if (quads) {
+                // tile t per half warp, its 16 lanes over interleaved row quads
+                for (int t = 2 * warp + (lane >> 4); t < ntiles; t += 2 * kThinWarps) {
+                    const int l0 = 4 * (t % (kPanelMaxCols / 4)), c0 = 4 * (t / (kPanelMaxCols / 4));
+                    float acc[16];
+#pragma unroll
+                    for (int e = 0; e < 16; ++e) acc[e] = 0.f;
+                    if (l0 < ib) {
+                        for (int r4 = rs + 4 * (lane & 15); r4 < r1; r4 += 64) {
+                            float4 v[4], c[4];
+#pragma unroll
+                            for (int a = 0; a < 4; ++a) v[a] = *reinterpret_cast<const float4 *>(sV + (size_t)(l0 + a) * R + (r4 - r0));
+#pragma unroll
+                            for (int q = 0; q < 4; ++q) c[q] = *reinterpret_cast<const float4 *>(sC + (size_t)(c0 + q) * ldcs + (r4 - r0));
+#pragma unroll
+                            for (int a = 0; a < 4; ++a)
+#pragma unroll
+                                for (int q = 0; q < 4; ++q) {
+                                    float x = acc[4 * a + q];
+                                    x = fmaf(v[a].x, c[q].x, x);
+                                    x = fmaf(v[a].y, c[q].y, x);
+                                    x = fmaf(v[a].z, c[q].z, x);
+                                    acc[4 * a + q] = fmaf(v[a].w, c[q].w, x);
+                                }
+                        }
+                    }
+                    // sum over the half warp's 16 lanes: lane (& 15) ends with entry (lane & 15)
+#pragma unroll
+                    for (int lvl = 0; lvl < 4; ++lvl) {
+                        const int o = 8 >> lvl, m = 8 >> lvl;
+                        const bool up = (lane & o) != 0;
+#pragma unroll
+                        for (int e = 0; e < m; ++e) {
+                            const float send = up ? acc[e] : acc[e + m], keep = up ? acc[e + m] : acc[e];
+                            acc[e] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+                        }
+                    }
+                    const int e = lane & 15;
+                    if (c0 + (e & 3) < n) mine[(l0 + (e >> 2)) + (size_t)(c0 + (e & 3)) * kPanelMaxCols] = acc[0];
+                }
+            }
+        }
+        for (int t = warp; t < ntiles && !quads; t += kThinWarps) {
             const int l0 = 4 * (t % (kPanelMaxCols / 4)), c0 = 4 * (t / (kPanelMaxCols / 4));
             T acc[4][4];
 #pragma unroll
@@ -154,19 +227,16 @@ template <class T, bool CSMEM, int VBUF> __global__ void __launch_bounds__(kThin
                         for (int q = 0; q < 4; ++q) acc[a][q] = fmac(v[a], c[q], acc[a][q]);
                 }
             }
+            // entry e = 4 a + q of the tile, summed over the warp's lanes
+            T v[16];
 #pragma unroll
             for (int a = 0; a < 4; ++a)
 #pragma unroll
-                for (int q = 0; q < 4; ++q) acc[a][q] = warp_sum(acc[a][q]);
-            if (lane < 16) {
-                const int a = lane & 3, q = lane >> 2;
-                T val = T(0);
-#pragma unroll
-                for (int aa = 0; aa < 4; ++aa)
-#pragma unroll
-                    for (int qq = 0; qq < 4; ++qq)
-                        if (aa == a && qq == q) val = acc[aa][qq];
-                if (c0 + q < n) mine[(l0 + a) + (size_t)(c0 + q) * kPanelMaxCols] = val;
+                for (int q = 0; q < 4; ++q) v[4 * a + q] = acc[a][q];
+            const int e = warp_reduce16(v, lane);
+            if ((lane & 1) == 0) {
+                const int a = e >> 2, q = e & 3;
+                if (c0 + q < n) mine[(l0 + a) + (size_t)(c0 + q) * kPanelMaxCols] = v[0];
             }
         }
         // the next block's V streams in while this one waits at the barriers
@@ -200,11 +270,38 @@ template <class T, bool CSMEM, int VBUF> __global__ void __launch_bounds__(kThin
                     for (int j = l; j < ib; ++j) acc = fmac(sT[l * (kPanelMaxCols + 1) + j], sW[j + c * kPanelMaxCols], acc);
                 }
             }
-            sY[e] = acc;
+            if (quads) sY[l * n + c] = acc;  // row-major for the quad update
+            else sY[e] = acc;
         }
         __syncthreads();
         // 5. C(r, c) -= sum_l V(r, l) Y(l, c) on own rows
-        const int nrc = (r1 > rs) ? (r1 - rs + 31) / 32 : 0;
+        if constexpr (kQuads) {
+            if (quads) {
+                const int nq = (r1 - rs + 3) / 4;
+                for (int w = tid; w < nq * ctiles; w += kThinThreads) {
+                    const int r4 = rs + 4 * (w % nq), c0 = 4 * (w / nq);
+                    float4 acc[4];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) acc[q] = *reinterpret_cast<const float4 *>(sC + (size_t)(c0 + q) * ldcs + (r4 - r0));
+                    const int lmax = min(ib, r4 + 4 - i);  // V(r, l) = 0 for l > r - i
+                    for (int l = 0; l < lmax; ++l) {
+                        const float4 v = *reinterpret_cast<const float4 *>(sV + (size_t)l * R + (r4 - r0));
+                        const float4 y = *reinterpret_cast<const float4 *>(sY + (size_t)l * n + c0);
+                        const float yq[4] = {y.x, y.y, y.z, y.w};
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) {
+                            acc[q].x = fmaf(-v.x, yq[q], acc[q].x);
+                            acc[q].y = fmaf(-v.y, yq[q], acc[q].y);
+                            acc[q].z = fmaf(-v.z, yq[q], acc[q].z);
+                            acc[q].w = fmaf(-v.w, yq[q], acc[q].w);
+                        }
+                    }
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) *reinterpret_cast<float4 *>(sC + (size_t)(c0 + q) * ldcs + (r4 - r0)) = acc[q];
+                }
+            }
+        }
+        const int nrc = (r1 > rs && !quads) ? (r1 - rs + 31) / 32 : 0;
         for (int w = warp; w < nrc * ctiles; w += kThinWarps) {
             const int rc = w % nrc, c0 = 4 * (w / nrc);
             const int r = rs + rc * 32 + lane;
@@ -235,7 +332,7 @@ template <class T, bool CSMEM, int VBUF> __global__ void __launch_bounds__(kThin
     __syncthreads();
     if (CSMEM) {
         for (int c = 0; c < n; ++c)
-            for (int r = r0 + tid; r < r1; r += kThinThreads) p.C[r + (size_t)c * p.ldc] = sC[(size_t)(r - r0) * ldsc + c];
+            for (int r = r0 + tid; r < r1; r += kThinThreads) p.C[r + (size_t)c * p.ldc] = sC[(size_t)c * ldcs + (r - r0)];
     }
 }
 

@@ -87,6 +87,26 @@ __device__ __forceinline__ float warp_sum(float v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
 }
+__device__ __forceinline__ double shfl_xor_t(double v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
+__device__ __forceinline__ float shfl_xor_t(float v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
+template <class R> __device__ __forceinline__ cplx<R> shfl_xor_t(cplx<R> v, int o) { return cplx<R>(shfl_xor_t(v.x, o), shfl_xor_t(v.y, o)); }
+// A warp's 16 sums at once: a butterfly that halves the entries at each of
+// four steps, then adds lane pairs; each even lane ends with the total of
+// one entry, whose index it returns (v[0] holds it).
+template <class T> __device__ __forceinline__ int warp_reduce16(T (&v)[16], int lane) {
+#pragma unroll
+    for (int lvl = 0; lvl < 4; ++lvl) {
+        const int o = 16 >> lvl, n = 8 >> lvl;
+        const bool up = (lane & o) != 0;
+#pragma unroll
+        for (int i = 0; i < n; ++i) {
+            const T send = up ? v[i] : v[i + n], keep = up ? v[i + n] : v[i];
+            v[i] = keep + shfl_xor_t(send, o);
+        }
+    }
+    v[0] = v[0] + shfl_xor_t(v[0], 1);
+    return ((lane >> 4) & 1) * 8 + ((lane >> 3) & 1) * 4 + ((lane >> 2) & 1) * 2 + ((lane >> 1) & 1);
+}
 template <class R> __device__ __forceinline__ cplx<R> warp_sum(cplx<R> v) {
     return cplx<R>(warp_sum(v.x), warp_sum(v.y));
 }
