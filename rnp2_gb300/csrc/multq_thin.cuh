@@ -242,6 +242,13 @@ template <class T, bool CSMEM, int VBUF> __global__ void __launch_bounds__(kThin
         // the next block's V streams in while this one waits at the barriers
         if (VBUF == 2 && s + 1 < p.nblk) stage_v(block_of(s + 1), (s & 1) ? sV0 : sV1);
         if (!bar.sync()) return;
+        // T_b (the previous step's Y is done with sT): its loads overlap the
+        // reduction and the second barrier
+        const T *Tb = p.Tf + (size_t)b * kPanelMaxCols * kPanelMaxCols;
+        for (int e = tid; e < kPanelMaxCols * kPanelMaxCols; e += kThinThreads) {
+            const int r = e % kPanelMaxCols, c = e / kPanelMaxCols;
+            sT[r * (kPanelMaxCols + 1) + c] = (r <= c && c < ib) ? Tb[r + (size_t)c * kPanelMaxCols] : T(0);
+        }
         // 3. this block's slice of the reduction, fixed order over blocks
         for (int e = g * slice + warp; e < min(nw, (g + 1) * slice); e += kThinWarps) {
             T a = T(0);
@@ -252,11 +259,6 @@ template <class T, bool CSMEM, int VBUF> __global__ void __launch_bounds__(kThin
         if (!bar.sync()) return;
         // 4. Y = op(T) (V^H C)
         for (int e = tid; e < nw; e += kThinThreads) sW[e] = ldcg(&p.wred[e]);
-        const T *Tb = p.Tf + (size_t)b * kPanelMaxCols * kPanelMaxCols;
-        for (int e = tid; e < kPanelMaxCols * kPanelMaxCols; e += kThinThreads) {
-            const int r = e % kPanelMaxCols, c = e / kPanelMaxCols;
-            sT[r * (kPanelMaxCols + 1) + c] = (r <= c && c < ib) ? Tb[r + (size_t)c * kPanelMaxCols] : T(0);
-        }
         __syncthreads();
         for (int e = tid; e < nw; e += kThinThreads) {
             const int l = e % kPanelMaxCols, c = e / kPanelMaxCols;
