@@ -148,8 +148,9 @@ template <bool VEC> __global__ void __launch_bounds__(kUfThreads, 2) k_update_f3
 // shared memory 64 at a time (cp.async, two stages, column-major with a
 // padded stride); thread (tn = tid % 16, tk = (tid / 16) % 8, h = tid / 128)
 // accumulates columns tn + 16 a against k = tk + 8 b (a, b < 4) over rows
-// 32 h .. 32 h + 31 of every chunk, four rows per shared-memory load; the two
-// halves are added in shared memory at the end.
+// 32 h .. 32 h + 31 of every chunk, four rows per shared-memory load, even and
+// odd rows in the two lanes of the packed FMAs; the lanes and the two halves
+// are added at the end.
 constexpr int kWfCols = 64, kWfRows = 64, kWfLd = kWfRows + 4;
 constexpr size_t kWfSmem = (size_t)2 * (kWfCols + 32) * kWfLd * sizeof(float);
 template <bool VEC> __global__ void __launch_bounds__(kUfThreads) k_w_f32(UpdArgs g, float *P, int rows_per_split) {
@@ -187,9 +188,13 @@ template <bool VEC> __global__ void __launch_bounds__(kUfThreads) k_w_f32(UpdArg
         }
         cp_async_commit();
     };
-    float2 acc[4][2];  // acc[a][q] = column tn + 16 a against (k = tk + 8 (2q), tk + 8 (2q + 1))
+    // acc[a][b] = column tn + 16 a against k = tk + 8 b, as (even rows, odd
+    // rows) partial sums: both FMA operands are adjacent rows of a 4-row load
+    float2 acc[4][4];
 #pragma unroll
-    for (int a = 0; a < 4; ++a) acc[a][0] = acc[a][1] = make_float2(0.f, 0.f);
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) acc[a][b] = make_float2(0.f, 0.f);
     int st = 0;
     if (ra < rb) issue(ra, 0);
     for (int m0 = ra; m0 < rb; m0 += kWfRows, st ^= 1) {
@@ -208,22 +213,12 @@ template <bool VEC> __global__ void __launch_bounds__(kUfThreads) k_w_f32(UpdArg
 #pragma unroll
             for (int b = 0; b < 4; ++b) v4[b] = *reinterpret_cast<const float4 *>(&sV[st][tk + 8 * b][r]);
 #pragma unroll
-            for (int e = 0; e < 4; ++e) {
-                const float cv[4] = {e == 0 ? c4[0].x : e == 1 ? c4[0].y : e == 2 ? c4[0].z : c4[0].w,
-                                     e == 0 ? c4[1].x : e == 1 ? c4[1].y : e == 2 ? c4[1].z : c4[1].w,
-                                     e == 0 ? c4[2].x : e == 1 ? c4[2].y : e == 2 ? c4[2].z : c4[2].w,
-                                     e == 0 ? c4[3].x : e == 1 ? c4[3].y : e == 2 ? c4[3].z : c4[3].w};
-                const float vv[4] = {e == 0 ? v4[0].x : e == 1 ? v4[0].y : e == 2 ? v4[0].z : v4[0].w,
-                                     e == 0 ? v4[1].x : e == 1 ? v4[1].y : e == 2 ? v4[1].z : v4[1].w,
-                                     e == 0 ? v4[2].x : e == 1 ? v4[2].y : e == 2 ? v4[2].z : v4[2].w,
-                                     e == 0 ? v4[3].x : e == 1 ? v4[3].y : e == 2 ? v4[3].z : v4[3].w};
-                const float2 v01 = make_float2(vv[0], vv[1]), v23 = make_float2(vv[2], vv[3]);
+            for (int a = 0; a < 4; ++a)
 #pragma unroll
-                for (int a = 0; a < 4; ++a) {
-                    acc[a][0] = __ffma2_rn(make_float2(cv[a], cv[a]), v01, acc[a][0]);
-                    acc[a][1] = __ffma2_rn(make_float2(cv[a], cv[a]), v23, acc[a][1]);
+                for (int b = 0; b < 4; ++b) {
+                    acc[a][b] = __ffma2_rn(make_float2(c4[a].x, c4[a].y), make_float2(v4[b].x, v4[b].y), acc[a][b]);
+                    acc[a][b] = __ffma2_rn(make_float2(c4[a].z, c4[a].w), make_float2(v4[b].z, v4[b].w), acc[a][b]);
                 }
-            }
         }
         __syncthreads();  // the stage is free for the chunk after next
     }
@@ -231,12 +226,9 @@ template <bool VEC> __global__ void __launch_bounds__(kUfThreads) k_w_f32(UpdArg
     float *red = s_wf;  // 128 threads x 16 values
     if (h == 1) {
 #pragma unroll
-        for (int a = 0; a < 4; ++a) {
-            red[(tid - 128) * 16 + 4 * a + 0] = acc[a][0].x;
-            red[(tid - 128) * 16 + 4 * a + 1] = acc[a][0].y;
-            red[(tid - 128) * 16 + 4 * a + 2] = acc[a][1].x;
-            red[(tid - 128) * 16 + 4 * a + 3] = acc[a][1].y;
-        }
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int b = 0; b < 4; ++b) red[(tid - 128) * 16 + 4 * a + b] = acc[a][b].x + acc[a][b].y;
     }
     __syncthreads();
     if (h == 0) {
@@ -244,8 +236,9 @@ template <bool VEC> __global__ void __launch_bounds__(kUfThreads) k_w_f32(UpdArg
 #pragma unroll
         for (int a = 0; a < 4; ++a) {
             const int n = n0 + tn + 16 * a;
-            const float sum[4] = {acc[a][0].x + red[tid * 16 + 4 * a + 0], acc[a][0].y + red[tid * 16 + 4 * a + 1],
-                                  acc[a][1].x + red[tid * 16 + 4 * a + 2], acc[a][1].y + red[tid * 16 + 4 * a + 3]};
+            float sum[4];
+#pragma unroll
+            for (int b = 0; b < 4; ++b) sum[b] = (acc[a][b].x + acc[a][b].y) + red[tid * 16 + 4 * a + b];
 #pragma unroll
             for (int b = 0; b < 4; ++b) {
                 const int k = tk + 8 * b;
