@@ -43,7 +43,7 @@ constexpr size_t kUfSmem = (size_t)(32 * kUfCols + 2 * 32 * kUfRows + 2 * kUfCol
 template <bool VEC> __global__ void __launch_bounds__(kUfThreads, 2) k_update_f32(UpdArgs g) {
     static_assert(kUfRows == 4 * 16 && kUfCols == 8 * (kUfThreads / 16), "thread tile");
     extern __shared__ __align__(16) float s_uf[];
-    float (*sW)[kUfCols] = reinterpret_cast<float (*)[kUfCols]>(s_uf);                             // [k][col]
+    float (*sW)[kUfCols] = reinterpret_cast<float (*)[kUfCols]>(s_uf);                             // [k][col], negated
     float (*sV)[32][kUfRows] = reinterpret_cast<float (*)[32][kUfRows]>(s_uf + 32 * kUfCols);      // [stage][k][row]
     float (*sC)[kUfCols][kUfRows] = reinterpret_cast<float (*)[kUfCols][kUfRows]>(s_uf + 32 * kUfCols + 2 * 32 * kUfRows);  // [stage][col][row]
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
@@ -51,7 +51,7 @@ template <bool VEC> __global__ void __launch_bounds__(kUfThreads, 2) k_update_f3
     const bool vecv = VEC && ((uintptr_t)g.V % 16 == 0) && (g.ldv % 4 == 0);
     for (int idx = tid; idx < 32 * kUfCols; idx += kUfThreads) {
         const int c = idx % kUfCols, k = idx / kUfCols, gn = n0 + c;
-        sW[k][c] = (k < K && gn < g.N) ? g.W[gn + (size_t)k * g.ldw] : 0.f;
+        sW[k][c] = (k < K && gn < g.N) ? -g.W[gn + (size_t)k * g.ldw] : 0.f;  // negated: C += V (-W)^T
     }
     const int ntiles = (g.M + kUfRows - 1) / kUfRows;
     const int gc = n0 + 8 * ty;
@@ -115,11 +115,11 @@ template <bool VEC> __global__ void __launch_bounds__(kUfThreads, 2) k_update_f3
             const float4 wa = *reinterpret_cast<const float4 *>(&sW[k][8 * ty]);
             const float4 wb = *reinterpret_cast<const float4 *>(&sW[k][8 * ty + 4]);
             const float2 w[4] = {make_float2(wa.x, wa.y), make_float2(wa.z, wa.w), make_float2(wb.x, wb.y), make_float2(wb.z, wb.w)};
-            const float nv[4] = {-v.x, -v.y, -v.z, -v.w};
+            const float vr[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
             for (int r = 0; r < 4; ++r)
 #pragma unroll
-                for (int p = 0; p < 4; ++p) acc[r][p] = __ffma2_rn(make_float2(nv[r], nv[r]), w[p], acc[r][p]);
+                for (int p = 0; p < 4; ++p) acc[r][p] = __ffma2_rn(make_float2(vr[r], vr[r]), w[p], acc[r][p]);
         }
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
