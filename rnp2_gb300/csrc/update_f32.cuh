@@ -223,12 +223,12 @@ template <bool VEC> __global__ void __launch_bounds__(kUfThreads) k_w_f32(UpdArg
         __syncthreads();  // the stage is free for the chunk after next
     }
     // add the two row halves (h = 1 into h = 0) and write the partial
-    float *red = s_wf;  // 128 threads x 16 values
+    float *red = s_wf;  // 128 threads x 16 values, stride 17 (no bank conflicts)
     if (h == 1) {
 #pragma unroll
         for (int a = 0; a < 4; ++a)
 #pragma unroll
-            for (int b = 0; b < 4; ++b) red[(tid - 128) * 16 + 4 * a + b] = acc[a][b].x + acc[a][b].y;
+            for (int b = 0; b < 4; ++b) red[(tid - 128) * 17 + 4 * a + b] = acc[a][b].x + acc[a][b].y;
     }
     __syncthreads();
     if (h == 0) {
@@ -238,7 +238,7 @@ template <bool VEC> __global__ void __launch_bounds__(kUfThreads) k_w_f32(UpdArg
             const int n = n0 + tn + 16 * a;
             float sum[4];
 #pragma unroll
-            for (int b = 0; b < 4; ++b) sum[b] = (acc[a][b].x + acc[a][b].y) + red[tid * 16 + 4 * a + b];
+            for (int b = 0; b < 4; ++b) sum[b] = (acc[a][b].x + acc[a][b].y) + red[tid * 17 + 4 * a + b];
 #pragma unroll
             for (int b = 0; b < 4; ++b) {
                 const int k = tk + 8 * b;
