@@ -146,10 +146,12 @@ template <class T, bool CSMEM, int VBUF> __global__ void __launch_bounds__(kThin
     }
     if (VBUF > 0 && p.nblk > 0) stage_v(block_of(0), sV0);
 
-    // FP32 with C and V in shared memory: 4-row quads as float4 (rows past the
-    // block's end are zeros in both), 4 x 4 register tiles
+    // FP32 with C and V in shared memory: 4-row quads as float4, 4 x 4
+    // register tiles.  Rows past the block's end must read zeros in both: C's
+    // are loaded as zeros, V's are written as zeros only by the 16-byte
+    // staging (A 16-byte aligned, lda a multiple of 4), so the quads need it.
     constexpr bool kQuads = std::is_same<T, float>::value && CSMEM && VBUF > 0;
-    const bool quads = kQuads && (n % 4 == 0) && (R % 4 == 0) && (r0 % 4 == 0);
+    const bool quads = kQuads && (n % 4 == 0) && (R % 4 == 0) && (r0 % 4 == 0) && ((uintptr_t)p.A % 16 == 0) && (p.lda % 4 == 0);
     const int nw = kPanelMaxCols * n;          // entries of V^H C
     const int ctiles = (n + 3) / 4;
     const int ntiles = (kPanelMaxCols / 4) * ctiles;

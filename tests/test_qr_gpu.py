@@ -196,8 +196,12 @@ def test_empty_inputs_are_quick_returns():
 # rows are held in shared memory or, when they do not fit, in place.
 # (k >= m / 4 takes the variant that re-splits the active rows per reflector
 # block: the last three and the 129-row case)
+# FP32 with a multiple of 4 columns, blocks of a multiple of 4 rows and a
+# 16-byte aligned A takes the 4-row-quad path (6000: 40 rows per block); 6001
+# (ld 6001) must leave it; LD_PAD below runs 6001 rows with ld 6004 through it,
+# a ragged last block whose quad past the end must read zeros
 THIN = [("d", 3000, 1, 70), ("d", 2000, 16, 256), ("s", 5000, 33, 100), ("z", 40000, 64, 64), ("c", 700, 64, 45), ("z", 129, 7, 129),
-        ("z", 600, 48, 600), ("d", 1000, 64, 999), ("s", 2000, 5, 1500)]
+        ("z", 600, 48, 600), ("d", 1000, 64, 999), ("s", 2000, 5, 1500), ("s", 6000, 16, 256), ("s", 6001, 8, 96), ("s", 20000, 64, 130)]
 
 
 @pytest.mark.parametrize("p,m,nrhs,k", THIN)
@@ -218,6 +222,29 @@ def test_mult_q_thin_against_oracle(oracle, p, m, nrhs, k):
         gq.mult_q("L", trans, A, t, dc, k)
         torch.cuda.synchronize()
         assert rel(from_dev(dc), co) <= tol, trans
+
+
+def test_mult_q_thin_quads_ragged_block(oracle):
+    # 6001 rows stored with leading dimension 6004 (16-byte aligned columns):
+    # the FP32 quad path with a ragged last block
+    p, m, nrhs, k, ld = "s", 6001, 8, 96, 6004
+    vals, _ = oracle.larnv("s", 2, [3, 1, 4, 1], m * k)
+    a = np.asfortranarray(vals.astype(np.float32).reshape(k, m).T)
+    fac, tau = run_factor(a, p, m, k)
+    cv, _ = oracle.larnv("s", 2, [5, 9, 2, 7], m * nrhs)
+    c0 = np.asfortranarray(cv.astype(np.float32).reshape(nrhs, m).T)
+    t = torch.from_numpy(np.ascontiguousarray(tau)).cuda()
+    Apad = torch.zeros((k, ld), dtype=torch.float32, device="cuda").t()
+    Apad[:m] = to_dev(fac)
+    A = Apad[:m]
+    assert A.stride(1) == ld
+    for trans in ("N", "C"):
+        co = c0.copy(order="F")
+        oracle.unmqr(p, "L", trans, m, nrhs, k, fac, tau, co)
+        dc = to_dev(c0)
+        gq.mult_q("L", trans, A, t, dc, k)
+        torch.cuda.synchronize()
+        assert rel(from_dev(dc), co) <= 1e-5, trans
 
 
 # FP32 panels sum squares error-free in FP32; columns whose magnitudes leave
