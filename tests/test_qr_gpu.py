@@ -149,6 +149,27 @@ def test_factor_against_oracle(oracle, p, mn):
     assert np.max(np.abs(tg - to)) <= 100 * R_TOL[p]
 
 
+@pytest.mark.parametrize("ld", [1029, 1032])
+def test_fp32_factor_ragged_rows(oracle, ld):
+    # 1029 rows: the FP32 trailing passes (W from 1024 rows up) with a ragged
+    # last row tile, through scalar loads (ld 1029) and through 16-byte
+    # copies with a padded leading dimension (ld 1032)
+    p, m, n = "s", 1029, 70
+    vals, _ = oracle.larnv("d", 2, [7, 3, 5, 1], m * n)
+    a = np.asfortranarray(vals.astype(np.float32).reshape(n, m).T)
+    fo = a.copy(order="F")
+    to = oracle.geqrf(p, m, n, fo)
+    apad = np.zeros((ld, n), dtype=np.float32, order="F")
+    apad[:m] = a
+    fg, tg = run_factor(apad, p, m, n)
+    R, V = split_factor(fg[:m], m, n)
+    Ro, Vo = split_factor(fo, m, n)
+    assert rel(R, Ro) <= R_TOL[p]
+    assert rel(V, Vo) <= V_TOL[p]
+    assert np.max(np.abs(tg - to)) <= 100 * R_TOL[p]
+    assert np.all(fg[m:] == 0)  # rows past m untouched
+
+
 @pytest.mark.parametrize("p", ["d", "z"])
 def test_apply_and_generate_against_oracle(oracle, p):
     m, n, nrhs = 1500, 200, 9
