@@ -3,7 +3,8 @@
 // be the reference's Householder QR): CholeskyQR2 with a double-float first
 // Gram matrix, then Householder reconstruction of the orthonormal factor.
 //
-//   G1 = A^T A (double-float sums), R1 = chol(G1) (double-float), Q1 = A R1^-1;
+//   G1 = A^T A, R1 = chol(G1), Q1 = A R1^-1 (FP32 first; double-float sums and
+//   factor when Q1 comes out too far from orthonormal);
 //   G2 = Q1^T Q1, R2 = chol(G2), Q = Q1 R2^-1, R = R2 R1   (both in FP32)
 //   (Yamamoto, Nakatsukasa, Yanagisawa and Fukaya, "Roundoff error analysis
 //   of the CholeskyQR2 algorithm", ETNA 44, 2015: the second pass restores
@@ -405,6 +406,7 @@ template <int kTag> __global__ void __launch_bounds__(kCqrThreads, 1) k_panel_cq
     __shared__ __align__(16) float sE[NB][LD];     // rows of the top block's LU, staged
     __shared__ float sR1inv[NB], sR2inv[NB], sMinv[NB], sS[NB], sD0[NB];
     __shared__ int s_fail;
+    __shared__ float s_dev;  // ||G2 - I||_F^2 of an FP32 first pass
 
     // the block's Gram partial of sQ into gpart[b]: double-float or FP32 sums,
     // entries of a tile row in packed pairs
@@ -481,49 +483,83 @@ template <int kTag> __global__ void __launch_bounds__(kCqrThreads, 1) k_panel_cq
         return s_fail != 0;
     };
 
-    // ---- the block's rows, row-major, zero padding columns ----
+    // ---- two passes: the first in FP32, accepted when Q1 comes out close to
+    // orthonormal (||G2 - I||_F <= 0.1: the FP32 second pass then restores
+    // orthogonality to working precision), else both again with the first in
+    // double-float.  Every block decides from the same summed G2, so all take
+    // the same barriers. ----
     if (tid == 0) s_fail = 0;
-    for (int r = tid; r < R; r += kCqrThreads) {
-        const float *src = p.A + (size_t)(r0 + r);
-        float v[NB];
+    for (int attempt = 0; attempt < 2; ++attempt) {
+        const bool df = attempt == 1;
+        // the block's rows, row-major, zero padding columns (again on the
+        // second attempt: the first left Q1 in sQ; A is written only at the end)
+        for (int r = tid; r < R; r += kCqrThreads) {
+            const float *src = p.A + (size_t)(r0 + r);
+            float v[NB];
 #pragma unroll
-        for (int c = 0; c < NB; ++c) v[c] = (c < N) ? src[(size_t)c * p.lda] : 0.f;
+            for (int c = 0; c < NB; ++c) v[c] = (c < N) ? src[(size_t)c * p.lda] : 0.f;
 #pragma unroll
-        for (int q = 0; q < 8; ++q) *reinterpret_cast<float4 *>(sQ + (size_t)r * LD + 4 * q) = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
-    }
-    __syncthreads();
+            for (int q = 0; q < 8; ++q) *reinterpret_cast<float4 *>(sQ + (size_t)r * LD + 4 * q) = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+        }
+        __syncthreads();
 
-    // ---- first pass: G1 = A^T A, R1 = chol(G1) (double-float), Q1 = A R1^-1 ----
-    gram_partial(true);
-    if (!bar.sync()) return;
-    gram_sum();
-    if (!bar.sync()) return;
-    gram_load();
-    cqr_cholesky<true>(sGram, sR1, sR1inv, sD0, 0x1p-38f, &s_fail);
-    if (failed()) return;
-    for (int r = tid; r < R; r += kCqrThreads) {
-        float2 x[NB / 2];
-        cqr_row_load(x, sQ + (size_t)r * LD);
-        // z = 0 (r < 2^30), but the compiler cannot tell: the factor's loads
-        // stay in the loop instead of being hoisted out of it (they would
-        // not fit in registers)
-        const int z = r & 0x40000000;
-        cqr_row_solve(x, sR1 + z, sR1inv + z);
-        cqr_row_store(sQ + (size_t)r * LD, x);
-    }
-    __syncthreads();
-    // the top 32 rows of Q1 for every block's reconstruction
-    if (b == 0)
-        for (int idx = tid; idx < NB * NB; idx += kCqrThreads) __stcg(&p.qtop[idx], sQ[(size_t)(idx >> 5) * LD + (idx & 31)]);
+        // first pass: G1 = A^T A, R1 = chol(G1), Q1 = A R1^-1
+        gram_partial(df);
+        if (!bar.sync()) return;
+        gram_sum();
+        if (!bar.sync()) return;
+        gram_load();
+        if (df) cqr_cholesky<true>(sGram, sR1, sR1inv, sD0, 0x1p-38f, &s_fail);
+        else cqr_cholesky<false>(sGram, sR1, sR1inv, sD0, 0x1p-20f, &s_fail);
+        if (s_fail != 0) {
+            if (df) {
+                failed();
+                return;
+            }
+            __syncthreads();  // every thread has read the flag
+            if (tid == 0) s_fail = 0;
+            __syncthreads();
+            continue;
+        }
+        for (int r = tid; r < R; r += kCqrThreads) {
+            float2 x[NB / 2];
+            cqr_row_load(x, sQ + (size_t)r * LD);
+            // z = 0 (r < 2^30), but the compiler cannot tell: the factor's loads
+            // stay in the loop instead of being hoisted out of it (they would
+            // not fit in registers)
+            const int z = r & 0x40000000;
+            cqr_row_solve(x, sR1 + z, sR1inv + z);
+            cqr_row_store(sQ + (size_t)r * LD, x);
+        }
+        __syncthreads();
+        // the top 32 rows of Q1 for every block's reconstruction
+        if (b == 0)
+            for (int idx = tid; idx < NB * NB; idx += kCqrThreads) __stcg(&p.qtop[idx], sQ[(size_t)(idx >> 5) * LD + (idx & 31)]);
 
-    // ---- second pass: G2 = Q1^T Q1, R2 = chol(G2) (FP32) ----
-    gram_partial(false);
-    if (!bar.sync()) return;
-    gram_sum();
-    if (!bar.sync()) return;
-    gram_load();
-    cqr_cholesky<false>(sGram, sR2, sR2inv, sD0, 0x1p-14f, &s_fail);
-    if (failed()) return;
+        // second pass: G2 = Q1^T Q1, R2 = chol(G2) (FP32)
+        gram_partial(false);
+        if (!bar.sync()) return;
+        gram_sum();
+        if (!bar.sync()) return;
+        gram_load();
+        if (!df) {
+            if (warp == 0) {
+                float d2 = 0.f;
+                for (int i = 0; i <= lane; ++i) {
+                    const float2 v = sGram[i][lane];
+                    const float d = (v.x + v.y) - (i == lane ? 1.f : 0.f);
+                    d2 = fmaf(i == lane ? d : 2.f * d, d, d2);
+                }
+                d2 = warp_sum(d2);
+                if (lane == 0) s_dev = d2;
+            }
+            __syncthreads();
+            if (!(s_dev <= 0.01f)) continue;
+        }
+        cqr_cholesky<false>(sGram, sR2, sR2inv, sD0, 0x1p-14f, &s_fail);
+        if (failed()) return;
+        break;
+    }
 
     // ---- Householder reconstruction: Q1_top - S R2 = L M (M = U R2) ----
     cqr_top_lu(p.qtop, sR2, sMt, sMinv, sLt, sS, sE);

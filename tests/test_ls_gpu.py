@@ -176,6 +176,23 @@ def test_mixed_fp32_factor_uses_cholesky_qr2_panels(mn, forward):
     check_refined(A, b, X, info)
 
 
+def test_mixed_fp32_factor_redoes_ill_conditioned_panels_in_double_float():
+    # two columns 1e-4 apart in angle: the FP32 first pass of their panel keeps
+    # a pivot of 1e-8 of the column's squared norm (below its 2^-20 limit), so
+    # the panel is redone with the double-float first pass (limit 2^-38) and
+    # stays a CholeskyQR2 panel; condition ~1e4, which the refinement handles
+    m, n = 4096, 96
+    rng = np.random.default_rng(22)
+    A = rng.standard_normal((m, n))
+    u = rng.standard_normal(m)
+    u -= A[:, 40] * (u @ A[:, 40]) / (A[:, 40] @ A[:, 40])
+    A[:, 41] = A[:, 40] + 1e-4 * np.linalg.norm(A[:, 40]) * u / np.linalg.norm(u)
+    b = A @ rng.standard_normal((n, 2)) + 1e-8 * rng.standard_normal((m, 2))
+    (X, info), kinds = panel_kinds(lambda: gls.gels_refine(to_dev(A), to_dev(b)))
+    assert kinds == {"panel_cqr": 3}, kinds
+    check_refined(A, b, X, info)
+
+
 def test_mixed_fp32_factor_falls_back_to_householder_panels():
     # two columns 1e-6 apart in angle: the first Cholesky pivot of their panel
     # keeps 1e-12 of the column's squared norm, below the CholeskyQR2 limit, so
