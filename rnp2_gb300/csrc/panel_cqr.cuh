@@ -1,7 +1,8 @@
 // panel_cqr.cuh — FP32 panel factorization for the internal FP32 factor of
 // the mixed least-squares solver (not the drop-in Factor, whose output must
-// be the reference's Householder QR): CholeskyQR2 with a double-float first
-// Gram matrix, then Householder reconstruction of the orthonormal factor.
+// be the reference's Householder QR): CholeskyQR2 (its first Gram matrix in
+// double-float when the panel needs it), then Householder reconstruction of
+// the orthonormal factor.
 //
 //   G1 = A^T A, R1 = chol(G1), Q1 = A R1^-1 (FP32 first; double-float sums and
 //   factor when Q1 comes out too far from orthonormal);
@@ -30,12 +31,14 @@
 // Panels narrower than 32 columns are padded with zero columns and a unit
 // Gram diagonal, which carries an identity through every step.
 //
-// A first-pass pivot that is not positive or below 2^-38 of its column's
-// squared norm, or a second-pass pivot below 2^-14 of its diagonal (Q1 far
-// from orthonormal), marks the panel as failed before anything is written;
-// the caller then refactors it with Householder panels.  That happens for
-// panels with condition numbers near 10^5 and above, zero columns and
-// non-finite data.
+// The first pass runs in FP32; a pivot of it below 2^-20 of its column's
+// squared norm, or ||G2 - I||_F > 0.1 after it, sends the panel through both
+// passes again with the first in double-float.  A double-float pivot that is
+// not positive or below 2^-38 of its column's squared norm, or a second-pass
+// pivot below 2^-14 of its diagonal (Q1 far from orthonormal), marks the panel
+// as failed before anything is written; the caller then refactors it with
+// Householder panels.  That happens for panels with condition numbers near
+// 10^5 and above, zero columns and non-finite data.
 #pragma once
 #include "qr_kernels.cuh"
 
