@@ -236,7 +236,7 @@ inline int choose_splits(int K, int tiles, int smax) {
 // split lanes per entry)
 template <class T> int sum_times_t(const T *P, size_t ldp, size_t pstride, int nsplit, int rows, int k, const T *Tm, int ldt, int opT, T *W, size_t ldw, cudaStream_t st) {
     if (nsplit > 8) {
-        k_reduce_times_t<T><<<(rows + 1) / 2, 256, 0, st>>>(P, ldp, pstride, nsplit, rows, k, Tm, ldt, opT, W, ldw);
+        k_reduce_times_t<T><<<rows, 256, 0, st>>>(P, ldp, pstride, nsplit, rows, k, Tm, ldt, opT, W, ldw);
         RNPGPU_CHECK_LAUNCH();
         return kOk;
     }

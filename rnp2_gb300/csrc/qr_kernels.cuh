@@ -870,48 +870,50 @@ __global__ void __launch_bounds__(256) k_sum_times_t(const T *P, size_t ldp, siz
 
 // ---------------------------------------------------------------------------
 // The same product when there are many partials: W(r, :) = (sum_s P_s(r, :))
-// op(T) in one launch.  Block: 2 rows of W, 256 threads = 4 split lanes x 2
-// rows x 32 columns (many small blocks keep every SM's loads in flight);
-// lane q sums partials q, q + 4, ... in independent batches of eight loads,
-// the four lane sums are added in a fixed order, then the row is multiplied
-// by op(T) as above.
+// op(T) in one launch.  Block: one row of W, 256 threads = 8 split lanes x 32
+// columns (one block per row: every SM has loads in flight, and each thread
+// has at most a few batches of eight); lane q sums partials q, q + 8, ... in
+// independent batches of eight loads, the eight lane sums are added in a
+// fixed order, then the row is multiplied by op(T) as above (T's loads go out
+// with the partials').
 // ---------------------------------------------------------------------------
 template <class T>
 __global__ void __launch_bounds__(256) k_reduce_times_t(const T *P, size_t ldp, size_t pstride, int nsplit, int rows, int k, const T *Tm, int ldt, int opT, T *W, size_t ldw) {
     __shared__ T sT[kPanelMaxCols][kPanelMaxCols + 1];
-    __shared__ T sP[4][2][kPanelMaxCols + 1];
-    const int tid = threadIdx.x, q = tid >> 6, rl = (tid >> 5) & 1, j = tid & 31;
+    __shared__ T sP[8][kPanelMaxCols + 1];
+    const int tid = threadIdx.x, q = tid >> 5, j = tid & 31, row = blockIdx.x;
     for (int idx = tid; idx < k * k; idx += blockDim.x) {
         const int r = idx % k, c = idx / k;
         sT[r][c] = (r <= c) ? Tm[r + (size_t)c * ldt] : T(0);
     }
-    const int row = blockIdx.x * 2 + rl;
     T a[8];
 #pragma unroll
     for (int u = 0; u < 8; ++u) a[u] = T(0);
     if (row < rows && j < k) {
         const T *base = P + row + (size_t)j * ldp;
         int sp = q;
-        for (; sp + 28 < nsplit; sp += 32) {
+        for (; sp + 56 < nsplit; sp += 64) {
 #pragma unroll
-            for (int u = 0; u < 8; ++u) a[u] = a[u] + base[(size_t)(sp + 4 * u) * pstride];
+            for (int u = 0; u < 8; ++u) a[u] = a[u] + base[(size_t)(sp + 8 * u) * pstride];
         }
 #pragma unroll
         for (int u = 0; u < 8; ++u)
-            if (sp + 4 * u < nsplit) a[u] = a[u] + base[(size_t)(sp + 4 * u) * pstride];
+            if (sp + 8 * u < nsplit) a[u] = a[u] + base[(size_t)(sp + 8 * u) * pstride];
     }
-    sP[q][rl][j] = ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7]));
+    sP[q][j] = ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7]));
     __syncthreads();
-    if (q == 0) sP[0][rl][j] = (sP[0][rl][j] + sP[1][rl][j]) + (sP[2][rl][j] + sP[3][rl][j]);
-    __syncthreads();
-    if (q == 0 && row < rows && j < k) {
-        T acc = T(0);
-        if (opT == kOpN) {
-            for (int l = 0; l <= j; ++l) acc = fmac(sP[0][rl][l], sT[l][j], acc);
-        } else {
-            for (int l = j; l < k; ++l) acc = fmac(sP[0][rl][l], Tr<T>::conj(sT[j][l]), acc);
+    if (q == 0) {
+        sP[0][j] = ((sP[0][j] + sP[1][j]) + (sP[2][j] + sP[3][j])) + ((sP[4][j] + sP[5][j]) + (sP[6][j] + sP[7][j]));
+        __syncwarp();
+        if (row < rows && j < k) {
+            T acc = T(0);
+            if (opT == kOpN) {
+                for (int l = 0; l <= j; ++l) acc = fmac(sP[0][l], sT[l][j], acc);
+            } else {
+                for (int l = j; l < k; ++l) acc = fmac(sP[0][l], Tr<T>::conj(sT[j][l]), acc);
+            }
+            W[row + (size_t)j * ldw] = acc;
         }
-        W[row + (size_t)j * ldw] = acc;
     }
 }
 
