@@ -444,7 +444,9 @@ def other_configs(torch, dev, gq, lib, peak64):
 # rows processed)
 NCU_TRAFFIC = {
     "panel": (8.494080e6 + 0.003072e6, 2.0 * 65408 * 32 * 4),              # profiles/k_panel_f32_65536x32.md
-    "panel_cqr": (8.482304e6 + 0.0, 2.0 * 65408 * 32 * 4),                 # profiles/k_panel_cqr_65536x32.md
+    "panel_cqr": (8.489984e6 + 0.0, 2.0 * 65408 * 32 * 4),                 # profiles/k_panel_cqr_65536x32.md
+    "larfb_update": (100.581632e6 + 32.246784e6, 2.0 * 65408 * 352 * 4 + 65408 * 32 * 4.0),  # profiles/k_update_f32_65536.md
+    "larfb_w": (100.586240e6 + 3.193088e6, 65408 * 352 * 4.0 + 65408 * 32 * 4.0),             # profiles/k_w_f32_65536.md
     "residual_fp64": (277.589248e6 + 5.319424e6, 65536 * 512 * 8.0 + 2.0 * 65536 * 16 * 8),    # profiles/k_oz_residual_65536x512x16.md
     "normal_eq_fp64": (285.316352e6 + 3.713280e6, 65536 * 512 * 8.0 + 65536 * 16 * 8.0 + 65536 * 256.0),
 }

@@ -159,8 +159,8 @@ inline int launch_update_f32(const GemmArgs<float> &g, cudaStream_t st) {
 // W partials P_g = C^T V (g < nsplit, leading dimension N, stride N*K) on the
 // FP32 pipe (update_f32.cuh), one partial per split of the rows; nsplit <=
 // maxsplit.
-inline bool w_tc_ok(int M, int N, int K) { return M >= 1024 && N <= kUpdMaxN && K <= 32; }
-inline int launch_w_tc(const float *C, size_t ldc, const float *V, size_t ldv, float *P, int M, int N, int K, int maxsplit, int &nsplit, cudaStream_t st) {
+inline bool w_partials_ok(int M, int N, int K) { return M >= 1024 && N <= kUpdMaxN && K <= 32; }
+inline int launch_w_partials(const float *C, size_t ldc, const float *V, size_t ldv, float *P, int M, int N, int K, int maxsplit, int &nsplit, cudaStream_t st) {
     static std::once_flag once;
     static cudaError_t attr = cudaSuccess;
     std::call_once(once, []() {
@@ -184,7 +184,7 @@ inline int launch_w_tc(const float *C, size_t ldc, const float *V, size_t ldv, f
     RNPGPU_CHECK_LAUNCH();
     return kOk;
 }
-template <class T> int launch_w_tc(const T *, size_t, const T *, size_t, T *, int, int, int, int, int &, cudaStream_t) { return kErrDevice; }
+template <class T> int launch_w_partials(const T *, size_t, const T *, size_t, T *, int, int, int, int, int &, cudaStream_t) { return kErrDevice; }
 
 inline int launch_gemm_tc(const GemmArgs<float> &g, int nsplit, cudaStream_t st) {
     if (is_trailing_update(g, nsplit)) return launch_update_f32(g, st);
@@ -263,12 +263,13 @@ template <class T> int apply_block(bool left, bool notran, int M, int N, int ib,
     if (M <= 0 || N <= 0 || ib <= 0) return kOk;
     int rc;
     if (left) {
-        if (std::is_same<T, float>::value && w_tc_ok(M, N, ib)) {
-            // FP32: W partials on the tensor cores, one per persistent block
+        if (std::is_same<T, float>::value && w_partials_ok(M, N, ib)) {
+            // FP32: W partials per split of the rows (update_f32.cuh), their
+            // sum times op(T), then the rank-ib update
             int nsplit = 1;
             {
                 KScope ks("larfb_w", st);
-                if ((rc = launch_w_tc(C, ldc, V, ldv, ws.P, M, N, ib, ws.smax, nsplit, st))) return rc;
+                if ((rc = launch_w_partials(C, ldc, V, ldv, ws.P, M, N, ib, ws.smax, nsplit, st))) return rc;
             }
             if ((rc = sum_times_t<T>(ws.P, (size_t)N, (size_t)N * ib, nsplit, N, ib, Tm, ldt, notran ? kOpC : kOpN, ws.W, (size_t)N, st))) return rc;
             GemmArgs<T> u = gemm_args<T>(V, ldv, kOpN, 1, ws.W, (size_t)N, kOpC, 0, C, ldc, M, N, ib, T(-1), kBetaOne);
