@@ -69,26 +69,14 @@ struct CqrArgs {
     int rows_per_cta;
 };
 
-// double-float helpers beyond rnp_common.cuh: a - b c with the sum left
-// unnormalized; square root and reciprocal with one correction step each
-// (Karp and Markstein, "High-precision division and square root", ACM TOMS
-// 23(4), 1997)
+// double-float helper beyond rnp_common.cuh: a - b c with the sum left
+// unnormalized
 __device__ __forceinline__ F2 f2_fms(F2 a, F2 b, F2 c) {
     const float p = b.h * c.h;
     const float e = fmaf(b.h, c.l, fmaf(b.l, c.h, fmaf(b.h, c.h, -p)));
     const float s = a.h - p, bp = s - a.h;
     const float err = (a.h - (s - bp)) + (-p - bp);
     return F2{s, (a.l + err) - e};
-}
-__device__ __forceinline__ F2 f2_sqrt(F2 a) {
-    const float s = sqrtf(a.h);
-    const float r = fmaf(-s, s, a.h) + a.l;
-    return f2_norm(s, r * (0.5f / s));
-}
-__device__ __forceinline__ F2 f2_rcp(F2 a) {
-    const float q = 1.0f / a.h;
-    const float r = fmaf(-a.h, q, 1.0f) - a.l * q;
-    return f2_norm(q, r * q);
 }
 // tile t of the 8 x 8 grid of 4 x 4 tiles over the upper triangle, row-major
 __device__ __forceinline__ void cqr_tile(int t, int &ti, int &tj) {
