@@ -10,7 +10,7 @@
 // or 32 outputs per thread, packed FP32x2 FMAs, plain FP32 rounding.
 // (Measured against tcgen05 forms with three-way BF16 operand splitting and
 // TMEM accumulators at one block per SM, for the 15 updates of a 65536 x 512
-// factor: update 0.73 against 1.01 ms, W 0.79 against 1.04 ms.)
+// factor: update 0.72 against 1.01 ms, W 0.58-0.61 against 1.04 ms.)
 #pragma once
 #include "rnp_common.cuh"
 
