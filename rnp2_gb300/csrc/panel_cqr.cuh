@@ -27,7 +27,11 @@
 // warp per tile with the rows split across its lanes, summed across the lanes
 // by a butterfly; the per-block partials are then summed across blocks by
 // all blocks at once (one warp per entry), and every block reads the total
-// back and factors it itself, identically — four grid barriers in all.
+// back and factors it itself, identically — four grid barriers in all (eight
+// when the first pass is redone in double-float).  The 32 x 32 factors are
+// formed four columns a step: one warp factors the diagonal block and
+// publishes the block's rows, then all warps update their entries.  Block 0
+// holds the top 32 rows and forms T at the end from two triangular inverses.
 // Panels narrower than 32 columns are padded with zero columns and a unit
 // Gram diagonal, which carries an identity through every step.
 //
