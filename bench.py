@@ -132,23 +132,78 @@ def ls_errors(torch, A, b, x):
     return float(eta.max()), float(torch.linalg.norm(r))
 
 
-def cpu_solve(A_np, b_np, threads):
-    """One FP64 QR least-squares solve with the CPU oracle (+ OpenBLAS)."""
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo), and its core count."""
+    name = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.strip().lower().startswith("model name"):
+                name = ln.split(":", 1)[1].strip()
+                break
+    except Exception:
+        pass
+    if not name:
+        try:
+            with open("/proc/cpuinfo") as f:
+                for ln in f:
+                    if ln.lower().startswith("model name"):
+                        name = ln.split(":", 1)[1].strip()
+                        break
+        except Exception:
+            pass
+    import platform
+
+    return "%s (%s, %d cores)" % (name or "unknown model", platform.machine(), os.cpu_count() or 1)
+
+
+BLAS_ROUTINES = "gemv, ger/gerc, trmv, gemm, trmm, trsm"
+
+
+def cpu_solve(A_np, b_np, threads, p="d"):
+    """One FP64 QR least-squares solve with the CPU oracle, every level-2/3
+    call (the routines the reference forwards to its BLAS) through OpenBLAS
+    on `threads` threads.  Returns (x, R, seconds, blas library name)."""
     import numpy as np
 
     import oracle as orc
 
     o = orc.load()
     blas = orc.find_openblas()
-    kind_blas = "none"
+    kind_blas = "none (plain loops)"
     if blas and orc.use_blas(o, blas, "scipy_", threads) == 0:
         kind_blas = os.path.basename(blas)
-    a = np.asfortranarray(A_np.copy())
-    bb = np.asfortranarray(b_np.copy())
-    t0 = time.perf_counter()
-    o.gels("d", a.shape[0], a.shape[1], bb.shape[1], a, bb)
-    dt = time.perf_counter() - t0
-    return bb[: a.shape[1]].copy(), dt, kind_blas
+    try:
+        a = np.asfortranarray(A_np.copy())
+        bb = np.asfortranarray(b_np.copy())
+        t0 = time.perf_counter()
+        o.gels(p, a.shape[0], a.shape[1], bb.shape[1], a, bb)
+        dt = time.perf_counter() - t0
+    finally:
+        orc.use_blas(o, None)
+    n = a.shape[1]
+    return bb[:n].copy(), np.triu(a[:n, :n]), dt, kind_blas
+
+
+def kw_backward_error(torch, A, b, x, R):
+    """Karlson-Walden estimate of the normwise least-squares backward error,
+    max over the right-hand sides: ||(A^T A + t^2 I)^{-1/2} A^T r|| / ||x||
+    with t = ||r|| / ||x||, r = b - A x (FP64 on the GPU), and A^T A = R^T R
+    taken from the SVD of an FP64 R factor of A (numpy, on the host)."""
+    import numpy as np
+
+    r = b - A @ x
+    g = (A.t() @ r).cpu().numpy()
+    rn = torch.linalg.norm(r, dim=0).cpu().numpy()
+    xn = torch.linalg.norm(x, dim=0).cpu().numpy()
+    _, s, vh = np.linalg.svd(R)
+    out = 0.0
+    for j in range(g.shape[1]):
+        if xn[j] == 0:
+            continue
+        th = rn[j] / xn[j]
+        out = max(out, float(np.linalg.norm((vh @ g[:, j]) / np.sqrt(s * s + th * th)) / xn[j]))
+    return out
 
 
 def cpu_arm(args, rank, world):
@@ -166,9 +221,11 @@ def cpu_arm(args, rank, world):
     b = np.asfortranarray(A @ rng.standard_normal((N, NRHS)) + 1e-10 * rng.standard_normal((M, NRHS)))
     times = []
     for i in range(args.warmup + args.steps):
-        _, dt, kind_blas = cpu_solve(A, b, threads)
+        _, _, dt, kind_blas = cpu_solve(A, b, threads)
         if i >= args.warmup:
             times.append(dt)
+    # one solve on a single thread beside the all-core figure
+    _, _, dt1, _ = cpu_solve(A, b, 1)
     tot = sum(times)
     val = len(times) / tot
     line = {
@@ -176,8 +233,9 @@ def cpu_arm(args, rank, world):
         "warmup": args.warmup, "ms_per_step": 1e3 * tot / len(times), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": DATA,
         "config": {"workload": WORKLOAD, "m": M, "n": N, "nrhs": NRHS},
-        "cpu_baseline": {"value": val, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": "full 65536x512x16 FP64 QR least-squares solve per step (oracle restatement of Factor + MultQ + SolveTrM, level-3 via %s)" % kind_blas},
+        "cpu_baseline": {"value": val, "unit": UNIT, "cores": threads, "kind": "port", "cpu": cpu_model(),
+                         "single_thread_value": 1.0 / dt1,
+                         "sample": "one full 65536x512x16 FP64 QR least-squares solve per step (oracle restatement of Factor + MultQ + SolveTrM with the reference's blocking; %s via %s on %d threads)" % (BLAS_ROUTINES, kind_blas, threads)},
         "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -401,7 +459,7 @@ def batched_ls_config(torch, dev, count=4096, check_sample=32):
     return out
 
 
-def other_configs(torch, dev, gq, lib, peak64):
+def other_configs(torch, dev, gq, lib, peak64, check=True):
     """The plain FP64 drop-in on the reference's other configurations:
     1024x256 real Factor + GenerateQ, and 4096x4096 complex Factor followed by
     MultQ("L","C") on a 4096x64 block (FP64 throughout)."""
@@ -433,21 +491,49 @@ def other_configs(torch, dev, gq, lib, peak64):
     fm = 4.0 * 2.0 * 64 * n * (2.0 * n - n)
     out["qr_4096x4096_c128"] = {"factor_ms": ms_z, "factor_tflops": fz / ms_z / 1e9, "factor_frac_of_fp64_peak": fz / ms_z / 1e9 / peak64 if peak64 else None,
                                 "multq_4096x64_ms": ms_m, "multq_tflops": fm / ms_m / 1e9}
+    if check:
+        # parity at this size: R and Q^H C against the CPU oracle on the same input
+        import numpy as np
+
+        import oracle as orc
+
+        o = orc.load()
+        blas = orc.find_openblas()
+        if blas:
+            orc.use_blas(o, blas, "scipy_", os.cpu_count() or 1)
+        try:
+            zo = np.asfortranarray(Z0.cpu().numpy())
+            t0 = time.perf_counter()
+            to = o.geqrf("z", n, n, zo)
+            co = np.asfortranarray(C0.cpu().numpy())
+            o.unmqr("z", "L", "C", n, 64, n, zo, to, co)
+            dt = time.perf_counter() - t0
+        finally:
+            orc.use_blas(o, None)
+        zg = Z.cpu().numpy()
+        rg, ro = np.triu(zg), np.triu(zo)
+        out["qr_4096x4096_c128"].update({
+            "r_rel_err_vs_oracle": float(np.linalg.norm(rg - ro) / np.linalg.norm(ro)),
+            "tau_max_abs_err_vs_oracle": float(np.max(np.abs(tz.cpu().numpy() - to))),
+            "multq_rel_err_vs_oracle": float(np.linalg.norm(Cc.cpu().numpy() - co) / np.linalg.norm(co)),
+            "parity_tolerance": 1e-12, "oracle_seconds": dt})
     del Z, Z0, wz
     return out
 
 
-# DRAM traffic of one captured launch per kernel class, from the ncu captures
-# summarised under profiles/ (dram__bytes_read.sum + dram__bytes_write.sum,
-# captured launch's algorithmic bytes): the reported traffic is scaled to the
-# average launch by the algorithmic bytes (traffic grows with the columns and
-# rows processed)
+# DRAM traffic of one launch per kernel class as ncu measured it on this
+# workload (dram__bytes_read.sum + dram__bytes_write.sum of one captured
+# launch, and that launch's algorithmic bytes): the reported traffic is scaled
+# to the average launch by the algorithmic bytes (traffic grows with the
+# columns and rows processed).  Captured launches: the 65,408 x 32 panels, the
+# update and W of the 65,408-row step with 352 trailing columns, one residual
+# r = b - A x and one A^T r of the 65536 x 512 x 16 refinement.
 NCU_TRAFFIC = {
-    "panel": (8.494080e6 + 0.003072e6, 2.0 * 65408 * 32 * 4),              # profiles/k_panel_f32_65536x32.md
-    "panel_cqr": (8.489984e6 + 0.0, 2.0 * 65408 * 32 * 4),                 # profiles/k_panel_cqr_65536x32.md
-    "larfb_update": (100.581632e6 + 32.246784e6, 2.0 * 65408 * 352 * 4 + 65408 * 32 * 4.0),  # profiles/k_update_f32_65536.md
-    "larfb_w": (100.586240e6 + 3.193088e6, 65408 * 352 * 4.0 + 65408 * 32 * 4.0),             # profiles/k_w_f32_65536.md
-    "residual_fp64": (277.589248e6 + 5.319424e6, 65536 * 512 * 8.0 + 2.0 * 65536 * 16 * 8),    # profiles/k_oz_residual_65536x512x16.md
+    "panel": (8.494080e6 + 0.003072e6, 2.0 * 65408 * 32 * 4),
+    "panel_cqr": (8.489984e6 + 0.0, 2.0 * 65408 * 32 * 4),
+    "larfb_update": (100.581632e6 + 32.246784e6, 2.0 * 65408 * 352 * 4 + 65408 * 32 * 4.0),
+    "larfb_w": (100.586240e6 + 3.193088e6, 65408 * 352 * 4.0 + 65408 * 32 * 4.0),
+    "residual_fp64": (277.589248e6 + 5.319424e6, 65536 * 512 * 8.0 + 2.0 * 65536 * 16 * 8),
     "normal_eq_fp64": (285.316352e6 + 3.713280e6, 65536 * 512 * 8.0 + 65536 * 16 * 8.0 + 65536 * 256.0),
 }
 
@@ -632,9 +718,34 @@ def gpu_arm(args, rank, world, local):
     bp.copy_(b)
     gls.gels(Ap, bp, tau, work=pwork)
     x_plain = bp[:N].clone()
+    R_plain = torch.triu(Ap[:N, :N]).cpu().numpy()
     eta_plain, _ = ls_errors(torch, A, b, x_plain)
     ferr_mixed_vs_plain = float(torch.linalg.norm(x_mixed - x_plain) / torch.linalg.norm(x_plain))
     del Ap, bp, pwork
+
+    # ---------------- mixed form in forward mode ----------------------------
+    # (seminormal-equation steps after the Q steps until the correction stops
+    # shrinking: FP64 forward accuracy, not only FP64 backward error)
+    Xf = gq.empty_colmajor(N, NRHS, torch.float64, dev)
+    info_f = None
+    for _ in range(2):
+        _, info_f = gls.gels_refine(A, b, Xf, work=work, forward=True)
+    torch.cuda.synchronize()
+    fwd_steps = max(2, min(args.steps, 10))
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    for _ in range(fwd_steps):
+        _, info_f = gls.gels_refine(A, b, Xf, work=work, forward=True)
+    f1.record(stream)
+    torch.cuda.synchronize()
+    ms_fwd = f0.elapsed_time(f1) / fwd_steps
+    x_fwd = Xf.clone()
+    eta_fwd, _ = ls_errors(torch, A, b, x_fwd)
+    # independent Karlson-Walden estimates of the LS backward error, from the
+    # SVD of the plain FP64 factor's R
+    kw_mixed = kw_backward_error(torch, A, b, x_mixed, R_plain)
+    kw_fwd = kw_backward_error(torch, A, b, x_fwd, R_plain)
+    kw_plain = kw_backward_error(torch, A, b, x_plain, R_plain)
 
     # ---------------- per-kernel profile of the mixed step ------------------
     lib.rnpgpu_timing_enable(1)
@@ -653,27 +764,29 @@ def gpu_arm(args, rank, world, local):
     roofline, roofline_others = kernel_rooflines(prof, tot_ms, top[0], peak64.value, prof_steps)
 
     # ---------------- the other plain configurations ------------------------
-    others = {} if args.no_configs else other_configs(torch, dev, gq, lib, peak64.value)
+    others = {} if args.no_configs else other_configs(torch, dev, gq, lib, peak64.value, check=(rank == 0 and not args.no_cpu))
     if not args.no_configs:
         others["batched"] = batched_config(torch, dev, gq, lib, peak64.value)
         others["batched_ls"] = batched_ls_config(torch, dev)
 
     # ---------------- CPU baseline (rank 0) ---------------------------------
     cpu = None
-    ferr_vs_cpu = None
+    ferr = {"mixed": None, "forward": None, "plain": None}
     if rank == 0 and not args.no_cpu:
         import numpy as np
 
         A_np = np.asfortranarray(A.cpu().numpy())
         b_np = np.asfortranarray(b.cpu().numpy())
         threads = os.cpu_count() or 1
-        x_cpu, dt, kind_blas = cpu_solve(A_np, b_np, threads)
-        x_cpu, dt2, _ = cpu_solve(A_np, b_np, threads)
+        x_cpu, _, dt, kind_blas = cpu_solve(A_np, b_np, threads)
+        _, _, dt2, _ = cpu_solve(A_np, b_np, threads)
         dt = min(dt, dt2)
-        cpu = {"value": 1.0 / dt, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": "2 full solves of the same problem, best taken (oracle restatement of Factor + MultQ + SolveTrM; level-3 via %s)" % kind_blas}
-        xm = x_mixed.cpu().numpy()
-        ferr_vs_cpu = float(np.linalg.norm(xm - x_cpu) / np.linalg.norm(x_cpu))
+        _, _, dt1, _ = cpu_solve(A_np, b_np, 1)
+        cpu = {"value": 1.0 / dt, "unit": UNIT, "cores": threads, "kind": "port", "cpu": cpu_model(),
+               "single_thread_value": 1.0 / dt1,
+               "sample": "2 full solves of the same problem on %d threads (best taken) and 1 on a single thread; oracle restatement of Factor + MultQ + SolveTrM with the reference's blocking, %s via %s" % (threads, BLAS_ROUTINES, kind_blas)}
+        for key, xg in (("mixed", x_mixed), ("forward", x_fwd), ("plain", x_plain)):
+            ferr[key] = float(np.linalg.norm(xg.cpu().numpy() - x_cpu) / np.linalg.norm(x_cpu))
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -685,9 +798,19 @@ def gpu_arm(args, rank, world, local):
                 "h2d_bytes_per_step": A.numel() * 8 + b.numel() * 8, "d2h_bytes_per_step": X.numel() * 8},
         "gpu_launches": int(launches),
         "mixed": {"iterations": info["iterations"] if info else None, "converged": info["converged"] if info else None,
-                  "backward_error": eta_mixed, "backward_error_bound": 10 * N * 2.0 ** -52,
-                  "forward_error_vs_cpu_fp64_oracle": ferr_vs_cpu, "forward_error_vs_plain_gpu": ferr_mixed_vs_plain},
-        "plain_fp64": {"solves_per_s": 1e3 / ms_plain, "ms_per_solve": ms_plain, "backward_error": eta_plain,
+                  "backward_error": kw_mixed, "backward_error_bound": 10 * N * 2.0 ** -52,
+                  "backward_error_kind": "Karlson-Walden estimate of the normwise LS backward error (max over RHS), from r = b - A x in FP64 and the SVD of the plain FP64 R",
+                  "driver_backward_error_bound_mu": info["backward_error"] if info else None,
+                  "normal_residual": eta_mixed,
+                  "normal_residual_kind": "max_j ||A^T r_j|| / (||A||_F (||A||_F ||x_j|| + ||b_j||))",
+                  "forward_error_vs_cpu_fp64_oracle": ferr["mixed"], "forward_error_vs_plain_gpu": ferr_mixed_vs_plain},
+        "mixed_forward_mode": {"solves_per_s": 1e3 / ms_fwd, "ms_per_solve": ms_fwd,
+                               "iterations": info_f["iterations"] if info_f else None, "converged": info_f["converged"] if info_f else None,
+                               "backward_error": kw_fwd, "driver_backward_error_bound_mu": info_f["backward_error"] if info_f else None,
+                               "normal_residual": eta_fwd, "forward_error_vs_cpu_fp64_oracle": ferr["forward"],
+                               "speedup_vs_plain": ms_plain / ms_fwd},
+        "plain_fp64": {"solves_per_s": 1e3 / ms_plain, "ms_per_solve": ms_plain, "backward_error": kw_plain, "normal_residual": eta_plain,
+                       "forward_error_vs_cpu_fp64_oracle": ferr["plain"],
                        "tflops": solve_flops(M, N, NRHS) / (ms_plain * 1e-3) / 1e12,
                        "profile_ms": {k: v[1] for k, v in sorted(prof_plain.items(), key=lambda kv: -kv[1][1])}},
         "speedup_mixed_vs_plain": ms_plain / ms,

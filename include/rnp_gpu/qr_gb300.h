@@ -51,10 +51,11 @@ int rnpgpu_zgeqrf(size_t m, size_t n, rnpgpu_complex_double *a, size_t lda, rnpg
  *      same factorization as rnpgpu_dgeqrf for callers that cannot allocate
  *      device memory (frameworks that own and pre-budget it, fixed-budget
  *      real-time loops).  It uses an 8 MiB scratch array built into the
- *      library, so n is limited to about 16,000 columns (status -2 beyond,
- *      message in rnpgpu_get_last_error()).  The first call on a device looks
- *      up the array's address and should come before any stream capture;
- *      calls that overlap on the GPU share the array and race. ---- */
+ *      library and always factors in the serial order, so n up to 16,000
+ *      columns always fits (status -2 past about 16,100, message in
+ *      rnpgpu_get_last_error()).  The first call on a device looks up the
+ *      array's address and should come before any stream capture; calls that
+ *      overlap on the GPU share the array and race. ---- */
 int rnpgpu_dgeqrf_noalloc(size_t m, size_t n, double *a, size_t lda, double *tau);
 
 /* ---- Factor_unblocked: RNP::LA::QR::Factor_unblocked (RNP/LA/QR.hpp:78-102), _geqr2; work: n ---- */
@@ -102,8 +103,9 @@ const char *rnpgpu_version(void);
 int rnpgpu_device_status(int reset);
 /* C = alpha op(A) op(B) + beta C in FP32 on the tensor cores (each operand
  * split into three BF16 terms, six products, FP32 accumulation); op "N" or
- * "T", beta 0 or 1.  No counterpart in the reference: the contraction of the
- * FP32 trailing updates, exported for checking. */
+ * "T", beta 0 or 1.  No counterpart in the reference: the tensor-core
+ * contraction the library uses for short FP32 contractions (K <= 64) that are
+ * not a trailing update, exported for checking. */
 int rnpgpu_sgemm_tc(const char *transa, const char *transb, size_t m, size_t n, size_t k, float alpha, const float *a, size_t lda, const float *b, size_t ldb, float beta, float *c, size_t ldc);
 /* Number of kernels this library has launched in this process. */
 unsigned long long rnpgpu_launch_count(void);

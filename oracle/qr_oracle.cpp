@@ -62,6 +62,20 @@ struct ExtBlas {
     void (*ctrmm)(const char *, const char *, const char *, const char *, const fint *, const fint *, const cf *, const cf *, const fint *, cf *, const fint *, size_t, size_t, size_t, size_t) = nullptr;
     void (*dtrsm)(const char *, const char *, const char *, const char *, const fint *, const fint *, const double *, const double *, const fint *, double *, const fint *, size_t, size_t, size_t, size_t) = nullptr;
     void (*ztrsm)(const char *, const char *, const char *, const char *, const fint *, const fint *, const cd *, const cd *, const fint *, cd *, const fint *, size_t, size_t, size_t, size_t) = nullptr;
+    void (*dgemv)(const char *, const fint *, const fint *, const double *, const double *, const fint *, const double *, const fint *, const double *, double *, const fint *, size_t) = nullptr;
+    void (*zgemv)(const char *, const fint *, const fint *, const cd *, const cd *, const fint *, const cd *, const fint *, const cd *, cd *, const fint *, size_t) = nullptr;
+    void (*sgemv)(const char *, const fint *, const fint *, const float *, const float *, const fint *, const float *, const fint *, const float *, float *, const fint *, size_t) = nullptr;
+    void (*cgemv)(const char *, const fint *, const fint *, const cf *, const cf *, const fint *, const cf *, const fint *, const cf *, cf *, const fint *, size_t) = nullptr;
+    void (*dger)(const fint *, const fint *, const double *, const double *, const fint *, const double *, const fint *, double *, const fint *) = nullptr;
+    void (*zgerc)(const fint *, const fint *, const cd *, const cd *, const fint *, const cd *, const fint *, cd *, const fint *) = nullptr;
+    void (*sger)(const fint *, const fint *, const float *, const float *, const fint *, const float *, const fint *, float *, const fint *) = nullptr;
+    void (*cgerc)(const fint *, const fint *, const cf *, const cf *, const fint *, const cf *, const fint *, cf *, const fint *) = nullptr;
+    void (*dtrmv)(const char *, const char *, const char *, const fint *, const double *, const fint *, double *, const fint *, size_t, size_t, size_t) = nullptr;
+    void (*ztrmv)(const char *, const char *, const char *, const fint *, const cd *, const fint *, cd *, const fint *, size_t, size_t, size_t) = nullptr;
+    void (*strmv)(const char *, const char *, const char *, const fint *, const float *, const fint *, float *, const fint *, size_t, size_t, size_t) = nullptr;
+    void (*ctrmv)(const char *, const char *, const char *, const fint *, const cf *, const fint *, cf *, const fint *, size_t, size_t, size_t) = nullptr;
+    void (*strsm)(const char *, const char *, const char *, const char *, const fint *, const fint *, const float *, const float *, const fint *, float *, const fint *, size_t, size_t, size_t, size_t) = nullptr;
+    void (*ctrsm)(const char *, const char *, const char *, const char *, const fint *, const fint *, const cf *, const cf *, const fint *, cf *, const fint *, size_t, size_t, size_t, size_t) = nullptr;
     void (*set_threads)(int) = nullptr;
 };
 static ExtBlas g_ext;
@@ -97,8 +111,46 @@ ORC_EXT_TR(float, ext_trmm, strmm)
 ORC_EXT_TR(cf, ext_trmm, ctrmm)
 ORC_EXT_TR(double, ext_trsm, dtrsm)
 ORC_EXT_TR(cd, ext_trsm, ztrsm)
-template <> inline bool ext_trsm<float>(const char *, const char *, const char *, const char *, size_t, size_t, float, const float *, size_t, float *, size_t) { return false; }
-template <> inline bool ext_trsm<cf>(const char *, const char *, const char *, const char *, size_t, size_t, cf, const cf *, size_t, cf *, size_t) { return false; }
+ORC_EXT_TR(float, ext_trsm, strsm)
+ORC_EXT_TR(cf, ext_trsm, ctrsm)
+
+// level 2: gemv, ger/gerc, trmv (src/BLAS_mix.cpp:112,122,248,256,374,384
+// forward the same calls of the reference to the Fortran BLAS)
+#define ORC_EXT_GEMV(T, fn)                                                                            \
+    inline bool ext_gemv(char trans, size_t m, size_t n, T alpha, const T *a, size_t lda, const T *x, size_t incx, T beta, T *y, size_t incy) { \
+        if (!g_use_ext || !g_ext.fn || m == 0 || n == 0) return false;                                 \
+        const char t[2] = {trans, 0};                                                                  \
+        fint M = (fint)m, N = (fint)n, LA = (fint)(lda ? lda : 1), IX = (fint)incx, IY = (fint)incy;   \
+        g_ext.fn(t, &M, &N, &alpha, a, &LA, x, &IX, &beta, y, &IY, 1);                                  \
+        return true;                                                                                   \
+    }
+ORC_EXT_GEMV(double, dgemv)
+ORC_EXT_GEMV(cd, zgemv)
+ORC_EXT_GEMV(float, sgemv)
+ORC_EXT_GEMV(cf, cgemv)
+#define ORC_EXT_GER(T, fn)                                                                             \
+    inline bool ext_gerc(size_t m, size_t n, T alpha, const T *x, size_t incx, const T *y, size_t incy, T *a, size_t lda) { \
+        if (!g_use_ext || !g_ext.fn || m == 0 || n == 0) return false;                                 \
+        fint M = (fint)m, N = (fint)n, LA = (fint)(lda ? lda : 1), IX = (fint)incx, IY = (fint)incy;   \
+        g_ext.fn(&M, &N, &alpha, x, &IX, y, &IY, a, &LA);                                              \
+        return true;                                                                                   \
+    }
+ORC_EXT_GER(double, dger)
+ORC_EXT_GER(cd, zgerc)
+ORC_EXT_GER(float, sger)
+ORC_EXT_GER(cf, cgerc)
+#define ORC_EXT_TRMV(T, fn)                                                                            \
+    inline bool ext_trmv_upper(char trans, size_t n, const T *a, size_t lda, T *x) {                   \
+        if (!g_use_ext || !g_ext.fn || n == 0) return false;                                           \
+        const char t[2] = {trans, 0};                                                                  \
+        fint N = (fint)n, LA = (fint)(lda ? lda : 1), IX = 1;                                          \
+        g_ext.fn("U", t, "N", &N, a, &LA, x, &IX, 1, 1, 1);                                            \
+        return true;                                                                                   \
+    }
+ORC_EXT_TRMV(double, dtrmv)
+ORC_EXT_TRMV(cd, ztrmv)
+ORC_EXT_TRMV(float, strmv)
+ORC_EXT_TRMV(cf, ctrmv)
 
 // ---------------------------------------------------------------------------
 // Level-1/2/3 helpers with reference-BLAS meaning (plain loops).
@@ -145,6 +197,7 @@ template <class T> void scal(size_t n, T a, T *x, size_t incx) {
 
 // y := alpha*op(A)*x + beta*y   (gemv)
 template <class T> void gemv(char trans, size_t m, size_t n, T alpha, const T *a, size_t lda, const T *x, size_t incx, T beta, T *y, size_t incy) {
+    if (ext_gemv(trans, m, n, alpha, a, lda, x, incx, beta, y, incy)) return;
     if (trans == 'N') {
         for (size_t i = 0; i < m; ++i) y[i * incy] = (beta == T(0)) ? T(0) : beta * y[i * incy];
         for (size_t j = 0; j < n; ++j) {
@@ -163,6 +216,7 @@ template <class T> void gemv(char trans, size_t m, size_t n, T alpha, const T *a
 
 // A := A + alpha*x*y^H   (ger / gerc; RNP "ConjugateRank1Update")
 template <class T> void gerc(size_t m, size_t n, T alpha, const T *x, size_t incx, const T *y, size_t incy, T *a, size_t lda) {
+    if (ext_gerc(m, n, alpha, x, incx, y, incy, a, lda)) return;
     for (size_t j = 0; j < n; ++j) {
         T t = alpha * Tr<T>::conj(y[j * incy]);
         if (t == T(0)) continue;
@@ -172,6 +226,7 @@ template <class T> void gerc(size_t m, size_t n, T alpha, const T *x, size_t inc
 
 // x := op(A)*x, A upper triangular, non-unit  (trmv "U", trans, "N")
 template <class T> void trmv_upper(char trans, size_t n, const T *a, size_t lda, T *x) {
+    if (ext_trmv_upper(trans, n, a, lda, x)) return;
     if (trans == 'N') {
         for (size_t j = 0; j < n; ++j) {
             T t = x[j];
@@ -690,7 +745,9 @@ extern "C" void oracle_slarnv(int dist, int *iseed, size_t n, float *x) { larnv_
 extern "C" void oracle_zlarnv(int dist, int *iseed, size_t n, cd *x) { larnv_cplx<double>(dist, n, x, iseed); }
 extern "C" void oracle_clarnv(int dist, int *iseed, size_t n, cf *x) { larnv_cplx<float>(dist, n, x, iseed); }
 
-// CPU baseline only: route the level-3 calls through an external Fortran BLAS
+// CPU baseline only: route the level-2 and level-3 calls (gemv, ger/gerc,
+// trmv, gemm, trmm, trsm: every routine the reference forwards to its BLAS)
+// through an external Fortran BLAS
 // (e.g. an OpenBLAS shared library; symbols looked up as prefix + "dgemm_").
 // Returns 0 on success, -1 if the library or a symbol is missing.
 extern "C" int oracle_use_blas(const char *path, const char *prefix, int nthreads) {
@@ -710,8 +767,23 @@ extern "C" int oracle_use_blas(const char *path, const char *prefix, int nthread
     g_ext.ctrmm = (decltype(g_ext.ctrmm))sym("ctrmm_");
     g_ext.dtrsm = (decltype(g_ext.dtrsm))sym("dtrsm_");
     g_ext.ztrsm = (decltype(g_ext.ztrsm))sym("ztrsm_");
+    g_ext.strsm = (decltype(g_ext.strsm))sym("strsm_");
+    g_ext.ctrsm = (decltype(g_ext.ctrsm))sym("ctrsm_");
+    g_ext.dgemv = (decltype(g_ext.dgemv))sym("dgemv_");
+    g_ext.zgemv = (decltype(g_ext.zgemv))sym("zgemv_");
+    g_ext.sgemv = (decltype(g_ext.sgemv))sym("sgemv_");
+    g_ext.cgemv = (decltype(g_ext.cgemv))sym("cgemv_");
+    g_ext.dger = (decltype(g_ext.dger))sym("dger_");
+    g_ext.zgerc = (decltype(g_ext.zgerc))sym("zgerc_");
+    g_ext.sger = (decltype(g_ext.sger))sym("sger_");
+    g_ext.cgerc = (decltype(g_ext.cgerc))sym("cgerc_");
+    g_ext.dtrmv = (decltype(g_ext.dtrmv))sym("dtrmv_");
+    g_ext.ztrmv = (decltype(g_ext.ztrmv))sym("ztrmv_");
+    g_ext.strmv = (decltype(g_ext.strmv))sym("strmv_");
+    g_ext.ctrmv = (decltype(g_ext.ctrmv))sym("ctrmv_");
     g_ext.set_threads = (decltype(g_ext.set_threads))sym("openblas_set_num_threads");
-    if (!g_ext.dgemm || !g_ext.zgemm || !g_ext.dtrmm || !g_ext.ztrmm) { g_use_ext = false; return -1; }
+    if (!g_ext.dgemm || !g_ext.zgemm || !g_ext.dtrmm || !g_ext.ztrmm || !g_ext.dgemv || !g_ext.zgemv || !g_ext.dger || !g_ext.zgerc ||
+        !g_ext.dtrmv || !g_ext.ztrmv) { g_use_ext = false; return -1; }
     if (g_ext.set_threads && nthreads > 0) g_ext.set_threads(nthreads);
     g_use_ext = true;
     return 0;

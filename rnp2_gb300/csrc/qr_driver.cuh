@@ -515,7 +515,10 @@ inline LookAhead *lookahead_ctx() {
 // those columns again.  The results are the same as in the serial order (the
 // same operations on the same data).  Without the larger workspace, inside
 // stream capture, or for a single trailing block the serial order is used.
-template <class T> int geqrf(size_t m, size_t n, T *a, size_t lda, T *tau, size_t *lwork, T *work, T *Tstore = nullptr, const CqrWs *cqr = nullptr) {
+//
+// lookahead_ok = false keeps the serial order (no side stream or events are
+// created, nothing beyond the serial plan is asked of the work block).
+template <class T> int geqrf(size_t m, size_t n, T *a, size_t lda, T *tau, size_t *lwork, T *work, T *Tstore = nullptr, const CqrWs *cqr = nullptr, bool lookahead_ok = true) {
     if (lwork == nullptr) return -6;
     const size_t k = std::min(m, n);
     if (k == 0) return kOk;
@@ -530,7 +533,7 @@ template <class T> int geqrf(size_t m, size_t n, T *a, size_t lda, T *tau, size_
     if (tau == nullptr) return -5;
     const size_t nb = GpuTuning::nb;
     cudaStream_t st = current_stream();
-    bool ahead = geqrf_lookahead<T>() && n > 2 * nb && k > nb && elems_for<T>(geqrf_bytes<T>(m, n, smax)) <= *lwork;
+    bool ahead = lookahead_ok && geqrf_lookahead<T>() && n > 2 * nb && k > nb && elems_for<T>(geqrf_bytes<T>(m, n, smax)) <= *lwork;
     if (ahead) {
         cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
         if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) ahead = false;

@@ -16,10 +16,13 @@
 //    up with cudaGetSymbolAddress once per device, with that device current,
 //    by the first call made on that device; make that first call before any
 //    stream capture.
-//  * Size limit: the factorization of an m x n matrix needs about
-//    43 KB + 8 KB + 512 * n bytes of scratch, so n up to about 16,000 columns
-//    (any m) fits; larger n is rejected with status -2 and a message in
-//    rnpgpu_get_last_error().
+//  * Size limit: this entry point always factors in the serial order (the
+//    look-ahead order of rnpgpu_dgeqrf would need a second update workspace,
+//    and a side stream and two events created on first use).  Its plan needs
+//    the panel records (about 120 KB on a 152-SM GPU), one 32 x 32 T factor
+//    and 512 * n bytes for W, so n up to 16,000 columns (any m) always fits;
+//    past about 16,100 columns the call is rejected with status -2 and a
+//    message in rnpgpu_get_last_error().
 //  * Every call uses the same array and leaves its contents behind.  The
 //    grid-barrier counter and error word that must start at zero are cleared
 //    before each panel launch; every other region is written before it is
@@ -76,8 +79,8 @@ extern "C" int rnpgpu_dgeqrf_noalloc(size_t m, size_t n, double *a, size_t lda, 
     if (k == 0) return rnpgpu::kOk;
     if (lda < (m > 1 ? m : 1)) return -4;
     if (m > (size_t)INT32_MAX || n > (size_t)INT32_MAX) return -1;
-    // the smallest plan (no split-K partials) must fit in the built-in scratch
-    const size_t need = rnpgpu::elems_for<double>(rnpgpu::geqrf_bytes<double>(m, n, 1)) * sizeof(double);
+    // the smallest serial plan (one split of W) must fit in the built-in scratch
+    const size_t need = rnpgpu::elems_for<double>(rnpgpu::geqrf_serial_bytes<double>(m, n, 1)) * sizeof(double);
     if (need > kFactorScratchBytes) {
         char msg[200];
         snprintf(msg, sizeof(msg), "rnpgpu_dgeqrf_noalloc: a %zu x %zu factorization needs %zu bytes of scratch; the built-in scratch holds %zu", m, n, need, kFactorScratchBytes);
@@ -90,5 +93,5 @@ extern "C" int rnpgpu_dgeqrf_noalloc(size_t m, size_t n, double *a, size_t lda, 
     int rc = factor_scratch(&scratch);
     if (rc) return rc;
     size_t lwork = kFactorScratchBytes / sizeof(double);
-    return rnpgpu::geqrf<double>(m, n, a, lda, tau, &lwork, static_cast<double *>(scratch));
+    return rnpgpu::geqrf<double>(m, n, a, lda, tau, &lwork, static_cast<double *>(scratch), nullptr, nullptr, false);
 }

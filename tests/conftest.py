@@ -80,3 +80,21 @@ def gpu_available():
         return torch.cuda.is_available()
     except Exception:
         return False
+
+
+@pytest.fixture
+def oracle_blas(oracle):
+    """The oracle with every level-2/3 call routed through OpenBLAS on all
+    host cores, as the reference forwards them to its BLAS: for checks at the
+    full workload sizes, where the restatement's plain loops take minutes.
+    Skips where no OpenBLAS is available; switched back to the plain loops
+    afterwards."""
+    import oracle as orc
+
+    blas = orc.find_openblas()
+    if not blas or orc.use_blas(oracle, blas, "scipy_", os.cpu_count() or 1) != 0:
+        pytest.skip("no OpenBLAS for the oracle")
+    try:
+        yield oracle
+    finally:
+        orc.use_blas(oracle, None)

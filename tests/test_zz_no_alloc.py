@@ -86,3 +86,23 @@ def test_noalloc_rejects_too_wide_matrices():
     rc = noalloc_fn()(40000, 40000, buf.data_ptr(), 40000, buf.data_ptr())
     assert rc == -2
     assert b"scratch" in rnp2_gb300.lib().rnpgpu_get_last_error()
+
+
+def test_noalloc_width_limit():
+    # the documented limit: 16,000 columns always fit (W alone needs 512 bytes
+    # a column of the 8 MiB scratch), and the result is the regular Factor's;
+    # 16,400 columns need more than the whole scratch and are rejected
+    m, n = 64, 16000
+    A = random_colmajor(m, n, 3)
+    A1 = gq.to_colmajor(A)
+    A2 = gq.to_colmajor(A)
+    t1 = factor_with_work(A1)
+    t2 = factor_noalloc(A2)
+    torch.cuda.synchronize()
+    R1, V1 = split_factor(A1.cpu().numpy(), m, n)
+    R2, V2 = split_factor(A2.cpu().numpy(), m, n)
+    assert rel(R2, R1) <= R_TOL["d"]
+    assert rel(V2, V1) <= V_TOL["d"]
+    assert np.max(np.abs(t2.cpu().numpy() - t1.cpu().numpy())) <= 10 * R_TOL["d"]
+    buf = torch.zeros(16, dtype=torch.float64, device="cuda")
+    assert noalloc_fn()(m, 16400, buf.data_ptr(), m, buf.data_ptr()) == -2
