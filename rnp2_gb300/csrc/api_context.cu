@@ -7,6 +7,7 @@
 #include <cstring>
 #include <cstdio>
 #include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -58,6 +59,61 @@ void ktimer_end(cudaStream_t st) {
     t_timer.open.pop_back();
     cudaEventRecord(t.stop, st);
     t_timer.done.push_back(t);
+}
+
+// ---------------------------------------------------------------------------
+// Kernel attributes, set once per (kernel host stub, device).  nvcc gives a
+// kernel's host stub internal linkage, so a kernel template that several
+// units instantiate has one stub and one device copy per unit; keying on the
+// stub a launch site actually uses keeps the attribute on the copy that runs.
+// ---------------------------------------------------------------------------
+struct AttrKey {
+    const void *kern;
+    int dev;
+    bool operator<(const AttrKey &o) const { return kern != o.kern ? kern < o.kern : dev < o.dev; }
+};
+struct AttrState {
+    int smem = -1;
+    bool carveout = false;
+};
+static std::mutex g_attr_mu;
+static std::map<AttrKey, AttrState> g_attr;
+static std::map<std::pair<AttrKey, std::pair<int, size_t> >, int> g_occ;
+
+int kernel_attr(const void *kern, int dyn_smem, bool max_carveout) {
+    int dev = 0;
+    RNPGPU_CHECK(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(g_attr_mu);
+    AttrState &a = g_attr[AttrKey{kern, dev}];
+    if (dyn_smem > a.smem) {
+        RNPGPU_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn_smem));
+        a.smem = dyn_smem;
+    }
+    if (max_carveout && !a.carveout) {
+        RNPGPU_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared));
+        a.carveout = true;
+    }
+    return kOk;
+}
+
+int kernel_blocks_per_sm(const void *kern, int threads, size_t dyn_smem) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return 1;
+    }
+    std::lock_guard<std::mutex> lk(g_attr_mu);
+    auto key = std::make_pair(AttrKey{kern, dev}, std::make_pair(threads, dyn_smem));
+    auto it = g_occ.find(key);
+    if (it != g_occ.end()) return it->second;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, dyn_smem) != cudaSuccess) {
+        cudaGetLastError();
+        per_sm = 1;
+    }
+    per_sm = std::max(per_sm, 1);
+    g_occ[key] = per_sm;
+    return per_sm;
 }
 
 // FP64 / FP32 FMA throughput probe (independent FMA chains, full occupancy)

@@ -40,15 +40,9 @@ template <int MR> constexpr int tile_for() { return MR >= 512 ? 16 : 32; }
 
 template <class T, int NT, int NB, int MR> int launch_batched_cfg(const BatchDesc *desc, int count, T *A, T *tau, unsigned *queue, cudaStream_t st) {
     typedef BatchSmem<T, NB, MR, tile_for<MR>()> L;
-    static std::once_flag once;
-    static cudaError_t attr = cudaSuccess;
-    static int per_sm = 1;
-    std::call_once(once, []() {
-        attr = cudaFuncSetAttribute((const void *)k_geqrf_batched<T, NT, NB, MR, tile_for<MR>()>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::kBytes);
-        if (attr == cudaSuccess) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_geqrf_batched<T, NT, NB, MR, tile_for<MR>()>, NT, L::kBytes);
-        if (per_sm < 1) per_sm = 1;
-    });
-    RNPGPU_CHECK(attr);
+    const void *kern = (const void *)k_geqrf_batched<T, NT, NB, MR, tile_for<MR>()>;
+    if (int rc = kernel_attr(kern, (int)L::kBytes)) return rc;
+    const int per_sm = kernel_blocks_per_sm(kern, NT, L::kBytes);
     const int grid = std::max(1, std::min(count, device_facts().sm_count * per_sm));
     KScope ks("geqrf_batched", st);
     k_geqrf_batched<T, NT, NB, MR, tile_for<MR>()><<<grid, NT, L::kBytes, st>>>(desc, count, A, tau, queue);
@@ -58,15 +52,9 @@ template <class T, int NT, int NB, int MR> int launch_batched_cfg(const BatchDes
 
 template <class T> int launch_batched_warp(const BatchDesc *desc, int count, T *A, T *tau, unsigned *queue, cudaStream_t st) {
     constexpr size_t smem = (size_t)kWarpsPerBlock * kWarpRows * kWarpLd * sizeof(T);
-    static std::once_flag once;
-    static cudaError_t attr = cudaSuccess;
-    static int per_sm = 1;
-    std::call_once(once, []() {
-        attr = cudaFuncSetAttribute((const void *)k_geqrf_warp<T, kWarpsPerBlock>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (attr == cudaSuccess) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_geqrf_warp<T, kWarpsPerBlock>, kWarpsPerBlock * 32, smem);
-        if (per_sm < 1) per_sm = 1;
-    });
-    RNPGPU_CHECK(attr);
+    const void *kern = (const void *)k_geqrf_warp<T, kWarpsPerBlock>;
+    if (int rc = kernel_attr(kern, (int)smem)) return rc;
+    const int per_sm = kernel_blocks_per_sm(kern, kWarpsPerBlock * 32, smem);
     const int blocks = (count + kWarpsPerBlock - 1) / kWarpsPerBlock;
     const int grid = std::max(1, std::min(blocks, device_facts().sm_count * per_sm));
     KScope ks("geqrf_batched", st);
@@ -114,12 +102,7 @@ template <class T> int launch_batched(int cls, BatchConfig cfg, const BatchDesc 
 
 // one warp per problem for the least-squares solves; MT = rows / 32 per lane
 template <class TH, class TL, int MT> int launch_ls_cls(LsBatchArgs<TH, TL> q, cudaStream_t st) {
-    static std::once_flag once;
-    static int per_sm = 1;
-    std::call_once(once, []() {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ls_batched<TH, TL, MT>, 256, 0);
-        if (per_sm < 1) per_sm = 1;
-    });
+    const int per_sm = kernel_blocks_per_sm((const void *)k_ls_batched<TH, TL, MT>, 256, 0);
     const int warps = device_facts().sm_count * per_sm * 8;
     const int grid = std::max(1, (std::min(q.count, warps) + 7) / 8);
     KScope ks(q.refine ? "ls_refine_batched" : "ls_solve_batched", st);

@@ -835,13 +835,7 @@ struct OzWork {
     }
 };
 
-inline int oz_attr() {
-    static std::once_flag once;
-    static cudaError_t attr = cudaSuccess;
-    std::call_once(once, []() { attr = cudaFuncSetAttribute((const void *)oz::k_oz<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, oz::kSmem); });
-    RNPGPU_CHECK(attr);
-    return kOk;
-}
+inline int oz_attr() { return kernel_attr((const void *)oz::k_oz<0>, oz::kSmem); }
 
 // once per A: column scales, the packed digits, and the FP32 copy Af when
 // given (with ||Af(:,k)||^2 into sumsq when both are given)

@@ -15,6 +15,7 @@
 #include <algorithm>
 #include <type_traits>
 #include <cstring>
+#include <cstdio>
 #include <mutex>
 
 namespace rnpgpu {
@@ -33,6 +34,12 @@ cudaStream_t current_stream();
 void set_last_error(const char *msg);
 const DeviceFacts &device_facts();
 int *device_status_ptr();  // library-wide device status word
+
+// Kernel attributes per launch site's kernel (api_context.cu): raise the
+// dynamic shared memory limit to dyn_smem (and prefer the largest shared
+// memory carveout); blocks of a kernel one SM holds (cached).
+int kernel_attr(const void *kern, int dyn_smem, bool max_carveout = false);
+int kernel_blocks_per_sm(const void *kern, int threads, size_t dyn_smem);
 
 // Launch accounting and optional per-kernel-class timing (CUDA events on the
 // launching stream; only while rnpgpu_timing_enable(1) is in effect).
@@ -100,12 +107,7 @@ template <class T> size_t elems_for(size_t bytes) { return (bytes + 256 + sizeof
 // Contraction launcher
 // ---------------------------------------------------------------------------
 template <int BN> int launch_gemm_tc_bn(const GemmArgs<float> &g, int nsplit, cudaStream_t st) {
-    static std::once_flag once;
-    static cudaError_t attr = cudaSuccess;
-    std::call_once(once, []() {
-        attr = cudaFuncSetAttribute((const void *)tc::k_gemm_tc<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SmemLayout<BN>::kBytes);
-    });
-    RNPGPU_CHECK(attr);
+    if (int rc = kernel_attr((const void *)tc::k_gemm_tc<BN>, tc::SmemLayout<BN>::kBytes)) return rc;
     int *err = device_status_ptr();
     if (err == nullptr) return kErrCuda;
     dim3 grid((g.M + tc::kBM - 1) / tc::kBM, (g.N + BN - 1) / BN, nsplit);
@@ -134,16 +136,8 @@ inline bool is_trailing_update(const GemmArgs<float> &g, int nsplit) {
 // two blocks of the update kernel per SM (96 KB of shared memory each: the
 // largest carveout), as many blocks as SMs hold: each walks its row tiles
 inline int launch_update_f32(const GemmArgs<float> &g, cudaStream_t st) {
-    static std::once_flag once;
-    static cudaError_t attr = cudaSuccess;
-    std::call_once(once, []() {
-        const void *ks[2] = {(const void *)k_update_f32<true>, (const void *)k_update_f32<false>};
-        for (const void *k : ks) {
-            if (attr == cudaSuccess) attr = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kUfSmem);
-            if (attr == cudaSuccess) attr = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
-        }
-    });
-    RNPGPU_CHECK(attr);
+    if (int rc = kernel_attr((const void *)k_update_f32<true>, (int)kUfSmem, true)) return rc;
+    if (int rc = kernel_attr((const void *)k_update_f32<false>, (int)kUfSmem, true)) return rc;
     UpdArgs u;
     u.V = g.A; u.ldv = g.lda; u.W = g.B; u.ldw = g.ldb; u.C = g.D; u.ldc = g.ldd;
     u.M = g.M; u.N = g.N; u.K = g.K;
@@ -161,16 +155,8 @@ inline int launch_update_f32(const GemmArgs<float> &g, cudaStream_t st) {
 // maxsplit.
 inline bool w_partials_ok(int M, int N, int K) { return M >= 1024 && N <= kUpdMaxN && K <= 32; }
 inline int launch_w_partials(const float *C, size_t ldc, const float *V, size_t ldv, float *P, int M, int N, int K, int maxsplit, int &nsplit, cudaStream_t st) {
-    static std::once_flag once;
-    static cudaError_t attr = cudaSuccess;
-    std::call_once(once, []() {
-        const void *ks[2] = {(const void *)k_w_f32<true>, (const void *)k_w_f32<false>};
-        for (const void *k : ks) {
-            if (attr == cudaSuccess) attr = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kWfSmem);
-            if (attr == cudaSuccess) attr = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
-        }
-    });
-    RNPGPU_CHECK(attr);
+    if (int rc = kernel_attr((const void *)k_w_f32<true>, (int)kWfSmem, true)) return rc;
+    if (int rc = kernel_attr((const void *)k_w_f32<false>, (int)kWfSmem, true)) return rc;
     const int nkb = (M + 127) / 128;
     nsplit = std::max(1, std::min(std::min(nkb, maxsplit), device_facts().sm_count));
     UpdArgs u;
@@ -210,6 +196,35 @@ template <class T> int launch_gemm(GemmArgs<T> g, int nsplit, cudaStream_t st, c
         k_gemm<T, 64, 64, 16, 4, 4><<<grid, 256, 0, st>>>(g);
     }
     RNPGPU_CHECK_LAUNCH();
+    return kOk;
+}
+
+// Cooperative launch; on failure the message names the kernel, its grid and
+// how many of its blocks an SM holds.
+inline int coop_launch(const char *name, const void *kern, int grid, int threads, void **args, size_t smem, cudaStream_t st) {
+    const cudaError_t e = cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(threads), args, smem, st);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        int per_sm = -1;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem) != cudaSuccess) {
+            cudaGetLastError();
+            per_sm = -1;
+        }
+        int per_sm0 = -1;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm0, kern, threads, 0) != cudaSuccess) {
+            cudaGetLastError();
+            per_sm0 = -1;
+        }
+        cudaFuncAttributes fa{};
+        if (cudaFuncGetAttributes(&fa, kern) != cudaSuccess) cudaGetLastError();
+        char msg[400];
+        snprintf(msg, sizeof msg, "%s: %s (grid %d x %d threads, %zu B dynamic shared memory; %d blocks per SM fit, %d without dynamic shared memory; %d SMs; %d registers, %zu B static shared memory, max %d threads, max dynamic %d B)",
+                 name, cudaGetErrorString(e), grid, threads, smem, per_sm, per_sm0, device_facts().sm_count, fa.numRegs, (size_t)fa.sharedSizeBytes, fa.maxThreadsPerBlock,
+                 fa.maxDynamicSharedSizeBytes);
+        set_last_error(msg);
+        return kErrCuda;
+    }
+    note_launch();
     return kOk;
 }
 
@@ -348,12 +363,7 @@ constexpr size_t kPanelSmemMax = 180 * 1024;
 
 template <class T> int panel_factor(int M, int N, T *A, size_t lda, T *tau, T *Tm, int ldt, const PanelWs<T> &ws, cudaStream_t st) {
     const int G = panel_grid(M, ws.gmax);
-    static std::once_flag attr_once;
-    static cudaError_t attr_err = cudaSuccess;
-    std::call_once(attr_once, []() {
-        attr_err = cudaFuncSetAttribute((const void *)k_panel<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPanelSmemMax);
-    });
-    RNPGPU_CHECK(attr_err);
+    if (int rc = kernel_attr((const void *)k_panel<T, true>, (int)kPanelSmemMax)) return rc;
     PanelArgs<T> p;
     p.A = A; p.lda = lda; p.M = M; p.N = N; p.tau = tau; p.Tm = Tm; p.ldt = ldt;
     p.rec = ws.rec;
@@ -364,12 +374,8 @@ template <class T> int panel_factor(int M, int N, T *A, size_t lda, T *tau, T *T
     void *args[] = {&p};
     KScope ks("panel", st);
     const size_t smem = (size_t)p.rows_per_cta * N * sizeof(T);
-    if (smem <= kPanelSmemMax && G <= device_facts().sm_count)
-        RNPGPU_CHECK(cudaLaunchCooperativeKernel((const void *)k_panel<T, true>, dim3(G), dim3(kPanelThreads), args, smem, st));
-    else
-        RNPGPU_CHECK(cudaLaunchCooperativeKernel((const void *)k_panel<T, false>, dim3(G), dim3(kPanelThreads), args, 0, st));
-    note_launch();
-    return kOk;
+    if (smem <= kPanelSmemMax && G <= device_facts().sm_count) return coop_launch("k_panel", (const void *)k_panel<T, true>, G, kPanelThreads, args, smem, st);
+    return coop_launch("k_panel", (const void *)k_panel<T, false>, G, kPanelThreads, args, 0, st);
 }
 
 template <class T> int panel_gmax() {
@@ -449,10 +455,7 @@ inline int cqr_grid(int M, int N) {
 inline int panel_factor_cqr(int M, int N, float *A, size_t lda, float *tau, float *Tm, int ldt, const PanelWs<float> &pw, const CqrWs &cw, cudaStream_t st) {
     const int G = cqr_grid(M, N);
     if (G == 0) return kErrDevice;
-    static std::once_flag once;
-    static cudaError_t attr = cudaSuccess;
-    std::call_once(once, []() { attr = cudaFuncSetAttribute((const void *)k_panel_cqr<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, kCqrMaxDynSmem); });
-    RNPGPU_CHECK(attr);
+    if (int rc = kernel_attr((const void *)k_panel_cqr<0>, kCqrMaxDynSmem)) return rc;
     CqrArgs p;
     p.A = A; p.lda = lda; p.M = M; p.N = N; p.tau = tau; p.Tm = Tm; p.ldt = ldt;
     p.gpart = cw.gpart; p.gfin = cw.gfin; p.qtop = cw.qtop; p.fail = cw.fail;
@@ -462,9 +465,7 @@ inline int panel_factor_cqr(int M, int N, float *A, size_t lda, float *tau, floa
     void *args[] = {&p};
     KScope ks("panel_cqr", st);
     const size_t smem = (size_t)cqr_rows_held(M, G) * kCqrLd * sizeof(float);
-    RNPGPU_CHECK(cudaLaunchCooperativeKernel((const void *)k_panel_cqr<0>, dim3(G), dim3(kCqrThreads), args, smem, st));
-    note_launch();
-    return kOk;
+    return coop_launch("k_panel_cqr", (const void *)k_panel_cqr<0>, G, kCqrThreads, args, smem, st);
 }
 
 // serial blocked form: panel workspace, one T, one update workspace
@@ -723,13 +724,7 @@ template <class T> int multq_thin(bool notran, size_t m, size_t n, size_t k, con
     const ThinPlan tp = thin_plan<T>(m, n, k);
     const void *kern = tp.dyn ? (const void *)k_multq_thin_dyn<T>
                               : tp.csmem ? (tp.vbuf == 2 ? thin_kernel<T, true, 2>() : tp.vbuf == 1 ? thin_kernel<T, true, 1>() : thin_kernel<T, true, 0>()) : thin_kernel<T, false, 0>();
-    static std::once_flag once;
-    static cudaError_t attr = cudaSuccess;
-    std::call_once(once, []() {
-        const void *ks[5] = {thin_kernel<T, true, 2>(), thin_kernel<T, true, 1>(), thin_kernel<T, true, 0>(), thin_kernel<T, false, 0>(), (const void *)k_multq_thin_dyn<T>};
-        for (int q = 0; q < 5 && attr == cudaSuccess; ++q) attr = cudaFuncSetAttribute(ks[q], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kThinSmemMax);
-    });
-    RNPGPU_CHECK(attr);
+    if (int rc = kernel_attr(kern, (int)kThinSmemMax)) return rc;
     Carver cv(ws);
     ThinArgs<T> p;
     p.A = a; p.lda = lda; p.Tf = Tf; p.C = c; p.ldc = ldc;
@@ -746,9 +741,7 @@ template <class T> int multq_thin(bool notran, size_t m, size_t n, size_t k, con
     RNPGPU_CHECK(cudaMemsetAsync(sync, 0, 2 * sizeof(unsigned), st));
     void *args[] = {&p};
     KScope ks("multq_thin", st);
-    RNPGPU_CHECK(cudaLaunchCooperativeKernel(kern, dim3(tp.grid), dim3(kThinThreads), args, tp.smem, st));
-    note_launch();
-    return kOk;
+    return coop_launch("k_multq_thin", kern, tp.grid, kThinThreads, args, tp.smem, st);
 }
 
 // ---------------------------------------------------------------------------

@@ -33,6 +33,12 @@
 #include "qr_driver.cuh"
 #include "../../include/rnp_gpu/qr_gb300.h"
 
+// the FP64 factorization (and every kernel it launches) is instantiated once,
+// by the double unit
+namespace rnpgpu {
+extern template int geqrf<double>(size_t, size_t, double *, size_t, double *, size_t *, double *, double *, const CqrWs *, bool);
+}
+
 #include <cstdio>
 #include <mutex>
 
