@@ -46,9 +46,14 @@ int rnpgpu_zgels(size_t m, size_t n, size_t nrhs, rnpgpu_complex_double *a, size
  *      flags bit 0 (RNPGPU_REFINE_FORWARD): continue with corrected
  *      seminormal-equation steps  x += R^{-1} R^{-H} A^H r  until the
  *      correction stops shrinking, for FP64-level forward accuracy.
+ *      flags bit 1 (RNPGPU_REFINE_RANK32_UPDATES): the real FP32 factor
+ *      updates its trailing matrix after every 32-column panel on the CUDA
+ *      cores instead of once per 128 columns on the tensor cores (for
+ *      comparisons; the result is the same up to FP32 rounding).
  *      The loop reads a few norms back per step, so these calls synchronize
  *      their stream. ---- */
 #define RNPGPU_REFINE_FORWARD 1
+#define RNPGPU_REFINE_RANK32_UPDATES 2
 typedef struct {
     int iterations;         /* refinement steps taken */
     int converged;          /* 1 if both error measures reached 10 n eps */

@@ -107,6 +107,18 @@ int rnpgpu_device_status(int reset);
  * contraction the library uses for short FP32 contractions (K <= 64) that are
  * not a trailing update, exported for checking. */
 int rnpgpu_sgemm_tc(const char *transa, const char *transb, size_t m, size_t n, size_t k, float alpha, const float *a, size_t lda, const float *b, size_t ldb, float beta, float *c, size_t ldc);
+/* The FP32 factorization the mixed least-squares solvers use internally
+ * (rnpgpu_dsgels), exported for checking; no counterpart in the reference.
+ * Same storage as rnpgpu_sgeqrf (R, V, tau) and the 32 x 32 T factor of every
+ * 32-column block in tstore (block b at tstore + 1024 b, leading dimension
+ * 32).  Panels: CholeskyQR2 with Householder reconstruction (Householder
+ * panels for the whole matrix when a panel is too ill-conditioned for it;
+ * *cqr_failed, if given, reports that, and the call then synchronizes).
+ * Trailing matrix: one update per 128 columns on the tensor cores when
+ * m >= n > 128, m >= 256, lda % 4 == 0 and a is 16-byte aligned, unless flags
+ * bit 1 (RNPGPU_REFINE_RANK32_UPDATES in ls_gb300.h) asks for the rank-32
+ * updates after every panel.  Workspace query as rnpgpu_sgeqrf. */
+int rnpgpu_sgeqrf_mixed(size_t m, size_t n, float *a, size_t lda, float *tau, float *tstore, int flags, int *cqr_failed, size_t *lwork, float *work);
 /* Number of kernels this library has launched in this process. */
 unsigned long long rnpgpu_launch_count(void);
 /* Per-kernel-class timing with CUDA events on the launching stream, for the

@@ -58,6 +58,7 @@ def _signatures():
     sig["rnpgpu_launch_count"] = []
     sig["rnpgpu_device_status"] = [C.c_int]
     sig["rnpgpu_sgemm_tc"] = [CH, CH, SZ, SZ, SZ, C.c_float, P, SZ, P, SZ, C.c_float, P, SZ]
+    sig["rnpgpu_sgeqrf_mixed"] = [SZ, SZ, P, SZ, P, P, C.c_int, C.POINTER(C.c_int), PSZ, P]
     sig["rnpgpu_timing_enable"] = [C.c_int]
     sig["rnpgpu_timing_report"] = [C.c_char_p, SZ]
     sig["rnpgpu_probe_peak"] = [C.c_int, P, SZ, C.POINTER(C.c_double)]

@@ -113,7 +113,7 @@ template <class T> int gels(size_t m, size_t n, size_t nrhs, T *a, size_t lda, T
 // mixed precision least squares with iterative refinement
 // ---------------------------------------------------------------------------
 template <class TH, class TL> struct RefinePlan {
-    size_t af, tauf, ts, wq, r, rf, p, g, norms, ozw, cqrw, total;
+    size_t af, tauf, ts, wq, r, rf, p, g, norms, ozw, cqrw, widew, total;
     int split;
     // the FP64 products r = b - A x and A^T r on the tensor cores (exact
     // integer slices) for real FP64 data; other types use FP64 FMA
@@ -133,7 +133,8 @@ template <class TH, class TL> struct RefinePlan {
         rf = std::max(rf, al(n * nrhs * sizeof(TL)));
         ozw = kOz ? OzWork::bytes(m, n, nrhs) : 0;
         cqrw = std::is_same<TL, float>::value ? cqr_ws_bytes() : 0;
-        total = af + tauf + ts + wq + r + rf + p + g + norms + ozw + cqrw;
+        widew = (std::is_same<TL, float>::value && wide::usable(m, n, reinterpret_cast<const float *>(256), m)) ? wide::ws_bytes(m, n) : 0;
+        total = af + tauf + ts + wq + r + rf + p + g + norms + ozw + cqrw + widew;
     }
 };
 
@@ -174,6 +175,10 @@ int gels_refine(size_t m, size_t n, size_t nrhs, const TH *a, size_t lda, const 
     if (use_oz) ow.carve(cv, m, n, nrhs);
     CqrWs cw;
     if (std::is_same<TL, float>::value) cw = carve_cqr(cv);
+    if (plan.widew > 0) {
+        cw.wide = wide::carve(cv, m, n);
+        cw.use_wide = (flags & 2) == 0;  // flag 2: rank-32 trailing updates only
+    }
     const size_t lwq = plan.wq / sizeof(TL);
     const dim3 gmn((unsigned)std::min<size_t>((m + 255) / 256, 2048), (unsigned)std::min<size_t>(n, 65535));
     const dim3 gmr((unsigned)std::min<size_t>((m + 255) / 256, 2048), (unsigned)std::min<size_t>(nrhs, 65535));

@@ -417,13 +417,20 @@ template <class T> size_t t_bytes() { return ((size_t)kPanelMaxCols * kPanelMaxC
 // ---------------------------------------------------------------------------
 template <class T> int geqr2(size_t m, size_t n, T *a, size_t lda, T *tau, T *work);
 
+}  // namespace rnpgpu
+#include "wide_f32.cuh"
+namespace rnpgpu {
+
 // CholeskyQR2 panels of the mixed solver's FP32 factor (panel_cqr.cuh):
-// Gram partials, the top rows of Q1, the failure flag
+// Gram partials, the top rows of Q1, the failure flag; optionally the
+// workspace of the 128-column tensor-core trailing update (wide_f32.cuh)
 struct CqrWs {
     float2 *gpart = nullptr;
     float2 *gfin = nullptr;
     float *qtop = nullptr;
     int *fail = nullptr;
+    wide::WideWs wide;
+    bool use_wide = false;
 };
 inline size_t cqr_ws_bytes() {
     const auto r = [](size_t b) { return (b + 255) / 256 * 256; };
@@ -561,6 +568,13 @@ template <class T> int geqrf(size_t m, size_t n, T *a, size_t lda, T *tau, size_
         Tm[1] = cv.take<T>((size_t)kPanelMaxCols * kPanelMaxCols);
         bw2 = carve_block<T>(cv, (int)n, smax);
     }
+    // the mixed solver's FP32 factor: 128-column blocks of four panels,
+    // updated among themselves by the rank-32 passes, the rest of the matrix
+    // by one tensor-core update per block (wide_f32.cuh)
+    bool wide_mode = false;
+    if constexpr (std::is_same<T, float>::value) {
+        wide_mode = !ahead && cqr != nullptr && cqr->use_wide && Tstore != nullptr && wide::usable(m, n, a, lda);
+    }
     bool big_pending = false;
     for (size_t i = 0; i < k; i += nb) {
         const int ib = (int)std::min(nb, k - i);
@@ -578,6 +592,30 @@ template <class T> int geqrf(size_t m, size_t n, T *a, size_t lda, T *tau, size_
         if (rc) return rc;
         const size_t c1 = i + ib;  // first trailing column
         if (c1 >= n) continue;
+        if constexpr (std::is_same<T, float>::value) {
+            if (wide_mode) {
+                const size_t j0 = i / wide::kNb * wide::kNb, jend = std::min(j0 + wide::kNb, n);
+                if (c1 < jend) {
+                    rc = apply_block<T>(true, false, (int)(m - i), (int)(jend - c1), ib, Ai, lda, Tb, kPanelMaxCols, a + i + c1 * lda, lda, bw, st);
+                    if (rc) return rc;
+                }
+                const bool block_done = (c1 == j0 + wide::kNb) || (c1 == k);
+                if (block_done && jend < n) {
+                    if (c1 == j0 + wide::kNb && m - j0 >= 128) {
+                        rc = wide::apply(a, lda, (int)m, (int)n, (int)j0, Tstore + (j0 / nb) * kPanelMaxCols * kPanelMaxCols, (size_t)kPanelMaxCols * kPanelMaxCols, cqr->wide, st);
+                        if (rc) return rc;
+                    } else {
+                        for (size_t p = j0; p < c1; p += nb) {
+                            const int pb = (int)std::min(nb, k - p);
+                            rc = apply_block<T>(true, false, (int)(m - p), (int)(n - jend), pb, a + p + p * lda, lda, Tstore + (p / nb) * kPanelMaxCols * kPanelMaxCols,
+                                                kPanelMaxCols, a + p + jend * lda, lda, bw, st);
+                            if (rc) return rc;
+                        }
+                    }
+                }
+                continue;
+            }
+        }
         if (!ahead) {
             rc = apply_block<T>(true, false, (int)(m - i), (int)(n - c1), ib, Ai, lda, Tb, kPanelMaxCols, a + i + c1 * lda, lda, bw, st);
             if (rc) return rc;

@@ -55,10 +55,12 @@ def refine_workspace(A, nrhs):
     return lw.value
 
 
-def gels_refine(A, B, X=None, max_iter=0, work=None, forward=False):
+def gels_refine(A, B, X=None, max_iter=0, work=None, forward=False, rank32=False):
     """Mixed-precision least squares (FP32 factor, FP64 refinement) of an FP64
     (or complex128) problem; A and B are not modified.  forward=True adds the
-    corrected seminormal-equation steps for FP64 forward accuracy.
+    corrected seminormal-equation steps for FP64 forward accuracy;
+    rank32=True keeps the real FP32 factor's trailing updates at 32 columns
+    on the CUDA cores (instead of 128 columns on the tensor cores).
     max_iter <= 0 selects the default (10 steps, 30 in forward mode).
     Returns (X, info)."""
     p = {torch.float64: "ds", torch.complex128: "zc"}[A.dtype]
@@ -75,7 +77,7 @@ def gels_refine(A, B, X=None, max_iter=0, work=None, forward=False):
         work = torch.empty(max(refine_workspace(A, nrhs), 1), dtype=A.dtype, device=A.device)
     info = RefineInfo()
     lw = C.c_size_t(work.numel())
-    _check("gels_refine", fn(m, n, nrhs, a, lda, b, ldb, x, ldx, int(max_iter), 1 if forward else 0, C.byref(info), C.byref(lw), work.data_ptr()))
+    _check("gels_refine", fn(m, n, nrhs, a, lda, b, ldb, x, ldx, int(max_iter), (1 if forward else 0) | (2 if rank32 else 0), C.byref(info), C.byref(lw), work.data_ptr()))
     return X, info.as_dict()
 
 
