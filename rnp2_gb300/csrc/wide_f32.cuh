@@ -120,11 +120,20 @@ template <int kTag = 0> __global__ void __launch_bounds__(256) k_wide_vsplit(con
     constexpr int LD = 129;
     const int t = blockIdx.x, tid = threadIdx.x;
     const int r0 = t * 128;
-    for (int idx = tid; idx < 128 * 128; idx += 256) {
-        const int r = idx & 127, k = idx >> 7, gr = r0 + r;
-        float v = 0.f;
-        if (gr < rows) v = gr > k ? A[gr + (size_t)k * lda] : (gr == k ? 1.f : 0.f);
-        s_v[k * LD + r] = v;
+    // 64 loads per thread, 16 in flight at a time
+    for (int i0 = 0; i0 < 64; i0 += 16) {
+        float v[16];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+            const int idx = tid + 256 * (i0 + i);
+            const int r = idx & 127, k = idx >> 7, gr = r0 + r;
+            v[i] = (gr < rows && gr > k) ? __ldg(A + gr + (size_t)k * lda) : (gr == k ? 1.f : 0.f);
+        }
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+            const int idx = tid + 256 * (i0 + i);
+            s_v[(idx >> 7) * LD + (idx & 127)] = v[i];
+        }
     }
     __syncthreads();
     // VA: unit (row, 8 consecutive K) -> one 16-byte chunk per slice
@@ -151,6 +160,14 @@ template <int kTag = 0> __global__ void __launch_bounds__(256) k_wide_vsplit(con
 // grid (nsplit, ntile): tile 0 is V^T V (A operand = VB), tile j >= 1 takes
 // C's columns c1 + 128 (j-1) ... .  P[(split * ntile + tile) * 128 * 128 +
 // v * 128 + c] = sum over the split's rows of V(row, v) X(row, c).
+//
+// The large-magnitude class (x0 y0) is accumulated by the tensor cores over
+// kWFlush chunks (128 rows) at a time only, in one of two TMEM buffers; four
+// drain warps add each finished buffer into FP32 registers (round to nearest)
+// while the MMAs fill the other.  The tensor cores' own accumulation then
+// spans 8 MMAs per value instead of the whole split, which keeps the partial
+// at FP32 accuracy for any split length.  The two small classes stay in TMEM
+// for the whole split.
 // ---------------------------------------------------------------------------
 struct WArgs {
     int rows;          // rows of the block (V and C)
@@ -163,14 +180,19 @@ struct WArgs {
 constexpr int kWStages = 3;
 constexpr int kWStageBytes = 2 * kVbChunk + 32 * 128 * 4;  // VB chunk, A slices, C FP32 tile
 constexpr int kWSmem = kWStages * kWStageBytes + 256;
-constexpr int kWThreads = 192;  // warp 0 copies, warps 1-4 convert (and drain), warp 5 issues MMAs
+constexpr int kWFlush = 4;      // chunks (of 32 rows) per class-0 accumulation
+constexpr int kWThreads = 320;  // warp 0 copies, 1-4 convert, 5 issues MMAs, 6-9 drain
+// TMEM columns: class 0 buffers at 0 and 384, class 1 at 128, class 2 at 256
+__host__ __device__ constexpr uint32_t w_col(int cls, int buf) { return cls == 0 ? (buf ? 384u : 0u) : (uint32_t)(cls * 128); }
 
 template <int kTag = 0> __global__ void __launch_bounds__(kWThreads, 1) k_wide_w(const __grid_constant__ CUtensorMap cmap, WArgs a) {
     extern __shared__ __align__(1024) unsigned char smem[];
     uint64_t *full = reinterpret_cast<uint64_t *>(smem + kWStages * kWStageBytes);
     uint64_t *ready = full + kWStages;
     uint64_t *freed = ready + kWStages;
-    uint64_t *done = freed + kWStages;
+    uint64_t *c0full = freed + kWStages;  // [2] class-0 buffer holds a finished group
+    uint64_t *c0free = c0full + 2;        // [2] class-0 buffer drained
+    uint64_t *done = c0free + 2;          // every MMA has completed
     uint32_t *tslot = reinterpret_cast<uint32_t *>(done + 1);
     int *abort_flag = reinterpret_cast<int *>(tslot + 1);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -178,6 +200,7 @@ template <int kTag = 0> __global__ void __launch_bounds__(kWThreads, 1) k_wide_w
     const int rbeg = split * a.rows_per_split;
     const int rend = min(a.rows, rbeg + a.rows_per_split);
     const int nch = rend > rbeg ? (rend - rbeg + 31) / 32 : 0;
+    const int ngrp = (nch + kWFlush - 1) / kWFlush;
     const bool gram = (tile == 0);
 
     if (tid == 0) {
@@ -185,6 +208,10 @@ template <int kTag = 0> __global__ void __launch_bounds__(kWThreads, 1) k_wide_w
             tc::mbar_init(&full[s], 1);
             tc::mbar_init(&ready[s], 4);
             tc::mbar_init(&freed[s], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            tc::mbar_init(&c0full[b], 1);
+            tc::mbar_init(&c0free[b], 4);
         }
         tc::mbar_init(done, 1);
         *abort_flag = 0;
@@ -235,11 +262,20 @@ template <int kTag = 0> __global__ void __launch_bounds__(kWThreads, 1) k_wide_w
         const int pa[6] = {0, 0, 1, 0, 1, 2};
         const int pb[6] = {0, 1, 0, 2, 1, 0};
         const int pc[6] = {0, 1, 1, 2, 2, 2};
-        const bool first_in_class[6] = {true, true, false, true, false, false};
         uint32_t rph[kWStages] = {0, 0, 0};
-        int issued = 0;
+        uint32_t fph[2] = {0, 0};
         for (int ch = 0; ch < nch; ++ch) {
             const int s = ch % kWStages;
+            const int grp = ch / kWFlush, buf = grp & 1;
+            const bool grp_first = (ch % kWFlush) == 0;
+            const bool grp_last = ((ch + 1) % kWFlush) == 0 || ch + 1 == nch;
+            if (grp_first && grp >= 2) {
+                // the class-0 buffer of group grp - 2 has been drained
+                const bool got = tc::mbar_wait(&c0free[buf], fph[buf]);
+                if (!__all_sync(0xFFFFFFFFu, got) || aborted()) { fail(); break; }
+                fph[buf] ^= 1u;
+                tc::tc_fence_after();
+            }
             const bool got = tc::mbar_wait(&ready[s], rph[s]);
             if (!__all_sync(0xFFFFFFFFu, got) || aborted()) { fail(); break; }
             rph[s] ^= 1u;
@@ -254,23 +290,22 @@ template <int kTag = 0> __global__ void __launch_bounds__(kWThreads, 1) k_wide_w
                     for (int q = 0; q < 6; ++q) {
                         const uint64_t ad = tc::smem_desc(aop + pa[q] * kVbSlice + kk * 256, 128, 4 * 128);
                         const uint64_t bd = tc::smem_desc(bop + pb[q] * kVbSlice + kk * 256, 128, 4 * 128);
-                        const bool fresh = (ch == 0 && kk == 0 && first_in_class[q]);
-                        tc::umma_bf16(tmem + (uint32_t)(pc[q] * 128), ad, bd, idesc, fresh ? 0u : 1u);
+                        const bool fresh = pc[q] == 0 ? (grp_first && kk == 0) : (ch == 0 && kk == 0 && (q == 1 || q == 3));
+                        tc::umma_bf16(tmem + w_col(pc[q], buf), ad, bd, idesc, fresh ? 0u : 1u);
                     }
                 }
                 tc::umma_commit(&freed[s]);
+                if (grp_last) tc::umma_commit(&c0full[buf]);
             }
             __syncwarp();
-            issued = ch + 1;
         }
-        // one commit after the last MMA: the drain waits for it, and an
+        // one commit after the last MMA: the final drain waits for it, and an
         // aborted CTA waits for it before freeing tensor memory
         __syncwarp();
         if (tc::elect_one()) tc::umma_commit(done);
         __syncwarp();
-        (void)issued;
-    } else {
-        // converters (warps 1-4): C's FP32 tile [col][32 rows] -> A slices
+    } else if (warp >= 1 && warp <= 4) {
+        // converters: C's FP32 tile [col][32 rows] -> A slices
         const int ct = tid - 32;  // 0..127
         uint32_t fph[kWStages] = {0, 0, 0};
         for (int ch = 0; ch < nch; ++ch) {
@@ -295,39 +330,51 @@ template <int kTag = 0> __global__ void __launch_bounds__(kWThreads, 1) k_wide_w
             __syncwarp();
             if (lane == 0) arrive(&ready[s]);
         }
-    }
-
-    // drain: warps 1-4 read TMEM lanes 32 (warp % 4) .. (tile columns c) and
-    // write the partial (128 V-columns x 128 tile columns)
-    const bool ok_loop = !aborted();
-    if (warp >= 1 && warp <= 4) {
-        bool ok = ok_loop && nch > 0;
-        if (ok && !tc::mbar_wait(done, 0)) { fail(); ok = false; }
-        tc::tc_fence_after();
+    } else {
+        // drain warps 6-9: thread = TMEM lane (tile column c); class-0 groups
+        // summed in registers, then the small classes, then the partial
         const int q = warp & 3;
         const int c = q * 32 + lane;
+        const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16);
+        float acc[128];
+#pragma unroll
+        for (int i = 0; i < 128; ++i) acc[i] = 0.f;
+        bool ok = nch > 0;
+        uint32_t gph[2] = {0, 0};
+        for (int grp = 0; ok && grp < ngrp; ++grp) {
+            const int buf = grp & 1;
+            if (!tc::mbar_wait(&c0full[buf], gph[buf]) || aborted()) { fail(); ok = false; break; }
+            gph[buf] ^= 1u;
+            tc::tc_fence_after();
+#pragma unroll
+            for (int v0 = 0; v0 < 128; v0 += 16) {
+                float t[16];
+                tc::tmem_ld16(lane_base + w_col(0, buf) + (uint32_t)v0, t);
+#pragma unroll
+                for (int i = 0; i < 16; ++i) acc[v0 + i] += t[i];
+            }
+            tc::tc_fence_before();
+            __syncwarp();
+            if (lane == 0) arrive(&c0free[buf]);
+        }
+        if (ok && !tc::mbar_wait(done, 0)) { fail(); ok = false; }
+        tc::tc_fence_after();
         float *P = a.P + ((size_t)split * a.ntile + tile) * 128 * 128;
+#pragma unroll
         for (int v0 = 0; v0 < 128; v0 += 16) {
-            float out[16];
+            float mid[16], small[16];
             if (ok) {
-                const uint32_t lb = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)v0;
-                float big[16], mid[16], small[16];
-                tc::tmem_ld16(lb, big);
-                tc::tmem_ld16(lb + 128, mid);
-                tc::tmem_ld16(lb + 256, small);
-#pragma unroll
-                for (int i = 0; i < 16; ++i) out[i] = big[i] + fmaf(small[i], 0x1p-16f, mid[i] * 0x1p-8f);
-            } else {
-#pragma unroll
-                for (int i = 0; i < 16; ++i) out[i] = 0.f;
+                tc::tmem_ld16(lane_base + w_col(1, 0) + (uint32_t)v0, mid);
+                tc::tmem_ld16(lane_base + w_col(2, 0) + (uint32_t)v0, small);
             }
 #pragma unroll
-            for (int i = 0; i < 16; ++i) P[(size_t)(v0 + i) * 128 + c] = out[i];
+            for (int i = 0; i < 16; ++i) {
+                const float out = ok ? acc[v0 + i] + fmaf(small[i], 0x1p-16f, mid[i] * 0x1p-8f) : 0.f;
+                P[(size_t)(v0 + i) * 128 + c] = out;
+            }
         }
-    } else if (warp == 5 && aborted()) {
-        // let MMAs in flight finish before tensor memory is freed
-        tc::mbar_wait(done, 0);
     }
+    if (aborted() && warp == 5) tc::mbar_wait(done, 0);  // MMAs in flight finish before TMEM is freed
     tc::tc_fence_before();
     __syncthreads();
     if (warp == 5) tc::tmem_dealloc(tmem, 512);
@@ -341,14 +388,15 @@ template <int kTag = 0> __global__ void __launch_bounds__(128) k_wide_reduce(con
     const int c = threadIdx.x;
     const size_t stride = (size_t)ntile * 128 * 128;
     const float *p = P + (size_t)row * 128 + c;
-    float s0 = 0.f, s1 = 0.f;
+    // eight partial sums in flight, combined in a fixed order
+    float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     int s = 0;
-    for (; s + 1 < nsplit; s += 2) {
-        s0 += p[(size_t)s * stride];
-        s1 += p[(size_t)(s + 1) * stride];
+    for (; s + 8 <= nsplit; s += 8) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) acc[i] += __ldg(p + (size_t)(s + i) * stride);
     }
-    if (s < nsplit) s0 += p[(size_t)s * stride];
-    GW[(size_t)row * 128 + c] = s0 + s1;
+    for (int i = 0; s + i < nsplit; ++i) acc[i] += __ldg(p + (size_t)(s + i) * stride);
+    GW[(size_t)row * 128 + c] = ((acc[0] + acc[1]) + (acc[2] + acc[3])) + ((acc[4] + acc[5]) + (acc[6] + acc[7]));
 }
 
 // ---------------------------------------------------------------------------
@@ -356,40 +404,78 @@ template <int kTag = 0> __global__ void __launch_bounds__(128) k_wide_reduce(con
 // factors Tp (column-major, 32 x 32 each, kTstride apart) and G = V^T V
 // (GW tile 0, G[v][c]).  T(0:32b, blk b) = -T(0:32b, 0:32b) G(0:32b, blk b) T_b.
 // ---------------------------------------------------------------------------
-constexpr int kTSmem = (128 * 129 + 128 * 33) * 4;
-template <int kTag = 0> __global__ void __launch_bounds__(256) k_wide_t(const float *GW, const float *Tp, size_t tstride, int nblk, float *Tout) {
+constexpr int kTSmem = (128 * 129 + 2 * 96 * 33) * 4;
+constexpr int kTThreads = 1024;
+template <int kTag = 0> __global__ void __launch_bounds__(kTThreads) k_wide_t(const float *GW, const float *Tp, size_t tstride, int nblk, float *Tout) {
     extern __shared__ __align__(16) float s_t[];
     float (*sT)[129] = reinterpret_cast<float (*)[129]>(s_t);
     float (*sX)[33] = reinterpret_cast<float (*)[33]>(s_t + 128 * 129);
+    float (*sG)[33] = reinterpret_cast<float (*)[33]>(s_t + 128 * 129 + 96 * 33);
     const int tid = threadIdx.x;
-    for (int idx = tid; idx < 128 * 128; idx += 256) {
-        const int r = idx >> 7, c = idx & 127;
-        const int br = r >> 5, bc = c >> 5;
-        float v = 0.f;
-        if (br == bc && br < nblk) v = Tp[(size_t)br * tstride + (r & 31) + (size_t)(c & 31) * 32];
-        sT[r][c] = v;
-    }
+    for (int idx = tid; idx < 128 * 128; idx += kTThreads) sT[idx >> 7][idx & 127] = 0.f;
     __syncthreads();
+    // the panel factors: 4 x 1024 values
+    {
+        float v[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const int idx = tid + kTThreads * i, b = idx >> 10, e = idx & 1023;
+            v[i] = b < nblk ? __ldg(Tp + (size_t)b * tstride + e) : 0.f;
+        }
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const int idx = tid + kTThreads * i, b = idx >> 10, e = idx & 1023;
+            if (b < nblk) sT[32 * b + (e & 31)][32 * b + (e >> 5)] = v[i];
+        }
+    }
     for (int b = 1; b < nblk; ++b) {
         const int nr = 32 * b;
-        // X = G(0:nr, blk b) T_b
-        for (int idx = tid; idx < nr * 32; idx += 256) {
-            const int r = idx >> 5, c = idx & 31;
-            float acc = 0.f;
-            for (int l = 0; l <= c; ++l) acc = fmaf(GW[(size_t)r * 128 + 32 * b + l], sT[32 * b + l][32 * b + c], acc);
-            sX[r][c] = acc;
+        // G(0:nr, blk b)
+        {
+            float v[3];
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                const int idx = tid + kTThreads * i;
+                v[i] = idx < nr * 32 ? __ldg(GW + (size_t)(idx >> 5) * 128 + 32 * b + (idx & 31)) : 0.f;
+            }
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                const int idx = tid + kTThreads * i;
+                if (idx < nr * 32) sG[idx >> 5][idx & 31] = v[i];
+            }
         }
         __syncthreads();
-        // T(0:nr, blk b) = -T(0:nr, 0:nr) X  (upper: l >= r)
-        for (int idx = tid; idx < nr * 32; idx += 256) {
+        // X = G(0:nr, blk b) T_b  (two partial sums per entry)
+        for (int idx = tid; idx < nr * 32; idx += kTThreads) {
             const int r = idx >> 5, c = idx & 31;
-            float acc = 0.f;
-            for (int l = r; l < nr; ++l) acc = fmaf(sT[r][l], sX[l][c], acc);
-            sT[r][32 * b + c] = -acc;
+            float a0 = 0.f, a1 = 0.f;
+            int l = 0;
+            for (; l + 1 <= c; l += 2) {
+                a0 = fmaf(sG[r][l], sT[32 * b + l][32 * b + c], a0);
+                a1 = fmaf(sG[r][l + 1], sT[32 * b + l + 1][32 * b + c], a1);
+            }
+            if (l <= c) a0 = fmaf(sG[r][l], sT[32 * b + l][32 * b + c], a0);
+            sX[r][c] = a0 + a1;
+        }
+        __syncthreads();
+        // T(0:nr, blk b) = -T(0:nr, 0:nr) X  (upper: l >= r), four partial sums
+        for (int idx = tid; idx < nr * 32; idx += kTThreads) {
+            const int r = idx >> 5, c = idx & 31;
+            float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+            int l = r;
+            for (; l + 3 < nr; l += 4) {
+                a0 = fmaf(sT[r][l], sX[l][c], a0);
+                a1 = fmaf(sT[r][l + 1], sX[l + 1][c], a1);
+                a2 = fmaf(sT[r][l + 2], sX[l + 2][c], a2);
+                a3 = fmaf(sT[r][l + 3], sX[l + 3][c], a3);
+            }
+            for (; l < nr; ++l) a0 = fmaf(sT[r][l], sX[l][c], a0);
+            sT[r][32 * b + c] = -((a0 + a1) + (a2 + a3));
         }
         __syncthreads();
     }
-    for (int idx = tid; idx < 128 * 128; idx += 256) Tout[idx] = sT[idx >> 7][idx & 127];
+    __syncthreads();
+    for (int idx = tid; idx < 128 * 128; idx += kTThreads) Tout[idx] = sT[idx >> 7][idx & 127];
 }
 
 // ---------------------------------------------------------------------------
@@ -403,10 +489,25 @@ template <int kTag = 0> __global__ void __launch_bounds__(256) k_wide_y(const fl
     float (*sW)[129] = reinterpret_cast<float (*)[129]>(s_y + 128 * 128);
     const int tid = threadIdx.x;
     const int c0 = blockIdx.x * 16;
-    for (int idx = tid; idx < 128 * 128; idx += 256) sT[idx >> 7][idx & 127] = Tm[idx];
-    for (int idx = tid; idx < 16 * 128; idx += 256) {
-        const int cc = idx & 15, v = idx >> 4, c = c0 + cc;
-        sW[cc][v] = c < nc ? GW[((size_t)(1 + c / 128) * 128 + v) * 128 + (c % 128)] : 0.f;
+    {
+        // T: 4096 float4, 16 per thread in flight
+        float4 v[16];
+        const float4 *t4 = reinterpret_cast<const float4 *>(Tm);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) v[i] = __ldg(t4 + tid + 256 * i);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) reinterpret_cast<float4 *>(&sT[0][0])[tid + 256 * i] = v[i];
+        float w[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            const int idx = tid + 256 * i, cc = idx & 15, vv = idx >> 4, c = c0 + cc;
+            w[i] = c < nc ? __ldg(GW + ((size_t)(1 + c / 128) * 128 + vv) * 128 + (c % 128)) : 0.f;
+        }
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            const int idx = tid + 256 * i;
+            sW[idx & 15][idx >> 4] = w[i];
+        }
     }
     __syncthreads();
     // thread: column cc = tid / 16, K values k = 8 (tid % 16) .. + 7
@@ -699,7 +800,7 @@ inline int apply(float *A, size_t lda, int m, int n, int r0, const float *Tp, si
         k_wide_reduce<0><<<ntile * 128, 128, 0, st>>>(w.P, nsplit, ntile, w.GW);
         RNPGPU_CHECK_LAUNCH();
         if ((rc = kernel_attr((const void *)k_wide_t<0>, kTSmem))) return rc;
-        k_wide_t<0><<<1, 256, kTSmem, st>>>(w.GW, Tp, tstride, 4, w.T);
+        k_wide_t<0><<<1, kTThreads, kTSmem, st>>>(w.GW, Tp, tstride, 4, w.T);
         RNPGPU_CHECK_LAUNCH();
         const int J = (nc + kUpdCols - 1) / kUpdCols;
         if ((rc = kernel_attr((const void *)k_wide_y<0>, kYSmem))) return rc;
