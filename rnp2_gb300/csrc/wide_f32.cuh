@@ -414,13 +414,14 @@ template <int kTag = 0> __global__ void __launch_bounds__(kTThreads) k_wide_t(co
     const int tid = threadIdx.x;
     for (int idx = tid; idx < 128 * 128; idx += kTThreads) sT[idx >> 7][idx & 127] = 0.f;
     __syncthreads();
-    // the panel factors: 4 x 1024 values
+    // the panel factors: 4 x 1024 values, upper triangles only (the panels
+    // leave whatever the workspace held below their diagonals)
     {
         float v[4];
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
             const int idx = tid + kTThreads * i, b = idx >> 10, e = idx & 1023;
-            v[i] = b < nblk ? __ldg(Tp + (size_t)b * tstride + e) : 0.f;
+            v[i] = (b < nblk && (e & 31) <= (e >> 5)) ? __ldg(Tp + (size_t)b * tstride + e) : 0.f;
         }
 #pragma unroll
         for (int i = 0; i < 4; ++i) {

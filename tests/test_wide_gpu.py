@@ -73,3 +73,22 @@ def test_wide_update_matches_rank32_updates(mnl):
     assert float(res) <= 2e-6 * np.sqrt(n), float(res)
     orth = torch.linalg.norm(Q.double().t() @ Q.double() - torch.eye(n, dtype=torch.float64, device="cuda"))
     assert float(orth) <= 2e-6 * n, float(orth)
+
+
+@pytest.mark.parametrize("fill", [0.0, 1e30, float("nan")])
+def test_mixed_solve_does_not_depend_on_workspace_contents(fill):
+    # every workspace region the wide path reads is written first in the same
+    # call (the panel T factors are read as upper triangles only): the result
+    # is the same bit for bit whatever the workspace held before
+    from rnp2_gb300 import ls as gls
+
+    m, n, nrhs = 4096, 384, 2
+    g = torch.Generator(device="cuda").manual_seed(5)
+    A = gq.to_colmajor(torch.randn((n, m), generator=g, dtype=torch.float64, device="cuda").t())
+    B = gq.to_colmajor(torch.randn((nrhs, m), generator=g, dtype=torch.float64, device="cuda").t())
+    lw = gls.refine_workspace(A, nrhs)
+    X0, info0 = gls.gels_refine(A, B, work=torch.zeros(lw, dtype=torch.float64, device="cuda"))
+    X1, info1 = gls.gels_refine(A, B, work=torch.full((lw,), fill, dtype=torch.float64, device="cuda"))
+    torch.cuda.synchronize()
+    assert info0["converged"] == 1 and info1 == info0
+    assert torch.equal(X0, X1)
