@@ -548,12 +548,17 @@ def measured_hbm_gbs():
 
 def kernel_rooflines(prof, tot_ms, top_name, peak64, steps):
     """Roofline of every main kernel class of the mixed step from its
-    algorithmic work per launch (exact for this workload's shapes: 16 panels of
-    32 columns on 65536 - 32 i rows, 15 trailing updates of the remaining
-    columns) and its average CUDA-event duration per launch."""
-    nb = 32
+    algorithmic work per launch (exact for this workload's shapes) and its
+    average CUDA-event duration per launch.  The FP32 factor runs in
+    128-column blocks: 16 panels of 32 columns on 65536 - 32 i rows; inside
+    each block the panels update the block's remaining 96, 64, 32 columns
+    with the rank-32 passes (12 updates); after each of the first three
+    blocks one tensor-core update covers the remaining 384, 256, 128
+    columns."""
+    nb, wb = 32, 128
     panels = [(M - nb * i, nb) for i in range(N // nb)]
-    updates = [(M - nb * i, N - nb * (i + 1)) for i in range(N // nb - 1)]
+    inner = [(M - wb * j - nb * p, wb - nb * (p + 1)) for j in range(N // wb) for p in range(wb // nb - 1)]
+    outer = [(M - wb * j, N - wb * (j + 1)) for j in range(N // wb - 1)]
     mean = lambda xs: sum(xs) / len(xs)
     hbm, hbm_src = measured_hbm_gbs()
     work = {
@@ -561,10 +566,16 @@ def kernel_rooflines(prof, tot_ms, top_name, peak64, steps):
                   "k_panel<float>: FP32 panel, rows read and written once (2 m 32 x 4 B)"),
         "panel_cqr": ("hbm", mean([2.0 * m * c * 4 for m, c in panels]),
                       "k_panel_cqr: FP32 CholeskyQR2 panel with Householder reconstruction, rows read and written once (2 m 32 x 4 B)"),
-        "larfb_update": ("hbm", mean([2.0 * m * c * 4 + m * nb * 4.0 for m, c in updates]),
-                         "k_update_f32: C -= V (W T)^T on the FP32 pipe, C read and written once, V read once"),
-        "larfb_w": ("hbm", mean([m * c * 4.0 + m * nb * 4.0 for m, c in updates]),
-                    "k_w_f32: W = C^T V partials on the FP32 pipe, C and V read once"),
+        "larfb_update": ("hbm", mean([2.0 * m * c * 4 + m * nb * 4.0 for m, c in inner]),
+                         "k_update_f32: rank-32 update inside a 128-column block, C read and written once, V read once"),
+        "larfb_w": ("hbm", mean([m * c * 4.0 + m * nb * 4.0 for m, c in inner]),
+                    "k_w_f32 + k_reduce_times_t: W = C^T V partials inside a 128-column block, C and V read once"),
+        "wide_w": ("hbm", mean([m * c * 4.0 + m * wb * 4.0 for m, c in outer]),
+                   "wide::k_wide_w: W = C^T V and V^T V for a 128-column block on tcgen05 (three BF16 slices), C and V read once"),
+        "wide_update": ("hbm", mean([2.0 * m * c * 4 + m * wb * 4.0 for m, c in outer]),
+                        "wide::k_wide_update: C -= V (W T)^T for a 128-column block on tcgen05 (three BF16 slices), C read and written once, V read once"),
+        "wide_vsplit": ("hbm", mean([m * wb * 4.0 + 2 * m * wb * 6.0 for m, c in outer]),
+                        "wide::k_wide_vsplit: V read once, its two BF16-slice images written"),
         "residual_fp64": ("hbm", M * N * 8.0 + 2.0 * M * NRHS * 8,
                           "k_xstack + oz::k_oz (residual): r = b - A x FP64-accurate from the packed digits of A (m n x 8 B read) on the FP16 tensor cores, b read, r written"),
         "normal_eq_fp64": ("hbm", M * N * 8.0 + M * NRHS * 8.0 + M * 256.0,

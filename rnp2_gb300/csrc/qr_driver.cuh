@@ -431,7 +431,6 @@ struct CqrWs {
     int *fail = nullptr;
     wide::WideWs wide;
     bool use_wide = false;
-    bool thin_inner = true;  // inner block updates by the one-launch thin MultQ
 };
 inline size_t cqr_ws_bytes() {
     const auto r = [](size_t b) { return (b + 255) / 256 * 256; };
@@ -513,11 +512,6 @@ inline LookAhead *lookahead_ctx() {
     }
     return state[dev] == 1 ? &la[dev] : nullptr;
 }
-
-// thin left MultQ in one cooperative launch (defined below)
-template <class T> size_t thin_ws_bytes(size_t n);
-template <class T> int multq_thin(bool notran, size_t m, size_t n, size_t k, const T *a, size_t lda, const T *Tf, T *c, size_t ldc, void *ws, cudaStream_t st,
-                                  const char *tag = "multq_thin");
 
 // Tstore (optional): receives the 32 x 32 T factor of every column block
 // (block b at Tstore + b*32*32, leading dimension 32) for later MultQ calls.
@@ -602,20 +596,11 @@ template <class T> int geqrf(size_t m, size_t n, T *a, size_t lda, T *tau, size_
             if (wide_mode) {
                 const size_t j0 = i / wide::kNb * wide::kNb, jend = std::min(j0 + wide::kNb, n);
                 if (c1 < jend) {
-                    // the rest of the block (at most 96 columns): one
-                    // cooperative launch per 64 columns (multq_thin.cuh), whose
-                    // partials fit in the update workspace
-                    const size_t wbytes = (size_t)bw.smax * n * kPanelMaxCols * sizeof(T);
-                    if (cqr->thin_inner && thin_ws_bytes<T>(kThinMaxCols) <= wbytes) {
-                        for (size_t c0 = c1; c0 < jend; c0 += kThinMaxCols) {
-                            const size_t nc = std::min<size_t>(kThinMaxCols, jend - c0);
-                            rc = multq_thin<T>(false, m - i, nc, (size_t)ib, Ai, lda, Tb, a + i + c0 * lda, lda, bw.P, st, "inner_update");
-                            if (rc) return rc;
-                        }
-                    } else {
-                        rc = apply_block<T>(true, false, (int)(m - i), (int)(jend - c1), ib, Ai, lda, Tb, kPanelMaxCols, a + i + c1 * lda, lda, bw, st);
-                        if (rc) return rc;
-                    }
+                    // the rest of the block: rank-32 passes (a one-launch thin
+                    // MultQ per 64 columns measured 86-92 us a launch at 65536
+                    // rows against 51 us for these three launches)
+                    rc = apply_block<T>(true, false, (int)(m - i), (int)(jend - c1), ib, Ai, lda, Tb, kPanelMaxCols, a + i + c1 * lda, lda, bw, st);
+                    if (rc) return rc;
                 }
                 const bool block_done = (c1 == j0 + wide::kNb) || (c1 == k);
                 if (block_done && jend < n) {
@@ -776,7 +761,7 @@ template <class T> ThinPlan thin_plan(size_t m, size_t n, size_t k) {
     return tp;
 }
 template <class T, bool CS, int VB> const void *thin_kernel() { return (const void *)k_multq_thin<T, CS, VB>; }
-template <class T> int multq_thin(bool notran, size_t m, size_t n, size_t k, const T *a, size_t lda, const T *Tf, T *c, size_t ldc, void *ws, cudaStream_t st, const char *tag) {
+template <class T> int multq_thin(bool notran, size_t m, size_t n, size_t k, const T *a, size_t lda, const T *Tf, T *c, size_t ldc, void *ws, cudaStream_t st) {
     const ThinPlan tp = thin_plan<T>(m, n, k);
     const void *kern = tp.dyn ? (const void *)k_multq_thin_dyn<T>
                               : tp.csmem ? (tp.vbuf == 2 ? thin_kernel<T, true, 2>() : tp.vbuf == 1 ? thin_kernel<T, true, 1>() : thin_kernel<T, true, 0>()) : thin_kernel<T, false, 0>();
@@ -796,7 +781,7 @@ template <class T> int multq_thin(bool notran, size_t m, size_t n, size_t k, con
     p.rows_per_cta = tp.rows;
     RNPGPU_CHECK(cudaMemsetAsync(sync, 0, 2 * sizeof(unsigned), st));
     void *args[] = {&p};
-    KScope ks(tag, st);
+    KScope ks("multq_thin", st);
     return coop_launch("k_multq_thin", kern, tp.grid, kThinThreads, args, tp.smem, st);
 }
 

@@ -50,7 +50,6 @@ extern "C" int rnpgpu_sgeqrf_mixed(size_t m, size_t n, float *a, size_t lda, flo
     if (wide_ok) {
         cw.wide = wide::carve(cv, m, n);
         cw.use_wide = (flags & 2) == 0;
-        cw.thin_inner = (flags & 4) == 0;
     }
     RNPGPU_CHECK(cudaMemsetAsync(cw.fail, 0, sizeof(int), st));
     size_t lw = fbytes / sizeof(float);

@@ -10,12 +10,13 @@ import pytest
 sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
 import bench  # noqa: E402
 
-CLASSES = ["panel_cqr", "larfb_w", "larfb_update", "residual_fp64", "normal_eq_fp64", "prepare_digits"]
+CLASSES = ["panel_cqr", "larfb_w", "larfb_update", "wide_w", "wide_update", "wide_vsplit", "residual_fp64", "normal_eq_fp64", "prepare_digits"]
 
 
 def fake_profile(steps):
     # (launches, total ms) over `steps` solves
-    per_step = {"panel_cqr": (16, 0.84), "larfb_w": (15, 0.60), "larfb_update": (15, 0.72), "residual_fp64": (3, 0.30),
+    per_step = {"panel_cqr": (16, 0.84), "larfb_w": (12, 0.33), "larfb_update": (12, 0.28), "wide_w": (3, 0.16), "wide_update": (3, 0.10),
+                "wide_vsplit": (3, 0.12), "wide_t": (3, 0.13), "residual_fp64": (3, 0.30),
                 "normal_eq_fp64": (1, 0.11), "prepare_digits": (1, 0.25), "multq_thin": (3, 0.62)}
     return {k: (c * steps, ms * steps) for k, (c, ms) in per_step.items()}
 
