@@ -259,7 +259,7 @@ def timed(torch, fn, reps):
     return best
 
 
-def batched_config(torch, dev, gq, lib, peak64, count=20000, loop_sample=200, check_sample=40):
+def batched_config(torch, dev, gq, lib, peak64, count=20000, loop_sample=200, check_sample=20000):
     """Batched FP64 QR of `count` matrices, m ~ U[16,256], n ~ U[8,m], N(0,1)
     entries, packed with lda = m: the tuned plan's run captured in a CUDA
     graph and replayed, against looping the plain Factor over a sample."""
@@ -299,18 +299,32 @@ def batched_config(torch, dev, gq, lib, peak64, count=20000, loop_sample=200, ch
         times.append(e0.elapsed_time(e1))
     ms_batched = min(times[1:])
     flops = float(sum(2.0 * m * min(m, n) * n - min(m, n) ** 2 * (m + n) + 2.0 * min(m, n) ** 3 / 3 for m, n in zip(ms, ns)))
-    # every R of a sample against the CPU oracle
-    o = orc.load()
+    # R of every matrix (or of a sample) against the CPU oracle, on all host
+    # cores (the oracle's calls release the interpreter lock)
     worst = 0.0
-    for i in rng.choice(count, check_sample, replace=False):
-        i = int(i)
-        m, n = int(ms[i]), int(ns[i])
-        x = np.asfortranarray(a0[int(b.a_off[i]):int(b.a_off[i]) + m * n].view(n, m).t().cpu().numpy())
-        o.geqrf("d", m, n, x)
-        k = min(m, n)
-        rg = np.triu(b.matrix(i).cpu().numpy()[:k])
-        ro = np.triu(x[:k])
-        worst = max(worst, float(np.linalg.norm(rg - ro) / np.linalg.norm(ro)))
+    t_check = 0.0
+    if check_sample > 0:
+        import concurrent.futures as cf
+
+        o = orc.load()
+        fac = b.a.cpu().numpy()
+        src = a0.cpu().numpy()
+        offs = b.a_off.cpu().numpy() if hasattr(b.a_off, "cpu") else np.asarray(b.a_off)
+        idx = range(count) if check_sample >= count else [int(i) for i in rng.choice(count, check_sample, replace=False)]
+
+        def one(i):
+            m, n, off = int(ms[i]), int(ns[i]), int(offs[i])
+            x = np.asfortranarray(src[off:off + m * n].reshape(n, m).T)
+            o.geqrf("d", m, n, x)
+            k = min(m, n)
+            rg = np.triu(fac[off:off + m * n].reshape(n, m).T[:k])
+            ro = np.triu(x[:k])
+            return float(np.linalg.norm(rg - ro) / np.linalg.norm(ro))
+
+        t0 = time.perf_counter()
+        with cf.ThreadPoolExecutor(max_workers=os.cpu_count() or 1) as ex:
+            worst = max(ex.map(one, idx))
+        t_check = time.perf_counter() - t0
     # looping the plain Factor over a sample of the same matrices
     idx = [int(i) for i in rng.choice(count, loop_sample, replace=False)]
     mats = [gq.to_colmajor(a0[int(b.a_off[i]):int(b.a_off[i]) + int(ms[i]) * int(ns[i])].view(int(ns[i]), int(ms[i])).t()) for i in idx]
@@ -339,7 +353,7 @@ def batched_config(torch, dev, gq, lib, peak64, count=20000, loop_sample=200, ch
         "loop_plain_solves_per_s": count / (loop_ms_total * 1e-3), "loop_plain_ms_per_matrix": loop_ms_per,
         "loop_sample": "plain Factor looped over %d random matrices of the batch, scaled to the batch by flops" % loop_sample,
         "speedup_vs_loop": loop_ms_total / ms_batched,
-        "r_max_rel_err_vs_oracle": worst, "r_check_sample": check_sample,
+        "r_max_rel_err_vs_oracle": worst, "r_check_sample": min(check_sample, count), "r_check_seconds": t_check,
     }
 
 
@@ -459,7 +473,7 @@ def batched_ls_config(torch, dev, count=4096, check_sample=32):
     return out
 
 
-def other_configs(torch, dev, gq, lib, peak64, check=True):
+def other_configs(torch, dev, gq, lib, peak64, check=True, only_c2=False):
     """The plain FP64 drop-in on the reference's other configurations:
     1024x256 real Factor + GenerateQ, and 4096x4096 complex Factor followed by
     MultQ("L","C") on a 4096x64 block (FP64 throughout)."""
@@ -467,26 +481,29 @@ def other_configs(torch, dev, gq, lib, peak64, check=True):
     g = torch.Generator(device=dev).manual_seed(7)
     # 1024 x 256 real, entries uniform[-1, 1]
     A0 = gq.to_colmajor(2 * torch.rand((1024, 256), generator=g, dtype=torch.float64, device=dev) - 1)
+    if only_c2:
+        g = torch.Generator(device=dev).manual_seed(8)
     A = gq.to_colmajor(A0)
     tau = torch.zeros(256, dtype=torch.float64, device=dev)
     wf = torch.empty(gq.workspace_query("geqrf", torch.float64, 1024, 256), dtype=torch.float64, device=dev)
     wq = torch.empty(gq.workspace_query("ungqr", torch.float64, 1024, 256, 256), dtype=torch.float64, device=dev)
-    ms_f = timed(torch, lambda: ((lambda: A.copy_(A0)), (lambda: gq.factor(A, tau, wf))), 5)
-    ms_q = timed(torch, lambda: ((lambda: (A.copy_(A0), gq.factor(A, tau, wf))), (lambda: gq.generate_q(A, tau, 256, wq))), 5)
-    f1 = 2.0 * 1024 * 256 ** 2 - 2.0 * 256 ** 3 / 3
-    q1 = 4.0 * 1024 * 256 * 256 - 2.0 * (1024 + 256) * 256 ** 2 + 4.0 * 256 ** 3 / 3
-    out["qr_1024x256_f64"] = {"factor_ms": ms_f, "generate_q_ms": ms_q, "factor_gflops": f1 / ms_f / 1e6, "generate_q_gflops": q1 / ms_q / 1e6}
+    ms_f = 0.0 if only_c2 else timed(torch, lambda: ((lambda: A.copy_(A0)), (lambda: gq.factor(A, tau, wf))), 5)
+    if not only_c2:
+        ms_q = timed(torch, lambda: ((lambda: (A.copy_(A0), gq.factor(A, tau, wf))), (lambda: gq.generate_q(A, tau, 256, wq))), 5)
+        f1 = 2.0 * 1024 * 256 ** 2 - 2.0 * 256 ** 3 / 3
+        q1 = 4.0 * 1024 * 256 * 256 - 2.0 * (1024 + 256) * 256 ** 2 + 4.0 * 256 ** 3 / 3
+        out["qr_1024x256_f64"] = {"factor_ms": ms_f, "generate_q_ms": ms_q, "factor_gflops": f1 / ms_f / 1e6, "generate_q_gflops": q1 / ms_q / 1e6}
     # 4096 x 4096 complex, re/im N(0,1); MultQ("L","C") on 4096 x 64
     n = 4096
     Z0 = gq.to_colmajor(torch.complex(torch.randn((n, n), generator=g, dtype=torch.float64, device=dev), torch.randn((n, n), generator=g, dtype=torch.float64, device=dev)))
     Z = gq.to_colmajor(Z0)
     tz = torch.zeros(n, dtype=torch.complex128, device=dev)
     wz = torch.empty(gq.workspace_query("geqrf", torch.complex128, n, n), dtype=torch.complex128, device=dev)
-    ms_z = timed(torch, lambda: ((lambda: Z.copy_(Z0)), (lambda: gq.factor(Z, tz, wz))), 2)
+    ms_z = timed(torch, lambda: ((lambda: Z.copy_(Z0)), (lambda: gq.factor(Z, tz, wz))), 1 if only_c2 else 2)
     C0 = gq.to_colmajor(torch.complex(torch.randn((n, 64), generator=g, dtype=torch.float64, device=dev), torch.randn((n, 64), generator=g, dtype=torch.float64, device=dev)))
     Cc = gq.to_colmajor(C0)
     wm = torch.empty(gq.workspace_query("unmqr", torch.complex128, n, 64, n, side="L", trans="C"), dtype=torch.complex128, device=dev)
-    ms_m = timed(torch, lambda: ((lambda: Cc.copy_(C0)), (lambda: gq.mult_q("L", "C", Z, tz, Cc, n, wm))), 3)
+    ms_m = timed(torch, lambda: ((lambda: Cc.copy_(C0)), (lambda: gq.mult_q("L", "C", Z, tz, Cc, n, wm))), 1 if only_c2 else 3)
     fz = 4.0 * (2.0 * n ** 3 - 2.0 * n ** 3 / 3)
     fm = 4.0 * 2.0 * 64 * n * (2.0 * n - n)
     out["qr_4096x4096_c128"] = {"factor_ms": ms_z, "factor_tflops": fz / ms_z / 1e9, "factor_frac_of_fp64_peak": fz / ms_z / 1e9 / peak64 if peak64 else None,
@@ -633,6 +650,18 @@ def gpu_arm(args, rank, world, local):
             dist.barrier()
         torch.cuda.synchronize()
 
+    if args.phase in ("batched", "c2"):
+        # profiling runs of the other configurations alone
+        if args.phase == "batched":
+            out = {"batched": batched_config(torch, dev, gq, lib, 0.0, check_sample=0), "batched_ls": batched_ls_config(torch, dev, check_sample=0)}
+        else:
+            out = other_configs(torch, dev, gq, lib, 0.0, check=False, only_c2=True)
+        if rank == 0:
+            print(json.dumps({"phase": args.phase, "configs": out}), flush=True)
+        if dist is not None:
+            dist.destroy_process_group()
+        return 0
+
     A, b = make_problem(torch, dev)
     X = gq.empty_colmajor(N, NRHS, torch.float64, dev)
     work = torch.empty(gls.refine_workspace(A, NRHS), dtype=torch.float64, device=dev)
@@ -770,6 +799,8 @@ def gpu_arm(args, rank, world, local):
     scratch = torch.empty(torch.cuda.get_device_properties(dev).multi_processor_count * 8 * 256, dtype=torch.float64, device=dev)
     peak64 = C.c_double(0)
     lib.rnpgpu_probe_peak(0, C.c_void_p(scratch.data_ptr()), scratch.numel() * 8, C.byref(peak64))
+    peak64_mma = C.c_double(0)
+    lib.rnpgpu_probe_peak(2, C.c_void_p(scratch.data_ptr()), scratch.numel() * 8, C.byref(peak64_mma))
     tot_ms = sum(v[1] for v in prof.values())
     top = max(prof.items(), key=lambda kv: kv[1][1]) if prof else ("none", (0, 0.0))
     roofline, roofline_others = kernel_rooflines(prof, tot_ms, top[0], peak64.value, prof_steps)
@@ -825,6 +856,8 @@ def gpu_arm(args, rank, world, local):
                        "tflops": solve_flops(M, N, NRHS) / (ms_plain * 1e-3) / 1e12,
                        "profile_ms": {k: v[1] for k, v in sorted(prof_plain.items(), key=lambda kv: -kv[1][1])}},
         "speedup_mixed_vs_plain": ms_plain / ms,
+        "fp64_peaks_measured_tflops": {"fma": peak64.value, "mma_m8n8k4": peak64_mma.value,
+                                       "note": "FP64 contractions run on the FMA pipe, the faster of the two on this GPU"},
         "profile_ms_per_step": {k: v[1] / prof_steps for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])},
         "top_kernel": top[0],
         "roofline": roofline,
@@ -848,8 +881,12 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-configs", action="store_true", help="skip the other plain configurations")
-    ap.add_argument("--phase", default="all", choices=["all", "mixed"], help="'mixed': only the timed mixed solves (for profiler runs)")
+    ap.add_argument("--phase", default="all", choices=["all", "mixed", "batched", "c2"],
+                    help="profiler runs: 'mixed' only the timed mixed solves, 'batched' only the batched configurations, 'c2' only the 4096^2 complex one")
+    ap.add_argument("--m", type=int, default=M, help="rows of the least-squares workload (profiler runs of a smaller case)")
     args = ap.parse_args()
+    global M
+    M = args.m
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
     rank, world, local = dist_env()
     if args.impl == "reference":

@@ -126,9 +126,11 @@ unsigned long long rnpgpu_launch_count(void);
  * (since the last report) into buf; returns the report's length. */
 int rnpgpu_timing_enable(int on);
 int rnpgpu_timing_report(char *buf, size_t len);
-/* Measured FMA throughput of the current device in TFLOP/s (kind 0: FP64,
- * kind 1: FP32), using scratch (>= SMs*8*256 doubles) for the probe's
- * outputs; synchronous.  Used as the roofline denominator of FP64 work. */
+/* Measured throughput of the current device in TFLOP/s (kind 0: FP64 FMA,
+ * kind 1: FP32 FMA, kind 2: FP64 tensor-core MMA, mma.sync m8n8k4), using
+ * scratch (>= SMs*8*256 doubles) for the probe's outputs; synchronous.  Used
+ * as the roofline denominator of FP64 work and to re-check that the FP64
+ * contractions belong on the FMA pipe. */
 int rnpgpu_probe_peak(int kind, void *scratch, size_t scratch_bytes, double *tflops);
 
 #ifdef __cplusplus

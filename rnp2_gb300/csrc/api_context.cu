@@ -176,6 +176,24 @@ __global__ void k_probe_ffma(float *out, int iters, float b, float c) {
     out[blockIdx.x * blockDim.x + threadIdx.x] = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
 }
 
+// FP64 tensor-core (DMMA) throughput probe: eight independent m8n8k4 FP64
+// MMA chains per warp (512 flops each per step)
+__global__ void k_probe_dmma(double *out, int iters) {
+    const double a = 1.0 + threadIdx.x * 1e-3, b = 0.999;
+    double c[8][2];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) c[j][0] = c[j][1] = 0.0;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+            asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0, %1}, {%2}, {%3}, {%0, %1};" : "+d"(c[j][0]), "+d"(c[j][1]) : "d"(a), "d"(b));
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) s += c[j][0] + c[j][1];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
 // per-type occupancy of the panel kernel (defined in the per-type units)
 int panel_blocks_per_sm_s();
 int panel_blocks_per_sm_d();
@@ -288,17 +306,20 @@ int rnpgpu_probe_peak(int kind, void *scratch, size_t scratch_bytes, double *tfl
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    const int iters = kind == 0 ? 4096 : 65536;
+    const int iters = kind == 0 ? 4096 : kind == 2 ? 2048 : 65536;
     double best = 0.0;
     for (int rep = 0; rep < 3; ++rep) {
         cudaEventRecord(e0, st);
         if (kind == 0) k_probe_dfma<<<blocks, threads, 0, st>>>((double *)scratch, iters, 0.999, 1e-3);
+        else if (kind == 2) k_probe_dmma<<<blocks, threads, 0, st>>>((double *)scratch, iters);
         else k_probe_ffma<<<blocks, threads, 0, st>>>((float *)scratch, iters, 0.999f, 1e-3f);
         cudaEventRecord(e1, st);
         cudaEventSynchronize(e1);
         float ms = 0.f;
         cudaEventElapsedTime(&ms, e0, e1);
-        double fl = 2.0 * 8 * (double)iters * blocks * threads;
+        // FMA kinds: 8 chains x 2 flops per thread per step; DMMA: 8 MMAs x
+        // 512 flops per warp per step
+        double fl = kind == 2 ? 8.0 * 512.0 * (double)iters * blocks * (threads / 32) : 2.0 * 8 * (double)iters * blocks * threads;
         if (ms > 0) best = std::max(best, fl / (ms * 1e-3) / 1e12);
     }
     cudaEventDestroy(e0);
