@@ -874,6 +874,7 @@ def gpu_arm(args, rank, world, local):
 
 
 def main():
+    global M
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=50)
@@ -885,7 +886,6 @@ def main():
                     help="profiler runs: 'mixed' only the timed mixed solves, 'batched' only the batched configurations, 'c2' only the 4096^2 complex one")
     ap.add_argument("--m", type=int, default=M, help="rows of the least-squares workload (profiler runs of a smaller case)")
     args = ap.parse_args()
-    global M
     M = args.m
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
     rank, world, local = dist_env()
