@@ -544,8 +544,13 @@ def other_configs(torch, dev, gq, lib, peak64, check=True, only_c2=False):
 # to the average launch by the algorithmic bytes (traffic grows with the
 # columns and rows processed).  Captured launches: the 65,408 x 32 panels, the
 # update and W of the 65,408-row step with 352 trailing columns, one residual
-# r = b - A x and one A^T r of the 65536 x 512 x 16 refinement.
+# r = b - A x and one A^T r of the 65536 x 512 x 16 refinement; the
+# tensor-core W and update of the first 128-column block at 32768 rows
+# (384 trailing columns; the update's writes of C were still in L2 when the
+# capture ended).
 NCU_TRAFFIC = {
+    "wide_w": (75.776000e6 + 2.950400e6, 32768 * (384 + 128) * 4.0),
+    "wide_update": (75.826944e6 + 2.329088e6, 2.0 * 32768 * 384 * 4 + 32768 * 128 * 4.0),
     "panel": (8.494080e6 + 0.003072e6, 2.0 * 65408 * 32 * 4),
     "panel_cqr": (8.489984e6 + 0.0, 2.0 * 65408 * 32 * 4),
     "larfb_update": (100.581632e6 + 32.246784e6, 2.0 * 65408 * 352 * 4 + 65408 * 32 * 4.0),
