@@ -90,6 +90,46 @@ class QRLib:
             w = np.zeros(max(n, 1), dtype=DT[p])
             self.fn(p, "ung2r")(SZ(m), SZ(n), SZ(k), ptr(a), SZ(a.shape[0]), ptr(tau), ptr(w))
 
+    # LQ / QL / RQ: kind in ("lq", "ql", "rq"); LAPACK-style names
+    XNAMES = {"lq": ("gelqf", "unmlq", "unglq"), "ql": ("geqlf", "unmql", "ungql"), "rq": ("gerqf", "unmrq", "ungrq")}
+
+    def xgeqrf(self, kind, p, m, n, a):
+        """Factor of kind on a (Fortran-ordered, ld = a.shape[0]); returns tau."""
+        tau = np.zeros(max(min(m, n), 1), dtype=DT[p])
+        f = self.fn(p, self.XNAMES[kind][0])
+        if self.pre == "ref_":
+            lw = SZ(0)
+            f(SZ(m), SZ(n), ptr(a), SZ(a.shape[0]), ptr(tau), C.byref(lw), None)
+            w = np.zeros(max(lw.value, 1), dtype=DT[p])
+            f(SZ(m), SZ(n), ptr(a), SZ(a.shape[0]), ptr(tau), C.byref(lw), ptr(w))
+        else:
+            f(SZ(m), SZ(n), ptr(a), SZ(a.shape[0]), ptr(tau))
+        return tau[: min(m, n)]
+
+    def xunmqr(self, kind, p, side, trans, m, n, k, a, tau, c):
+        """MultQ of kind: a holds the k reflectors (k x nq for lq/rq, nq x k for ql)."""
+        tau = np.ascontiguousarray(tau)
+        f = self.fn(p, self.XNAMES[kind][1])
+        args = (side.encode(), trans.encode(), SZ(m), SZ(n), SZ(k), ptr(a), SZ(a.shape[0]), ptr(tau), ptr(c), SZ(c.shape[0]))
+        if self.pre == "ref_":
+            lw = SZ(0)
+            f(*args, C.byref(lw), None)
+            w = np.zeros(max(lw.value, 1), dtype=DT[p])
+            f(*args, C.byref(lw), ptr(w))
+        else:
+            f(*args)
+
+    def xungqr(self, kind, p, m, n, k, a, tau):
+        tau = np.ascontiguousarray(tau)
+        f = self.fn(p, self.XNAMES[kind][2])
+        if self.pre == "ref_":
+            lw = SZ(0)
+            f(SZ(m), SZ(n), SZ(k), ptr(a), SZ(a.shape[0]), ptr(tau), C.byref(lw), None)
+            w = np.zeros(max(lw.value, 1), dtype=DT[p])
+            f(SZ(m), SZ(n), SZ(k), ptr(a), SZ(a.shape[0]), ptr(tau), C.byref(lw), ptr(w))
+        else:
+            f(SZ(m), SZ(n), SZ(k), ptr(a), SZ(a.shape[0]), ptr(tau))
+
     def gels(self, p, m, n, nrhs, a, b):
         """Least squares by Factor + MultQ("L","C") + triangular solve; a, b overwritten."""
         tau = np.zeros(max(min(m, n), 1), dtype=DT[p])

@@ -22,6 +22,7 @@
 #include <cstdint>
 #include <limits>
 #include <vector>
+#include <utility>
 #include <string>
 #include <dlfcn.h>
 
@@ -717,6 +718,81 @@ template <class R> static void larnv_cplx(int dist, size_t n, std::complex<R> *x
     }
 }
 
+// ---------------------------------------------------------------------------
+// LQ, QL and RQ (RNP/LA/LQ.hpp, QL.hpp, RQ.hpp) restated through the QR of a
+// transformed matrix (J = reversal, X^H = conjugate transpose):
+//   LQ(A) = [QR(A^H)]^H,  QL(A) = J QR(J A J) J,  RQ(A) = [J QR(J A^H J) J]^H,
+// tau in reverse order for QL and RQ.  The reference's row-wise generation
+// of a conjugated row (LQ.hpp:79-97, RQ.hpp:80-112), its bottom-up columns
+// (QL.hpp:80-109) and its blocked updates with storev "R" / direction "B"
+// (Reflector.hpp:627-676, 816-1062) perform the transformed operations of
+// the QR's, so the results agree to rounding; the golden vectors of the
+// reference build pin them.  MultQ: LQ and RQ flip trans; QL and RQ apply to
+// C with its rows (side L) or columns (side R) reversed.
+// ---------------------------------------------------------------------------
+enum { kLQ = 0, kQL = 1, kRQ = 2 };
+// dst (ldd) = X(src), src rows x cols
+template <class T> void xform(int kind, size_t rows, size_t cols, const T *src, size_t lds, T *dst, size_t ldd) {
+    for (size_t j = 0; j < cols; ++j)
+        for (size_t i = 0; i < rows; ++i) {
+            const T v = src[i + j * lds];
+            if (kind == kLQ) dst[j + i * ldd] = Tr<T>::conj(v);
+            else if (kind == kQL) dst[(rows - 1 - i) + (cols - 1 - j) * ldd] = v;
+            else dst[(cols - 1 - j) + (rows - 1 - i) * ldd] = Tr<T>::conj(v);
+        }
+}
+template <class T> void x_factor(int kind, size_t m, size_t n, T *a, size_t lda, T *tau) {
+    const size_t k = m < n ? m : n;
+    if (k == 0) return;
+    const size_t mt = kind == kQL ? m : n, nt = kind == kQL ? n : m;
+    std::vector<T> b(mt * nt), t(k);
+    xform(kind, m, n, a, lda, b.data(), mt);
+    size_t lw = 0;
+    factor<T>(mt, nt, b.data(), mt, t.data(), &lw, nullptr);
+    std::vector<T> w(lw > 0 ? lw : 1);
+    factor<T>(mt, nt, b.data(), mt, t.data(), &lw, w.data());
+    xform(kind, mt, nt, b.data(), mt, a, lda);
+    for (size_t i = 0; i < k; ++i) tau[i] = kind == kLQ ? t[i] : t[k - 1 - i];
+}
+template <class T> void x_multq(int kind, char side, char trans, size_t m, size_t n, size_t k, const T *a, size_t lda, const T *tau, T *c, size_t ldc) {
+    if (m == 0 || n == 0 || k == 0) return;
+    const bool left = side == 'L';
+    const size_t nq = left ? m : n;
+    std::vector<T> b(nq * k), t(k);
+    if (kind == kQL) xform(kind, nq, k, a, lda, b.data(), nq);
+    else xform(kind, k, nq, a, lda, b.data(), nq);
+    for (size_t i = 0; i < k; ++i) t[i] = kind == kLQ ? tau[i] : tau[k - 1 - i];
+    const char tr = kind == kQL ? trans : (trans == 'N' ? 'C' : 'N');
+    auto flip = [&]() {
+        if (kind == kLQ) return;
+        if (left) {
+            for (size_t j = 0; j < n; ++j)
+                for (size_t i = 0; i < m / 2; ++i) std::swap(c[i + j * ldc], c[(m - 1 - i) + j * ldc]);
+        } else {
+            for (size_t j = 0; j < n / 2; ++j)
+                for (size_t i = 0; i < m; ++i) std::swap(c[i + j * ldc], c[i + (n - 1 - j) * ldc]);
+        }
+    };
+    flip();
+    size_t lw = 0;
+    multq<T>(side, tr, m, n, k, b.data(), nq, t.data(), c, ldc, &lw, nullptr);
+    std::vector<T> w(lw > 0 ? lw : 1);
+    multq<T>(side, tr, m, n, k, b.data(), nq, t.data(), c, ldc, &lw, w.data());
+    flip();
+}
+template <class T> void x_genq(int kind, size_t m, size_t n, size_t k, T *a, size_t lda, const T *tau) {
+    if (m == 0 || n == 0) return;
+    const size_t mt = kind == kQL ? m : n, nt = kind == kQL ? n : m;
+    std::vector<T> b(mt * nt), t(k > 0 ? k : 1);
+    xform(kind, m, n, a, lda, b.data(), mt);
+    for (size_t i = 0; i < k; ++i) t[i] = kind == kLQ ? tau[i] : tau[k - 1 - i];
+    size_t lw = 0;
+    genq<T>(mt, nt, k, b.data(), mt, t.data(), &lw, nullptr);
+    std::vector<T> w(lw > 0 ? lw : 1);
+    genq<T>(mt, nt, k, b.data(), mt, t.data(), &lw, w.data());
+    xform(kind, mt, nt, b.data(), mt, a, lda);
+}
+
 } // namespace orc
 
 // ---------------------------------------------------------------------------
@@ -733,6 +809,19 @@ using namespace orc;
     extern "C" void oracle_##P##larfg(size_t n, T *alpha, T *x, size_t incx, T *tau) { generate<T>(n, alpha, x, incx, tau); } \
     extern "C" void oracle_##P##larft(size_t n, size_t k, const T *v, size_t ldv, const T *tau, T *t, size_t ldt) { block_tr<T>(n, k, v, ldv, tau, t, ldt); } \
     extern "C" void oracle_##P##gels(size_t m, size_t n, size_t nrhs, T *a, size_t lda, T *tau, T *b, size_t ldb) { gels<T>(m, n, nrhs, a, lda, tau, b, ldb); }
+#define ORC_XDEF(P, T, F, M, G, KIND)                                                                                   \
+    extern "C" void oracle_##P##F(size_t m, size_t n, T *a, size_t lda, T *tau) { x_factor<T>(KIND, m, n, a, lda, tau); } \
+    extern "C" void oracle_##P##M(const char *side, const char *trans, size_t m, size_t n, size_t k, const T *a, size_t lda, \
+                                  const T *tau, T *c, size_t ldc) { x_multq<T>(KIND, side[0], trans[0], m, n, k, a, lda, tau, c, ldc); } \
+    extern "C" void oracle_##P##G(size_t m, size_t n, size_t k, T *a, size_t lda, const T *tau) { x_genq<T>(KIND, m, n, k, a, lda, tau); }
+#define ORC_XDEF3(P, T)                             \
+    ORC_XDEF(P, T, gelqf, unmlq, unglq, kLQ)        \
+    ORC_XDEF(P, T, geqlf, unmql, ungql, kQL)        \
+    ORC_XDEF(P, T, gerqf, unmrq, ungrq, kRQ)
+ORC_XDEF3(s, float)
+ORC_XDEF3(d, double)
+ORC_XDEF3(c, cf)
+ORC_XDEF3(z, cd)
 ORC_DEF(s, float)
 ORC_DEF(d, double)
 ORC_DEF(c, cf)

@@ -11,9 +11,13 @@
 // Entry points mirror the reference API:
 //   RNP::LA::QR::Factor / Factor_unblocked / MultQ / MultQ_unblocked /
 //   GenerateQ / GenerateQ_unblocked   (RNP/LA/QR.hpp:78-570)
+//   the same six for RNP::LA::LQ, QL and RQ (RNP/LA/LQ.hpp, QL.hpp, RQ.hpp)
 //   RNP::Random::GenerateVector       (RNP/Random.hpp:262-320)
 //   RNP::BLAS::SolveTrM               (RNP/BLAS/BLAS_mix.hpp:2096-2113)
 #include <RNP/LA/QR.hpp>
+#include <RNP/LA/LQ.hpp>
+#include <RNP/LA/QL.hpp>
+#include <RNP/LA/RQ.hpp>
 #include <RNP/Random.hpp>
 #include <RNP/BLAS.hpp>
 #include <complex>
@@ -48,6 +52,34 @@ typedef std::complex<double> cd;
         RNP::BLAS::SolveTrM("L", "U", "N", "N", n, nrhs, T(1), a, lda, b, ldb);                                      \
     }
 
+// LQ / QL / RQ under LAPACK-style names (factor, unblocked factor, MultQ,
+// unblocked MultQ, GenerateQ, unblocked GenerateQ)
+#define REF_DEF2(P, T, NS, F, F2, M, M2, G, G2)                                                                         \
+    extern "C" void ref_##P##F(size_t m, size_t n, T *a, size_t lda, T *tau, size_t *lwork, T *work) {                \
+        RNP::LA::NS::Factor<T>(m, n, a, lda, tau, lwork, work);                                                       \
+    }                                                                                                                 \
+    extern "C" void ref_##P##F2(size_t m, size_t n, T *a, size_t lda, T *tau, T *work) {                              \
+        RNP::LA::NS::Factor_unblocked<T>(m, n, a, lda, tau, work);                                                    \
+    }                                                                                                                 \
+    extern "C" void ref_##P##M(const char *side, const char *trans, size_t m, size_t n, size_t k, const T *a,         \
+                               size_t lda, const T *tau, T *c, size_t ldc, size_t *lwork, T *work) {                  \
+        RNP::LA::NS::MultQ<T>(side, trans, m, n, k, a, lda, tau, c, ldc, lwork, work);                                \
+    }                                                                                                                 \
+    extern "C" void ref_##P##M2(const char *side, const char *trans, size_t m, size_t n, size_t k, const T *a,        \
+                                size_t lda, const T *tau, T *c, size_t ldc, T *work) {                                \
+        RNP::LA::NS::MultQ_unblocked<T>(side, trans, m, n, k, a, lda, tau, c, ldc, work);                             \
+    }                                                                                                                 \
+    extern "C" void ref_##P##G(size_t m, size_t n, size_t k, T *a, size_t lda, const T *tau, size_t *lwork, T *work) { \
+        RNP::LA::NS::GenerateQ<T>(m, n, k, a, lda, tau, lwork, work);                                                 \
+    }                                                                                                                 \
+    extern "C" void ref_##P##G2(size_t m, size_t n, size_t k, T *a, size_t lda, const T *tau, T *work) {              \
+        RNP::LA::NS::GenerateQ_unblocked<T>(m, n, k, a, lda, tau, work);                                              \
+    }
+#define REF_DEF3(P, T)                                                             \
+    REF_DEF2(P, T, LQ, gelqf, gelq2, unmlq, unml2, unglq, ungl2)                   \
+    REF_DEF2(P, T, QL, geqlf, geql2, unmql, unm2l, ungql, ung2l)                   \
+    REF_DEF2(P, T, RQ, gerqf, gerq2, unmrq, unmr2, ungrq, ungr2)
+
 #define REF_RNG(P, T)                                                                                                   \
     extern "C" void ref_##P##larnv(int dist, int *iseed, size_t n, T *x) {                                            \
         RNP::Random::GenerateVector<T>((RNP::Random::Distribution::Distribution)dist, n, x, iseed);                   \
@@ -57,6 +89,10 @@ REF_DEF(s, float)
 REF_DEF(d, double)
 REF_DEF(c, cf)
 REF_DEF(z, cd)
+REF_DEF3(s, float)
+REF_DEF3(d, double)
+REF_DEF3(c, cf)
+REF_DEF3(z, cd)
 // GenerateVector<std::complex<float> > does not compile in the reference
 // (RNP/Random.hpp:213 mixes double and float), so no "c" generator here.
 REF_RNG(s, float)

@@ -48,6 +48,10 @@ def _signatures():
         sig["rnpgpu_%sung2r" % p] = [SZ, SZ, SZ, P, SZ, P, P]
         sig["rnpgpu_%strsm_lunn" % p] = [SZ, SZ, P, SZ, P, SZ]
         sig["rnpgpu_%sgels" % p] = [SZ, SZ, SZ, P, SZ, P, P, SZ, PSZ, P]
+        for f, mq, g in (("gelqf", "unmlq", "unglq"), ("geqlf", "unmql", "ungql"), ("gerqf", "unmrq", "ungrq")):
+            sig["rnpgpu_%s%s" % (p, f)] = [SZ, SZ, P, SZ, P, PSZ, P]
+            sig["rnpgpu_%s%s" % (p, mq)] = [CH, CH, SZ, SZ, SZ, P, SZ, P, P, SZ, PSZ, P]
+            sig["rnpgpu_%s%s" % (p, g)] = [SZ, SZ, SZ, P, SZ, P, PSZ, P]
     for name in ("rnpgpu_dsgels", "rnpgpu_zcgels"):
         sig[name] = [SZ, SZ, SZ, P, SZ, P, SZ, P, SZ, C.c_int, C.c_int, C.POINTER(RefineInfo), PSZ, P]
     sig["rnpgpu_dls_residual"] = [SZ, SZ, SZ, P, SZ, P, SZ, P, SZ, P, SZ, P, SZ, P, PSZ]
