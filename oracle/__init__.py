@@ -130,6 +130,16 @@ class QRLib:
         else:
             f(SZ(m), SZ(n), SZ(k), ptr(a), SZ(a.shape[0]), ptr(tau))
 
+    def random_matrix(self, p, sym, dist, mode, reverse, cond, dmax, m, n, seed, d=None):
+        """RNP::MatrixGen::RandomMatrix (real p only): returns (a, d, seed_out)."""
+        R = C.c_double if p == "d" else C.c_float
+        a = np.zeros((max(m, 1), max(n, 1)), dtype=DT[p], order="F")
+        k = min(m, n)
+        dd = np.zeros(max(k, 1), dtype=DT[p]) if d is None else np.array(d, dtype=DT[p])
+        s = (C.c_int * 4)(*seed)
+        self.fn(p, "random_matrix")(C.c_int(sym), C.c_int(dist), C.c_int(mode), C.c_int(reverse), R(cond), R(dmax), ptr(dd), SZ(m), SZ(n), ptr(a), SZ(a.shape[0]), s)
+        return a[:m, :n], dd[:k], list(s)
+
     def gels(self, p, m, n, nrhs, a, b):
         """Least squares by Factor + MultQ("L","C") + triangular solve; a, b overwritten."""
         tau = np.zeros(max(min(m, n), 1), dtype=DT[p])

@@ -679,6 +679,18 @@ template <class R> static void uniform01(size_t n, R *x, int iseed[4]) {
 // dist: 0 = Uniform01, 1 = Uniform_11, 2 = Normal01 (RNP/Random.hpp:262-289)
 template <class R> static void larnv_real(int dist, size_t n, R *x, int iseed[4]) {
     if (dist == 0) { uniform01(n, x, iseed); return; }
+    if (dist == 3 || dist == 4) {
+        // UnitDisc / UnitCircle for real numbers (RNP/Random.hpp:291-315):
+        // a whole chunk of 128 uniforms per 64 outputs, from the even ones
+        R pool[128];
+        for (size_t i0 = 0; i0 < n; i0 += 64) {
+            size_t ilim = 64;
+            if (n < i0 + ilim) ilim = n - i0;
+            uniform01(128, pool, iseed);
+            for (size_t i = 0; i < ilim; ++i) x[i0 + i] = dist == 3 ? R(2) * pool[2 * i] - R(1) : ((R(2) * pool[2 * i] < R(1)) ? R(-1) : R(1));
+        }
+        return;
+    }
     if (dist == 1) {
         uniform01(n, x, iseed);
         for (size_t i = 0; i < n; ++i) x[i] = R(2) * x[i] - R(1);
@@ -716,6 +728,121 @@ template <class R> static void larnv_cplx(int dist, size_t n, std::complex<R> *x
             x[i0 + i] = std::sqrt(R(-2) * std::log1p(-pool[2 * i])) * std::complex<R>(std::cos(ang), std::sin(ang));
         }
     }
+}
+
+// ---------------------------------------------------------------------------
+// MatrixGen (RNP/MatrixGen.hpp): GenerateDiagonal (:31-109) and RandomMatrix
+// (:120-272) for real types (the reference's RandomMatrix does not compile
+// for complex types).  sym: 0 Nonsymmetric, 1 Hermitian, 2 Hermitian
+// positive definite, 3 Symmetric (the last three are one path for reals).
+// ---------------------------------------------------------------------------
+template <class T> void gen_diagonal(int dist, int mode, bool reverse, bool randsign, T cond, T dscale, size_t n, T *d, int iseed[4]) {
+    if (n == 0) return;
+    const T rcond = T(1) / cond;
+    switch (mode) {
+    case 1:
+        d[0] = T(1);
+        for (size_t i = 1; i < n; ++i) d[i] = rcond;
+        break;
+    case 2:
+        for (size_t i = 0; i + 1 < n; ++i) d[i] = T(1);
+        d[n - 1] = rcond;
+        break;
+    case 3:
+        for (size_t i = 0; i < n; ++i) d[i] = std::pow(rcond, T(i) / T(n - 1));
+        break;
+    case 4:
+        for (size_t i = 0; i < n; ++i) {
+            const T t = T(i) / T(n - 1);
+            d[i] = (T(1) - t) + t * rcond;
+        }
+        break;
+    case 5:
+        uniform01(n, d, iseed);
+        for (size_t i = 0; i < n; ++i) d[i] = std::pow(rcond, d[i]);
+        break;
+    case 6:
+        larnv_real(dist, n, d, iseed);
+        break;
+    default:
+        break;
+    }
+    // RNP/MatrixGen.hpp:79-85 swaps d[i] and d[n-1-i] for every i in [0, n):
+    // each pair is swapped twice, so "reverse" leaves d as it was; restated
+    // as written
+    if (reverse)
+        for (size_t i = 0; i < n; ++i) std::swap(d[i], d[n - 1 - i]);
+    if (randsign)
+        for (size_t i = 0; i < n; ++i) {
+            T r;
+            uniform01(1, &r, iseed);
+            if (T(2) * r > T(1)) d[i] = -d[i];
+        }
+    if (mode != 0 && mode != 6) {
+        T maxabs = std::fabs(d[0]);
+        for (size_t i = 1; i < n; ++i) maxabs = std::max(maxabs, std::fabs(d[i]));
+        scal(n, dscale / maxabs, d, 1);
+    }
+}
+// the reflector of a Normal01 vector w (length len): u = w / (w0 + wa) with
+// u0 = 1, tau = (w0 + wa) / wa, wa = ||w|| sign(w0)  (RNP/MatrixGen.hpp:170-180)
+template <class T> T mg_reflector(size_t len, T *w, int iseed[4]) {
+    larnv_real(2, len, w, iseed);
+    const T wn = norm2(len, w, 1);
+    const T wa = (wn / std::fabs(w[0])) * w[0];
+    T tau(0);
+    if (wn != T(0)) {
+        const T wb = w[0] + wa;
+        scal(len - 1, T(1) / wb, w + 1, 1);
+        w[0] = T(1);
+        tau = wb / wa;
+    }
+    return tau;
+}
+template <class T> void random_matrix(int sym, int dist, int mode, bool reverse, T cond, T dmax, T *d_, size_t m, size_t n, T *a, size_t lda, int iseed[4]) {
+    const size_t k = m < n ? m : n;
+    if (k == 0) return;
+    std::vector<T> dd(k), work(m + n);
+    T *d = d_ ? d_ : dd.data();
+    gen_diagonal(dist, mode, reverse, sym == 1, cond, dmax, k, d, iseed);
+    for (size_t j = 0; j < n; ++j)
+        for (size_t i = 0; i < m; ++i) a[i + j * lda] = (i == j) ? d[i] : T(0);
+    T *w = work.data();
+    if (sym == 0) {
+        for (size_t i = k; i-- > 0;) {
+            if (i + 1 < m) {
+                const T tau = mg_reflector(m - i, w, iseed);
+                gemv('C', m - i, n - i, T(1), &a[i + i * lda], lda, w, 1, T(0), w + m, 1);
+                gerc(m - i, n - i, -tau, w, 1, w + m, 1, &a[i + i * lda], lda);
+            }
+            if (i + 1 < n) {
+                const T tau = mg_reflector(n - i, w, iseed);
+                gemv('N', m - i, n - i, T(1), &a[i + i * lda], lda, w, 1, T(0), w + n, 1);
+                gerc(m - i, n - i, -tau, w + n, 1, w, 1, &a[i + i * lda], lda);
+            }
+        }
+        return;
+    }
+    for (size_t i = n; i-- > 0;) {
+        const size_t len = n - i;
+        const T tau = mg_reflector(len, w, iseed);
+        T *A = &a[i + i * lda];
+        T *y = w + n;
+        // y = tau A u (lower triangle of A)
+        for (size_t r = 0; r < len; ++r) {
+            T acc(0);
+            for (size_t c = 0; c < len; ++c) acc += (r >= c ? A[r + c * lda] : A[c + r * lda]) * w[c];
+            y[r] = tau * acc;
+        }
+        T dot(0);
+        for (size_t r = 0; r < len; ++r) dot += y[r] * w[r];
+        const T alpha = -(T(1) / T(2)) * tau * dot;
+        for (size_t r = 0; r < len; ++r) y[r] += alpha * w[r];
+        for (size_t c = 0; c < len; ++c)
+            for (size_t r = c; r < len; ++r) A[r + c * lda] -= w[r] * y[c] + y[r] * w[c];
+    }
+    for (size_t j = 0; j < n; ++j)
+        for (size_t i = j + 1; i < n; ++i) a[j + i * lda] = a[i + j * lda];
 }
 
 // ---------------------------------------------------------------------------
@@ -827,6 +954,12 @@ ORC_DEF(d, double)
 ORC_DEF(c, cf)
 ORC_DEF(z, cd)
 
+extern "C" void oracle_srandom_matrix(int sym, int dist, int mode, int reverse, float cond, float dmax, float *d, size_t m, size_t n, float *a, size_t lda, int *iseed) {
+    random_matrix<float>(sym, dist, mode, reverse != 0, cond, dmax, d, m, n, a, lda, iseed);
+}
+extern "C" void oracle_drandom_matrix(int sym, int dist, int mode, int reverse, double cond, double dmax, double *d, size_t m, size_t n, double *a, size_t lda, int *iseed) {
+    random_matrix<double>(sym, dist, mode, reverse != 0, cond, dmax, d, m, n, a, lda, iseed);
+}
 extern "C" double oracle_dnrm2(size_t n, const double *x, size_t incx) { return norm2<double>(n, x, incx); }
 extern "C" double oracle_dznrm2(size_t n, const cd *x, size_t incx) { return norm2<cd>(n, x, incx); }
 extern "C" void oracle_dlarnv(int dist, int *iseed, size_t n, double *x) { larnv_real<double>(dist, n, x, iseed); }

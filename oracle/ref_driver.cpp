@@ -13,12 +13,14 @@
 //   GenerateQ / GenerateQ_unblocked   (RNP/LA/QR.hpp:78-570)
 //   the same six for RNP::LA::LQ, QL and RQ (RNP/LA/LQ.hpp, QL.hpp, RQ.hpp)
 //   RNP::Random::GenerateVector       (RNP/Random.hpp:262-320)
+//   RNP::MatrixGen::RandomMatrix      (RNP/MatrixGen.hpp:120-203)
 //   RNP::BLAS::SolveTrM               (RNP/BLAS/BLAS_mix.hpp:2096-2113)
 #include <RNP/LA/QR.hpp>
 #include <RNP/LA/LQ.hpp>
 #include <RNP/LA/QL.hpp>
 #include <RNP/LA/RQ.hpp>
 #include <RNP/Random.hpp>
+#include <RNP/MatrixGen.hpp>
 #include <RNP/BLAS.hpp>
 #include <complex>
 #include <cstddef>
@@ -84,6 +86,17 @@ typedef std::complex<double> cd;
     extern "C" void ref_##P##larnv(int dist, int *iseed, size_t n, T *x) {                                            \
         RNP::Random::GenerateVector<T>((RNP::Random::Distribution::Distribution)dist, n, x, iseed);                   \
     }
+
+#define REF_MG(P, T, R)                                                                                                 \
+    extern "C" void ref_##P##random_matrix(int sym, int dist, int mode, int reverse, R cond, R dmax, R *d, size_t m,   \
+                                           size_t n, T *a, size_t lda, int *iseed) {                                  \
+        RNP::MatrixGen::RandomMatrix<T>((RNP::MatrixGen::Symmetry::Sym)sym, (RNP::Random::Distribution::Distribution)dist, \
+                                        (RNP::MatrixGen::DiagonalMode::Mode)mode, reverse != 0, cond, dmax, d, m, n, a, lda, iseed); \
+    }
+// RandomMatrix compiles for real types only in the reference
+// (RNP/MatrixGen.hpp:175 scales a real vector by a complex 1/wb)
+REF_MG(s, float, float)
+REF_MG(d, double, double)
 
 REF_DEF(s, float)
 REF_DEF(d, double)

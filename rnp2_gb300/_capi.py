@@ -54,6 +54,8 @@ def _signatures():
             sig["rnpgpu_%s%s" % (p, g)] = [SZ, SZ, SZ, P, SZ, P, PSZ, P]
     for name in ("rnpgpu_dsgels", "rnpgpu_zcgels"):
         sig[name] = [SZ, SZ, SZ, P, SZ, P, SZ, P, SZ, C.c_int, C.c_int, C.POINTER(RefineInfo), PSZ, P]
+    sig["rnpgpu_srandom_matrix"] = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, P, SZ, SZ, P, SZ, C.POINTER(C.c_int), PSZ, P]
+    sig["rnpgpu_drandom_matrix"] = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, P, SZ, SZ, P, SZ, C.POINTER(C.c_int), PSZ, P]
     sig["rnpgpu_dls_residual"] = [SZ, SZ, SZ, P, SZ, P, SZ, P, SZ, P, SZ, P, SZ, P, PSZ]
     sig["rnpgpu_set_stream"] = [P]
     sig["rnpgpu_get_stream"] = []

@@ -4,6 +4,7 @@
 #define RNPGPU_P d
 #define RNPGPU_LOW_T float
 #define RNPGPU_MIXED_FN rnpgpu_dsgels
+#define RNPGPU_REAL 1
 #include "qr_type.inc"
 
 extern "C" int rnpgpu_dls_residual(size_t m, size_t n, size_t nrhs, const double *a, size_t lda, const double *x, size_t ldx, const double *b, size_t ldb, double *r, size_t ldr,

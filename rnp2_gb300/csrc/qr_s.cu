@@ -2,6 +2,7 @@
 #define RNPGPU_T float
 #define RNPGPU_CT float
 #define RNPGPU_P s
+#define RNPGPU_REAL 1
 #include "qr_type.inc"
 
 // C = alpha op(A) op(B) + beta C for FP32 on the tensor cores (three-term
