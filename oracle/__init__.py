@@ -140,6 +140,76 @@ class QRLib:
         self.fn(p, "random_matrix")(C.c_int(sym), C.c_int(dist), C.c_int(mode), C.c_int(reverse), R(cond), R(dmax), ptr(dd), SZ(m), SZ(n), ptr(a), SZ(a.shape[0]), s)
         return a[:m, :n], dd[:k], list(s)
 
+    # callers of QR / QL (Hessenberg and tridiagonal Q, generalized
+    # eigensystem QR step); the reference build takes a workspace query first
+    def _call_lw(self, f, args):
+        if self.pre == "ref_":
+            lw = SZ(0)
+            f(*args, C.byref(lw), None)
+            # generous: some of the reference's queries return less than the
+            # blocked path then takes (Tridiagonal::MultQHerm asks nw*nb, its
+            # QL::MultQ uses nw*nb + nb*nb and mis-sizes nb below that)
+            w = np.zeros(max(lw.value, 1) + 65536, dtype=self._dt)
+            lw = SZ(w.size)
+            f(*args, C.byref(lw), ptr(w))
+        else:
+            f(*args)
+
+    def gehrd(self, p, n, ilo, ihi, a):
+        """Hessenberg::Reduce (reference build only); returns tau (n - 1)."""
+        tau = np.zeros(max(n - 1, 1), dtype=DT[p])
+        self._dt = DT[p]
+        self._call_lw(self.fn(p, "gehrd"), (SZ(n), SZ(ilo), SZ(ihi), ptr(a), SZ(a.shape[0]), ptr(tau)))
+        return tau[: max(n - 1, 0)]
+
+    def unmhr(self, p, side, trans, m, n, ilo, ihi, a, tau, c):
+        tau = np.ascontiguousarray(tau)
+        self._dt = DT[p]
+        self._call_lw(self.fn(p, "unmhr"), (side.encode(), trans.encode(), SZ(m), SZ(n), SZ(ilo), SZ(ihi), ptr(a), SZ(a.shape[0]), ptr(tau), ptr(c), SZ(c.shape[0])))
+
+    def unghr(self, p, n, ilo, ihi, a, tau):
+        tau = np.ascontiguousarray(tau)
+        self._dt = DT[p]
+        self._call_lw(self.fn(p, "unghr"), (SZ(n), SZ(ilo), SZ(ihi), ptr(a), SZ(a.shape[0]), ptr(tau)))
+
+    def hetrd(self, p, uplo, n, a):
+        """Tridiagonal::ReduceHerm (reference build only); returns tau, diag, offdiag."""
+        R = np.float32 if p in "sc" else np.float64
+        tau = np.zeros(max(n - 1, 1), dtype=DT[p])
+        d = np.zeros(max(n, 1), dtype=R)
+        e = np.zeros(max(n - 1, 1), dtype=R)
+        # one call with a workspace: ReduceHerm answers a query only when work
+        # is given (RNP/LA/Tridiagonal.hpp:939-947) and reduces in place when
+        # it is NULL
+        w = np.zeros(64 * max(n, 1) + 65536, dtype=DT[p])
+        lw = SZ(w.size)
+        self.fn(p, "hetrd")(uplo.encode(), SZ(n), ptr(a), SZ(a.shape[0]), ptr(d), ptr(e), ptr(tau), C.byref(lw), ptr(w))
+        return tau[: max(n - 1, 0)], d[:n], e[: max(n - 1, 0)]
+
+    def unmtr(self, p, side, uplo, trans, m, n, a, tau, c):
+        tau = np.ascontiguousarray(tau)
+        self._dt = DT[p]
+        self._call_lw(self.fn(p, "unmtr"), (side.encode(), uplo.encode(), trans.encode(), SZ(m), SZ(n), ptr(a), SZ(a.shape[0]), ptr(tau), ptr(c), SZ(c.shape[0])))
+
+    def ungtr(self, p, uplo, n, a, tau):
+        tau = np.ascontiguousarray(tau)
+        self._dt = DT[p]
+        self._call_lw(self.fn(p, "ungtr"), (uplo.encode(), SZ(n), ptr(a), SZ(a.shape[0]), ptr(tau)))
+
+    def gg_triangularize_b(self, p, n, ilo, ihi, a, b, vl=None, vr=None):
+        """The complex generalized eigensystem's QR step (p in "cz"); returns tau (n)."""
+        f = self.fn(p, "gg_triangularize_b")
+        pv = lambda x: ptr(x) if x is not None else None
+        ld = lambda x: SZ(x.shape[0] if x is not None else 1)
+        head = (SZ(n), SZ(ilo), SZ(ihi), ptr(a), SZ(a.shape[0]), ptr(b), SZ(b.shape[0]), pv(vl), ld(vl), pv(vr), ld(vr))
+        if self.pre == "ref_":
+            w = np.zeros(n + 64 * max(n, 1) + 4096, dtype=DT[p])
+            f(*head, SZ(w.size), ptr(w))
+            return w[:n].copy()
+        tau = np.zeros(max(n, 1), dtype=DT[p])
+        f(*head, ptr(tau))
+        return tau[:n]
+
     def gels(self, p, m, n, nrhs, a, b):
         """Least squares by Factor + MultQ("L","C") + triangular solve; a, b overwritten."""
         tau = np.zeros(max(min(m, n), 1), dtype=DT[p])

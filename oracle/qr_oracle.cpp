@@ -920,6 +920,110 @@ template <class T> void x_genq(int kind, size_t m, size_t n, size_t k, T *a, siz
     xform(kind, mt, nt, b.data(), mt, a, lda);
 }
 
+// ---------------------------------------------------------------------------
+// Callers of QR / QL: the Q of a Hessenberg reduction and of a Hermitian
+// tridiagonal reduction, and the QR step of the complex generalized
+// eigensystem driver.  Each is the reference's composition restated over the
+// restated QR / QL above.
+// ---------------------------------------------------------------------------
+template <class T> void q_multq(char side, char trans, size_t m, size_t n, size_t k, const T *a, size_t lda, const T *tau, T *c, size_t ldc) {
+    size_t lw = 0;
+    multq<T>(side, trans, m, n, k, a, lda, tau, c, ldc, &lw, nullptr);
+    std::vector<T> w(lw > 0 ? lw : 1);
+    multq<T>(side, trans, m, n, k, a, lda, tau, c, ldc, &lw, w.data());
+}
+template <class T> void q_genq(size_t m, size_t n, size_t k, T *a, size_t lda, const T *tau) {
+    size_t lw = 0;
+    genq<T>(m, n, k, a, lda, tau, &lw, nullptr);
+    std::vector<T> w(lw > 0 ? lw : 1);
+    genq<T>(m, n, k, a, lda, tau, &lw, w.data());
+}
+// Hessenberg::MultQ (RNP/LA/Hessenberg.hpp:477-512): QR MultQ with the nh =
+// ihi-ilo-1 reflectors below the subdiagonal of columns ilo.., on rows (left)
+// or columns (right) ilo+1 .. ihi-1 of C
+template <class T> void hess_multq(char side, char trans, size_t m, size_t n, size_t ilo, size_t ihi, const T *a, size_t lda, const T *tau, T *c, size_t ldc) {
+    const bool left = side == 'L';
+    const size_t nh = ihi - ilo - 1;
+    const size_t mi = left ? nh : m, ni = left ? n : nh;
+    const size_t off = left ? ilo + 1 : (ilo + 1) * ldc;
+    q_multq<T>(side, trans, mi, ni, nh, a + (ilo + 1) + ilo * lda, lda, tau + ilo, c + off, ldc);
+}
+// Hessenberg::GenerateQ (Hessenberg.hpp:539-590): reflector vectors moved one
+// column right (columns ihi-1 down to ilo+1), the rest of the matrix set to
+// the identity, then QR GenerateQ of the nh x nh block at (ilo+1, ilo+1)
+template <class T> void hess_genq(size_t n, size_t ilo, size_t ihi, T *a, size_t lda, const T *tau) {
+    if (n == 0) return;
+    for (size_t j = ihi - 1; j > ilo; --j) {
+        T *col = a + j * lda;
+        const T *prev = a + (j - 1) * lda;
+        for (size_t i = 0; i < j; ++i) col[i] = T(0);
+        for (size_t i = j + 1; i < ihi; ++i) col[i] = prev[i];
+        for (size_t i = ihi; i < n; ++i) col[i] = T(0);
+    }
+    for (size_t j = 0; j < n; ++j) {
+        if (j > ilo && j < ihi) continue;
+        for (size_t i = 0; i < n; ++i) a[i + j * lda] = (i == j) ? T(1) : T(0);
+    }
+    const size_t nh = ihi - ilo - 1;
+    if (nh > 0) q_genq<T>(nh, nh, nh, a + (ilo + 1) * (lda + 1), lda, tau + ilo);
+}
+// Tridiagonal::GenerateQHerm (Tridiagonal.hpp:1037-1097): "U" moves the
+// vectors one column left and generates a QL factor's Q in the leading
+// (n-1) x (n-1) block; "L" moves them one column right and generates a QR
+// factor's Q in the trailing block
+template <class T> void trid_genq(char uplo, size_t n, T *a, size_t lda, const T *tau) {
+    if (n == 0) return;
+    if (uplo == 'U') {
+        for (size_t j = 0; j + 1 < n; ++j) {
+            for (size_t i = 0; i < j; ++i) a[i + j * lda] = a[i + (j + 1) * lda];
+            a[(n - 1) + j * lda] = T(0);
+        }
+        for (size_t i = 0; i + 1 < n; ++i) a[i + (n - 1) * lda] = T(0);
+        a[(n - 1) + (n - 1) * lda] = T(1);
+        if (n > 1) x_genq<T>(kQL, n - 1, n - 1, n - 1, a, lda, tau);
+    } else {
+        for (size_t j = n - 1; j >= 1; --j) {
+            a[j * lda] = T(0);
+            for (size_t i = j + 1; i < n; ++i) a[i + j * lda] = a[i + (j - 1) * lda];
+        }
+        a[0] = T(1);
+        for (size_t i = 1; i < n; ++i) a[i] = T(0);
+        if (n > 1) q_genq<T>(n - 1, n - 1, n - 1, a + 1 + lda, lda, tau);
+    }
+}
+// Tridiagonal::MultQHerm (Tridiagonal.hpp:1140-1188)
+template <class T> void trid_multq(char side, char uplo, char trans, size_t m, size_t n, const T *a, size_t lda, const T *tau, T *c, size_t ldc) {
+    const bool left = side == 'L';
+    const size_t nq = left ? m : n;
+    if (m == 0 || n == 0 || nq == 1) return;
+    const size_t mi = left ? m - 1 : m, ni = left ? n : n - 1;
+    if (uplo == 'U') x_multq<T>(kQL, side, trans, mi, ni, nq - 1, a + lda, lda, tau, c, ldc);
+    else q_multq<T>(side, trans, mi, ni, nq - 1, a + 1, lda, tau, c + (left ? 1 : ldc), ldc);
+}
+// The QR step of ComplexGeneralizedEigensystem (GeneralizedEigensystems.hpp:
+// 457-472): B(ilo:ihi, ilo:ilo+icols) factored, Q^H applied to A's block,
+// vl = I with Q generated in its (ilo:ihi, ilo:ihi) block from B's strictly
+// lower part, vr = I; tau (n) returned
+template <class T> void gg_triangularize_b(size_t n, size_t ilo, size_t ihi, T *a, size_t lda, T *b, size_t ldb, T *vl, size_t ldvl, T *vr, size_t ldvr, T *tau) {
+    const size_t irows = ihi - ilo, icols = (vl || vr) ? n - ilo : irows;
+    T *bb = b + ilo + ilo * ldb;
+    size_t lw = 0;
+    factor<T>(irows, icols, bb, ldb, tau, &lw, nullptr);
+    std::vector<T> w(lw > 0 ? lw : 1);
+    factor<T>(irows, icols, bb, ldb, tau, &lw, w.data());
+    q_multq<T>('L', 'C', irows, icols, irows, bb, ldb, tau, a + ilo + ilo * lda, lda);
+    if (vl) {
+        for (size_t j = 0; j < n; ++j)
+            for (size_t i = 0; i < n; ++i) vl[i + j * ldvl] = (i == j) ? T(1) : T(0);
+        for (size_t j = 0; j + 1 < irows; ++j)
+            for (size_t i = j; i + 1 < irows; ++i) vl[(ilo + 1 + i) + (ilo + j) * ldvl] = b[(ilo + 1 + i) + (ilo + j) * ldb];
+        q_genq<T>(irows, irows, irows, vl + ilo + ilo * ldvl, ldvl, tau);
+    }
+    if (vr)
+        for (size_t j = 0; j < n; ++j)
+            for (size_t i = 0; i < n; ++i) vr[i + j * ldvr] = (i == j) ? T(1) : T(0);
+}
+
 } // namespace orc
 
 // ---------------------------------------------------------------------------
@@ -945,6 +1049,23 @@ using namespace orc;
     ORC_XDEF(P, T, gelqf, unmlq, unglq, kLQ)        \
     ORC_XDEF(P, T, geqlf, unmql, ungql, kQL)        \
     ORC_XDEF(P, T, gerqf, unmrq, ungrq, kRQ)
+#define ORC_CONS(P, T)                                                                                                  \
+    extern "C" void oracle_##P##unmhr(const char *side, const char *trans, size_t m, size_t n, size_t ilo, size_t ihi, const T *a, size_t lda, \
+                                      const T *tau, T *c, size_t ldc) { hess_multq<T>(side[0], trans[0], m, n, ilo, ihi, a, lda, tau, c, ldc); } \
+    extern "C" void oracle_##P##unghr(size_t n, size_t ilo, size_t ihi, T *a, size_t lda, const T *tau) { hess_genq<T>(n, ilo, ihi, a, lda, tau); } \
+    extern "C" void oracle_##P##ungtr(const char *uplo, size_t n, T *a, size_t lda, const T *tau) { trid_genq<T>(uplo[0], n, a, lda, tau); } \
+    extern "C" void oracle_##P##unmtr(const char *side, const char *uplo, const char *trans, size_t m, size_t n, const T *a, size_t lda, \
+                                      const T *tau, T *c, size_t ldc) { trid_multq<T>(side[0], uplo[0], trans[0], m, n, a, lda, tau, c, ldc); }
+ORC_CONS(s, float)
+ORC_CONS(d, double)
+ORC_CONS(c, cf)
+ORC_CONS(z, cd)
+extern "C" void oracle_cgg_triangularize_b(size_t n, size_t ilo, size_t ihi, cf *a, size_t lda, cf *b, size_t ldb, cf *vl, size_t ldvl, cf *vr, size_t ldvr, cf *tau) {
+    gg_triangularize_b<cf>(n, ilo, ihi, a, lda, b, ldb, vl, ldvl, vr, ldvr, tau);
+}
+extern "C" void oracle_zgg_triangularize_b(size_t n, size_t ilo, size_t ihi, cd *a, size_t lda, cd *b, size_t ldb, cd *vl, size_t ldvl, cd *vr, size_t ldvr, cd *tau) {
+    gg_triangularize_b<cd>(n, ilo, ihi, a, lda, b, ldb, vl, ldvl, vr, ldvr, tau);
+}
 ORC_XDEF3(s, float)
 ORC_XDEF3(d, double)
 ORC_XDEF3(c, cf)

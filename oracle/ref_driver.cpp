@@ -15,12 +15,20 @@
 //   RNP::Random::GenerateVector       (RNP/Random.hpp:262-320)
 //   RNP::MatrixGen::RandomMatrix      (RNP/MatrixGen.hpp:120-203)
 //   RNP::BLAS::SolveTrM               (RNP/BLAS/BLAS_mix.hpp:2096-2113)
+//   RNP::LA::Hessenberg::Reduce / MultQ / GenerateQ   (RNP/LA/Hessenberg.hpp:351-590)
+//   RNP::LA::Tridiagonal::ReduceHerm / MultQHerm / GenerateQHerm
+//                                     (RNP/LA/Tridiagonal.hpp:924-1188)
+//   the QR step of ComplexGeneralizedEigensystem, as the reference's own
+//   calls in the order of RNP/LA/GeneralizedEigensystems.hpp:457-472
 #include <RNP/LA/QR.hpp>
 #include <RNP/LA/LQ.hpp>
 #include <RNP/LA/QL.hpp>
 #include <RNP/LA/RQ.hpp>
 #include <RNP/Random.hpp>
 #include <RNP/MatrixGen.hpp>
+#include <RNP/LA/Hessenberg.hpp>
+#include <RNP/LA/Tridiagonal.hpp>
+#include <RNP/LA/Triangular.hpp>
 #include <RNP/BLAS.hpp>
 #include <complex>
 #include <cstddef>
@@ -111,3 +119,61 @@ REF_DEF3(z, cd)
 REF_RNG(s, float)
 REF_RNG(d, double)
 REF_RNG(z, cd)
+
+// callers of QR / QL (LAPACK names: gehrd, unmhr, unghr, hetrd, unmtr, ungtr)
+#define REF_CONS(P, T, R)                                                                                               \
+    extern "C" void ref_##P##gehrd(size_t n, size_t ilo, size_t ihi, T *a, size_t lda, T *tau, size_t *lwork, T *work) { \
+        RNP::LA::Hessenberg::Reduce<T>(n, ilo, ihi, a, lda, tau, lwork, work);                                        \
+    }                                                                                                                 \
+    extern "C" void ref_##P##unmhr(const char *side, const char *trans, size_t m, size_t n, size_t ilo, size_t ihi,  \
+                                   const T *a, size_t lda, const T *tau, T *c, size_t ldc, size_t *lwork, T *work) {  \
+        RNP::LA::Hessenberg::MultQ<T>(side, trans, m, n, ilo, ihi, a, lda, tau, c, ldc, lwork, work);                 \
+    }                                                                                                                 \
+    extern "C" void ref_##P##unghr(size_t n, size_t ilo, size_t ihi, T *a, size_t lda, const T *tau, size_t *lwork,  \
+                                   T *work) {                                                                         \
+        RNP::LA::Hessenberg::GenerateQ<T>(n, ilo, ihi, a, lda, tau, lwork, work);                                     \
+    }                                                                                                                 \
+    extern "C" void ref_##P##hetrd(const char *uplo, size_t n, T *a, size_t lda, R *diag, R *offdiag, T *tau,         \
+                                   size_t *lwork, T *work) {                                                          \
+        RNP::LA::Tridiagonal::ReduceHerm<T>(uplo, n, a, lda, diag, offdiag, tau, lwork, work);                        \
+    }                                                                                                                 \
+    extern "C" void ref_##P##ungtr(const char *uplo, size_t n, T *a, size_t lda, const T *tau, size_t *lwork,         \
+                                   T *work) {                                                                         \
+        RNP::LA::Tridiagonal::GenerateQHerm<T>(uplo, n, a, lda, tau, lwork, work);                                    \
+    }                                                                                                                 \
+    extern "C" void ref_##P##unmtr(const char *side, const char *uplo, const char *trans, size_t m, size_t n,         \
+                                   const T *a, size_t lda, const T *tau, T *c, size_t ldc, size_t *lwork, T *work) {  \
+        RNP::LA::Tridiagonal::MultQHerm<T>(side, uplo, trans, m, n, a, lda, tau, c, ldc, lwork, work);                \
+    }
+REF_CONS(s, float, float)
+REF_CONS(d, double, double)
+REF_CONS(c, cf, float)
+REF_CONS(z, cd, double)
+
+// ComplexGeneralizedEigensystem's QR step: the reference's calls of
+// RNP/LA/GeneralizedEigensystems.hpp:457-472 in their order, with its
+// workspace layout [tau | work] (the driver itself also balances, reduces and
+// iterates, none of which calls QR)
+#define REF_GG(P, T)                                                                                                    \
+    extern "C" void ref_##P##gg_triangularize_b(size_t n, size_t ilo, size_t ihi, T *a, size_t lda, T *b, size_t ldb, \
+                                                T *vl, size_t ldvl, T *vr, size_t ldvr, size_t lwork, T *work) {      \
+        const T zero(0), one(1);                                                                                      \
+        const size_t irows = ihi - ilo;                                                                               \
+        const size_t icols = (NULL != vl || NULL != vr) ? n - ilo : irows;                                            \
+        T *tau = work;                                                                                                \
+        T *work2 = tau + n;                                                                                           \
+        size_t lwork2 = lwork - n;                                                                                    \
+        RNP::LA::QR::Factor(irows, icols, &b[ilo + ilo * ldb], ldb, tau, &lwork2, work2);                             \
+        RNP::LA::QR::MultQ("L", "C", irows, icols, irows, &b[ilo + ilo * ldb], ldb, tau, &a[ilo + ilo * lda], lda,    \
+                           &lwork2, work2);                                                                           \
+        if (NULL != vl) {                                                                                             \
+            RNP::BLAS::Set(n, n, zero, one, vl, ldvl);                                                                \
+            if (irows > 1)                                                                                            \
+                RNP::LA::Triangular::Copy("L", irows - 1, irows - 1, &b[ilo + 1 + ilo * ldb], ldb,                    \
+                                          &vl[ilo + 1 + ilo * ldvl], ldvl);                                           \
+            RNP::LA::QR::GenerateQ(irows, irows, irows, &vl[ilo + ilo * ldvl], ldvl, tau, &lwork2, work2);            \
+        }                                                                                                             \
+        if (NULL != vr) RNP::BLAS::Set(n, n, zero, one, vr, ldvr);                                                    \
+    }
+REF_GG(c, cf)
+REF_GG(z, cd)

@@ -52,6 +52,12 @@ def _signatures():
             sig["rnpgpu_%s%s" % (p, f)] = [SZ, SZ, P, SZ, P, PSZ, P]
             sig["rnpgpu_%s%s" % (p, mq)] = [CH, CH, SZ, SZ, SZ, P, SZ, P, P, SZ, PSZ, P]
             sig["rnpgpu_%s%s" % (p, g)] = [SZ, SZ, SZ, P, SZ, P, PSZ, P]
+        sig["rnpgpu_%sunmhr" % p] = [CH, CH, SZ, SZ, SZ, SZ, P, SZ, P, P, SZ, PSZ, P]
+        sig["rnpgpu_%sunghr" % p] = [SZ, SZ, SZ, P, SZ, P, PSZ, P]
+        sig["rnpgpu_%sungtr" % p] = [CH, SZ, P, SZ, P, PSZ, P]
+        sig["rnpgpu_%sunmtr" % p] = [CH, CH, CH, SZ, SZ, P, SZ, P, P, SZ, PSZ, P]
+    for p in "cz":
+        sig["rnpgpu_%sgg_triangularize_b" % p] = [SZ, SZ, SZ, P, SZ, P, SZ, P, SZ, P, SZ, PSZ, P]
     for name in ("rnpgpu_dsgels", "rnpgpu_zcgels"):
         sig[name] = [SZ, SZ, SZ, P, SZ, P, SZ, P, SZ, C.c_int, C.c_int, C.POINTER(RefineInfo), PSZ, P]
     sig["rnpgpu_srandom_matrix"] = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, P, SZ, SZ, P, SZ, C.POINTER(C.c_int), PSZ, P]

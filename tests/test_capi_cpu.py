@@ -91,3 +91,35 @@ def test_workspace_shrinks_then_rejects(lib):
     # below n it is an lwork error (argument 6), never an out-of-bounds write
     lw = C.c_size_t(3)
     assert lib.rnpgpu_dgeqrf(10, 5, C.c_void_p(256), 10, C.c_void_p(512), C.byref(lw), C.c_void_p(1024)) == -6
+
+
+def test_consumer_arguments_are_rejected(lib):
+    """Hessenberg / tridiagonal Q and the generalized QR step validate their
+    arguments before any device work (argument positions as the reference's
+    signatures)."""
+    lw = C.c_size_t(0)
+    # Hessenberg::MultQ: ilo > nq, ihi <= ilo, lda < nq, ldc < m
+    assert lib.rnpgpu_dunmhr(b"L", b"N", 10, 4, 11, 12, None, 10, None, None, 10, C.byref(lw), None) == -5
+    assert lib.rnpgpu_dunmhr(b"L", b"N", 10, 4, 3, 3, None, 10, None, None, 10, C.byref(lw), None) == -6
+    assert lib.rnpgpu_zunmhr(b"R", b"C", 4, 10, 0, 10, None, 9, None, None, 4, C.byref(lw), None) == -8
+    assert lib.rnpgpu_sunmhr(b"L", b"N", 10, 4, 0, 10, None, 10, None, None, 9, C.byref(lw), None) == -11
+    assert lib.rnpgpu_cunmhr(b"X", b"N", 10, 4, 0, 10, None, 10, None, None, 10, C.byref(lw), None) == -1
+    assert lib.rnpgpu_dunmhr(b"L", b"N", 10, 4, 0, 10, None, 10, None, None, 10, None, None) == -12
+    # Hessenberg::GenerateQ: ihi > n, lda < n; the query answers
+    assert lib.rnpgpu_dunghr(10, 2, 11, None, 10, None, C.byref(lw), None) == -3
+    assert lib.rnpgpu_zunghr(10, 0, 10, None, 9, None, C.byref(lw), None) == -5
+    lw = C.c_size_t(0)
+    assert lib.rnpgpu_dunghr(300, 0, 300, None, 300, None, C.byref(lw), None) == 0 and lw.value >= 299
+    # Tridiagonal::GenerateQHerm / MultQHerm
+    assert lib.rnpgpu_dungtr(b"X", 10, None, 10, None, C.byref(lw), None) == -1
+    assert lib.rnpgpu_cungtr(b"U", 10, None, 9, None, C.byref(lw), None) == -4
+    assert lib.rnpgpu_dunmtr(b"L", b"U", b"N", 10, 4, None, 9, None, None, 10, C.byref(lw), None) == -7
+    assert lib.rnpgpu_zunmtr(b"L", b"L", b"Q", 10, 4, None, 10, None, None, 10, C.byref(lw), None) == -3
+    lw = C.c_size_t(0)
+    assert lib.rnpgpu_zungtr(b"U", 200, None, 200, None, C.byref(lw), None) == 0 and lw.value >= 199
+    # the generalized step: ihi > n, ldb < n, a missing workspace length
+    assert lib.rnpgpu_zgg_triangularize_b(10, 0, 11, None, 10, None, 10, None, 1, None, 1, C.byref(lw), None) == -3
+    assert lib.rnpgpu_zgg_triangularize_b(10, 0, 10, None, 10, None, 9, None, 1, None, 1, C.byref(lw), None) == -7
+    assert lib.rnpgpu_cgg_triangularize_b(10, 0, 10, None, 10, None, 10, None, 1, None, 1, None, None) == -12
+    lw = C.c_size_t(0)
+    assert lib.rnpgpu_zgg_triangularize_b(100, 0, 100, None, 100, None, 100, None, 1, None, 1, C.byref(lw), None) == 0 and lw.value > 100
