@@ -473,26 +473,30 @@ def batched_ls_config(torch, dev, count=4096, check_sample=32):
     return out
 
 
+def c1_config(torch, dev, gq, g, reps=5):
+    """1024 x 256 real (entries uniform[-1, 1]): Factor, then GenerateQ."""
+    A0 = gq.to_colmajor(2 * torch.rand((1024, 256), generator=g, dtype=torch.float64, device=dev) - 1)
+    A = gq.to_colmajor(A0)
+    tau = torch.zeros(256, dtype=torch.float64, device=dev)
+    wf = torch.empty(gq.workspace_query("geqrf", torch.float64, 1024, 256), dtype=torch.float64, device=dev)
+    wq = torch.empty(gq.workspace_query("ungqr", torch.float64, 1024, 256, 256), dtype=torch.float64, device=dev)
+    ms_f = timed(torch, lambda: ((lambda: A.copy_(A0)), (lambda: gq.factor(A, tau, wf))), reps)
+    ms_q = timed(torch, lambda: ((lambda: (A.copy_(A0), gq.factor(A, tau, wf))), (lambda: gq.generate_q(A, tau, 256, wq))), reps)
+    f1 = 2.0 * 1024 * 256 ** 2 - 2.0 * 256 ** 3 / 3
+    q1 = 4.0 * 1024 * 256 * 256 - 2.0 * (1024 + 256) * 256 ** 2 + 4.0 * 256 ** 3 / 3
+    return {"factor_ms": ms_f, "generate_q_ms": ms_q, "factor_gflops": f1 / ms_f / 1e6, "generate_q_gflops": q1 / ms_q / 1e6}
+
+
 def other_configs(torch, dev, gq, lib, peak64, check=True, only_c2=False):
     """The plain FP64 drop-in on the reference's other configurations:
     1024x256 real Factor + GenerateQ, and 4096x4096 complex Factor followed by
     MultQ("L","C") on a 4096x64 block (FP64 throughout)."""
     out = {}
     g = torch.Generator(device=dev).manual_seed(7)
-    # 1024 x 256 real, entries uniform[-1, 1]
-    A0 = gq.to_colmajor(2 * torch.rand((1024, 256), generator=g, dtype=torch.float64, device=dev) - 1)
     if only_c2:
         g = torch.Generator(device=dev).manual_seed(8)
-    A = gq.to_colmajor(A0)
-    tau = torch.zeros(256, dtype=torch.float64, device=dev)
-    wf = torch.empty(gq.workspace_query("geqrf", torch.float64, 1024, 256), dtype=torch.float64, device=dev)
-    wq = torch.empty(gq.workspace_query("ungqr", torch.float64, 1024, 256, 256), dtype=torch.float64, device=dev)
-    ms_f = 0.0 if only_c2 else timed(torch, lambda: ((lambda: A.copy_(A0)), (lambda: gq.factor(A, tau, wf))), 5)
-    if not only_c2:
-        ms_q = timed(torch, lambda: ((lambda: (A.copy_(A0), gq.factor(A, tau, wf))), (lambda: gq.generate_q(A, tau, 256, wq))), 5)
-        f1 = 2.0 * 1024 * 256 ** 2 - 2.0 * 256 ** 3 / 3
-        q1 = 4.0 * 1024 * 256 * 256 - 2.0 * (1024 + 256) * 256 ** 2 + 4.0 * 256 ** 3 / 3
-        out["qr_1024x256_f64"] = {"factor_ms": ms_f, "generate_q_ms": ms_q, "factor_gflops": f1 / ms_f / 1e6, "generate_q_gflops": q1 / ms_q / 1e6}
+    else:
+        out["qr_1024x256_f64"] = c1_config(torch, dev, gq, g)
     # 4096 x 4096 complex, re/im N(0,1); MultQ("L","C") on 4096 x 64
     n = 4096
     Z0 = gq.to_colmajor(torch.complex(torch.randn((n, n), generator=g, dtype=torch.float64, device=dev), torch.randn((n, n), generator=g, dtype=torch.float64, device=dev)))
@@ -655,10 +659,12 @@ def gpu_arm(args, rank, world, local):
             dist.barrier()
         torch.cuda.synchronize()
 
-    if args.phase in ("batched", "c2"):
+    if args.phase in ("batched", "c2", "c1"):
         # profiling runs of the other configurations alone
         if args.phase == "batched":
             out = {"batched": batched_config(torch, dev, gq, lib, 0.0, check_sample=0), "batched_ls": batched_ls_config(torch, dev, check_sample=0)}
+        elif args.phase == "c1":
+            out = {"qr_1024x256_f64": c1_config(torch, dev, gq, torch.Generator(device=dev).manual_seed(7), reps=max(args.steps, 1))}
         else:
             out = other_configs(torch, dev, gq, lib, 0.0, check=False, only_c2=True)
         if rank == 0:
@@ -806,6 +812,11 @@ def gpu_arm(args, rank, world, local):
     lib.rnpgpu_probe_peak(0, C.c_void_p(scratch.data_ptr()), scratch.numel() * 8, C.byref(peak64))
     peak64_mma = C.c_double(0)
     lib.rnpgpu_probe_peak(2, C.c_void_p(scratch.data_ptr()), scratch.numel() * 8, C.byref(peak64_mma))
+    lat = {}
+    for kind, name in ((3, "dfma_dependent"), (4, "fp64_issue_interval_one_warp"), (5, "ddiv_dependent")):
+        v = C.c_double(0.0)
+        lib.rnpgpu_probe_peak(kind, C.c_void_p(scratch.data_ptr()), scratch.numel() * 8, C.byref(v))
+        lat[name] = v.value
     tot_ms = sum(v[1] for v in prof.values())
     top = max(prof.items(), key=lambda kv: kv[1][1]) if prof else ("none", (0, 0.0))
     roofline, roofline_others = kernel_rooflines(prof, tot_ms, top[0], peak64.value, prof_steps)
@@ -863,6 +874,7 @@ def gpu_arm(args, rank, world, local):
         "speedup_mixed_vs_plain": ms_plain / ms,
         "fp64_peaks_measured_tflops": {"fma": peak64.value, "mma_m8n8k4": peak64_mma.value,
                                        "note": "FP64 contractions run on the FMA pipe, the faster of the two on this GPU"},
+        "fp64_latency_cycles": lat,
         "profile_ms_per_step": {k: v[1] / prof_steps for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])},
         "top_kernel": top[0],
         "roofline": roofline,
@@ -887,7 +899,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-configs", action="store_true", help="skip the other plain configurations")
-    ap.add_argument("--phase", default="all", choices=["all", "mixed", "batched", "c2"],
+    ap.add_argument("--phase", default="all", choices=["all", "mixed", "batched", "c2", "c1"],
                     help="profiler runs: 'mixed' only the timed mixed solves, 'batched' only the batched configurations, 'c2' only the 4096^2 complex one")
     ap.add_argument("--m", type=int, default=M, help="rows of the least-squares workload (profiler runs of a smaller case)")
     args = ap.parse_args()

@@ -130,7 +130,10 @@ int rnpgpu_timing_report(char *buf, size_t len);
  * kind 1: FP32 FMA, kind 2: FP64 tensor-core MMA, mma.sync m8n8k4), using
  * scratch (>= SMs*8*256 doubles) for the probe's outputs; synchronous.  Used
  * as the roofline denominator of FP64 work and to re-check that the FP64
- * contractions belong on the FMA pipe. */
+ * contractions belong on the FMA pipe.  Kinds 3-5 return SM clock cycles
+ * instead: 3 the latency of a dependent FP64 FMA, 4 the interval between FP64
+ * instructions of one warp with independent work, 5 the latency of an FP64
+ * division (the figures behind keeping FP64 work off serial paths). */
 int rnpgpu_probe_peak(int kind, void *scratch, size_t scratch_bytes, double *tflops);
 
 #ifdef __cplusplus

@@ -75,6 +75,7 @@ struct AttrKey {
 struct AttrState {
     int smem = -1;
     bool carveout = false;
+    bool cluster16 = false;
 };
 static std::mutex g_attr_mu;
 static std::map<AttrKey, AttrState> g_attr;
@@ -116,6 +117,55 @@ int kernel_blocks_per_sm(const void *kern, int threads, size_t dyn_smem) {
     return per_sm;
 }
 
+// Largest cluster (<= 16 blocks, non-portable sizes above 8 allowed) of
+// `threads` threads and `dyn_smem` bytes that the device can co-schedule for
+// this kernel; 0 when none of 2 .. 16 blocks fits.  Cached per size.
+static std::map<std::pair<AttrKey, std::pair<int, size_t> >, int> g_cluster;
+int kernel_max_cluster(const void *kern, int threads, size_t dyn_smem, int want) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    std::lock_guard<std::mutex> lk(g_attr_mu);
+    AttrState &a = g_attr[AttrKey{kern, dev}];
+    if (!a.cluster16) {
+        if (cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+            cudaGetLastError();
+            return 0;
+        }
+        a.cluster16 = true;
+    }
+    auto key = std::make_pair(AttrKey{kern, dev}, std::make_pair(threads * 64 + want, dyn_smem));
+    auto it = g_cluster.find(key);
+    if (it != g_cluster.end()) return it->second;
+    int best = 0;
+    for (int c = want; c >= 2; --c) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(c);
+        cfg.blockDim = dim3(threads);
+        cfg.dynamicSmemBytes = dyn_smem;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = c;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        int n = 0;
+        if (cudaOccupancyMaxActiveClusters(&n, kern, &cfg) != cudaSuccess) {
+            cudaGetLastError();
+            n = 0;
+        }
+        if (n > 0) {
+            best = c;
+            break;
+        }
+    }
+    g_cluster[key] = best;
+    return best;
+}
+
 // ---------------------------------------------------------------------------
 // TMA tensor maps (cuTensorMapEncodeTiled through the runtime's driver entry
 // point: no link against the driver library)
@@ -136,7 +186,9 @@ static EncodeTiledFn encode_tiled_fn() {
     return fn;
 }
 
-int encode_map_f32(CUtensorMap *map, const float *base, uint64_t rows, uint64_t cols, uint64_t ld, uint32_t box_rows, uint32_t box_cols) {
+// swizzle128: the box's 128-byte rows (box_rows == 32) land in shared memory
+// with their 16-byte chunks XOR-permuted by the row index mod 8
+int encode_map_f32(CUtensorMap *map, const float *base, uint64_t rows, uint64_t cols, uint64_t ld, uint32_t box_rows, uint32_t box_cols, bool swizzle128) {
     EncodeTiledFn fn = encode_tiled_fn();
     if (fn == nullptr) {
         set_last_error("cuTensorMapEncodeTiled is not available");
@@ -147,7 +199,8 @@ int encode_map_f32(CUtensorMap *map, const float *base, uint64_t rows, uint64_t 
     const cuuint32_t box[2] = {box_rows, box_cols};
     const cuuint32_t estride[2] = {1, 1};
     const CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float *>(base), dims, strides, box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                          CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+                          swizzle128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) {
         char msg[160];
         snprintf(msg, sizeof msg, "cuTensorMapEncodeTiled failed (%d) for a %llu x %llu FP32 matrix, ld %llu, box %u x %u", (int)r, (unsigned long long)rows,
@@ -192,6 +245,29 @@ __global__ void k_probe_dmma(double *out, int iters) {
 #pragma unroll
     for (int j = 0; j < 8; ++j) s += c[j][0] + c[j][1];
     out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+// FP64 latency probes (one block, SM clock cycles from clock64):
+// kind 3: one thread, a dependent chain of DFMA (cycles per DFMA);
+// kind 4: one warp, eight independent DFMA chains (cycles per warp
+//         instruction: how often one warp can issue FP64 work);
+// kind 5: one thread, a dependent chain of FP64 divisions (cycles each)
+__global__ void k_probe_fp64_lat(int kind, double *out, long long *cyc, int n, double b, double c) {
+    double a0 = threadIdx.x + 1.5, a1 = a0 + 1, a2 = a0 + 2, a3 = a0 + 3, a4 = a0 + 4, a5 = a0 + 5, a6 = a0 + 6, a7 = a0 + 7;
+    const long long t0 = clock64();
+    if (kind == 3) {
+        for (int i = 0; i < n; ++i) a0 = fma(a0, b, c);
+    } else if (kind == 4) {
+        for (int i = 0; i < n; ++i) {
+            a0 = fma(a0, b, c); a1 = fma(a1, b, c); a2 = fma(a2, b, c); a3 = fma(a3, b, c);
+            a4 = fma(a4, b, c); a5 = fma(a5, b, c); a6 = fma(a6, b, c); a7 = fma(a7, b, c);
+        }
+    } else {
+        for (int i = 0; i < n; ++i) a0 = b / a0;
+    }
+    const long long t1 = clock64();
+    if (threadIdx.x == 0) cyc[0] = t1 - t0;
+    out[threadIdx.x] = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
 }
 
 // per-type occupancy of the panel kernel (defined in the per-type units)
@@ -302,7 +378,27 @@ int rnpgpu_probe_peak(int kind, void *scratch, size_t scratch_bytes, double *tfl
     const DeviceFacts &f = device_facts();
     const int blocks = f.sm_count * 8, threads = 256;
     if (scratch_bytes < (size_t)blocks * threads * sizeof(double) || tflops == nullptr) return -2;
+    if (kind < 0 || kind > 5) return -1;
     cudaStream_t st = current_stream();
+    if (kind >= 3) {
+        // latencies in cycles: scratch holds 32 doubles of outputs and the count
+        const int n = kind == 5 ? 1024 : 4096;
+        long long *cyc = reinterpret_cast<long long *>((double *)scratch + 64);
+        double best = 1e300;
+        for (int rep = 0; rep < 3; ++rep) {
+            k_probe_fp64_lat<<<1, kind == 4 ? 32 : 1, 0, st>>>(kind, (double *)scratch, cyc, n, 0.999, 1e-3);
+            long long h = 0;
+            if (cudaMemcpyAsync(&h, cyc, sizeof h, cudaMemcpyDeviceToHost, st) != cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess) break;
+            best = std::min(best, (double)h / (kind == 4 ? 8.0 * n : (double)n));
+        }
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) {
+            set_last_error(cudaGetErrorString(e));
+            return 1;
+        }
+        *tflops = best;
+        return 0;
+    }
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);

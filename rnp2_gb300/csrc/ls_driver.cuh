@@ -75,8 +75,8 @@ template <class T> int trsm_lunn(size_t n, size_t nrhs, const T *a, size_t lda, 
 template <class T> size_t tstore_bytes(size_t n) { return ((n + GpuTuning::nb - 1) / GpuTuning::nb) * t_bytes<T>(); }
 
 template <class T> size_t gels_bytes(size_t m, size_t n, size_t nrhs) {
-    size_t f = geqrf_bytes<T>(m, n, smax_for(m));
-    size_t q = unmqr_bytes<T>(m, nrhs, n, smax_for(m), smax_for(m));
+    size_t f = geqrf_bytes<T>(m, n, smax_for<T>(m));
+    size_t q = unmqr_bytes<T>(m, nrhs, n, smax_for<T>(m), smax_for<T>(m));
     return std::max(f, q) + tstore_bytes<T>(n) + 512;
 }
 
@@ -123,10 +123,10 @@ template <class TH, class TL> struct RefinePlan {
         af = al(m * n * sizeof(TL));
         tauf = al(n * sizeof(TL));
         ts = al(tstore_bytes<TL>(n));
-        wq = al(std::max(geqrf_bytes<TL>(m, n, smax_for(m)), unmqr_bytes<TL>(m, nrhs, n, smax_for(m), smax_for(m))) + 256);
+        wq = al(std::max(geqrf_bytes<TL>(m, n, smax_for<TL>(m)), unmqr_bytes<TL>(m, nrhs, n, smax_for<TL>(m), smax_for<TL>(m))) + 256);
         r = al(m * nrhs * sizeof(TH));
         rf = al(m * nrhs * sizeof(TL));
-        split = smax_for(m);
+        split = smax_for<TL>(m);
         p = al((size_t)split * n * nrhs * sizeof(TH));
         g = al(n * nrhs * sizeof(TH));
         norms = al((n + 6 * nrhs) * sizeof(double));

@@ -14,6 +14,7 @@
 #include "tc_gemm.cuh"
 #include <algorithm>
 #include <type_traits>
+#include <cstdlib>
 #include <cstring>
 #include <cstdio>
 #include <mutex>
@@ -40,6 +41,7 @@ int *device_status_ptr();  // library-wide device status word
 // memory carveout); blocks of a kernel one SM holds (cached).
 int kernel_attr(const void *kern, int dyn_smem, bool max_carveout = false);
 int kernel_blocks_per_sm(const void *kern, int threads, size_t dyn_smem);
+int kernel_max_cluster(const void *kern, int threads, size_t dyn_smem, int want);
 
 // Launch accounting and optional per-kernel-class timing (CUDA events on the
 // launching stream; only while rnpgpu_timing_enable(1) is in effect).
@@ -185,7 +187,17 @@ template <class T> int launch_gemm(GemmArgs<T> g, int nsplit, cudaStream_t st, c
     if (g.kchunk <= 0) g.kchunk = g.K > 0 ? g.K : 1;
     KScope ks(tag, st);
     if (use_tensor_cores(g)) return launch_gemm_tc(g, nsplit, st);
-    if (g.N <= 16) {
+    // FP64 work: an SM retires an FP64 warp instruction only every ~16
+    // cycles, so a grid that leaves SMs idle takes the smaller tiles
+    constexpr bool f64 = sizeof(typename Tr<T>::R) == 8;
+    const long sms = device_facts().sm_count > 0 ? device_facts().sm_count : 148;
+    if (f64 && g.N <= 16 && (long)((g.M + 127) / 128) * nsplit < sms) {
+        dim3 grid((g.M + 31) / 32, (g.N + 15) / 16, nsplit);
+        k_gemm<T, 32, 16, 16, 2, 1><<<grid, 256, 0, st>>>(g);
+    } else if (f64 && g.N > 16 && (long)((g.M + 63) / 64) * ((g.N + 63) / 64) * nsplit < sms) {
+        dim3 grid((g.M + 31) / 32, (g.N + 31) / 32, nsplit);
+        k_gemm<T, 32, 32, 16, 2, 2><<<grid, 256, 0, st>>>(g);
+    } else if (g.N <= 16) {
         dim3 grid((g.M + 127) / 128, (g.N + 15) / 16, nsplit);
         k_gemm<T, 128, 16, 16, 8, 1><<<grid, 256, 0, st>>>(g);
     } else if (g.N <= 32) {
@@ -228,6 +240,32 @@ inline int coop_launch(const char *name, const void *kern, int grid, int threads
     return kOk;
 }
 
+// one thread-block cluster of `grid` blocks
+inline int cluster_launch(const char *name, const void *kern, int grid, int threads, void **args, size_t smem, cudaStream_t st) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(threads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = grid;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    const cudaError_t e = cudaLaunchKernelExC(&cfg, kern, args);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        char msg[200];
+        snprintf(msg, sizeof msg, "%s: %s (cluster of %d x %d threads, %zu B dynamic shared memory)", name, cudaGetErrorString(e), grid, threads, smem);
+        set_last_error(msg);
+        return kErrCuda;
+    }
+    note_launch();
+    return kOk;
+}
+
 template <class T> GemmArgs<T> gemm_args(const T *A, size_t lda, int opA, int vunitA, const T *B, size_t ldb, int opB, int vunitB, T *D, size_t ldd, int M, int N, int K, T alpha, int beta_mode) {
     GemmArgs<T> g;
     g.A = A; g.lda = lda; g.B = B; g.ldb = ldb; g.D = D; g.ldd = ldd;
@@ -239,10 +277,15 @@ template <class T> GemmArgs<T> gemm_args(const T *A, size_t lda, int opA, int vu
 }
 
 // split-K plan for a reduction of length K producing 'tiles' output tiles
-inline int choose_splits(int K, int tiles, int smax) {
+// Fewest rows a split-K partial may cover: FP64 arithmetic runs at 1/64 of
+// the FP32 rate on this GPU, so FP64 contractions with few output tiles need
+// many short splits to occupy the SMs.
+template <class T> constexpr int split_min_rows() { return sizeof(typename Tr<T>::R) == 8 ? 32 : 256; }
+
+inline int choose_splits(int K, int tiles, int smax, int min_rows = 256) {
     const int sm = device_facts().sm_count > 0 ? device_facts().sm_count : 148;
     int s = (2 * sm + tiles - 1) / std::max(tiles, 1);
-    s = std::min(s, std::max(1, K / 256));
+    s = std::min(s, std::max(1, K / min_rows));
     s = std::min(s, smax);
     return std::max(s, 1);
 }
@@ -292,7 +335,7 @@ template <class T> int apply_block(bool left, bool notran, int M, int N, int ib,
         }
         // W = C^H V  (N x ib), reduction over the M rows
         const int tiles = (N + 63) / 64;
-        const int S = choose_splits(M, tiles, ws.smax);
+        const int S = choose_splits(M, tiles, ws.smax, split_min_rows<T>());
         int kchunk = ((M + S - 1) / S + 15) / 16 * 16;
         if (std::is_same<T, float>::value) {
             // tensor-core path: at most ~1024 rows per accumulator, within
@@ -313,7 +356,7 @@ template <class T> int apply_block(bool left, bool notran, int M, int N, int ib,
     } else {
         // W = C V  (M x ib), reduction over the N columns
         const int tiles = (M + 63) / 64;
-        const int S = choose_splits(N, tiles, ws.smax);
+        const int S = choose_splits(N, tiles, ws.smax, split_min_rows<T>());
         const int kchunk = ((N + S - 1) / S + 15) / 16 * 16;
         const int nsplit = (N + kchunk - 1) / kchunk;
         GemmArgs<T> g = gemm_args<T>(C, ldc, kOpN, 0, V, ldv, kOpN, 1, ws.P, (size_t)M, M, ib, N, T(1), kBetaZero);
@@ -330,7 +373,7 @@ template <class T> int apply_block(bool left, bool notran, int M, int N, int ib,
 // T factor of one reflector block from V and tau (GenerateBlockTr "F","C"):
 // Gram matrix V^H V by a split-K contraction, then the recurrence.
 template <class T> int block_t(int rows, int ib, const T *V, size_t ldv, const T *tau, T *Tout, int ldt, T *Pg, int smax, cudaStream_t st) {
-    const int S = choose_splits(rows, 1, smax);
+    const int S = choose_splits(rows, 1, smax, split_min_rows<T>());
     const int kchunk = ((rows + S - 1) / S + 15) / 16 * 16;
     const int nsplit = (rows + kchunk - 1) / kchunk;
     GemmArgs<T> g = gemm_args<T>(V, ldv, kOpC, 1, V, ldv, kOpN, 1, Pg, (size_t)kPanelMaxCols, ib, ib, rows, T(1), kBetaZero);
@@ -361,7 +404,52 @@ inline int panel_grid(int M, int gmax) {
 // shared-memory budget for a block's rows of the panel
 constexpr size_t kPanelSmemMax = 180 * 1024;
 
+// Panels of at most this many rows (default 4096; the environment variable
+// RNPGPU_PANEL_CLUSTER_ROWS overrides it, 0 turns the form off) run as one
+// thread-block cluster of up to 16 blocks of about 64 rows or more.
+inline int panel_cluster_rows() {
+    static const int rows = []() {
+        const char *e = getenv("RNPGPU_PANEL_CLUSTER_ROWS");
+        return e ? atoi(e) : 4096;
+    }();
+    return rows;
+}
+constexpr int kPanelClusterRowsPerBlock = 64;
+// the short panels' blocks hold few rows: four warps, so that the per-column
+// reductions (FP64, whose one pipe per SM takes a warp instruction every 16
+// cycles) run in few warps
+constexpr int kPanelClusterThreads = 128;
+
 template <class T> int panel_factor(int M, int N, T *A, size_t lda, T *tau, T *Tm, int ldt, const PanelWs<T> &ws, cudaStream_t st) {
+    if (M <= panel_cluster_rows() && M > kPanelClusterRowsPerBlock) {
+        // short panel: one cluster, records in distributed shared memory
+        const void *kc = (const void *)k_panel<T, true, true, kPanelClusterThreads>;
+        if (int rc = kernel_attr(kc, (int)kPanelSmemMax)) return rc;
+        // the largest cluster (<= 16 blocks) that fits with its rows' shared
+        // memory; g falls strictly until the query agrees
+        int g = std::min(16, (M + kPanelClusterRowsPerBlock - 1) / kPanelClusterRowsPerBlock);
+        while (g >= 2) {
+            const size_t smem = (size_t)((M + g - 1) / g) * N * sizeof(T);
+            if (smem > kPanelSmemMax) {
+                g = 0;
+                break;
+            }
+            const int c = kernel_max_cluster(kc, kPanelClusterThreads, smem, g);
+            if (c == g) break;
+            g = c;
+        }
+        if (g >= 2 && (M + g - 1) / g <= 1024) {
+            PanelArgs<T> p;
+            p.A = A; p.lda = lda; p.M = M; p.N = N; p.tau = tau; p.Tm = Tm; p.ldt = ldt;
+            p.rec = nullptr;
+            p.counter = nullptr; p.err = nullptr;
+            p.status = device_status_ptr();
+            p.rows_per_cta = (M + g - 1) / g;
+            void *args[] = {&p};
+            KScope ks("panel", st);
+            return cluster_launch("k_panel(cluster)", kc, g, kPanelClusterThreads, args, (size_t)p.rows_per_cta * N * sizeof(T), st);
+        }
+    }
     const int G = panel_grid(M, ws.gmax);
     if (int rc = kernel_attr((const void *)k_panel<T, true>, (int)kPanelSmemMax)) return rc;
     PanelArgs<T> p;
@@ -409,7 +497,9 @@ template <class T> BlockWs<T> carve_block(Carver &cv, int rows_w, int smax) {
 }
 // split-K slots of the W partials: up to one per SM (the tensor-core W
 // reduction writes one partial per persistent block)
-inline int smax_for(size_t K) { return (int)std::max<size_t>(1, std::min<size_t>((size_t)std::max(64, device_facts().sm_count), K / 256)); }
+template <class T> inline int smax_for(size_t K) {
+    return (int)std::max<size_t>(1, std::min<size_t>((size_t)std::max(64, device_facts().sm_count), K / (size_t)split_min_rows<T>()));
+}
 template <class T> size_t t_bytes() { return ((size_t)kPanelMaxCols * kPanelMaxCols * sizeof(T) + 255) / 256 * 256; }
 
 // ---------------------------------------------------------------------------
@@ -532,7 +622,7 @@ template <class T> int geqrf(size_t m, size_t n, T *a, size_t lda, T *tau, size_
     if (k == 0) return kOk;
     if (lda < std::max<size_t>(1, m)) return -4;
     if (m > (size_t)INT32_MAX || n > (size_t)INT32_MAX) return -1;
-    int smax = smax_for(m);
+    int smax = smax_for<T>(m);
     if (work == nullptr || *lwork == 0) {
         *lwork = elems_for<T>(geqrf_bytes<T>(m, n, smax));
         return kOk;
@@ -689,23 +779,23 @@ template <class T> int geqr2(size_t m, size_t n, T *a, size_t lda, T *tau, T *wo
 // in one launch (row chunks of every block in parallel), then the
 // recurrence for all blocks in one launch.
 // ---------------------------------------------------------------------------
-inline int gram_splits(size_t rows, size_t nblk, int scap) {
-    size_t s = std::min<size_t>((size_t)std::max(scap, 1), std::max<size_t>(1, (rows + 511) / 512));
+inline int gram_splits(size_t rows, size_t nblk, int scap, int min_rows) {
+    size_t s = std::min<size_t>((size_t)std::max(scap, 1), std::max<size_t>(1, (rows + min_rows - 1) / (size_t)min_rows));
     s = std::min<size_t>(s, std::max<size_t>(1, 4096 / std::max<size_t>(nblk, 1)));
     return (int)std::max<size_t>(s, 1);
 }
 template <class T> size_t gram_bytes(size_t rows, size_t nblk, int scap) {
-    return (nblk * (size_t)gram_splits(rows, nblk, scap) * kPanelMaxCols * kPanelMaxCols * sizeof(T) + 255) / 256 * 256;
+    return (nblk * (size_t)gram_splits(rows, nblk, scap, 2 * split_min_rows<T>()) * kPanelMaxCols * kPanelMaxCols * sizeof(T) + 255) / 256 * 256;
 }
 template <class T> int build_all_t(size_t rows, size_t k, const T *a, size_t lda, const T *tau, T *Tout, T *Pg, int scap, cudaStream_t st) {
     const size_t nblk = (k + kPanelMaxCols - 1) / kPanelMaxCols;
     if (nblk == 0) return kOk;
-    const int S = gram_splits(rows, nblk, scap);
+    const int S = gram_splits(rows, nblk, scap, 2 * split_min_rows<T>());
     const int chunk = (int)((rows + S - 1) / S);
     KScope ks("larft_all", st);
     k_gram_blocks<T><<<dim3((unsigned)S, (unsigned)nblk), 256, 0, st>>>(a, lda, (int)rows, (int)k, chunk, Pg);
     RNPGPU_CHECK_LAUNCH();
-    k_build_t<T><<<(unsigned)nblk, kPanelMaxCols, 0, st>>>(Pg, (size_t)kPanelMaxCols * kPanelMaxCols, (size_t)S * kPanelMaxCols * kPanelMaxCols, S, tau, kPanelMaxCols, (int)k,
+    k_build_t<T><<<(unsigned)nblk, kBuildTThreads, 0, st>>>(Pg, (size_t)kPanelMaxCols * kPanelMaxCols, (size_t)S * kPanelMaxCols * kPanelMaxCols, S, tau, kPanelMaxCols, (int)k,
                                                            Tout, (size_t)kPanelMaxCols * kPanelMaxCols, kPanelMaxCols);
     RNPGPU_CHECK_LAUNCH();
     return kOk;
@@ -813,8 +903,8 @@ template <class T> int unmqr(const char *side, const char *trans, size_t m, size
     if (lda < std::max<size_t>(1, nq)) return -7;
     if (ldc < std::max<size_t>(1, m)) return -10;
     if (m > (size_t)INT32_MAX || n > (size_t)INT32_MAX) return -3;
-    int smax = smax_for(nq);
-    int sgram = smax_for(nq);
+    int smax = smax_for<T>(nq);
+    int sgram = smax_for<T>(nq);
     if (work == nullptr || *lwork == 0) {
         *lwork = elems_for<T>(unmqr_bytes<T>(nq, nw, k, smax, sgram));
         return kOk;
@@ -905,7 +995,7 @@ template <class T> int ungqr(size_t m, size_t n, size_t k, T *a, size_t lda, con
     if (n > m) return -2;
     if (lda < std::max<size_t>(1, m)) return -5;
     if (m > (size_t)INT32_MAX) return -1;
-    int smax = smax_for(m), sgram = smax_for(m);
+    int smax = smax_for<T>(m), sgram = smax_for<T>(m);
     if (work == nullptr || *lwork == 0) {
         *lwork = elems_for<T>(ungqr_bytes<T>(m, n, k, smax, sgram));
         return kOk;

@@ -14,12 +14,14 @@
 //   k_build_t      T recurrence from a Gram matrix and tau
 //   k_larfg / k_larf_*   level-2 kernels for the *_unblocked entry points
 #pragma once
+#include <cooperative_groups.h>
 #include "rnp_common.cuh"
 
 namespace rnpgpu {
 
 constexpr int kPanelMaxCols = 32;
 constexpr int kPanelThreads = 512;
+constexpr int kBuildTThreads = 256;
 
 template <class T> __device__ __forceinline__ T ldcg(const T *p) { return *(volatile const T *)p; }
 __device__ __forceinline__ double ldcg(const double *p) { return __ldcg(p); }
@@ -63,12 +65,70 @@ template <class T> __device__ __forceinline__ void set_f32_scale(ReflScalars<T> 
     s.si_lo = (float)(si - (double)s.si_hi);
 }
 
+// FP64 reciprocal square root and reciprocal by Newton-Raphson iteration
+// from the FP32 hardware approximations (y <- y (3 - x y^2) / 2 and
+// y <- y (2 - d y), two steps each: the seed's 2^-22 relative error squares
+// twice), and the square root s = x y with one Newton correction
+// s <- s + y (x - s^2) / 2 (Markstein, "Computation of elementary functions
+// on the IBM RISC System/6000 processor", IBM J. Res. Dev. 34(1), 1990).
+// On this GPU a dependent FP64 operation takes about 64 cycles and a
+// division or square root about 600, so these short chains shorten the
+// reflector's serial path.  x and d must lie in the normal FP32 range.
+__device__ __forceinline__ double rsqrt_nr(double x) {
+    double y = (double)rsqrtf((float)x);
+    const double h = 0.5 * x;
+    y = fma(y, fma(-h * y, y, 0.5), y);
+    y = fma(y, fma(-h * y, y, 0.5), y);
+    return y;
+}
+__device__ __forceinline__ double sqrt_from_rsqrt(double x, double y) {
+    const double s = x * y;
+    return fma(fma(-s, s, x), 0.5 * y, s);
+}
+__device__ __forceinline__ double rcp_nr(double d) {
+    double y = (double)__frcp_rn((float)d);
+    y = fma(y, fma(-d, y, 1.0), y);
+    y = fma(y, fma(-d, y, 1.0), y);
+    return y;
+}
+
 template <class T> __device__ ReflScalars<T> reflector_scalars(T alpha, const NormAcc &nacc) {
     typedef typename Tr<T>::R R;
     ReflScalars<T> s;
-    const double xnorm = nacc.result();
     double ar = (double)Tr<T>::re(alpha), ai = (double)Tr<T>::im(alpha);
     s.knt = 0;
+    if (sizeof(R) == 8 && nacc.sml == 0.0 && nacc.big == 0.0) {
+        // FP64 data, squared norm of x in med: when |alpha|^2 + ||x||^2 lies
+        // well inside the FP32 range the scalars come from the short
+        // Newton chains (no rescaling can be needed there)
+        const double q = fma(ar, ar, fma(ai, ai, nacc.med));
+        if (q >= 0x1p-120 && q <= 0x1p120 && (nacc.med > 0.0 || ai != 0.0)) {
+            const double y = rsqrt_nr(q);
+            const double sq = sqrt_from_rsqrt(q, y);
+            const double beta = ar > 0.0 ? -sq : sq, invb = ar > 0.0 ? -y : y;
+            const double d = ar - beta;  // |d| = |ar| + |beta|: no cancellation
+            double tr, ti = 0.0, sr, si = 0.0;
+            tr = fma(-ar, invb, 1.0);
+            if (Tr<T>::is_complex) {
+                ti = -ai * invb;
+                const double inv = rcp_nr(fma(d, d, ai * ai));
+                sr = d * inv;
+                si = -ai * inv;
+            } else {
+                sr = rcp_nr(d);
+            }
+            s.identity = false;
+            s.tau = Tr<T>::make((R)tr, (R)ti);
+            s.scal = Tr<T>::make((R)sr, (R)si);
+            s.sr = sr;
+            s.si = si;
+            s.sr_hi = 0.0f; s.sr_lo = 0.0f; s.si_hi = 0.0f; s.si_lo = 0.0f;
+            s.sh = 0;
+            s.beta = beta;
+            return s;
+        }
+    }
+    const double xnorm = nacc.result();
     if (xnorm == 0.0 && ai == 0.0) {
         s.identity = true;
         s.tau = T(0);
@@ -281,16 +341,36 @@ template <class T> __device__ ReflScalars<T> reflector_scalars_f32(T alpha, F2 n
     return s;
 }
 
+// m = max(|x|, |y|) >= 2^486 or 0 < m < 2^-511 (outside the range where
+// squares and their sums stay normal FP64 numbers), from the exponent bits
+// (integer pipe); non-finite values count as unsafe
+__device__ __forceinline__ bool exp_unsafe64(double x, double y = 0.0) {
+    const int ex = (__double2hiint(x) >> 20) & 0x7ff, ey = (__double2hiint(y) >> 20) & 0x7ff;  // biased exponents
+    const int e = max(ex, ey);
+    const bool nonzero = ((__double_as_longlong(x) | __double_as_longlong(y)) << 1) != 0;
+    return e >= 1023 + 486 || (e < 1023 - 511 && nonzero);
+}
+
+// cluster barrier (all threads of every block of the cluster arrive; the
+// release / acquire pair carries each thread's prior shared-memory writes to
+// the other blocks)
+__device__ __forceinline__ void cluster_arrive() { asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory"); }
+__device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory"); }
+
 // SMEM = true: the block's rows of the panel live in dynamic shared memory
 // for the whole launch (loaded once, written back at the end); SMEM = false:
 // they are read and written in place in global memory (panels too tall for
 // shared memory).
-template <class T, bool SMEM> __global__ void __launch_bounds__(kPanelThreads) k_panel(PanelArgs<T> p) {
+// CL = true: the grid is one thread-block cluster (up to 16 blocks, short
+// panels): the partial records live in each block's shared memory and are
+// read by the others through distributed shared memory, and the grid barrier
+// is the cluster's hardware barrier (no global-memory round trip, no spin).
+template <class T, bool SMEM, bool CL = false, int NT = kPanelThreads> __global__ void __launch_bounds__(NT) k_panel(PanelArgs<T> p) {
     typedef typename Tr<T>::R R;
     constexpr bool is64 = sizeof(R) == 8;
-    constexpr int nwarps = kPanelThreads / 32;
+    constexpr int nwarps = NT / 32;
     constexpr int kSlots = kRecT + kRecD;            // one thread per record entry ...
-    constexpr int kGroups = kPanelThreads / kSlots;  // ... and kGroups subsets of the records
+    constexpr int kGroups = NT / kSlots;  // ... and kGroups subsets of the records
     constexpr int UNR = (sizeof(T) <= 4) ? 32 : (sizeof(T) <= 8 ? 16 : 8);
     const int G = gridDim.x, b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int r0 = b * p.rows_per_cta;
@@ -299,7 +379,26 @@ template <class T, bool SMEM> __global__ void __launch_bounds__(kPanelThreads) k
     T *A = p.A;
     GridBarrier bar{p.counter, p.err, (unsigned)G, 0u};
     bar.status = p.status;
+    auto bar_arrive = [&]() {
+        if (CL) cluster_arrive();
+        else bar.arrive();
+    };
+    auto bar_wait = [&]() -> bool {
+        if (CL) {
+            cluster_wait();
+            return true;
+        }
+        return bar.wait();
+    };
+    auto bar_sync = [&]() -> bool {
+        bar_arrive();
+        return bar_wait();
+    };
 
+    __shared__ PanelRec<T> s_rec[CL ? 2 : 1];  // CL: this block's records of the two phase parities
+    constexpr bool kColLanes = CL && is64;       // FP64 short panels: lanes over columns (below)
+    __shared__ T s_part[kColLanes ? nwarps : 1][kPanelMaxCols];  // per-warp record partials
+    __shared__ T s_cvr[kColLanes ? 1024 : 1];                   // -conj(tau) v of the last reflector, own rows
     __shared__ T s_T[kPanelMaxCols][kPanelMaxCols + 1];
     __shared__ T s_cv[kRecT];          // combined record
     __shared__ double s_cd[kRecD];     // combined FP64 sums
@@ -323,17 +422,28 @@ template <class T, bool SMEM> __global__ void __launch_bounds__(kPanelThreads) k
     };
     if (SMEM) {
         for (int c = 0; c < p.N; ++c)
-            for (int r = r0 + tid; r < r1; r += kPanelThreads) sP[(size_t)c * ldp + (r - r0)] = A[r + (size_t)c * lda];
+            for (int r = r0 + tid; r < r1; r += NT) sP[(size_t)c * ldp + (r - r0)] = A[r + (size_t)c * lda];
     }
     __syncthreads();
 
     int phase = 0;  // records of phase k live in buffer k & 1
-    auto my_rec = [&]() -> PanelRec<T> & { return p.rec[(size_t)(phase & 1) * G + b]; };
+    auto my_rec = [&]() -> PanelRec<T> & {
+        if (CL) return s_rec[phase & 1];
+        return p.rec[(size_t)(phase & 1) * G + b];
+    };
+    // block q's record of the current phase (CL: in block q's shared memory)
+    auto rec_of = [&](int q) -> const PanelRec<T> * {
+        if (CL) return cooperative_groups::this_cluster().map_shared_rank(&s_rec[phase & 1], q);
+        return p.rec + (size_t)(phase & 1) * G + q;
+    };
+    auto ldr = [](const auto *ptr) {
+        if (CL) return *ptr;
+        return ldcg(ptr);
+    };
     // combine the records of the current phase into s_cv and s_cd (FP64
     // sums) or s_ch/s_cl (FP32 pair sums)
     auto combine = [&](bool pairs) {
         const int slot = tid % kSlots, grp = tid / kSlots;
-        const PanelRec<T> *rb = p.rec + (size_t)(phase & 1) * G;
         if (grp < kGroups) {
             if (slot < kRecT) {
                 T a = T(0);
@@ -342,7 +452,7 @@ template <class T, bool SMEM> __global__ void __launch_bounds__(kPanelThreads) k
 #pragma unroll
                     for (int u = 0; u < UNR; ++u) {
                         const int q = base + u * kGroups;
-                        v[u] = (q < G) ? ldcg(&rb[q].v[slot]) : T(0);
+                        v[u] = (q < G) ? ldr(&rec_of(q)->v[slot]) : T(0);
                     }
                     a = a + tree_sum(v);
                 }
@@ -355,8 +465,8 @@ template <class T, bool SMEM> __global__ void __launch_bounds__(kPanelThreads) k
 #pragma unroll
                     for (int u = 0; u < 16; ++u) {
                         const int q = base + u * kGroups;
-                        vh[u] = (q < G) ? __ldcg(&rb[q].fh[d]) : 0.f;
-                        vl[u] = (q < G) ? __ldcg(&rb[q].fl[d]) : 0.f;
+                        vh[u] = (q < G) ? ldr(&rec_of(q)->fh[d]) : 0.f;
+                        vl[u] = (q < G) ? ldr(&rec_of(q)->fl[d]) : 0.f;
                     }
 #pragma unroll
                     for (int u = 0; u < 16; ++u) {
@@ -374,7 +484,7 @@ template <class T, bool SMEM> __global__ void __launch_bounds__(kPanelThreads) k
 #pragma unroll
                     for (int u = 0; u < 16; ++u) {
                         const int q = base + u * kGroups;
-                        v[u] = (q < G) ? __ldcg(&rb[q].d[d]) : 0.0;
+                        v[u] = (q < G) ? ldr(&rec_of(q)->d[d]) : 0.0;
                     }
                     a += tree_sum(v);
                 }
@@ -408,7 +518,7 @@ template <class T, bool SMEM> __global__ void __launch_bounds__(kPanelThreads) k
     auto exact_record = [&](int col) {
         NormAcc acc;
         acc.zero();
-        for (int r = max(r0, col + 1) + tid; r < r1; r += kPanelThreads) acc.add(at(r, col));
+        for (int r = max(r0, col + 1) + tid; r < r1; r += NT) acc.add(at(r, col));
         acc.warp_reduce();
         if (lane == 0) {
             s_red[warp][0] = acc.sml;
@@ -456,7 +566,7 @@ template <class T, bool SMEM> __global__ void __launch_bounds__(kPanelThreads) k
 
     // prologue: exact norm of column 0
     exact_record(0);
-    if (!bar.sync()) return;
+    if (!bar_sync()) return;
     combine(false);
     scalars_from_exact();
     ReflScalars<T> prev;
@@ -468,7 +578,7 @@ template <class T, bool SMEM> __global__ void __launch_bounds__(kPanelThreads) k
             // 1. one thread of the last warp (which owns no rows to update
             //    when the block holds fewer rows than threads) forms the
             //    downdated norm of column j and its reflector scalars
-            if (tid == kPanelThreads - 1) {
+            if (tid == NT - 1) {
                 const T a_pre = s_cv[kPanelMaxCols], vn = s_cv[kPanelMaxCols + 1];
                 T alpha = a_pre, c = T(0);
                 if (!prev.identity) {
@@ -512,17 +622,30 @@ template <class T, bool SMEM> __global__ void __launch_bounds__(kPanelThreads) k
             }
             // 2. apply H[j-1]^H to own rows r >= j-1 of columns j..N-1
             if (!prev.identity) {
-                const T ctau = Tr<T>::conj(prev.tau);
-                for (int r = max(r0, j - 1) + tid; r < r1; r += kPanelThreads) {
-                    const T v = (r == j - 1) ? T(1) : at(r, j - 1);
-                    const T cv = ctau * v;
-                    for (int c = j; c < p.N; ++c) at(r, c) = fmac(-cv, s_cv[c], at(r, c));
+                if constexpr (kColLanes) {
+                    // one FP64 FMA per (row, column) pair, the pairs spread
+                    // over all warps but the last (whose last thread forms
+                    // the scalars meanwhile); row factors from s_cvr
+                    constexpr int NA = NT - 32;
+                    const int rs2 = max(r0, j - 1), nr = r1 - rs2, nc = p.N - j;
+                    if (tid < NA)
+                        for (int e = tid; e < nr * nc; e += NA) {
+                            const int r = rs2 + e % nr, c = j + e / nr;
+                            at(r, c) = fmac(s_cvr[r - r0], s_cv[c], at(r, c));
+                        }
+                } else {
+                    const T ctau = Tr<T>::conj(prev.tau);
+                    for (int r = max(r0, j - 1) + tid; r < r1; r += NT) {
+                        const T v = (r == j - 1) ? T(1) : at(r, j - 1);
+                        const T cv = ctau * v;
+                        for (int c = j; c < p.N; ++c) at(r, c) = fmac(-cv, s_cv[c], at(r, c));
+                    }
                 }
             }
             __syncthreads();
             if (s_exact) {
                 exact_record(j);
-                if (!bar.sync()) return;
+                if (!bar_sync()) return;
                 combine(false);
                 scalars_from_exact();
             }
@@ -530,7 +653,7 @@ template <class T, bool SMEM> __global__ void __launch_bounds__(kPanelThreads) k
         // 3. scale x into v
         const ReflScalars<T> rs = s_refl;
         if (!rs.identity) {
-            for (int r = max(r0, j + 1) + tid; r < r1; r += kPanelThreads) at(r, j) = scale_x(at(r, j), rs);
+            for (int r = max(r0, j + 1) + tid; r < r1; r += NT) at(r, j) = scale_x(at(r, j), rs);
             if (tid == 0 && j >= r0 && j < r1) at(j, j) = Tr<T>::make((R)rs.beta, 0);
         }
         if (b == 0 && tid == 0) p.tau[j] = rs.tau;
@@ -538,99 +661,165 @@ template <class T, bool SMEM> __global__ void __launch_bounds__(kPanelThreads) k
         // 4. partial record of this phase
         ++phase;
         PanelRec<T> &rc = my_rec();
-        // two columns per warp at a time, two rows per step (four
-        // independent chains)
-        for (int c0 = warp; c0 < p.N; c0 += 2 * nwarps) {
-            const int c1 = c0 + nwarps;
-            const bool u0 = (c0 != j), u1 = (c1 < p.N && c1 != j);
-            T a00 = T(0), a01 = T(0), a10 = T(0), a11 = T(0);
-            auto step = [&](int r, T &x0, T &x1) {
-                const T v = (r == j) ? T(1) : at(r, j);
-                if (u0) {
-                    const T a = at(r, c0);
-                    x0 = (c0 > j) ? fmac(Tr<T>::conj(v), a, x0) : fmac(Tr<T>::conj(a), v, x0);
-                }
-                if (u1) {
-                    const T a = at(r, c1);
-                    x1 = (c1 > j) ? fmac(Tr<T>::conj(v), a, x1) : fmac(Tr<T>::conj(a), v, x1);
-                }
-            };
-            int r = max(r0, j) + lane;
-            for (; r + 32 < r1; r += 64) {
-                step(r, a00, a10);
-                step(r + 32, a01, a11);
-            }
-            if (r < r1) step(r, a00, a10);
-            const T acc0 = warp_sum(a00 + a01), acc1 = warp_sum(a10 + a11);
-            if (lane == 0) {
-                rc.v[c0] = acc0;
-                if (c1 < p.N) rc.v[c1] = acc1;
-            }
-        }
-        for (int c = p.N + tid; c < kPanelMaxCols; c += kPanelThreads) rc.v[c] = T(0);
         T anext = T(0), vnext = T(0);
-        if (is64) {
-            double e1 = 0.0, e3 = 0.0, eu = 0.0, e2r = 0.0, e2i = 0.0;
-            if (j + 1 < p.N) {
-                const double tsml = 0x1p-511, tbig = 0x1p486;
-                for (int r = max(r0, j + 2) + tid; r < r1; r += kPanelThreads) {
-                    const T a = at(r, j + 1), v = at(r, j);
-                    const double ar = re_of(a), ai = im_of(a), vr = re_of(v), vi = im_of(v);
-                    e1 = fma(ar, ar, fma(ai, ai, e1));
-                    e3 = fma(vr, vr, fma(vi, vi, e3));
-                    // conj(v) a
-                    e2r = fma(vr, ar, fma(vi, ai, e2r));
-                    e2i = fma(vr, ai, fma(-vi, ar, e2i));
-                    const double m = fmax(fabs(ar), fabs(ai));
-                    if (m > tbig || (m < tsml && m != 0.0)) eu = 1.0;
+        if constexpr (kColLanes) {
+            // FP64 short panels: lane c accumulates record entry c over the
+            // warp's chunk of rows >= j (no shuffle reductions: an FP64 warp
+            // instruction costs the same for one lane as for 32).  Lane j,
+            // which has no entry, sums |v|^2 and lane j+1 skips rows j and
+            // j+1: over rows >= j+2 they are s3 and s2 of the downdating;
+            // w_{j+1} gets rows j and j+1 back after the warps are summed.
+            const int rs4 = max(r0, j), nr = max(0, r1 - rs4);
+            const int per = (nr + nwarps - 1) / nwarps;
+            const int ra = rs4 + warp * per, rb = min(r1, ra + per);
+            const int c = lane;
+            T acc = T(0);
+            if (c < p.N) {
+                const bool tail = (c == j || c == j + 1);
+                for (int r = ra; r < rb; ++r) {
+                    const T v = (r == j) ? T(1) : at(r, j);
+                    const T a = at(r, c);
+                    if (!tail || r >= j + 2) acc = (c >= j) ? fmac(Tr<T>::conj(v), a, acc) : fmac(Tr<T>::conj(a), v, acc);
                 }
             }
-            e1 = warp_sum(e1);
-            e3 = warp_sum(e3);
-            eu = warp_sum(eu);
-            e2r = warp_sum(e2r);
-            e2i = warp_sum(e2i);
-            if (lane == 0) {
-                s_red[warp][0] = e1;
-                s_red[warp][1] = e3;
-                s_red[warp][2] = eu;
-                s_red[warp][3] = e2r;
-                s_red[warp][4] = e2i;
+            s_part[warp][c] = acc;
+            if (c == j) s_red[warp][1] = re_of(acc);
+            if (c == j + 1) {
+                s_red[warp][3] = re_of(acc);
+                s_red[warp][4] = im_of(acc);
             }
-        } else {
-            // FP32 data: error-free FP32 accumulation; magnitudes outside
-            // [2^-40, 2^48] (squares that could leave the FP32 range or lose
-            // their low parts) send the column to the exact FP64 norm
-            float h1 = 0.f, l1 = 0.f, h3 = 0.f, l3 = 0.f, h2r = 0.f, l2r = 0.f, h2i = 0.f, l2i = 0.f, eu = 0.f;
+            // s1 and the magnitude flag of column j+1: lanes over rows
+            double e1 = 0.0;
+            bool unsafe = false;
             if (j + 1 < p.N) {
-                for (int r = max(r0, j + 2) + tid; r < r1; r += kPanelThreads) {
-                    const T a = at(r, j + 1), v = at(r, j);
-                    const float ar = re_f(a), vr = re_f(v), ai = im_f(a), vi = im_f(v);
-                    const float m = fmaxf(fabsf(ar), fabsf(ai));
-                    if (m > 0x1p48f || (m < 0x1p-40f && m != 0.f)) eu = 1.f;
-                    df_add_prod(h1, l1, ar, ar);
-                    df_add_prod(h3, l3, vr, vr);
-                    df_add_prod(h2r, l2r, vr, ar);
+                for (int r = max(r0, j + 2) + tid; r < r1; r += NT) {
+                    const T a = at(r, j + 1);
+                    const double ar = re_of(a);
                     if (Tr<T>::is_complex) {
-                        df_add_prod(h1, l1, ai, ai);
-                        df_add_prod(h3, l3, vi, vi);
-                        df_add_prod(h2r, l2r, vi, ai);
-                        df_add_prod(h2i, l2i, vr, ai);
-                        df_add_prod(h2i, l2i, -vi, ar);
+                        const double ai = im_of(a);
+                        unsafe |= exp_unsafe64(ar, ai);
+                        e1 = fma(ar, ar, fma(ai, ai, e1));
+                    } else {
+                        unsafe |= exp_unsafe64(ar);
+                        e1 = fma(ar, ar, e1);
                     }
                 }
             }
-            df_warp_sum(h1, l1);
-            df_warp_sum(h3, l3);
-            df_warp_sum(h2r, l2r);
-            if (Tr<T>::is_complex) df_warp_sum(h2i, l2i);
-            eu = warp_sum(eu);
+            const bool any_unsafe = __any_sync(0xffffffffu, unsafe);
+            e1 = warp_sum(e1);
             if (lane == 0) {
-                s_rh[warp][0] = h1; s_rl[warp][0] = l1;
-                s_rh[warp][1] = h3; s_rl[warp][1] = l3;
-                s_rh[warp][2] = eu; s_rl[warp][2] = 0.f;
-                s_rh[warp][3] = h2r; s_rl[warp][3] = l2r;
-                s_rh[warp][4] = h2i; s_rl[warp][4] = l2i;
+                s_red[warp][0] = e1;
+                s_red[warp][2] = any_unsafe ? 1.0 : 0.0;
+                if (j + 1 >= p.N) {
+                    s_red[warp][1] = 0.0;
+                    s_red[warp][3] = 0.0;
+                    s_red[warp][4] = 0.0;
+                }
+            }
+        } else {
+            // two columns per warp at a time, two rows per step (four
+            // independent chains)
+            for (int c0 = warp; c0 < p.N; c0 += 2 * nwarps) {
+                const int c1 = c0 + nwarps;
+                const bool u0 = (c0 != j), u1 = (c1 < p.N && c1 != j);
+                T a00 = T(0), a01 = T(0), a10 = T(0), a11 = T(0);
+                auto step = [&](int r, T &x0, T &x1) {
+                    const T v = (r == j) ? T(1) : at(r, j);
+                    if (u0) {
+                        const T a = at(r, c0);
+                        x0 = (c0 > j) ? fmac(Tr<T>::conj(v), a, x0) : fmac(Tr<T>::conj(a), v, x0);
+                    }
+                    if (u1) {
+                        const T a = at(r, c1);
+                        x1 = (c1 > j) ? fmac(Tr<T>::conj(v), a, x1) : fmac(Tr<T>::conj(a), v, x1);
+                    }
+                };
+                int r = max(r0, j) + lane;
+                for (; r + 32 < r1; r += 64) {
+                    step(r, a00, a10);
+                    step(r + 32, a01, a11);
+                }
+                if (r < r1) step(r, a00, a10);
+                const T acc0 = warp_sum(a00 + a01), acc1 = warp_sum(a10 + a11);
+                if (lane == 0) {
+                    rc.v[c0] = acc0;
+                    if (c1 < p.N) rc.v[c1] = acc1;
+                }
+            }
+            for (int c = p.N + tid; c < kPanelMaxCols; c += NT) rc.v[c] = T(0);
+            if (is64) {
+                // FP64 instructions share one slow pipe per SM here, so the
+                // real case skips the imaginary parts, the magnitude test reads
+                // the exponent bits (integer pipe) and the flag is a warp vote
+                double e1 = 0.0, e3 = 0.0, e2r = 0.0, e2i = 0.0;
+                bool unsafe = false;
+                if (j + 1 < p.N) {
+                    for (int r = max(r0, j + 2) + tid; r < r1; r += NT) {
+                        const T a = at(r, j + 1), v = at(r, j);
+                        const double ar = re_of(a), vr = re_of(v);
+                        if (Tr<T>::is_complex) {
+                            const double ai = im_of(a), vi = im_of(v);
+                            unsafe |= exp_unsafe64(ar, ai);
+                            e1 = fma(ar, ar, fma(ai, ai, e1));
+                            e3 = fma(vr, vr, fma(vi, vi, e3));
+                            // conj(v) a
+                            e2r = fma(vr, ar, fma(vi, ai, e2r));
+                            e2i = fma(vr, ai, fma(-vi, ar, e2i));
+                        } else {
+                            unsafe |= exp_unsafe64(ar);
+                            e1 = fma(ar, ar, e1);
+                            e3 = fma(vr, vr, e3);
+                            e2r = fma(vr, ar, e2r);
+                        }
+                    }
+                }
+                const double eu = __any_sync(0xffffffffu, unsafe) ? 1.0 : 0.0;
+                e1 = warp_sum(e1);
+                e3 = warp_sum(e3);
+                e2r = warp_sum(e2r);
+                if (Tr<T>::is_complex) e2i = warp_sum(e2i);
+                if (lane == 0) {
+                    s_red[warp][0] = e1;
+                    s_red[warp][1] = e3;
+                    s_red[warp][2] = eu;
+                    s_red[warp][3] = e2r;
+                    s_red[warp][4] = e2i;
+                }
+            } else {
+                // FP32 data: error-free FP32 accumulation; magnitudes outside
+                // [2^-40, 2^48] (squares that could leave the FP32 range or lose
+                // their low parts) send the column to the exact FP64 norm
+                float h1 = 0.f, l1 = 0.f, h3 = 0.f, l3 = 0.f, h2r = 0.f, l2r = 0.f, h2i = 0.f, l2i = 0.f, eu = 0.f;
+                if (j + 1 < p.N) {
+                    for (int r = max(r0, j + 2) + tid; r < r1; r += NT) {
+                        const T a = at(r, j + 1), v = at(r, j);
+                        const float ar = re_f(a), vr = re_f(v), ai = im_f(a), vi = im_f(v);
+                        const float m = fmaxf(fabsf(ar), fabsf(ai));
+                        if (m > 0x1p48f || (m < 0x1p-40f && m != 0.f)) eu = 1.f;
+                        df_add_prod(h1, l1, ar, ar);
+                        df_add_prod(h3, l3, vr, vr);
+                        df_add_prod(h2r, l2r, vr, ar);
+                        if (Tr<T>::is_complex) {
+                            df_add_prod(h1, l1, ai, ai);
+                            df_add_prod(h3, l3, vi, vi);
+                            df_add_prod(h2r, l2r, vi, ai);
+                            df_add_prod(h2i, l2i, vr, ai);
+                            df_add_prod(h2i, l2i, -vi, ar);
+                        }
+                    }
+                }
+                df_warp_sum(h1, l1);
+                df_warp_sum(h3, l3);
+                df_warp_sum(h2r, l2r);
+                if (Tr<T>::is_complex) df_warp_sum(h2i, l2i);
+                eu = warp_sum(eu);
+                if (lane == 0) {
+                    s_rh[warp][0] = h1; s_rl[warp][0] = l1;
+                    s_rh[warp][1] = h3; s_rl[warp][1] = l3;
+                    s_rh[warp][2] = eu; s_rl[warp][2] = 0.f;
+                    s_rh[warp][3] = h2r; s_rl[warp][3] = l2r;
+                    s_rh[warp][4] = h2i; s_rl[warp][4] = l2i;
+                }
             }
         }
         if (j + 1 < p.N && j + 1 >= r0 && j + 1 < r1 && tid == 0) {
@@ -658,14 +847,30 @@ template <class T, bool SMEM> __global__ void __launch_bounds__(kPanelThreads) k
             rc.fh[5] = 0.f;
             rc.fl[5] = 0.f;
         }
+        if constexpr (kColLanes) {
+            // the warps' partials of every entry (fixed order); w_{j+1}
+            // adds back rows j and j+1 where this block holds them
+            if (tid < p.N) {
+                T w = s_part[0][tid];
+                for (int q = 1; q < nwarps; ++q) w = w + s_part[q][tid];
+                if (tid == j) w = T(0);  // no entry for the reflector's own column
+                if (tid == j + 1) {
+                    if (j >= r0 && j < r1) w = w + at(j, j + 1);
+                    if (j + 1 >= r0 && j + 1 < r1) w = fmac(Tr<T>::conj(at(j + 1, j)), at(j + 1, j + 1), w);
+                }
+                rc.v[tid] = w;
+            } else if (tid < kPanelMaxCols) {
+                rc.v[tid] = T(0);
+            }
+        }
         if (tid == 0) {
             rc.v[kPanelMaxCols] = anext;
             rc.v[kPanelMaxCols + 1] = vnext;
         }
         // block 0 extends T by the previous column while the barrier settles
-        bar.arrive();
+        bar_arrive();
         if (b == 0 && warp == 1) t_column();
-        if (!bar.wait()) return;
+        if (!bar_wait()) return;
         combine(!is64);
         if (b == 0) {
             if (tid < kPanelMaxCols) s_g[tid] = s_cv[tid];
@@ -676,16 +881,26 @@ template <class T, bool SMEM> __global__ void __launch_bounds__(kPanelThreads) k
             }
         }
         prev = rs;
+        if constexpr (kColLanes) {
+            // row factors of the next apply step: -conj(tau_j) v_r, own rows >= j
+            if (!rs.identity && j + 1 < p.N) {
+                const T mct = -Tr<T>::conj(rs.tau);
+                for (int r = max(r0, j) + tid; r < r1; r += NT) s_cvr[r - r0] = (r == j) ? mct : mct * at(r, j);
+            }
+            __syncthreads();
+        }
     }
+    // CL: no block leaves while another may still read its records
+    if (CL) bar_sync();
     __syncthreads();
     if (b == 0 && warp == 1) t_column();
     __syncthreads();
     if (SMEM) {
         for (int c = 0; c < p.N; ++c)
-            for (int r = r0 + tid; r < r1; r += kPanelThreads) A[r + (size_t)c * lda] = sP[(size_t)c * ldp + (r - r0)];
+            for (int r = r0 + tid; r < r1; r += NT) A[r + (size_t)c * lda] = sP[(size_t)c * ldp + (r - r0)];
     }
     if (b == 0 && p.Tm != nullptr) {
-        for (int idx = tid; idx < p.N * p.N; idx += kPanelThreads) {
+        for (int idx = tid; idx < p.N * p.N; idx += NT) {
             int r = idx % p.N, c = idx / p.N;
             if (r <= c) p.Tm[r + (size_t)c * p.ldt] = s_T[r][c];
         }
@@ -954,21 +1169,26 @@ __global__ void __launch_bounds__(256) k_reduce_splits(const T *P, size_t ldp, s
 // with G = V^H V (sum of nsplit partials).  One block per reflector block.
 // ---------------------------------------------------------------------------
 template <class T>
-__global__ void __launch_bounds__(kPanelMaxCols) k_build_t(const T *P, size_t pstride_split, size_t pstride_blk, int nsplit, const T *tau, int nb, int k_total, T *Tout, size_t tstride, int ldt) {
+__global__ void __launch_bounds__(kBuildTThreads) k_build_t(const T *P, size_t pstride_split, size_t pstride_blk, int nsplit, const T *tau, int nb, int k_total, T *Tout, size_t tstride, int ldt) {
     __shared__ T sG[kPanelMaxCols][kPanelMaxCols + 1];
     __shared__ T sT[kPanelMaxCols][kPanelMaxCols + 1];
     const int blk = blockIdx.x, tid = threadIdx.x;
     const int i0 = blk * nb;
     const int k = min(nb, k_total - i0);
     const T *Pb = P + (size_t)blk * pstride_blk;
-    for (int c = 0; c < k; ++c) {
-        if (tid < k) {
+    // the split partials of the strictly upper Gram entries, summed by all
+    // threads of the block (one entry per thread, a fixed order)
+    for (int e = tid; e < kPanelMaxCols * kPanelMaxCols; e += blockDim.x) {
+        const int r = e % kPanelMaxCols, c = e / kPanelMaxCols;
+        if (r < c && c < k) {
             T s = T(0);
-            for (int q = 0; q < nsplit; ++q) s = s + Pb[(size_t)q * pstride_split + tid + (size_t)c * kPanelMaxCols];
-            sG[tid][c] = s;
+            for (int q = 0; q < nsplit; ++q) s = s + Pb[(size_t)q * pstride_split + r + (size_t)c * kPanelMaxCols];
+            sG[r][c] = s;
         }
     }
     __syncthreads();
+    // the recurrence in one warp
+    if (tid >= kPanelMaxCols) return;
     for (int i = 0; i < k; ++i) {
         T ti = tau[i0 + i];
         if (tid < i) {
@@ -977,7 +1197,7 @@ __global__ void __launch_bounds__(kPanelMaxCols) k_build_t(const T *P, size_t ps
             sT[tid][i] = (ti == T(0)) ? T(0) : (-ti) * acc;
         }
         if (tid == 0) sT[i][i] = ti;
-        __syncthreads();
+        __syncwarp();
     }
     T *To = Tout + (size_t)blk * tstride;
     for (int c = 0; c < k; ++c)

@@ -33,7 +33,7 @@ extern "C" int rnpgpu_sgeqrf_mixed(size_t m, size_t n, float *a, size_t lda, flo
     if (k == 0) return kOk;
     if (lda < std::max<size_t>(1, m)) return -4;
     if (m > (size_t)INT32_MAX / 2 || n > (size_t)INT32_MAX / 2) return -1;
-    const size_t fbytes = (geqrf_bytes<float>(m, n, smax_for(m)) + 255) / 256 * 256;
+    const size_t fbytes = (geqrf_bytes<float>(m, n, smax_for<float>(m)) + 255) / 256 * 256;
     const bool wide_ok = wide::usable(m, n, reinterpret_cast<const float *>(256), 4);  // sized by the shape alone
     const size_t need = elems_for<float>(fbytes + cqr_ws_bytes() + (wide_ok ? wide::ws_bytes(m, n) : 0) + 256);
     if (work == nullptr || *lwork == 0) {

@@ -305,7 +305,12 @@ template <int kTag = 0> __global__ void __launch_bounds__(kWThreads, 1) k_wide_w
         if (tc::elect_one()) tc::umma_commit(done);
         __syncwarp();
     } else if (warp >= 1 && warp <= 4) {
-        // converters: C's FP32 tile [col][32 rows] -> A slices
+        // converters: C's FP32 tile [col][32 rows] -> A slices.  The tile
+        // arrives 128-byte swizzled: the 16-byte chunk q of column c (rows
+        // 4q .. 4q+3) sits at chunk q ^ (c & 7) of its 128-byte row.  Eight
+        // consecutive threads take eight consecutive columns and the same
+        // row group, so both their loads (distinct swizzled chunks) and their
+        // slice stores (eight rows of one core matrix) hit distinct banks.
         const int ct = tid - 32;  // 0..127
         uint32_t fph[kWStages] = {0, 0, 0};
         for (int ch = 0; ch < nch; ++ch) {
@@ -319,9 +324,10 @@ template <int kTag = 0> __global__ void __launch_bounds__(kWThreads, 1) k_wide_w
 #pragma unroll
                 for (int i = 0; i < 4; ++i) {
                     const int u = ct + 128 * i;
-                    const int c = u >> 2, g = u & 3;
-                    const float4 lo = *reinterpret_cast<const float4 *>(cf + c * 32 + g * 8);
-                    const float4 hi = *reinterpret_cast<const float4 *>(cf + c * 32 + g * 8 + 4);
+                    const int c = (u & 7) + 8 * (u >> 5), g = (u >> 3) & 3;
+                    const int sw = c & 7;
+                    const float4 lo = *reinterpret_cast<const float4 *>(cf + c * 32 + (((2 * g) ^ sw) << 2));
+                    const float4 hi = *reinterpret_cast<const float4 *>(cf + c * 32 + (((2 * g + 1) ^ sw) << 2));
                     const float x[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
                     put8(as, kVbSlice, core_off(c, g * 8, 4), x);
                 }
@@ -730,7 +736,7 @@ namespace rnpgpu {
 
 // 2-D tensor map of a column-major FP32 matrix (rows x cols, leading
 // dimension ld elements) with box_rows x box_cols tiles (api_context.cu)
-int encode_map_f32(CUtensorMap *map, const float *base, uint64_t rows, uint64_t cols, uint64_t ld, uint32_t box_rows, uint32_t box_cols);
+int encode_map_f32(CUtensorMap *map, const float *base, uint64_t rows, uint64_t cols, uint64_t ld, uint32_t box_rows, uint32_t box_cols, bool swizzle128 = false);
 
 namespace wide {
 
@@ -788,7 +794,7 @@ inline int apply(float *A, size_t lda, int m, int n, int r0, const float *Tp, si
     {
         KScope ks("wide_w", st);
         CUtensorMap map;
-        if ((rc = encode_map_f32(&map, A, (uint64_t)m, (uint64_t)n, lda, 32, 128))) return rc;
+        if ((rc = encode_map_f32(&map, A, (uint64_t)m, (uint64_t)n, lda, 32, 128, true))) return rc;
         if ((rc = kernel_attr((const void *)k_wide_w<0>, kWSmem))) return rc;
         WArgs wa;
         wa.rows = rows; wa.r0 = r0; wa.c1 = c1; wa.ntile = ntile; wa.nsplit = nsplit; wa.rows_per_split = rps;

@@ -72,7 +72,8 @@ def test_consumers_match_reference_golden(name):
         torch.cuda.synchronize()
         assert rel(from_dev(dA), c["a"]) <= TOL[p]
         assert rel(from_dev(dB), c["b"]) <= TOL[p]
-        assert rel(tau.cpu().numpy(), c["tau"]) <= TOL[p]
+        k = int(c["ihi"]) - int(c["ilo"])  # entries past irows are workspace, set by neither
+        assert rel(tau.cpu().numpy()[:k], c["tau"][:k]) <= TOL[p]
         if dVL is not None:
             assert rel(from_dev(dVL), c["vl"]) <= TOL[p]
         if dVR is not None:
@@ -174,7 +175,7 @@ def test_generalized_step_against_oracle(oracle, p, n, ilo, ihi, vl, vr):
     dVR = to_dev(np.full((n, n), 5.0, dtype=DT[p])) if vr else None
     tau = consumers.generalized_triangularize_b(ilo, ihi, dA, dB, dVL, dVR)
     torch.cuda.synchronize()
-    assert rel(tau.cpu().numpy(), tau_o) <= TOL[p]
+    assert rel(tau.cpu().numpy()[: ihi - ilo], tau_o[: ihi - ilo]) <= TOL[p]
     assert rel(from_dev(dA), ao) <= TOL[p] and rel(from_dev(dB), bo) <= TOL[p]
     if vl:
         assert rel(from_dev(dVL), vlo) <= TOL[p]
