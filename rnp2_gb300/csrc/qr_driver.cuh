@@ -194,6 +194,9 @@ template <class T> int launch_gemm(GemmArgs<T> g, int nsplit, cudaStream_t st, c
     if (f64 && g.N <= 16 && (long)((g.M + 127) / 128) * nsplit < sms) {
         dim3 grid((g.M + 31) / 32, (g.N + 15) / 16, nsplit);
         k_gemm<T, 32, 16, 16, 2, 1><<<grid, 256, 0, st>>>(g);
+    } else if (f64 && g.N > 16 && (long)((g.M + 31) / 32) * ((g.N + 31) / 32) * nsplit < sms / 2) {
+        dim3 grid((g.M + 15) / 16, (g.N + 31) / 32, nsplit);
+        k_gemm<T, 16, 32, 16, 1, 2><<<grid, 256, 0, st>>>(g);
     } else if (f64 && g.N > 16 && (long)((g.M + 63) / 64) * ((g.N + 63) / 64) * nsplit < sms) {
         dim3 grid((g.M + 31) / 32, (g.N + 31) / 32, nsplit);
         k_gemm<T, 32, 32, 16, 2, 2><<<grid, 256, 0, st>>>(g);
@@ -381,7 +384,7 @@ template <class T> int block_t(int rows, int ib, const T *V, size_t ldv, const T
     g.dstride = (size_t)kPanelMaxCols * kPanelMaxCols;
     int rc = launch_gemm(g, nsplit, st, "larft_gram");
     if (rc) return rc;
-    k_build_t<T><<<1, kPanelMaxCols, 0, st>>>(Pg, (size_t)kPanelMaxCols * kPanelMaxCols, 0, nsplit, tau, ib, ib, Tout, 0, ldt);
+    k_build_t<T><<<1, kBuildTThreads, 0, st>>>(Pg, (size_t)kPanelMaxCols * kPanelMaxCols, 0, nsplit, tau, ib, ib, Tout, 0, ldt);
     RNPGPU_CHECK_LAUNCH();
     return kOk;
 }
@@ -429,7 +432,7 @@ template <class T> int panel_factor(int M, int N, T *A, size_t lda, T *tau, T *T
         // memory; g falls strictly until the query agrees
         int g = std::min(16, (M + kPanelClusterRowsPerBlock - 1) / kPanelClusterRowsPerBlock);
         while (g >= 2) {
-            const size_t smem = (size_t)((M + g - 1) / g) * N * sizeof(T);
+            const size_t smem = (size_t)(((M + g - 1) / g) | 1) * N * sizeof(T);
             if (smem > kPanelSmemMax) {
                 g = 0;
                 break;
@@ -447,7 +450,7 @@ template <class T> int panel_factor(int M, int N, T *A, size_t lda, T *tau, T *T
             p.rows_per_cta = (M + g - 1) / g;
             void *args[] = {&p};
             KScope ks("panel", st);
-            return cluster_launch("k_panel(cluster)", kc, g, kPanelClusterThreads, args, (size_t)p.rows_per_cta * N * sizeof(T), st);
+            return cluster_launch("k_panel(cluster)", kc, g, kPanelClusterThreads, args, (size_t)(p.rows_per_cta | 1) * N * sizeof(T), st);
         }
     }
     const int G = panel_grid(M, ws.gmax);
@@ -1039,7 +1042,7 @@ template <class T> int ungqr(size_t m, size_t n, size_t k, T *a, size_t lda, con
             rc = apply_block<T>(true, true, (int)(m - i), (int)(n - i - ib), ib, V, lda, Tm, kPanelMaxCols, a + i + (i + ib) * lda, lda, bw, st);
             if (rc) return rc;
         }
-        k_t_v1h<T><<<1, kPanelMaxCols * kPanelMaxCols, 0, st>>>(Tm, kPanelMaxCols, V, lda, ib, Y, kPanelMaxCols);
+        k_t_v1h<T><<<(unsigned)ib, kPanelMaxCols, 0, st>>>(Tm, kPanelMaxCols, V, lda, ib, Y, kPanelMaxCols);
         RNPGPU_CHECK_LAUNCH();
         // V block columns <- I - V Y  (in place: each thread block owns whole rows)
         GemmArgs<T> g = gemm_args<T>(V, lda, kOpN, 1, Y, (size_t)kPanelMaxCols, kOpN, 0, V, lda, (int)(m - i), ib, ib, T(-1), kBetaIdentity);

@@ -22,6 +22,7 @@ namespace rnpgpu {
 constexpr int kPanelMaxCols = 32;
 constexpr int kPanelThreads = 512;
 constexpr int kBuildTThreads = 256;
+constexpr int kBuildTWarps = 4;  // warps of k_build_t's recurrence
 
 template <class T> __device__ __forceinline__ T ldcg(const T *p) { return *(volatile const T *)p; }
 __device__ __forceinline__ double ldcg(const double *p) { return __ldcg(p); }
@@ -371,7 +372,9 @@ template <class T, bool SMEM, bool CL = false, int NT = kPanelThreads> __global_
     constexpr int nwarps = NT / 32;
     constexpr int kSlots = kRecT + kRecD;            // one thread per record entry ...
     constexpr int kGroups = NT / kSlots;  // ... and kGroups subsets of the records
-    constexpr int UNR = (sizeof(T) <= 4) ? 32 : (sizeof(T) <= 8 ? 16 : 8);
+    // records summed per thread, unrolled; a cluster has at most 16 blocks
+    // over the kGroups subsets, and every FP64 add is a 64-cycle instruction
+    constexpr int UNR = CL ? 8 : ((sizeof(T) <= 4) ? 32 : (sizeof(T) <= 8 ? 16 : 8));
     const int G = gridDim.x, b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int r0 = b * p.rows_per_cta;
     const int r1 = min(p.M, r0 + p.rows_per_cta);
@@ -415,7 +418,9 @@ template <class T, bool SMEM, bool CL = false, int NT = kPanelThreads> __global_
     __shared__ int s_gid, s_gcol;
     extern __shared__ __align__(16) unsigned char s_dyn[];
     T *sP = reinterpret_cast<T *>(s_dyn);
-    const int ldp = p.rows_per_cta;
+    // cluster panels read rows across columns (lanes over columns): an odd
+    // leading dimension keeps those loads free of bank conflicts
+    const int ldp = CL ? (p.rows_per_cta | 1) : p.rows_per_cta;
     auto at = [&](int r, int c) -> T & {
         if (SMEM) return sP[(size_t)c * ldp + (r - r0)];
         return A[r + (size_t)c * lda];
@@ -627,12 +632,22 @@ template <class T, bool SMEM, bool CL = false, int NT = kPanelThreads> __global_
                     // over all warps but the last (whose last thread forms
                     // the scalars meanwhile); row factors from s_cvr
                     constexpr int NA = NT - 32;
-                    const int rs2 = max(r0, j - 1), nr = r1 - rs2, nc = p.N - j;
-                    if (tid < NA)
-                        for (int e = tid; e < nr * nc; e += NA) {
-                            const int r = rs2 + e % nr, c = j + e / nr;
+                    const int rs2 = max(r0, j - 1), nr = r1 - rs2;
+                    if (tid < NA && nr > 0) {
+                        // pair e = (row rs2 + e % nr, column j + e / nr), stepped
+                        // by NA with a carry instead of a division per pair
+                        const int dq = NA / nr, dr = NA % nr;
+                        int r = rs2 + tid % nr, c = j + tid / nr;
+                        while (c < p.N) {
                             at(r, c) = fmac(s_cvr[r - r0], s_cv[c], at(r, c));
+                            r += dr;
+                            c += dq;
+                            if (r >= r1) {
+                                r -= nr;
+                                ++c;
+                            }
                         }
+                    }
                 } else {
                     const T ctau = Tr<T>::conj(prev.tau);
                     for (int r = max(r0, j - 1) + tid; r < r1; r += NT) {
@@ -1187,28 +1202,44 @@ __global__ void __launch_bounds__(kBuildTThreads) k_build_t(const T *P, size_t p
         }
     }
     __syncthreads();
-    // the recurrence in one warp
-    if (tid >= kPanelMaxCols) return;
+    // the recurrence: each step's products T(r, l) G(l, i) split over the
+    // first kBuildTWarps warps by l (a warp issues an FP64 instruction only
+    // every 64 cycles), the partials summed by warp 0
+    __shared__ T sP4[kBuildTWarps][kPanelMaxCols];
+    const int w = tid / kPanelMaxCols, r = tid % kPanelMaxCols;
+    constexpr int kChunk = kPanelMaxCols / kBuildTWarps;
     for (int i = 0; i < k; ++i) {
-        T ti = tau[i0 + i];
-        if (tid < i) {
+        if (w < kBuildTWarps) {
             T acc = T(0);
-            for (int l = tid; l < i; ++l) acc = fmac(sT[tid][l], sG[l][i], acc);
-            sT[tid][i] = (ti == T(0)) ? T(0) : (-ti) * acc;
+            const int l0 = max(r, w * kChunk), l1 = min(i, (w + 1) * kChunk);
+            for (int l = l0; l < l1; ++l) acc = fmac(sT[r][l], sG[l][i], acc);
+            sP4[w][r] = acc;
         }
-        if (tid == 0) sT[i][i] = ti;
-        __syncwarp();
+        __syncthreads();
+        if (tid < kPanelMaxCols) {
+            const T ti = tau[i0 + i];
+            if (r < i) {
+                T acc = sP4[0][r];
+#pragma unroll
+                for (int q = 1; q < kBuildTWarps; ++q) acc = acc + sP4[q][r];
+                sT[r][i] = (ti == T(0)) ? T(0) : (-ti) * acc;
+            }
+            if (r == 0) sT[i][i] = ti;
+        }
+        __syncthreads();
     }
     T *To = Tout + (size_t)blk * tstride;
-    for (int c = 0; c < k; ++c)
-        if (tid <= c) To[tid + (size_t)c * ldt] = sT[tid][c];
+    if (tid < kPanelMaxCols)
+        for (int c = 0; c < k; ++c)
+            if (tid <= c) To[tid + (size_t)c * ldt] = sT[tid][c];
 }
 
 // Y = T * V1^H (k x k) with V1 the unit lower triangular top of V (stored at
-// v with leading dimension ldv).  One block of kPanelMaxCols^2 threads.
+// v with leading dimension ldv).  k blocks of kPanelMaxCols threads.
 template <class T>
-__global__ void __launch_bounds__(1024) k_t_v1h(const T *Tm, int ldt, const T *v, size_t ldv, int k, T *Y, int ldy) {
-    const int r = threadIdx.x % kPanelMaxCols, c = threadIdx.x / kPanelMaxCols;
+__global__ void __launch_bounds__(kPanelMaxCols) k_t_v1h(const T *Tm, int ldt, const T *v, size_t ldv, int k, T *Y, int ldy) {
+    // one warp per column of Y: the FP64 chains spread over k SMs
+    const int r = threadIdx.x, c = blockIdx.x;
     if (r >= k || c >= k) return;
     // Y(r,c) = sum_l T(r,l) * conj(V1(c,l)),  T(r,l)=0 for l<r, V1(c,l)=0 for l>c, V1(c,c)=1
     T acc = T(0);

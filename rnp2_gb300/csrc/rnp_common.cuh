@@ -133,6 +133,14 @@ struct NormAcc {
     double sml, med, big;
     __device__ __forceinline__ void zero() { sml = 0.0; med = 0.0; big = 0.0; }
     __device__ __forceinline__ void add(double v) {
+        // 2^-511 <= |v| < 2^486 (the medium range, all but extreme data),
+        // told from the exponent bits on the integer pipe: one FP64
+        // instruction for the common case, the same accumulator as below
+        const int e = (__double2hiint(v) >> 20) & 0x7ff;
+        if (e >= 1023 - 511 && e < 1023 + 486) {
+            med = fma(v, v, med);
+            return;
+        }
         const double tsml = 0x1p-511, tbig = 0x1p486, ssml = 0x1p537, sbig = 0x1p-538;
         double a = fabs(v);
         if (a > tbig) {
@@ -151,7 +159,14 @@ struct NormAcc {
     }
     template <class R> __device__ __forceinline__ void add(cplx<R> v) { add(v.x); add(v.y); }
     __device__ __forceinline__ void merge(const NormAcc &o) { sml += o.sml; med += o.med; big += o.big; }
-    __device__ __forceinline__ void warp_reduce() { sml = warp_sum(sml); med = warp_sum(med); big = warp_sum(big); }
+    // the extreme-range accumulators only when some lane holds one
+    __device__ __forceinline__ void warp_reduce() {
+        if (__any_sync(0xffffffffu, sml != 0.0 || big != 0.0)) {
+            sml = warp_sum(sml);
+            big = warp_sum(big);
+        }
+        med = warp_sum(med);
+    }
     __device__ double result() const { return result_scaled(1.0); }
     // mult * ||x|| for a power-of-two mult, without rounding through the
     // subnormal range when ||x|| itself is subnormal
