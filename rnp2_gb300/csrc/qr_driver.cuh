@@ -318,7 +318,6 @@ template <class T> struct BlockWs {
     T *P;
     T *W;
     int smax;
-    size_t p_bytes;  // bytes at P
 };
 
 template <class T> int apply_block(bool left, bool notran, int M, int N, int ib, const T *V, size_t ldv, const T *Tm, int ldt, T *C, size_t ldc, const BlockWs<T> &ws, cudaStream_t st) {
@@ -497,7 +496,6 @@ template <class T> BlockWs<T> carve_block(Carver &cv, int rows_w, int smax) {
     w.P = cv.take<T>((size_t)smax * rows_w * kPanelMaxCols);
     w.W = cv.take<T>((size_t)rows_w * kPanelMaxCols);
     w.smax = smax;
-    w.p_bytes = (size_t)smax * rows_w * kPanelMaxCols * sizeof(T);
     return w;
 }
 // split-K slots of the W partials: up to one per SM (the tensor-core W
@@ -511,8 +509,6 @@ template <class T> size_t t_bytes() { return ((size_t)kPanelMaxCols * kPanelMaxC
 // Factor (geqrf): RNP/LA/QR.hpp:129-197
 // ---------------------------------------------------------------------------
 template <class T> int geqr2(size_t m, size_t n, T *a, size_t lda, T *tau, T *work);
-template <class T> size_t thin_ws_bytes(size_t n);
-template <class T> int multq_thin(bool notran, size_t m, size_t n, size_t k, const T *a, size_t lda, const T *Tf, T *c, size_t ldc, void *ws, cudaStream_t st);
 
 }  // namespace rnpgpu
 #include "wide_f32.cuh"
@@ -672,12 +668,6 @@ template <class T> int geqrf(size_t m, size_t n, T *a, size_t lda, T *tau, size_
     if constexpr (std::is_same<T, float>::value) {
         wide_mode = !ahead && cqr != nullptr && cqr->use_wide && Tstore != nullptr && wide::usable(m, n, a, lda);
     }
-    // within a 128-column block the panels are brought up to date left-
-    // looking: before panel p its own 32 columns take the block's p earlier
-    // reflector blocks in one thin MultQ launch (rows from the block's top),
-    // instead of right-looking rank-32 passes over the rest of the block
-    // after every panel
-    const bool left_looking = wide_mode && thin_ws_bytes<T>((size_t)nb) <= (size_t)bw.p_bytes;
     bool big_pending = false;
     for (size_t i = 0; i < k; i += nb) {
         const int ib = (int)std::min(nb, k - i);
@@ -685,13 +675,6 @@ template <class T> int geqrf(size_t m, size_t n, T *a, size_t lda, T *tau, size_
         T *Tb = Tstore ? Tstore + (i / nb) * kPanelMaxCols * kPanelMaxCols : Tm[(i / nb) & 1];
         int rc;
         if constexpr (std::is_same<T, float>::value) {
-            if (left_looking) {
-                const size_t j0 = i / wide::kNb * wide::kNb;
-                if (i > j0) {
-                    rc = multq_thin<T>(false, m - j0, (size_t)ib, i - j0, a + j0 + j0 * lda, lda, Tstore + (j0 / nb) * kPanelMaxCols * kPanelMaxCols, a + j0 + i * lda, lda, bw.P, st);
-                    if (rc) return rc;
-                }
-            }
             if (cqr != nullptr && cqr_grid((int)(m - i), ib) > 0)
                 rc = panel_factor_cqr((int)(m - i), ib, Ai, lda, tau + i, Tb, kPanelMaxCols, pw, *cqr, st);
             else
@@ -705,7 +688,7 @@ template <class T> int geqrf(size_t m, size_t n, T *a, size_t lda, T *tau, size_
         if constexpr (std::is_same<T, float>::value) {
             if (wide_mode) {
                 const size_t j0 = i / wide::kNb * wide::kNb, jend = std::min(j0 + wide::kNb, n);
-                if (c1 < jend && !left_looking) {
+                if (c1 < jend) {
                     // the rest of the block: rank-32 passes (a one-launch thin
                     // MultQ per 64 columns measured 86-92 us a launch at 65536
                     // rows against 51 us for these three launches)
