@@ -32,7 +32,7 @@ template <class T, int NB, int MR, int TILE> struct BatchSmem {
     static constexpr size_t kP = (size_t)MR * NB;    // panel
     static constexpr size_t kC = (size_t)MR * TILE;  // trailing tile
     static constexpr size_t kW = (size_t)TILE * NB;
-    static constexpr size_t kBytes = (kP + kC + kW + NB * NB + 2 * NB) * sizeof(T);
+    static constexpr size_t kBytes = (kP + kC + kW + NB * NB + 2 * NB + MR) * sizeof(T);
 };
 
 template <class T, int NT, int NB, int MR, int TILE>
@@ -45,7 +45,9 @@ __global__ void __launch_bounds__(NT) k_geqrf_batched(const BatchDesc *__restric
     T *sW = sC + L::kC;                    // W (TILE x NB), ld TILE
     T *sT = sW + L::kW;                    // T (NB x NB), ld NB
     T *sG = sT + NB * NB;                  // w / Gram column (NB)
+    T *sCv = sG + 2 * NB;                  // -conj(tau) v of the current reflector (MR)
     __shared__ NormAcc s_nacc[NT / 32];
+    __shared__ T s_wp[NT / 32][NB];        // per-warp partials of w / Gram
     __shared__ ReflScalars<T> s_refl;
     __shared__ int s_idx;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -89,25 +91,53 @@ __global__ void __launch_bounds__(NT) k_geqrf_batched(const BatchDesc *__restric
                 if (!rs.identity)
                     for (int r = jj + 1 + tid; r < mp; r += NT) col[r] = scale_x(col[r], rs);
                 __syncthreads();
-                // w_c = v^H P[:,c] (c > jj) and Gram g_c = V[:,c]^H v (c < jj), rows >= jj
-                for (int c = warp; c < jb; c += NW) {
-                    if (c == jj) continue;
-                    const T *pc = sP + c * MR;
+                // the update's row factors -conj(tau) v_r, once per row
+                if (!rs.identity && jj + 1 < jb) {
+                    const T mct = -Tr<T>::conj(rs.tau);
+                    for (int r = jj + tid; r < mp; r += NT) sCv[r] = (r == jj) ? mct : mct * col[r];
+                }
+                // w_c = v^H P[:,c] (c > jj) and Gram g_c = V[:,c]^H v (c < jj),
+                // rows >= jj.  FP64 instructions cost the same for one lane as
+                // for 32 on this GPU: lane = (column lane % NB, row group
+                // lane / NB), the warps and row groups split the rows, the row
+                // groups meet by log2(32 / NB) shuffles and the warps in
+                // shared memory (no 32-lane reduction per column)
+                {
+                    constexpr int SUB = 32 / NB;
+                    const int c = lane % NB, sg = lane / NB;
                     T s = T(0);
-                    for (int r = jj + lane; r < mp; r += 32) {
-                        const T v = (r == jj) ? T(1) : col[r];
-                        s = (c > jj) ? fmac(Tr<T>::conj(v), pc[r], s) : fmac(Tr<T>::conj(pc[r]), v, s);
+                    if (c < jb && c != jj) {
+                        const T *pc = sP + c * MR;
+                        for (int r = jj + sg + SUB * warp; r < mp; r += SUB * NW) {
+                            const T v = (r == jj) ? T(1) : col[r];
+                            s = (c > jj) ? fmac(Tr<T>::conj(v), pc[r], s) : fmac(Tr<T>::conj(pc[r]), v, s);
+                        }
                     }
-                    s = warp_sum(s);
-                    if (lane == 0) sG[c] = s;
+#pragma unroll
+                    for (int o = NB; o < 32; o <<= 1) s = s + shfl_xor_t(s, o);
+                    if (sg == 0) s_wp[warp][c] = s;
+                }
+                __syncthreads();
+                if (tid < jb && tid != jj) {
+                    T s = s_wp[0][tid];
+#pragma unroll
+                    for (int w = 1; w < NW; ++w) s = s + s_wp[w][tid];
+                    sG[tid] = s;
                 }
                 __syncthreads();
                 if (!rs.identity && jj + 1 < jb) {
-                    const T ctau = Tr<T>::conj(rs.tau);
-                    for (int e = tid; e < (mp - jj) * (jb - jj - 1); e += NT) {
-                        const int r = jj + e % (mp - jj), c = jj + 1 + e / (mp - jj);
-                        const T v = (r == jj) ? T(1) : col[r];
-                        sP[c * MR + r] = fmac(-(ctau * v), sG[c], sP[c * MR + r]);
+                    // (row, column) pairs stepped with a carry (no division per pair)
+                    const int nr = mp - jj;
+                    const int dq = NT / nr, dr = NT % nr;
+                    int r = jj + tid % nr, c = jj + 1 + tid / nr;
+                    while (c < jb) {
+                        sP[c * MR + r] = fmac(sCv[r], sG[c], sP[c * MR + r]);
+                        r += dr;
+                        c += dq;
+                        if (r >= mp) {
+                            r -= nr;
+                            ++c;
+                        }
                     }
                 }
                 // T(0:jj, jj) = -tau T(0:jj, 0:jj) g(0:jj), T(jj, jj) = tau
