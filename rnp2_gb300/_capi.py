@@ -58,7 +58,7 @@ def _signatures():
         sig["rnpgpu_%sunmtr" % p] = [CH, CH, CH, SZ, SZ, P, SZ, P, P, SZ, PSZ, P]
     for p in "cz":
         sig["rnpgpu_%sgg_triangularize_b" % p] = [SZ, SZ, SZ, P, SZ, P, SZ, P, SZ, P, SZ, PSZ, P]
-    for name in ("rnpgpu_dsgels", "rnpgpu_zcgels"):
+    for name in ("rnpgpu_dsgels", "rnpgpu_zcgels", "rnpgpu_dsgels_host"):
         sig[name] = [SZ, SZ, SZ, P, SZ, P, SZ, P, SZ, C.c_int, C.c_int, C.POINTER(RefineInfo), PSZ, P]
     sig["rnpgpu_srandom_matrix"] = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, P, SZ, SZ, P, SZ, C.POINTER(C.c_int), PSZ, P]
     sig["rnpgpu_drandom_matrix"] = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, P, SZ, SZ, P, SZ, C.POINTER(C.c_int), PSZ, P]

@@ -66,7 +66,7 @@ template <class T> int launch_batched_warp(const BatchDesc *desc, int count, T *
 template <class T> size_t batched_smem(int cls, BatchConfig cfg) {
     if (cfg.threads == 32) return (size_t)kWarpsPerBlock * kWarpRows * kWarpLd * sizeof(T);
     const int mr = kClassMR[cls], tile = mr >= 512 ? 16 : 32;
-    return ((size_t)mr * cfg.nb + (size_t)mr * tile + (size_t)tile * cfg.nb + (size_t)cfg.nb * cfg.nb + 2 * (size_t)cfg.nb) * sizeof(T);
+    return ((size_t)mr * cfg.nb + (size_t)mr * tile + (size_t)tile * cfg.nb + (size_t)cfg.nb * cfg.nb + 2 * (size_t)cfg.nb + (size_t)mr) * sizeof(T);
 }
 inline bool fits_smem(size_t bytes) {
     static int optin = 0;

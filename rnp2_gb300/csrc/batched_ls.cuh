@@ -166,7 +166,10 @@ template <class TH, class TL, int MT> __device__ void ls_problem(const LsBatchAr
         }
     };
 
-    if (!q.refine) {
+    // a batch in one precision only ever takes the plain solve, and the
+    // refinement is compiled for mixed precisions only (the plain kernels
+    // keep their registers for the solve)
+    if (std::is_same<TH, TL>::value || !q.refine) {
         // plain: x = R^{-1} (Q^H b)(0:n) in the working precision
 #pragma unroll
         for (int t = 0; t < MT; ++t) {
@@ -184,6 +187,7 @@ template <class TH, class TL, int MT> __device__ void ls_problem(const LsBatchAr
         return;
     }
 
+    if constexpr (!std::is_same<TH, TL>::value) {
     // ---- mixed refinement
     TH r[MT];
     double bn2 = 0.0;
@@ -201,6 +205,9 @@ template <class TH, class TL, int MT> __device__ void ls_problem(const LsBatchAr
     // sweep, not the load latency)
     auto residual = [&]() {
         double a2 = 0.0;
+        // the ||A||_F test once, not per element (FP64 compares share the
+        // slow FP64 pipe)
+        const bool first = an2 < 0.0;
 #pragma unroll
         for (int t = 0; t < MT; ++t) {
             const int i = lane + 32 * t;
@@ -214,36 +221,47 @@ template <class TH, class TL, int MT> __device__ void ls_problem(const LsBatchAr
                 const int i = lane + 32 * t;
                 const TH a = (i < m) ? aj[i] : TH(0);
                 r[t] = fmac(-a, xj, r[t]);
-                if (an2 < 0.0) a2 += abs2(a);
+                if (first) a2 += abs2(a);
             }
         }
-        if (an2 < 0.0) an2 = warp_sum(a2);
+        if (first) an2 = warp_sum(a2);
     };
     // g = A^H r (FP64) into y as TL (g kept in FP64 only for its norm)
     double gn2 = 0.0;
     auto normal_eq = [&]() {
-        gn2 = 0.0;
+        double g2 = 0.0;
 #pragma unroll
         for (int t = 0; t < MT; ++t) y[t] = TL(0);
+        // 16 columns at a time: every lane's partial dot products over its
+        // rows, then one butterfly over the warp (16 adds for 16 columns
+        // instead of a 32-lane reduction per column); lanes 2e and 2e+1 end
+        // with column 16 g + e, which lane (16 g + e) % 32 keeps in y
+        for (int g = 0; 16 * g < n; ++g) {
+            TH acc[16];
 #pragma unroll
-        for (int tj = 0; tj < MT; ++tj) {
-            if (32 * tj >= n) continue;
-            for (int jl = 0; jl < 32; ++jl) {
-                const int j = 32 * tj + jl;
-                if (j >= n) break;
-                const TH *aj = Ap + (size_t)j * lda;
+            for (int e = 0; e < 16; ++e) {
+                const int j = 16 * g + e;
                 TH s = TH(0);
+                if (j < n) {
+                    const TH *aj = Ap + (size_t)j * lda;
 #pragma unroll
-                for (int t = 0; t < MT; ++t) {
-                    const int i = lane + 32 * t;
-                    const TH a = (i < m) ? aj[i] : TH(0);
-                    s = fmac(Tr<TH>::conj(a), r[t], s);
+                    for (int t = 0; t < MT; ++t) {
+                        const int i = lane + 32 * t;
+                        const TH a = (i < m) ? aj[i] : TH(0);
+                        s = fmac(Tr<TH>::conj(a), r[t], s);
+                    }
                 }
-                s = warp_sum(s);
-                gn2 += abs2(s);
-                if (lane == jl) y[tj] = convert_scalar<TH, TL>(s);
+                acc[e] = s;
             }
+            const int e = warp_reduce16(acc, lane);
+            if ((lane & 1) == 0 && 16 * g + e < n) g2 += abs2(acc[0]);
+            const TL got = shfl(convert_scalar<TH, TL>(acc[0]), 2 * (lane & 15));
+            const bool mine = (lane >> 4) == (g & 1) && 16 * g + (lane & 15) < n;
+#pragma unroll
+            for (int t = 0; t < MT; ++t)
+                if (mine && t == (g >> 1)) y[t] = got;
         }
+        gn2 = warp_sum(g2);
     };
     const double eps = 0x1p-52;
     const double tol = 10.0 * (double)n * eps;
@@ -279,6 +297,8 @@ template <class TH, class TL, int MT> __device__ void ls_problem(const LsBatchAr
         mu = xn > 0.0 ? sqrt(t2) / xn : 0.0;
         const double den = an * (an * xn + sqrt(bn2));
         eta = den > 0.0 ? sqrt(gn2) / den : 0.0;
+        // a non-finite x or product never passes the test
+        if (!isfinite(xn + t2 + den + gn2)) mu = eta = nan("");
     };
 
     bool csne = false, checked = false;
@@ -318,6 +338,7 @@ template <class TH, class TL, int MT> __device__ void ls_problem(const LsBatchAr
         if (q.iters) q.iters[d.index] = it;
         if (q.berr) q.berr[d.index] = mu;
         if (q.eta) q.eta[d.index] = eta;
+    }
     }
 }
 

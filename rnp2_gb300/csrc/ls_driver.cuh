@@ -138,8 +138,20 @@ template <class TH, class TL> struct RefinePlan {
     }
 };
 
+// Host staging of A (gels_refine_host): A's device copy arrives in ranges of
+// kStageCols columns on a copy stream, ev_copy[c] recorded after range c.
+constexpr int kStageCols = 128;
+struct HostStage {
+    cudaStream_t prep;        // prepares each range once it has landed
+    const cudaEvent_t *ev_copy;
+    int nchunk;
+    cudaEvent_t ev_first;     // the first range prepared
+    cudaEvent_t ev_all;       // every range prepared
+};
+
 template <class TH, class TL>
-int gels_refine(size_t m, size_t n, size_t nrhs, const TH *a, size_t lda, const TH *b, size_t ldb, TH *x, size_t ldx, int max_iter, int flags, RefineInfo *info, size_t *lwork, TH *work) {
+int gels_refine(size_t m, size_t n, size_t nrhs, const TH *a, size_t lda, const TH *b, size_t ldb, TH *x, size_t ldx, int max_iter, int flags, RefineInfo *info, size_t *lwork, TH *work,
+                const HostStage *hs = nullptr) {
     if (lwork == nullptr) return -13;
     if (n > m) return -2;
     if (m == 0 || n == 0 || nrhs == 0) return kOk;
@@ -190,7 +202,23 @@ int gels_refine(size_t m, size_t n, size_t nrhs, const TH *a, size_t lda, const 
     // same pass writes the packed digits of A for the residual products)
     if constexpr (use_oz) {
         KScope ks("prepare_digits", st);
-        if ((rc = oz_prepare_a((int)m, (int)n, a, lda, ow, dn, Af, m, st))) return rc;
+        if (hs != nullptr) {
+            // A arrives range by range: each range is prepared on the staging
+            // stream once its copy has landed; the factor starts after the
+            // first range and waits for the rest before it updates columns
+            // past its first block
+            for (int c = 0; c < hs->nchunk; ++c) {
+                const int c0 = c * kStageCols, w = (int)std::min<size_t>(kStageCols, n - (size_t)c0);
+                RNPGPU_CHECK(cudaStreamWaitEvent(hs->prep, hs->ev_copy[c], 0));
+                if ((rc = oz_prepare_cols((int)m, (int)n, c0, w, a, lda, ow, dn, Af, m, hs->prep))) return rc;
+                if (c == 0) RNPGPU_CHECK(cudaEventRecord(hs->ev_first, hs->prep));
+            }
+            RNPGPU_CHECK(cudaEventRecord(hs->ev_all, hs->prep));
+            RNPGPU_CHECK(cudaStreamWaitEvent(st, hs->ev_first, 0));
+            if constexpr (std::is_same<TL, float>::value) cw.rest_ready = hs->ev_all;
+        } else {
+            if ((rc = oz_prepare_a((int)m, (int)n, a, lda, ow, dn, Af, m, st))) return rc;
+        }
     } else {
         k_convert<TH, TL><<<gmn, 256, 0, st>>>((int)m, (int)n, a, lda, Af, m);
         RNPGPU_CHECK_LAUNCH();
@@ -202,6 +230,9 @@ int gels_refine(size_t m, size_t n, size_t nrhs, const TH *a, size_t lda, const 
         // Householder panels
         RNPGPU_CHECK(cudaMemsetAsync(cw.fail, 0, sizeof(int), st));
         if ((rc = geqrf<TL>(m, n, Af, m, tauf, &lw, wq, Tf, &cw))) return rc < 0 ? -13 : rc;
+        // everything after (the flag, a refactorization, the residuals) reads
+        // all of A's preparation
+        if (hs != nullptr) RNPGPU_CHECK(cudaStreamWaitEvent(st, hs->ev_all, 0));
         int failed = 0;
         RNPGPU_CHECK(cudaMemcpyAsync(&failed, cw.fail, sizeof(int), cudaMemcpyDeviceToHost, st));
         RNPGPU_CHECK(cudaStreamSynchronize(st));
@@ -214,6 +245,7 @@ int gels_refine(size_t m, size_t n, size_t nrhs, const TH *a, size_t lda, const 
     } else {
         if ((rc = geqrf<TL>(m, n, Af, m, tauf, &lw, wq, Tf))) return rc < 0 ? -13 : rc;
     }
+    if (hs != nullptr) RNPGPU_CHECK(cudaStreamWaitEvent(st, hs->ev_all, 0));
 
     // ||A||_F (real FP64 data: from the FP32 working copy, which only scales
     // the stopping test) and ||b_j|| in FP64
@@ -245,6 +277,12 @@ int gels_refine(size_t m, size_t n, size_t nrhs, const TH *a, size_t lda, const 
         corr_out = 0.0;
         for (size_t j = 0; j < nrhs; ++j) {
             double xs = h[n + 2 * nrhs + j], ds = h[n + nrhs + j];
+            // a non-finite x or correction (Inf or NaN in A or b, or a
+            // broken-down factor) makes the size NaN, which ends the steps
+            if (!std::isfinite(xs) || !std::isfinite(ds)) {
+                corr_out = std::nan("");
+                return kOk;
+            }
             corr_out = std::max(corr_out, xs > 0.0 ? std::sqrt(ds / xs) : (ds > 0.0 ? HUGE_VAL : 0.0));
         }
         return kOk;
@@ -280,12 +318,18 @@ int gels_refine(size_t m, size_t n, size_t nrhs, const TH *a, size_t lda, const 
         RNPGPU_CHECK(cudaStreamSynchronize(st));
         eta = 0.0;
         mu = 0.0;
+        bool finite = std::isfinite(anorm);
         for (size_t j = 0; j < nrhs; ++j) {
             const double xn = std::sqrt(h[n + 2 * nrhs + j]);
             const double den = anorm * (anorm * xn + bn[j]);
-            eta = std::max(eta, den > 0.0 ? std::sqrt(h[n + 3 * nrhs + j]) / den : 0.0);
-            mu = std::max(mu, xn > 0.0 ? std::sqrt(h[n + 4 * nrhs + j]) / xn : 0.0);
+            const double gn = std::sqrt(h[n + 3 * nrhs + j]), yn = std::sqrt(h[n + 4 * nrhs + j]);
+            finite = finite && std::isfinite(xn) && std::isfinite(bn[j]) && std::isfinite(gn) && std::isfinite(yn);
+            eta = std::max(eta, den > 0.0 ? gn / den : 0.0);
+            mu = std::max(mu, xn > 0.0 ? yn / xn : 0.0);
         }
+        // non-finite data never passes the stopping test (std::max would
+        // drop a NaN)
+        if (!finite) eta = mu = std::nan("");
         return kOk;
     };
 
@@ -324,6 +368,12 @@ int gels_refine(size_t m, size_t n, size_t nrhs, const TH *a, size_t lda, const 
         }
         ++it;
         if ((rc = correction_size(corr))) return rc;
+        if (std::isnan(corr)) {
+            if ((rc = check())) return rc;
+            checked = true;
+            converged = 0;
+            break;
+        }
         // Q steps contract fast, so failing to halve means they have stalled;
         // CSNE steps contract more slowly and count as stalled only when the
         // correction no longer shrinks noticeably
@@ -362,6 +412,104 @@ int gels_refine(size_t m, size_t n, size_t nrhs, const TH *a, size_t lda, const 
         info->correction = corr;
         info->anorm = anorm;
     }
+    return kOk;
+}
+
+
+// ---------------------------------------------------------------------------
+// The mixed solve from host buffers (real FP64 data): A is copied to the
+// device in ranges of kStageCols columns on a copy stream while the ranges
+// already landed are prepared and the factor's first block runs; b, then the
+// solution x, travel on the caller's stream.  Pinned host buffers let the
+// copies run asynchronously (pageable ones still give the same result).
+// Workspace: A, b and x on the device, then gels_refine's.
+// ---------------------------------------------------------------------------
+struct StageCtx {
+    cudaStream_t copy = nullptr, prep = nullptr;
+    cudaEvent_t ev_start = nullptr, ev_first = nullptr, ev_all = nullptr;
+    std::vector<cudaEvent_t> ev_copy;
+};
+inline StageCtx *stage_ctx(int nchunk) {
+    constexpr int kMaxDev = 16;
+    static thread_local StageCtx ctx[kMaxDev];
+    static thread_local int state[kMaxDev] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDev) return nullptr;
+    StageCtx &c = ctx[dev];
+    if (state[dev] == 0) {
+        const bool ok = cudaStreamCreateWithFlags(&c.copy, cudaStreamNonBlocking) == cudaSuccess && cudaStreamCreateWithFlags(&c.prep, cudaStreamNonBlocking) == cudaSuccess &&
+                        cudaEventCreateWithFlags(&c.ev_start, cudaEventDisableTiming) == cudaSuccess &&
+                        cudaEventCreateWithFlags(&c.ev_first, cudaEventDisableTiming) == cudaSuccess && cudaEventCreateWithFlags(&c.ev_all, cudaEventDisableTiming) == cudaSuccess;
+        state[dev] = ok ? 1 : 2;
+        if (!ok) cudaGetLastError();
+    }
+    if (state[dev] != 1) return nullptr;
+    while ((int)c.ev_copy.size() < nchunk) {
+        cudaEvent_t e;
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        c.ev_copy.push_back(e);
+    }
+    return &c;
+}
+
+template <class TH, class TL>
+int gels_refine_host(size_t m, size_t n, size_t nrhs, const TH *a, size_t lda, const TH *b, size_t ldb, TH *x, size_t ldx, int max_iter, int flags, RefineInfo *info, size_t *lwork,
+                     TH *work) {
+    if (lwork == nullptr) return -13;
+    if (n > m) return -2;
+    if (m == 0 || n == 0 || nrhs == 0) return kOk;
+    if (lda < m) return -5;
+    if (ldb < m) return -7;
+    if (ldx < n) return -9;
+    if (m > (size_t)INT32_MAX || nrhs > (size_t)INT32_MAX) return -1;
+    auto al = [](size_t bytes) { return (bytes + 255) / 256 * 256; };
+    const size_t da = al(m * n * sizeof(TH)), db = al(m * nrhs * sizeof(TH)), dx = al(n * nrhs * sizeof(TH));
+    size_t inner = 0;
+    int rc = gels_refine<TH, TL>(m, n, nrhs, nullptr, m, nullptr, m, nullptr, n, max_iter, flags, nullptr, &inner, nullptr);
+    if (rc) return rc;
+    const size_t need = elems_for<TH>(da + db + dx) + inner;
+    if (work == nullptr || *lwork == 0) {
+        *lwork = need;
+        return kOk;
+    }
+    if (a == nullptr) return -4;
+    if (b == nullptr) return -6;
+    if (x == nullptr) return -8;
+    if (*lwork < need) return -13;
+    const int nchunk = (int)((n + kStageCols - 1) / kStageCols);
+    StageCtx *sc = stage_ctx(nchunk);
+    if (sc == nullptr) return kErrCuda;
+    cudaStream_t st = current_stream();
+    Carver cv(work);
+    TH *dA = cv.take<TH>(da / sizeof(TH));
+    TH *dB = cv.take<TH>(db / sizeof(TH));
+    TH *dX = cv.take<TH>(dx / sizeof(TH));
+    TH *wrest = cv.take<TH>(0);
+    size_t lw = *lwork - (size_t)(wrest - work);
+    // the staging streams start after the caller's earlier work on this
+    // workspace
+    RNPGPU_CHECK(cudaEventRecord(sc->ev_start, st));
+    RNPGPU_CHECK(cudaStreamWaitEvent(sc->copy, sc->ev_start, 0));
+    RNPGPU_CHECK(cudaStreamWaitEvent(sc->prep, sc->ev_start, 0));
+    RNPGPU_CHECK(cudaMemcpy2DAsync(dB, m * sizeof(TH), b, ldb * sizeof(TH), m * sizeof(TH), nrhs, cudaMemcpyHostToDevice, st));
+    for (int c = 0; c < nchunk; ++c) {
+        const size_t c0 = (size_t)c * kStageCols, w = std::min<size_t>(kStageCols, n - c0);
+        RNPGPU_CHECK(cudaMemcpy2DAsync(dA + c0 * m, m * sizeof(TH), a + c0 * lda, lda * sizeof(TH), m * sizeof(TH), w, cudaMemcpyHostToDevice, sc->copy));
+        RNPGPU_CHECK(cudaEventRecord(sc->ev_copy[c], sc->copy));
+    }
+    HostStage hs{sc->prep, sc->ev_copy.data(), nchunk, sc->ev_first, sc->ev_all};
+    rc = gels_refine<TH, TL>(m, n, nrhs, dA, m, dB, m, dX, n, max_iter, flags, info, &lw, wrest, &hs);
+    // the caller's stream also waits for every copy (a failed call may have
+    // returned before it waited for them)
+    RNPGPU_CHECK(cudaEventRecord(sc->ev_start, sc->copy));
+    RNPGPU_CHECK(cudaStreamWaitEvent(st, sc->ev_start, 0));
+    RNPGPU_CHECK(cudaEventRecord(sc->ev_start, sc->prep));
+    RNPGPU_CHECK(cudaStreamWaitEvent(st, sc->ev_start, 0));
+    if (rc) return rc;
+    RNPGPU_CHECK(cudaMemcpy2DAsync(x, ldx * sizeof(TH), dX, n * sizeof(TH), n * sizeof(TH), nrhs, cudaMemcpyDeviceToHost, st));
     return kOk;
 }
 

@@ -121,7 +121,9 @@ template <class T, bool CT> __global__ void __launch_bounds__(512) k_trsm_small(
     };
     for (int col = blockIdx.x; col < nrhs; col += gridDim.x) {
         T *y = B + (size_t)col * ldb;
-        for (int i = tid; i < n; i += blockDim.x) sy[i] = y[i];
+        // the unrolled updates read whole 32-entry blocks of sy: the entries
+        // past n are zeros (0 * stale shared memory could be NaN)
+        for (int i = tid; i < 32 * nblk; i += blockDim.x) sy[i] = (i < n) ? y[i] : T(0);
         load_diag(0, 0, tid, blockDim.x);
         __syncthreads();
         for (int s = 0; s < nblk; ++s) {

@@ -853,6 +853,26 @@ inline int oz_prepare_a(int m, int n, const double *A, size_t lda, const OzWork 
     return kOk;
 }
 
+// the same for columns [c0, c0 + w) only (c0 a multiple of 128; the last
+// range also writes the zero blocks that pad the packed digits to whole
+// 128-column groups): a matrix prepared range by range as it arrives
+inline int oz_prepare_cols(int m, int n, int c0, int w, const double *A, size_t lda, const OzWork &ow, double *sumsq, float *Af, size_t ldf, cudaStream_t st) {
+    if (w <= 0) return kOk;
+    oz::k_col_exp<0><<<(unsigned)std::min(w, 8192), 256, 0, st>>>(m, w, A + (size_t)c0 * lda, lda, ow.colexp + c0);
+    RNPGPU_CHECK_LAUNCH();
+    const int nbr = OzWork::nbr((size_t)m);
+    const int nbc = (c0 + w >= n) ? OzWork::nbc((size_t)n) - c0 / 16 : w / 16;
+    const dim3 grid((unsigned)std::min(nbr / 8, 65535), (unsigned)std::min(nbc, 65535));
+    oz::k_adigits<0><<<grid, 256, 0, st>>>(m, w, nbr, nbc, A + (size_t)c0 * lda, lda, ow.colexp + c0, ow.Ad + (size_t)(c0 / 16) * nbr * oz::kBlock,
+                                           Af ? Af + (size_t)c0 * ldf : nullptr, ldf);
+    RNPGPU_CHECK_LAUNCH();
+    if (sumsq && Af) {
+        oz::k_col_sumsq_f32<0><<<(unsigned)std::min(w, 8192), 256, 0, st>>>(m, w, Af + (size_t)c0 * ldf, ldf, sumsq + c0);
+        RNPGPU_CHECK_LAUNCH();
+    }
+    return kOk;
+}
+
 // r = b - A x (m x nrhs), FP64-accurate, A prepared by oz_prepare_a
 inline int oz_residual(int m, int n, int nrhs, const OzWork &w, const double *x, size_t ldx, const double *b, size_t ldb, double *r, size_t ldr, cudaStream_t st) {
     if (int rc = oz_attr()) return rc;

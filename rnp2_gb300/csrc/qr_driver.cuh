@@ -524,6 +524,10 @@ struct CqrWs {
     int *fail = nullptr;
     wide::WideWs wide;
     bool use_wide = false;
+    // when set, the matrix right of the first 128 columns may still be
+    // arriving (host staging): the factor waits for this event before its
+    // first update of those columns
+    cudaEvent_t rest_ready = nullptr;
 };
 inline size_t cqr_ws_bytes() {
     const auto r = [](size_t b) { return (b + 255) / 256 * 256; };
@@ -669,6 +673,15 @@ template <class T> int geqrf(size_t m, size_t n, T *a, size_t lda, T *tau, size_
         wide_mode = !ahead && cqr != nullptr && cqr->use_wide && Tstore != nullptr && wide::usable(m, n, a, lda);
     }
     bool big_pending = false;
+    bool rest_waited = cqr == nullptr || cqr->rest_ready == nullptr;
+    auto wait_rest = [&]() -> int {
+        if (!rest_waited) {
+            RNPGPU_CHECK(cudaStreamWaitEvent(st, cqr->rest_ready, 0));
+            if (la) RNPGPU_CHECK(cudaStreamWaitEvent(la->side, cqr->rest_ready, 0));
+            rest_waited = true;
+        }
+        return kOk;
+    };
     for (size_t i = 0; i < k; i += nb) {
         const int ib = (int)std::min(nb, k - i);
         T *Ai = a + i + i * lda;
@@ -697,6 +710,7 @@ template <class T> int geqrf(size_t m, size_t n, T *a, size_t lda, T *tau, size_
                 }
                 const bool block_done = (c1 == j0 + wide::kNb) || (c1 == k);
                 if (block_done && jend < n) {
+                    if ((rc = wait_rest())) return rc;
                     if (c1 == j0 + wide::kNb && m - j0 >= 128) {
                         rc = wide::apply(a, lda, (int)m, (int)n, (int)j0, Tstore + (j0 / nb) * kPanelMaxCols * kPanelMaxCols, (size_t)kPanelMaxCols * kPanelMaxCols, cqr->wide, st);
                         if (rc) return rc;
@@ -712,6 +726,7 @@ template <class T> int geqrf(size_t m, size_t n, T *a, size_t lda, T *tau, size_
                 continue;
             }
         }
+        if ((rc = wait_rest())) return rc;
         if (!ahead) {
             rc = apply_block<T>(true, false, (int)(m - i), (int)(n - c1), ib, Ai, lda, Tb, kPanelMaxCols, a + i + c1 * lda, lda, bw, st);
             if (rc) return rc;

@@ -81,6 +81,42 @@ def gels_refine(A, B, X=None, max_iter=0, work=None, forward=False, rank32=False
     return X, info.as_dict()
 
 
+def _host_colmajor(t):
+    """(pointer, leading dimension) of a column-major CPU tensor (m, n)."""
+    if t.dim() != 2 or t.is_cuda:
+        raise ValueError("expected a 2-D CPU tensor")
+    m, n = t.shape
+    if m > 1 and t.stride(0) != 1:
+        raise ValueError("expected a column-major tensor (stride(0) == 1)")
+    return t.data_ptr(), max(t.stride(1) if n > 1 else m, 1)
+
+
+def host_refine_workspace(m, n, nrhs):
+    lw = C.c_size_t(0)
+    _check("gels_refine_host", lib().rnpgpu_dsgels_host(m, n, nrhs, None, max(m, 1), None, max(m, 1), None, max(n, 1), 0, 0, None, C.byref(lw), None))
+    return lw.value
+
+
+def gels_refine_host(A, B, X, max_iter=0, work=None, forward=False, rank32=False, device="cuda"):
+    """The mixed-precision solve of gels_refine from HOST (CPU, preferably
+    pinned) FP64 tensors A (m x n), B (m x nrhs) into the host tensor X
+    (n x nrhs), all column-major: A is copied in 128-column ranges that the
+    GPU starts on as they land.  X is complete once the current stream is
+    synchronized.  Returns info."""
+    m, n = A.shape
+    nrhs = B.shape[1]
+    a, lda = _host_colmajor(A)
+    b, ldb = _host_colmajor(B)
+    x, ldx = _host_colmajor(X)
+    _bind_stream()
+    if work is None:
+        work = torch.empty(max(host_refine_workspace(m, n, nrhs), 1), dtype=torch.float64, device=device)
+    info = RefineInfo()
+    lw = C.c_size_t(work.numel())
+    _check("gels_refine_host", lib().rnpgpu_dsgels_host(m, n, nrhs, a, lda, b, ldb, x, ldx, int(max_iter), (1 if forward else 0) | (2 if rank32 else 0), C.byref(info), C.byref(lw), work.data_ptr()))
+    return info.as_dict()
+
+
 def residual(A, X, B, R=None, normal=False, work=None):
     """R = B - A X (and G = A^T R when normal=True) for FP64 A (m x n), X
     (n x nrhs), B (m x nrhs), computed from exact fixed-point slices on the

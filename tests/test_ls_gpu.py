@@ -217,3 +217,56 @@ def test_mixed_fp32_factor_falls_back_to_householder_panels():
     assert info["backward_error"] <= 1e-9 and be <= 1e-9, (info, be)
     if info["converged"] == 1:
         assert be <= 10 * n * np.finfo(np.float64).eps
+
+
+@pytest.mark.parametrize("m,n,nrhs", [(4096, 300, 3), (2000, 130, 1), (1000, 100, 2), (8192, 512, 16)])
+def test_gels_refine_host_matches_device_solve(m, n, nrhs):
+    """rnpgpu_dsgels_host (host buffers, A staged in 128-column ranges while
+    the GPU starts on the ranges already landed) gives the device solve's
+    result bit for bit."""
+    from rnp2_gb300 import ls as gls
+    from rnp2_gb300.qr import to_colmajor
+
+    g = torch.Generator(device="cuda").manual_seed(m + n)
+    A = to_colmajor(torch.randn((m, n), generator=g, dtype=torch.float64, device="cuda"))
+    B = to_colmajor(torch.randn((m, nrhs), generator=g, dtype=torch.float64, device="cuda"))
+    X, info = gls.gels_refine(A, B)
+    A_h = torch.empty((n, m), dtype=torch.float64).pin_memory().t()
+    A_h.copy_(A)
+    B_h = torch.empty((nrhs, m), dtype=torch.float64).pin_memory().t()
+    B_h.copy_(B)
+    X_h = torch.full((nrhs, n), float("nan"), dtype=torch.float64).pin_memory().t()
+    info_h = gls.gels_refine_host(A_h, B_h, X_h)
+    torch.cuda.synchronize()
+    assert bool(torch.isfinite(X).all()) and info["converged"] == 1, info
+    assert torch.equal(X_h, X.cpu())
+    assert info_h["iterations"] == info["iterations"] and info_h["converged"] == info["converged"]
+
+
+@pytest.mark.parametrize("m,n", [(2000, 130), (3000, 130), (1500, 70), (4096, 97)])
+def test_refinement_with_partial_last_block(m, n):
+    """n not a multiple of 32: the corrected seminormal steps solve with R over
+    a partial last 32-row block (entries past n must not enter the update;
+    stale shared memory once turned them into NaN)."""
+    rng = np.random.default_rng(m + n)
+    A, b = rng.standard_normal((m, n)), rng.standard_normal((m, 2))
+    for forward in (False, True):
+        X, info = gls.gels_refine(to_dev(A), to_dev(b), forward=forward)
+        torch.cuda.synchronize()
+        assert bool(torch.isfinite(X).all()), (forward, info)
+        assert info["converged"] == 1, (forward, info)
+        assert ls_backward_error(A, b, X.cpu().numpy()) <= 10 * n * np.finfo(np.float64).eps
+
+
+def test_refinement_reports_nonfinite_data():
+    """A NaN in A never passes the stopping test: converged 0 and a NaN
+    backward error (the solve does not fault or loop)."""
+    m, n = 1000, 64
+    rng = np.random.default_rng(8)
+    A = rng.standard_normal((m, n))
+    A[17, 5] = np.nan
+    b = rng.standard_normal((m, 1))
+    X, info = gls.gels_refine(to_dev(A), to_dev(b))
+    torch.cuda.synchronize()
+    assert info["converged"] == 0, info
+    assert not np.isfinite(info["backward_error"]), info
