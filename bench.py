@@ -719,7 +719,6 @@ def gpu_arm(args, rank, world, local):
     b_h.copy_(b)
     x_h = torch.empty((NRHS, N), dtype=torch.float64).pin_memory().t()
     work_h = torch.empty(gls.host_refine_workspace(M, N, NRHS), dtype=torch.float64, device=dev)
-    del work
     for _ in range(max(1, args.warmup)):
         gls.gels_refine_host(A_h, b_h, x_h, work=work_h)
     barrier()

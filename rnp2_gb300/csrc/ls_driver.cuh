@@ -29,13 +29,15 @@ struct RefineInfo {
     double anorm;            // ||A||_F
 };
 
-template <class T> int trsm_upper(size_t n, size_t nrhs, const T *a, size_t lda, T *b, size_t ldb, cudaStream_t st) {
+// dinv (optional, n <= kTrsmSmallMax): the inverted diagonal blocks of R
+// (k_trinv_diag), formed once per factorization
+template <class T> int trsm_upper(size_t n, size_t nrhs, const T *a, size_t lda, T *b, size_t ldb, cudaStream_t st, const T *dinv = nullptr) {
     if (n == 0 || nrhs == 0) return kOk;
     KScope ks("trsm", st);
     bool small = false;
     if constexpr (sizeof(T) <= 8) {
         if (n <= (size_t)kTrsmSmallMax) {
-            k_trsm_small<T, false><<<(unsigned)std::min<size_t>(nrhs, 65535), 512, 0, st>>>((int)n, (int)nrhs, a, lda, b, ldb);
+            k_trsm_small<T, false><<<(unsigned)std::min<size_t>(nrhs, 65535), 512, 0, st>>>((int)n, (int)nrhs, a, lda, b, ldb, dinv);
             small = true;
         }
     }
@@ -44,13 +46,13 @@ template <class T> int trsm_upper(size_t n, size_t nrhs, const T *a, size_t lda,
     return kOk;
 }
 
-template <class T> int trsm_upper_ct(size_t n, size_t nrhs, const T *a, size_t lda, T *b, size_t ldb, cudaStream_t st) {
+template <class T> int trsm_upper_ct(size_t n, size_t nrhs, const T *a, size_t lda, T *b, size_t ldb, cudaStream_t st, const T *dinv = nullptr) {
     if (n == 0 || nrhs == 0) return kOk;
     KScope ks("trsm", st);
     bool small = false;
     if constexpr (sizeof(T) <= 8) {
         if (n <= (size_t)kTrsmSmallMax) {
-            k_trsm_small<T, true><<<(unsigned)std::min<size_t>(nrhs, 65535), 512, 0, st>>>((int)n, (int)nrhs, a, lda, b, ldb);
+            k_trsm_small<T, true><<<(unsigned)std::min<size_t>(nrhs, 65535), 512, 0, st>>>((int)n, (int)nrhs, a, lda, b, ldb, dinv);
             small = true;
         }
     }
@@ -113,7 +115,7 @@ template <class T> int gels(size_t m, size_t n, size_t nrhs, T *a, size_t lda, T
 // mixed precision least squares with iterative refinement
 // ---------------------------------------------------------------------------
 template <class TH, class TL> struct RefinePlan {
-    size_t af, tauf, ts, wq, r, rf, p, g, norms, ozw, cqrw, widew, total;
+    size_t af, tauf, ts, wq, r, rf, p, g, norms, ozw, cqrw, widew, t128, dinv, total;
     int split;
     // the FP64 products r = b - A x and A^T r on the tensor cores (exact
     // integer slices) for real FP64 data; other types use FP64 FMA
@@ -134,7 +136,12 @@ template <class TH, class TL> struct RefinePlan {
         ozw = kOz ? OzWork::bytes(m, n, nrhs) : 0;
         cqrw = std::is_same<TL, float>::value ? cqr_ws_bytes() : 0;
         widew = (std::is_same<TL, float>::value && wide::usable(m, n, reinterpret_cast<const float *>(256), m)) ? wide::ws_bytes(m, n) : 0;
-        total = af + tauf + ts + wq + r + rf + p + g + norms + ozw + cqrw + widew;
+        // the wide blocks' T factors, kept for the Q^T r steps
+        t128 = widew > 0 ? al((n / wide::kNb) * wide::kNb * wide::kNb * sizeof(float)) : 0;
+        if (widew > 0 && nrhs <= (size_t)kQtcMaxCols) wq = std::max(wq, al(qtc_ws_bytes(nrhs) + 256));
+        // the inverted 32 x 32 diagonal blocks of R for the small triangular solves
+        dinv = (sizeof(TL) <= 8 && n <= (size_t)kTrsmSmallMax) ? al((n + 31) / 32 * 1024 * sizeof(TL)) : 0;
+        total = af + tauf + ts + wq + r + rf + p + g + norms + ozw + cqrw + widew + t128 + dinv;
     }
 };
 
@@ -190,7 +197,9 @@ int gels_refine(size_t m, size_t n, size_t nrhs, const TH *a, size_t lda, const 
     if (plan.widew > 0) {
         cw.wide = wide::carve(cv, m, n);
         cw.use_wide = (flags & 2) == 0;  // flag 2: rank-32 trailing updates only
+        if (plan.t128 > 0) cw.t128 = cv.take<float>(plan.t128 / sizeof(float));
     }
+    TL *dinv = plan.dinv > 0 ? cv.take<TL>(plan.dinv / sizeof(TL)) : nullptr;
     const size_t lwq = plan.wq / sizeof(TL);
     const dim3 gmn((unsigned)std::min<size_t>((m + 255) / 256, 2048), (unsigned)std::min<size_t>(n, 65535));
     const dim3 gmr((unsigned)std::min<size_t>((m + 255) / 256, 2048), (unsigned)std::min<size_t>(nrhs, 65535));
@@ -237,6 +246,7 @@ int gels_refine(size_t m, size_t n, size_t nrhs, const TH *a, size_t lda, const 
         RNPGPU_CHECK(cudaMemcpyAsync(&failed, cw.fail, sizeof(int), cudaMemcpyDeviceToHost, st));
         RNPGPU_CHECK(cudaStreamSynchronize(st));
         if (failed) {
+            cw.nwide = 0;  // the Householder refactorization keeps no wide T's
             k_convert<TH, TL><<<gmn, 256, 0, st>>>((int)m, (int)n, a, lda, Af, m);
             RNPGPU_CHECK_LAUNCH();
             lw = lwq;
@@ -246,6 +256,10 @@ int gels_refine(size_t m, size_t n, size_t nrhs, const TH *a, size_t lda, const 
         if ((rc = geqrf<TL>(m, n, Af, m, tauf, &lw, wq, Tf))) return rc < 0 ? -13 : rc;
     }
     if (hs != nullptr) RNPGPU_CHECK(cudaStreamWaitEvent(st, hs->ev_all, 0));
+    if (dinv) {
+        k_trinv_diag<TL><<<(unsigned)((n + 31) / 32), 32, 0, st>>>((int)n, Af, m, dinv);
+        RNPGPU_CHECK_LAUNCH();
+    }
 
     // ||A||_F (real FP64 data: from the FP32 working copy, which only scales
     // the stopping test) and ||b_j|| in FP64
@@ -311,7 +325,7 @@ int gels_refine(size_t m, size_t n, size_t nrhs, const TH *a, size_t lda, const 
         RNPGPU_CHECK_LAUNCH();
         k_convert<TH, TL><<<gnr, 256, 0, st>>>((int)n, (int)nrhs, g, n, gf, n);
         RNPGPU_CHECK_LAUNCH();
-        if ((rc2 = trsm_upper_ct<TL>(n, nrhs, Af, m, gf, n, st))) return rc2;
+        if ((rc2 = trsm_upper_ct<TL>(n, nrhs, Af, m, gf, n, st, dinv))) return rc2;
         k_col_sumsq<TL><<<(unsigned)std::min<size_t>(nrhs, 4096), 256, 0, st>>>((int)n, (int)nrhs, gf, n, dn + n + 4 * nrhs);
         RNPGPU_CHECK_LAUNCH();
         RNPGPU_CHECK(cudaMemcpyAsync(h.data() + n + 3 * nrhs, dn + n + 3 * nrhs, 2 * nrhs * sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -345,11 +359,20 @@ int gels_refine(size_t m, size_t n, size_t nrhs, const TH *a, size_t lda, const 
             k_convert<TH, TL><<<gmr, 256, 0, st>>>((int)m, (int)nrhs, r, m, rf, m);
             RNPGPU_CHECK_LAUNCH();
             lw = lwq;
-            if ((rc = unmqr<TL>("L", "C", m, nrhs, n, Af, m, tauf, rf, m, &lw, wq, Tf))) return rc < 0 ? -13 : rc;
-            if ((rc = trsm_upper<TL>(n, nrhs, Af, m, rf, m, st))) return rc;
+            bool done = false;
+            if constexpr (std::is_same<TL, float>::value) {
+                // Q^T r with the wide blocks' T's: 2 grid barriers per
+                // 128-column block instead of per 32-column panel
+                if (qtc_usable(m, nrhs, n, Af, m, cw.nwide) && lwq * sizeof(TL) >= qtc_ws_bytes(nrhs)) {
+                    if ((rc = qtc_blocks(m, nrhs, n, Af, m, Tf, cw.t128, cw.nwide, rf, m, wq, st))) return rc;
+                    done = true;
+                }
+            }
+            if (!done && (rc = unmqr<TL>("L", "C", m, nrhs, n, Af, m, tauf, rf, m, &lw, wq, Tf))) return rc < 0 ? -13 : rc;
+            if ((rc = trsm_upper<TL>(n, nrhs, Af, m, rf, m, st, dinv))) return rc;
         } else {
             // gf already holds R^{-H} A^H r from the last check
-            if ((rc = trsm_upper<TL>(n, nrhs, Af, m, gf, n, st))) return rc;
+            if ((rc = trsm_upper<TL>(n, nrhs, Af, m, gf, n, st, dinv))) return rc;
         }
         const size_t ldd = csne ? n : m;
         k_add_correction<TL, TH><<<gnr, 256, 0, st>>>((int)n, (int)nrhs, rf, ldd, x, ldx);

@@ -104,9 +104,11 @@ template <class T> __global__ void __launch_bounds__(512) k_trsm_upper_ct(int n,
 // is loaded by warps 1..15 while warp 0 solves the current one (two buffers),
 // the reciprocals of the diagonal are formed by all lanes at once, and every
 // thread loads the 32 coefficients of its row's update before the barrier
-// that waits for the block solve.
+// that waits for the block solve.  With Dinv (the inverses of R's 32 x 32
+// diagonal blocks, k_trinv_diag) the block solve is one product by the
+// block's inverse (32 independent sums instead of a 32-step chain).
 constexpr int kTrsmSmallMax = 512;
-template <class T, bool CT> __global__ void __launch_bounds__(512) k_trsm_small(int n, int nrhs, const T *R, size_t ldr, T *B, size_t ldb) {
+template <class T, bool CT> __global__ void __launch_bounds__(512) k_trsm_small(int n, int nrhs, const T *R, size_t ldr, T *B, size_t ldb, const T *Dinv) {
     __shared__ T sy[kTrsmSmallMax];
     __shared__ T sD[2][32][33];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -114,9 +116,10 @@ template <class T, bool CT> __global__ void __launch_bounds__(512) k_trsm_small(
     auto first_row = [&](int s) { return 32 * (CT ? s : nblk - 1 - s); };
     auto load_diag = [&](int s, int buf, int t0, int nt) {
         const int i0 = first_row(s), nbk = min(32, n - i0);
+        const T *D = Dinv ? Dinv + (size_t)(i0 / 32) * 1024 : nullptr;
         for (int idx = t0; idx < 32 * 32; idx += nt) {
             const int r = idx & 31, c = idx >> 5;
-            sD[buf][r][c] = (r < nbk && c < nbk && r <= c) ? R[(i0 + r) + (size_t)(i0 + c) * ldr] : T(0);
+            sD[buf][r][c] = (r < nbk && c < nbk && r <= c) ? (D ? D[r + 32 * c] : R[(i0 + r) + (size_t)(i0 + c) * ldr]) : T(0);
         }
     };
     for (int col = blockIdx.x; col < nrhs; col += gridDim.x) {
@@ -135,7 +138,14 @@ template <class T, bool CT> __global__ void __launch_bounds__(512) k_trsm_small(
 #pragma unroll
                 for (int c = 0; c < 32; ++c) coef[c] = (c < nbk) ? (CT ? Tr<T>::conj(R[(i0 + c) + (size_t)r * ldr]) : R[r + (size_t)(i0 + c) * ldr]) : T(0);
             }
-            if (warp == 0) {
+            if (warp == 0 && Dinv) {
+                // y_B <- D_B^-1 y_B (CT: D_B^-H y_B), entries past n zero
+                T acc = T(0);
+#pragma unroll 8
+                for (int c = 0; c < 32; ++c) acc = fmac(CT ? Tr<T>::conj(sD[buf][c][lane]) : sD[buf][lane][c], sy[i0 + c], acc);
+                __syncwarp();
+                if (lane < nbk) sy[i0 + lane] = acc;
+            } else if (warp == 0) {
                 T yv = (lane < nbk) ? sy[i0 + lane] : T(0);
                 const T d = (lane < nbk) ? (CT ? Tr<T>::conj(sD[buf][lane][lane]) : sD[buf][lane][lane]) : T(1);
                 const T dinv = T(1) / d;
@@ -168,6 +178,28 @@ template <class T, bool CT> __global__ void __launch_bounds__(512) k_trsm_small(
         for (int i = tid; i < n; i += blockDim.x) y[i] = sy[i];
         __syncthreads();
     }
+}
+
+// Dinv: the inverse of every 32 x 32 diagonal block of the upper triangular
+// R (n x n), block b at Dinv + b * 1024 (column-major, zero below the
+// diagonal and past n).  One warp per block; lane j forms column j of the
+// inverse by back substitution.
+template <class T> __global__ void __launch_bounds__(32) k_trinv_diag(int n, const T *R, size_t ldr, T *Dinv) {
+    __shared__ T sU[32][33], sX[32][33];
+    const int b = blockIdx.x, j = threadIdx.x, i0 = 32 * b, nb = min(32, n - i0);
+    for (int r = 0; r < 32; ++r) sU[r][j] = (r < nb && j < nb && r <= j) ? R[(i0 + r) + (size_t)(i0 + j) * ldr] : T(0);
+    __syncwarp();
+    for (int i = 31; i >= 0; --i) {
+        T x = T(0);
+        if (j < nb && i <= j) {
+            T acc = (i == j) ? T(1) : T(0);
+            for (int k = i + 1; k <= j; ++k) acc = fmac(-sU[i][k], sX[k][j], acc);
+            x = acc / sU[i][i];
+        }
+        sX[i][j] = x;
+        __syncwarp();
+    }
+    for (int r = 0; r < 32; ++r) Dinv[(size_t)b * 1024 + r + 32 * j] = sX[r][j];
 }
 
 template <class Tin, class Tout> __device__ __forceinline__ Tout convert_scalar(Tin v);

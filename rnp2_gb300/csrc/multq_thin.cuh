@@ -474,4 +474,303 @@ template <class T> __global__ void __launch_bounds__(256) k_gram_blocks(const T 
     for (int q = 0; q < 4; ++q) out[l1 + (size_t)(lq + 8 * q) * kPanelMaxCols] = acc[q];
 }
 
+
+// ---------------------------------------------------------------------------
+// Q^T C for a thin FP32 C (at most kQtcMaxCols columns) with wide reflector
+// blocks: the same one-launch structure as k_multq_thin, but a reflector
+// block may be 128 columns wide when its 128 x 128 T is at hand (the mixed
+// factor's tensor-core path forms one per 128-column block), so that a
+// 512-column Q takes 3 + 4 steps of two grid barriers instead of 16.  Each
+// step (columns [i, i + w), T_s) is
+//   1. W = V_s^T C over the block's rows, 32 reflectors (one staged chunk of
+//      V) at a time,
+//   2./3. the cross-block sum (two grid barriers, fixed order),
+//   4. Y = T_s^T W (T_s staged in shared memory during the barriers),
+//   5. C -= V_s Y, chunk by chunk.
+// V's 32-column chunks (the block's rows of 32 columns, one bulk copy per
+// column, completing on the buffer's mbarrier) stream through two buffers in
+// the order they are used (a 32-column step keeps its chunk for both
+// phases), so that each copy overlaps the previous chunk's work or the
+// barriers; the triangle of the chunk (zeros above the diagonal, ones on it)
+// is written over the copied rows by the block that holds them.  C's rows
+// stay in shared memory for the whole launch (columns padded to a multiple
+// of 4 with zeros).  Requires A 16-byte aligned, lda and m multiples of 4.
+// Every wait is bounded.
+// ---------------------------------------------------------------------------
+constexpr int kQtcMaxW = 128;
+constexpr int kQtcMaxCols = 16;
+constexpr size_t kQtcSmemMax = 226 * 1024;
+struct QtcArgs {
+    const float *A;
+    size_t lda;
+    const float *Tf;    // 32-column panel T's: panel p at Tf + p * 32 * 32 (column-major, ld 32)
+    const float *T128;  // 128-column block T's: block b at T128 + b * 128 * 128 (row-major, ld 128)
+    float *C;
+    size_t ldc;
+    int m, n, k, nwide;
+    float *part;        // [gridDim.x][kQtcMaxW * nq]
+    float *wred;        // [kQtcMaxW * nq]
+    unsigned *counter;
+    int *err;
+    int *status;
+    int rows_per_cta;
+};
+inline size_t qtc_smem_bytes(int rows, int nq) {
+    return ((size_t)2 * kQtcMaxW * nq + (size_t)kQtcMaxW * kQtcMaxW + (size_t)2 * kPanelMaxCols * rows + (size_t)(rows + 4) * nq) * sizeof(float);
+}
+
+namespace qtc {
+__device__ __forceinline__ uint32_t saddr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void bar_init(uint64_t *b) { asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(saddr(b)) : "memory"); }
+__device__ __forceinline__ void bar_init_fence() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+// the generic proxy's accesses to a buffer before the async proxy writes it
+__device__ __forceinline__ void proxy_fence() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void arrive_tx(uint64_t *b, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(saddr(b)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void copy(void *dst, const void *src, uint32_t bytes, uint64_t *b) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(saddr(dst)), "l"(src), "r"(bytes), "r"(saddr(b)) : "memory");
+}
+// bounded wait for the phase of the given parity
+__device__ __forceinline__ bool wait(uint64_t *b, uint32_t parity) {
+    const long long t0 = clock64();
+    while (true) {
+        uint32_t done;
+        asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n" : "=r"(done) : "r"(saddr(b)), "r"(parity) : "memory");
+        if (done) return true;
+        if (clock64() - t0 > 2000000000LL) return false;
+    }
+}
+} // namespace qtc
+
+template <int kTag> __global__ void __launch_bounds__(kThinThreads) k_qtc_blocks(QtcArgs p) {
+    extern __shared__ __align__(128) unsigned char s_dyn[];
+    __shared__ __align__(8) uint64_t s_bar[3];  // V buffers 0 and 1, T
+    const int n = p.n, nq = (n + 3) & ~3, R = p.rows_per_cta, ldcs = R + 4;
+    float *sT = reinterpret_cast<float *>(s_dyn);           // T_s as stored (row- or column-major)
+    float *sW = sT + kQtcMaxW * kQtcMaxW;                   // W(l, c) at l * nq + c
+    float *sY = sW + kQtcMaxW * nq;                         // Y(l, c) at l * nq + c
+    float *sV0 = sY + kQtcMaxW * nq;                        // two chunks, 32 x R each (ld R)
+    float *sC = sV0 + (size_t)2 * kPanelMaxCols * R;        // R x nq, column-major (ldcs)
+    const int G = gridDim.x, g = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int r0 = g * R;
+    const int r1 = min(p.m, r0 + R);
+    GridBarrier bar{p.counter, p.err, (unsigned)G, 0u};
+    bar.status = p.status;
+    const int wide_cols = kQtcMaxW * p.nwide;
+    const int nsteps = p.nwide + (p.k - wide_cols + kPanelMaxCols - 1) / kPanelMaxCols;
+    auto step_i = [&](int s) { return s < p.nwide ? kQtcMaxW * s : wide_cols + kPanelMaxCols * (s - p.nwide); };
+    auto step_w = [&](int s) { return s < p.nwide ? kQtcMaxW : min(kPanelMaxCols, p.k - step_i(s)); };
+    auto vbuf = [&](int b) { return sV0 + (size_t)b * kPanelMaxCols * R; };
+    uint32_t par0 = 0, par1 = 0, part = 0;
+    auto fail = [&]() {
+        atomicExch(p.err, (int)kStatusBarrierTimeout);
+        if (p.status) atomicExch(p.status, (int)kStatusBarrierTimeout);
+    };
+    // warp 0: rows [max(r0, ic), r1) of reflector columns [ic, ic + wc) into
+    // buffer b, one bulk copy per column from lane l (the block's earlier
+    // accesses to the buffer are ordered before by a block barrier)
+    auto stage = [&](int ic, int wc, int b) {
+        if (warp != 0) return;
+        qtc::proxy_fence();
+        const int rs = max(r0, ic);
+        const uint32_t bytes = rs < r1 ? (uint32_t)(r1 - rs) * 4u : 0u;
+        if (lane == 0) qtc::arrive_tx(&s_bar[b], bytes * (uint32_t)wc);
+        __syncwarp();
+        if (bytes && lane < wc) qtc::copy(vbuf(b) + (size_t)lane * R + (rs - r0), p.A + (size_t)(ic + lane) * p.lda + rs, bytes, &s_bar[b]);
+    };
+    // the chunk after (s, ph, q) in the order of use: phase 0 (W) chunks, then
+    // phase 1 (update) chunks when the step has more than one
+    auto stage_next = [&](int s, int ph, int q, int b) {
+        const int nchk = (step_w(s) + kPanelMaxCols - 1) / kPanelMaxCols;
+        if (q + 1 < nchk) {
+            ++q;
+        } else if (ph == 0 && nchk > 1) {
+            ph = 1;
+            q = 0;
+        } else {
+            ++s;
+            q = 0;
+            if (s >= nsteps) return;
+        }
+        const int ic = step_i(s) + kPanelMaxCols * q;
+        stage(ic, min(kPanelMaxCols, step_i(s) + step_w(s) - ic), b);
+    };
+    // wait for chunk (ic, wc) in buffer b, then write its triangle: zeros
+    // above the diagonal, ones on it (rows [ic, ic + wc) that this block holds)
+    auto land = [&](int ic, int wc, int b) -> bool {
+        uint32_t &par = b ? par1 : par0;
+        if (!qtc::wait(&s_bar[b], par)) return false;
+        par ^= 1u;
+        const int t0 = max(r0, ic), t1 = min(r1, ic + wc);
+        if (t0 < t1) {
+            float *buf = vbuf(b);
+            for (int e = tid; e < wc * (t1 - t0); e += kThinThreads) {
+                const int l = e / (t1 - t0), rr = t0 + e % (t1 - t0);
+                if (rr <= ic + l) buf[(size_t)l * R + (rr - r0)] = (rr == ic + l) ? 1.f : 0.f;
+            }
+        }
+        return true;
+    };
+    if (tid == 0) {
+        qtc::bar_init(&s_bar[0]);
+        qtc::bar_init(&s_bar[1]);
+        qtc::bar_init(&s_bar[2]);
+        qtc::bar_init_fence();
+    }
+    for (int c = 0; c < nq; ++c)
+        for (int r = r0 + tid; r < r0 + R; r += kThinThreads) sC[(size_t)c * ldcs + (r - r0)] = (r < r1 && c < n) ? p.C[r + (size_t)c * p.ldc] : 0.f;
+    __syncthreads();
+    int ck = 0;  // chunks consumed so far: chunk ck sits in buffer ck & 1
+    if (nsteps > 0) stage(step_i(0), min(kPanelMaxCols, step_w(0)), 0);
+    const int ctiles = nq / 4;
+    bool ok = true;
+    for (int s = 0; s < nsteps && ok; ++s) {
+        const int i = step_i(s), w = step_w(s);
+        const int nchk = (w + kPanelMaxCols - 1) / kPanelMaxCols;
+        const int nw = w * nq;
+        float *mine = p.part + (size_t)g * kQtcMaxW * nq;
+        // 1. partial W = V^T C over own rows, one chunk of 32 reflectors at a time
+        for (int q = 0; q < nchk; ++q, ++ck) {
+            const int ic = i + kPanelMaxCols * q, wc = min(kPanelMaxCols, i + w - ic);
+            if (!land(ic, wc, ck & 1)) { ok = false; break; }
+            __syncthreads();
+            stage_next(s, 0, q, (ck + 1) & 1);
+            const float *sV = vbuf(ck & 1);
+            const int rs = max(r0, ic);
+            // tile t per half warp: reflectors 4 (t % 8) .., columns 4 (t / 8) ..
+            for (int t = 2 * warp + (lane >> 4); t < 8 * ctiles; t += 2 * kThinWarps) {
+                const int l0 = 4 * (t % 8), c0 = 4 * (t / 8);
+                float acc[16];
+#pragma unroll
+                for (int e = 0; e < 16; ++e) acc[e] = 0.f;
+                // (every lane takes part in the shuffles below, whatever l0)
+                for (int r4 = rs + 4 * (lane & 15); l0 < wc && r4 < r1; r4 += 64) {
+                    float4 v[4], c[4];
+#pragma unroll
+                    for (int a = 0; a < 4; ++a) v[a] = *reinterpret_cast<const float4 *>(sV + (size_t)(l0 + a) * R + (r4 - r0));
+#pragma unroll
+                    for (int qq = 0; qq < 4; ++qq) c[qq] = *reinterpret_cast<const float4 *>(sC + (size_t)(c0 + qq) * ldcs + (r4 - r0));
+#pragma unroll
+                    for (int a = 0; a < 4; ++a)
+#pragma unroll
+                        for (int qq = 0; qq < 4; ++qq) {
+                            float x = acc[4 * a + qq];
+                            x = fmaf(v[a].x, c[qq].x, x);
+                            x = fmaf(v[a].y, c[qq].y, x);
+                            x = fmaf(v[a].z, c[qq].z, x);
+                            acc[4 * a + qq] = fmaf(v[a].w, c[qq].w, x);
+                        }
+                }
+                // butterfly over the half warp: lane (& 15) ends with entry (lane & 15)
+#pragma unroll
+                for (int lvl = 0; lvl < 4; ++lvl) {
+                    const int o = 8 >> lvl, mm = 8 >> lvl;
+                    const bool up = (lane & o) != 0;
+#pragma unroll
+                    for (int e = 0; e < mm; ++e) {
+                        const float send = up ? acc[e] : acc[e + mm], keep = up ? acc[e + mm] : acc[e];
+                        acc[e] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+                    }
+                }
+                const int e = lane & 15, l = l0 + (e >> 2);
+                if (l < wc) mine[(ic - i + l) + (size_t)(c0 + (e & 3)) * kQtcMaxW] = acc[0];
+            }
+        }
+        if (!ok) break;
+        if (nchk == 1) --ck;  // the step keeps its one chunk for the update
+        if (!bar.sync()) return;
+        // T_s into shared memory while the blocks sum and wait (the previous
+        // step's Y is done with sT: block barriers since)
+        const bool wide = s < p.nwide;
+        if (tid == 0) {
+            qtc::proxy_fence();
+            const float *src = wide ? p.T128 + (size_t)s * kQtcMaxW * kQtcMaxW : p.Tf + (size_t)(i / kPanelMaxCols) * kPanelMaxCols * kPanelMaxCols;
+            const uint32_t bytes = (uint32_t)(wide ? kQtcMaxW * kQtcMaxW : kPanelMaxCols * kPanelMaxCols) * 4u;
+            qtc::arrive_tx(&s_bar[2], bytes);
+            qtc::copy(sT, src, bytes, &s_bar[2]);
+        }
+        // 3. this block's slice of the cross-block sum, fixed order over blocks
+        const int slice = (nw + G - 1) / G;
+        for (int e = g * slice + warp; e < min(nw, (g + 1) * slice); e += kThinWarps) {
+            const int idx = (e % w) + (e / w) * kQtcMaxW;
+            float a = 0.f;
+            for (int qb = lane; qb < G; qb += 32) a += ldcg(&p.part[(size_t)qb * kQtcMaxW * nq + idx]);
+            a = warp_sum(a);
+            if (lane == 0) p.wred[idx] = a;
+        }
+        if (!bar.sync()) return;
+        // 4. Y = T^T W: Y(l, c) = sum_{j <= l} T(j, l) W(j, c)
+        for (int e = tid; e < nw; e += kThinThreads) {
+            const int l = e % w, c = e / w;
+            sW[l * nq + c] = ldcg(&p.wred[l + c * kQtcMaxW]);
+        }
+        if (!qtc::wait(&s_bar[2], part)) { ok = false; break; }
+        part ^= 1u;
+        __syncthreads();
+        {
+            const int tr = wide ? kQtcMaxW : 1, tc = wide ? 1 : kPanelMaxCols;  // T(j, l) at sT[j tr + l tc]
+            for (int e = tid; e < nw; e += kThinThreads) {
+                const int l = e / nq, c = e % nq;
+                const float *tl = sT + l * tc;
+                const float *wcol = sW + c;  // W(j, c) at wcol[j nq]
+                float a0 = 0.f, a1 = 0.f;
+                int j = 0;
+                for (; j + 1 <= l; j += 2) {
+                    a0 = fmaf(tl[j * tr], wcol[j * nq], a0);
+                    a1 = fmaf(tl[(j + 1) * tr], wcol[(j + 1) * nq], a1);
+                }
+                if (j <= l) a0 = fmaf(tl[j * tr], wcol[j * nq], a0);
+                sY[l * nq + c] = a0 + a1;
+            }
+        }
+        // 5. C -= V Y on own rows, chunk by chunk
+        for (int q = 0; q < nchk; ++q, ++ck) {
+            const int ic = i + kPanelMaxCols * q, wc = min(kPanelMaxCols, i + w - ic);
+            if (nchk > 1) {
+                if (!land(ic, wc, ck & 1)) { ok = false; break; }
+                __syncthreads();
+                stage_next(s, 1, q, (ck + 1) & 1);
+            } else {
+                __syncthreads();  // sY complete; the next step's first chunk is already on its way
+            }
+            const float *sV = vbuf(ck & 1);
+            const int rs = max(r0, ic);
+            const int nqr = (r1 - rs + 3) / 4;
+            for (int u = tid; u < nqr * ctiles; u += kThinThreads) {
+                const int r4 = rs + 4 * (u % nqr), c0 = 4 * (u / nqr);
+                float4 acc[4];
+#pragma unroll
+                for (int qq = 0; qq < 4; ++qq) acc[qq] = *reinterpret_cast<const float4 *>(sC + (size_t)(c0 + qq) * ldcs + (r4 - r0));
+                const int lmax = min(wc, r4 + 4 - ic);  // V(r, l) = 0 for l > r - ic
+                for (int l = 0; l < lmax; ++l) {
+                    const float4 v = *reinterpret_cast<const float4 *>(sV + (size_t)l * R + (r4 - r0));
+                    const float4 y = *reinterpret_cast<const float4 *>(sY + (size_t)(ic - i + l) * nq + c0);
+                    const float yq[4] = {y.x, y.y, y.z, y.w};
+#pragma unroll
+                    for (int qq = 0; qq < 4; ++qq) {
+                        acc[qq].x = fmaf(-v.x, yq[qq], acc[qq].x);
+                        acc[qq].y = fmaf(-v.y, yq[qq], acc[qq].y);
+                        acc[qq].z = fmaf(-v.z, yq[qq], acc[qq].z);
+                        acc[qq].w = fmaf(-v.w, yq[qq], acc[qq].w);
+                    }
+                }
+#pragma unroll
+                for (int qq = 0; qq < 4; ++qq) *reinterpret_cast<float4 *>(sC + (size_t)(c0 + qq) * ldcs + (r4 - r0)) = acc[qq];
+            }
+        }
+    }
+    if (!ok) {
+        // a copy did not land in time: stop every block, let the copies in
+        // flight finish (bounded), leave C as it was
+        fail();
+        qtc::wait(&s_bar[0], par0);
+        qtc::wait(&s_bar[1], par1);
+        return;
+    }
+    __syncthreads();
+    for (int c = 0; c < n; ++c)
+        for (int r = r0 + tid; r < r1; r += kThinThreads) p.C[r + (size_t)c * p.ldc] = sC[(size_t)c * ldcs + (r - r0)];
+}
+
 } // namespace rnpgpu

@@ -528,6 +528,11 @@ struct CqrWs {
     // arriving (host staging): the factor waits for this event before its
     // first update of those columns
     cudaEvent_t rest_ready = nullptr;
+    // when set, the 128 x 128 T of every wide block is kept here (block b at
+    // t128 + b * 128 * 128, row-major); geqrf reports in nwide how many
+    // leading 128-column blocks have one
+    float *t128 = nullptr;
+    mutable int nwide = 0;
 };
 inline size_t cqr_ws_bytes() {
     const auto r = [](size_t b) { return (b + 255) / 256 * 256; };
@@ -672,6 +677,7 @@ template <class T> int geqrf(size_t m, size_t n, T *a, size_t lda, T *tau, size_
     if constexpr (std::is_same<T, float>::value) {
         wide_mode = !ahead && cqr != nullptr && cqr->use_wide && Tstore != nullptr && wide::usable(m, n, a, lda);
     }
+    if (cqr != nullptr) cqr->nwide = 0;
     bool big_pending = false;
     bool rest_waited = cqr == nullptr || cqr->rest_ready == nullptr;
     auto wait_rest = [&]() -> int {
@@ -712,8 +718,11 @@ template <class T> int geqrf(size_t m, size_t n, T *a, size_t lda, T *tau, size_
                 if (block_done && jend < n) {
                     if ((rc = wait_rest())) return rc;
                     if (c1 == j0 + wide::kNb && m - j0 >= 128) {
-                        rc = wide::apply(a, lda, (int)m, (int)n, (int)j0, Tstore + (j0 / nb) * kPanelMaxCols * kPanelMaxCols, (size_t)kPanelMaxCols * kPanelMaxCols, cqr->wide, st);
+                        const int wb = (int)(j0 / wide::kNb);
+                        float *tsave = cqr->t128 ? cqr->t128 + (size_t)wb * wide::kNb * wide::kNb : nullptr;
+                        rc = wide::apply(a, lda, (int)m, (int)n, (int)j0, Tstore + (j0 / nb) * kPanelMaxCols * kPanelMaxCols, (size_t)kPanelMaxCols * kPanelMaxCols, cqr->wide, st, tsave);
                         if (rc) return rc;
+                        if (tsave && cqr->nwide == wb) cqr->nwide = wb + 1;
                     } else {
                         for (size_t p = j0; p < c1; p += nb) {
                             const int pb = (int)std::min(nb, k - p);
@@ -891,6 +900,47 @@ template <class T> int multq_thin(bool notran, size_t m, size_t n, size_t k, con
     void *args[] = {&p};
     KScope ks("multq_thin", st);
     return coop_launch("k_multq_thin", kern, tp.grid, kThinThreads, args, tp.smem, st);
+}
+
+// Q^T C with wide reflector blocks (k_qtc_blocks): C is m x n FP32 with n at
+// most kQtcMaxCols, the first nwide 128-column blocks of the reflectors have
+// their T in t128, the rest are 32-column panels with their T in Tf.
+inline size_t qtc_ws_bytes(size_t n) {
+    const int G = std::max(1, device_facts().sm_count);
+    const size_t nq = (n + 3) / 4 * 4;
+    return ((size_t)(G + 1) * kQtcMaxW * nq * sizeof(float) + 255) / 256 * 256 + 1024;
+}
+inline int qtc_rows(size_t m) {
+    const int G = std::max(1, device_facts().sm_count);
+    return (int)(((m + G - 1) / G + 3) / 4 * 4);
+}
+inline bool qtc_usable(size_t m, size_t n, size_t k, const float *a, size_t lda, int nwide) {
+    if (nwide <= 0 || n == 0 || n > (size_t)kQtcMaxCols || k > m || m > (size_t)INT32_MAX / 2) return false;
+    if (((uintptr_t)a % 16) != 0 || lda % 4 != 0 || m % 4 != 0) return false;
+    if ((size_t)nwide * kQtcMaxW > k) return false;
+    return qtc_smem_bytes(qtc_rows(m), (int)((n + 3) / 4 * 4)) <= kQtcSmemMax;
+}
+inline int qtc_blocks(size_t m, size_t n, size_t k, const float *a, size_t lda, const float *Tf, const float *t128, int nwide, float *c, size_t ldc, void *ws, cudaStream_t st) {
+    const int G = std::max(1, device_facts().sm_count);
+    const int R = qtc_rows(m), nq = (int)((n + 3) / 4 * 4);
+    const size_t smem = qtc_smem_bytes(R, nq);
+    const void *kern = (const void *)k_qtc_blocks<0>;
+    if (int rc = kernel_attr(kern, (int)kQtcSmemMax)) return rc;
+    Carver cv(ws);
+    QtcArgs p;
+    p.A = a; p.lda = lda; p.Tf = Tf; p.T128 = t128; p.C = c; p.ldc = ldc;
+    p.m = (int)m; p.n = (int)n; p.k = (int)k; p.nwide = nwide;
+    p.part = cv.take<float>((size_t)G * kQtcMaxW * nq);
+    p.wred = cv.take<float>((size_t)kQtcMaxW * nq);
+    unsigned *sync = cv.take<unsigned>(2);
+    p.counter = sync;
+    p.err = (int *)(sync + 1);
+    p.status = device_status_ptr();
+    p.rows_per_cta = R;
+    RNPGPU_CHECK(cudaMemsetAsync(sync, 0, 2 * sizeof(unsigned), st));
+    void *args[] = {&p};
+    KScope ks("multq_thin", st);
+    return coop_launch("k_qtc_blocks", kern, G, kThinThreads, args, smem, st);
 }
 
 // ---------------------------------------------------------------------------

@@ -773,7 +773,9 @@ inline bool usable(size_t m, size_t n, const float *a, size_t lda) {
 
 // C = A(r0:m, c1:n) -= V Y^T for the 128-column block V = A(r0:m, r0:r0+128)
 // (c1 = r0 + 128) with the four 32 x 32 panel factors at Tp (tstride apart).
-inline int apply(float *A, size_t lda, int m, int n, int r0, const float *Tp, size_t tstride, const WideWs &w, cudaStream_t st) {
+// The block's 128 x 128 T (row-major) goes to Tsave when given (kept for
+// later applications of Q), else to the workspace.
+inline int apply(float *A, size_t lda, int m, int n, int r0, const float *Tp, size_t tstride, const WideWs &w, cudaStream_t st, float *Tsave = nullptr) {
     const int rows = m - r0, c1 = r0 + kNb, nc = n - c1;
     if (rows <= 0 || nc <= 0) return kOk;
     const int sms = std::max(1, device_facts().sm_count);
@@ -807,11 +809,12 @@ inline int apply(float *A, size_t lda, int m, int n, int r0, const float *Tp, si
         k_wide_reduce<0><<<ntile * 128, 128, 0, st>>>(w.P, nsplit, ntile, w.GW);
         RNPGPU_CHECK_LAUNCH();
         if ((rc = kernel_attr((const void *)k_wide_t<0>, kTSmem))) return rc;
-        k_wide_t<0><<<1, kTThreads, kTSmem, st>>>(w.GW, Tp, tstride, 4, w.T);
+        float *Tb = Tsave ? Tsave : w.T;
+        k_wide_t<0><<<1, kTThreads, kTSmem, st>>>(w.GW, Tp, tstride, 4, Tb);
         RNPGPU_CHECK_LAUNCH();
         const int J = (nc + kUpdCols - 1) / kUpdCols;
         if ((rc = kernel_attr((const void *)k_wide_y<0>, kYSmem))) return rc;
-        k_wide_y<0><<<J * kUpdCols / 16, 256, kYSmem, st>>>(w.GW, w.T, nc, w.y);
+        k_wide_y<0><<<J * kUpdCols / 16, 256, kYSmem, st>>>(w.GW, Tb, nc, w.y);
         RNPGPU_CHECK_LAUNCH();
     }
     {
