@@ -403,9 +403,67 @@ template <int kTag> __global__ void __launch_bounds__(kCqrThreads, 1) k_panel_cq
     __shared__ int s_fail;
     __shared__ float s_dev;  // ||G2 - I||_F^2 of an FP32 first pass
 
+    // FP32 Gram partial with 8 x 8 tiles (10 over the upper triangle, one per
+    // warp): per row 4 shared loads for 64 FMAs (4 x 4 tiles: 2 for 16, and
+    // 36 tiles over 16 warps take three rounds), then a reduce-scatter of
+    // the 64 sums over the warp (lane L ends with entries 2L, 2L + 1 of the
+    // tile, row L / 4) written into the 4 x 4 tile-major layout
+    auto gram_partial_f32 = [&]() {
+        if (warp < 10) {
+            int TI = 0, t = warp;
+            while (t >= 4 - TI) {
+                t -= 4 - TI;
+                ++TI;
+            }
+            const int TJ = TI + t;
+            float2 acc[32];
+#pragma unroll
+            for (int e = 0; e < 32; ++e) acc[e] = make_float2(0.f, 0.f);
+            for (int r = lane; r < R; r += 32) {
+                const float *row = sQ + (size_t)r * LD;
+                const float4 a0 = *reinterpret_cast<const float4 *>(row + 8 * TI), a1 = *reinterpret_cast<const float4 *>(row + 8 * TI + 4);
+                const float4 c0 = *reinterpret_cast<const float4 *>(row + 8 * TJ), c1 = *reinterpret_cast<const float4 *>(row + 8 * TJ + 4);
+                const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+                const float2 cp[4] = {make_float2(c0.x, c0.y), make_float2(c0.z, c0.w), make_float2(c1.x, c1.y), make_float2(c1.z, c1.w)};
+#pragma unroll
+                for (int a = 0; a < 8; ++a)
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) acc[4 * a + q] = __ffma2_rn(cqr_dup(av[a]), cp[q], acc[4 * a + q]);
+            }
+            float v[64];
+#pragma unroll
+            for (int e = 0; e < 32; ++e) {
+                v[2 * e] = acc[e].x;
+                v[2 * e + 1] = acc[e].y;
+            }
+#pragma unroll
+            for (int lvl = 0; lvl < 5; ++lvl) {
+                const int o = 16 >> lvl, n = 32 >> lvl;
+                const bool up = (lane & o) != 0;
+#pragma unroll
+                for (int e = 0; e < n; ++e) {
+                    const float send = up ? v[e] : v[e + n], keep = up ? v[e + n] : v[e];
+                    v[e] = keep + __shfl_xor_sync(0xFFFFFFFFu, send, o);
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                const int x = 2 * lane + k, i = 8 * TI + (x >> 3), j = 8 * TJ + (x & 7);
+                if (i <= j) {
+                    const int ti = i >> 2, tj = j >> 2;
+                    const int tt = ti * 8 - (ti * (ti - 1)) / 2 + (tj - ti);
+                    p.gpart[(size_t)b * kCqrEntries + tt * 16 + 4 * (i & 3) + (j & 3)] = make_float2(v[k], 0.f);
+                }
+            }
+        }
+    };
     // the block's Gram partial of sQ into gpart[b]: double-float or FP32 sums,
     // entries of a tile row in packed pairs
     auto gram_partial = [&](bool df) {
+        if (!df) {
+            gram_partial_f32();
+            return;
+        }
         for (int t = warp; t < kCqrTiles; t += kCqrThreads / 32) {
             int ti, tj;
             cqr_tile(t, ti, tj);
