@@ -129,14 +129,29 @@ template <class T, bool CT> __global__ void __launch_bounds__(512) k_trsm_small(
         for (int i = tid; i < 32 * nblk; i += blockDim.x) sy[i] = (i < n) ? y[i] : T(0);
         load_diag(0, 0, tid, blockDim.x);
         __syncthreads();
+        // this thread's 32 update coefficients of step s (row r = tid)
+        auto load_coef = [&](int s, T (&cf)[32]) {
+            const int i0 = first_row(s), nbk = min(32, n - i0), r = tid;
+            const bool upd = CT ? (r >= i0 + nbk && r < n) : (r < i0);
+            if (upd) {
+#pragma unroll
+                for (int c = 0; c < 32; ++c) cf[c] = (c < nbk) ? (CT ? Tr<T>::conj(R[(i0 + c) + (size_t)r * ldr]) : R[r + (size_t)(i0 + c) * ldr]) : T(0);
+            }
+        };
+        // 4-byte elements: the next step's coefficients are loaded during
+        // this step (their latency was most of a step)
+        constexpr bool kPref = sizeof(T) == 4;
+        T coef[32];
+        if (kPref) load_coef(0, coef);
         for (int s = 0; s < nblk; ++s) {
             const int i0 = first_row(s), nbk = min(32, n - i0), buf = s & 1;
             const int r = tid;
             const bool upd = CT ? (r >= i0 + nbk && r < n) : (r < i0);
-            T coef[32];
-            if (upd) {
-#pragma unroll
-                for (int c = 0; c < 32; ++c) coef[c] = (c < nbk) ? (CT ? Tr<T>::conj(R[(i0 + c) + (size_t)r * ldr]) : R[r + (size_t)(i0 + c) * ldr]) : T(0);
+            T coefn[kPref ? 32 : 1];
+            if constexpr (kPref) {
+                if (s + 1 < nblk) load_coef(s + 1, coefn);
+            } else {
+                load_coef(s, coef);
             }
             if (warp == 0 && Dinv) {
                 // y_B <- D_B^-1 y_B (CT: D_B^-H y_B), entries past n zero
@@ -172,6 +187,10 @@ template <class T, bool CT> __global__ void __launch_bounds__(512) k_trsm_small(
 #pragma unroll
                 for (int c = 0; c < 32; ++c) a[c & 3] = fmac(coef[c], sy[i0 + c], a[c & 3]);
                 sy[r] = sy[r] - ((a[0] + a[1]) + (a[2] + a[3]));
+            }
+            if constexpr (kPref) {
+#pragma unroll
+                for (int c = 0; c < 32; ++c) coef[c] = coefn[c];
             }
             __syncthreads();
         }

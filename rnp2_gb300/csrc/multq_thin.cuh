@@ -694,8 +694,14 @@ template <int kTag> __global__ void __launch_bounds__(kThinThreads) k_qtc_blocks
         const int slice = (nw + G - 1) / G;
         for (int e = g * slice + warp; e < min(nw, (g + 1) * slice); e += kThinWarps) {
             const int idx = (e % w) + (e / w) * kQtcMaxW;
+            // the lane's partials in flight together (G <= 256), summed in order
+            float v[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) v[u] = (lane + 32 * u < G) ? ldcg(&p.part[(size_t)(lane + 32 * u) * kQtcMaxW * nq + idx]) : 0.f;
             float a = 0.f;
-            for (int qb = lane; qb < G; qb += 32) a += ldcg(&p.part[(size_t)qb * kQtcMaxW * nq + idx]);
+#pragma unroll
+            for (int u = 0; u < 8; ++u)
+                if (lane + 32 * u < G) a += v[u];
             a = warp_sum(a);
             if (lane == 0) p.wred[idx] = a;
         }

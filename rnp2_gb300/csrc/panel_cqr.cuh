@@ -510,11 +510,18 @@ template <int kTag> __global__ void __launch_bounds__(kCqrThreads, 1) k_panel_cq
     // the partials summed across blocks, one warp per entry, into gfin
     auto gram_sum = [&]() {
         for (int e = b + G * warp; e < kCqrEntries; e += G * (kCqrThreads / 32)) {
-            F2 s{0.f, 0.f};
-            for (int q = lane; q < G; q += 32) {
-                const float2 v = __ldcg(&p.gpart[(size_t)q * kCqrEntries + e]);
-                s = f2_add(s, F2{v.x, v.y});
+            // all of the lane's partials in flight at once (G <= 256), then
+            // summed in the same order
+            float2 v[kPanelMaxBlocksCqr / 32];
+#pragma unroll
+            for (int u = 0; u < kPanelMaxBlocksCqr / 32; ++u) {
+                const int q = lane + 32 * u;
+                v[u] = (q < G) ? __ldcg(&p.gpart[(size_t)q * kCqrEntries + e]) : make_float2(0.f, 0.f);
             }
+            F2 s{0.f, 0.f};
+#pragma unroll
+            for (int u = 0; u < kPanelMaxBlocksCqr / 32; ++u)
+                if (lane + 32 * u < G) s = f2_add(s, F2{v[u].x, v[u].y});
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) s = f2_add(s, F2{__shfl_xor_sync(0xFFFFFFFFu, s.h, o), __shfl_xor_sync(0xFFFFFFFFu, s.l, o)});
             if (lane == 0) __stcg(&p.gfin[e], make_float2(s.h, s.l));

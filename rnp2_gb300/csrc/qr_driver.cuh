@@ -916,6 +916,7 @@ inline int qtc_rows(size_t m) {
 }
 inline bool qtc_usable(size_t m, size_t n, size_t k, const float *a, size_t lda, int nwide) {
     if (nwide <= 0 || n == 0 || n > (size_t)kQtcMaxCols || k > m || m > (size_t)INT32_MAX / 2) return false;
+    if (device_facts().sm_count > 256) return false;  // the cross-block sum keeps 8 partials per lane
     if (((uintptr_t)a % 16) != 0 || lda % 4 != 0 || m % 4 != 0) return false;
     if ((size_t)nwide * kQtcMaxW > k) return false;
     return qtc_smem_bytes(qtc_rows(m), (int)((n + 3) / 4 * 4)) <= kQtcSmemMax;
