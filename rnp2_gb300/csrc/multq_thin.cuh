@@ -779,4 +779,189 @@ template <int kTag> __global__ void __launch_bounds__(kThinThreads) k_qtc_blocks
         for (int r = r0 + tid; r < r1; r += kThinThreads) p.C[r + (size_t)c * p.ldc] = sC[(size_t)c * ldcs + (r - r0)];
 }
 
+// ---------------------------------------------------------------------------
+// One block reflector (K <= 32 columns, compact WY with T) applied from the
+// left to an FP32 C of at most kA32MaxCols columns in one cooperative launch:
+// C -= V (T^T (V^T C)), the mixed factor's updates inside a 128-column block.
+// Every block copies its rows of V and C into shared memory once (bulk
+// copies on one mbarrier), forms its part of V^T C (4 x 4 tiles per half
+// warp, as k_qtc_blocks), the blocks sum the partials (two grid barriers,
+// fixed order), then each block forms Y = T^T W and updates and stores its
+// rows of C.  One launch instead of three (W partials, their sum times T, the
+// update), C read and written once.  Requires V and C 16-byte aligned,
+// ldv, ldc and M multiples of 4.
+// ---------------------------------------------------------------------------
+constexpr int kA32MaxCols = 64;
+struct A32Args {
+    const float *V;
+    size_t ldv;
+    const float *T;  // K x K upper (column-major, leading dimension 32)
+    float *C;
+    size_t ldc;
+    int M, N, K;
+    float *part;     // [gridDim.x][32 * N]
+    float *wred;     // [32 * N]
+    unsigned *counter;
+    int *err;
+    int *status;
+    int rows_per_cta;
+};
+inline size_t a32_smem_bytes(int rows, int n) { return ((size_t)2 * kPanelMaxCols * n + (size_t)kPanelMaxCols * rows + (size_t)(rows + 4) * n) * sizeof(float); }
+
+template <int kTag> __global__ void __launch_bounds__(kThinThreads) k_apply32(A32Args p) {
+    extern __shared__ __align__(128) unsigned char s_dyn[];
+    __shared__ __align__(8) uint64_t s_bar;
+    const int N = p.N, K = p.K, R = p.rows_per_cta, ldcs = R + 4;
+    float *sW = reinterpret_cast<float *>(s_dyn);           // W(l, c) at l * N + c
+    float *sY = sW + kPanelMaxCols * N;                     // Y(l, c) at l * N + c
+    float *sV = sY + kPanelMaxCols * N;                     // 32 x R (ld R)
+    float *sC = sV + (size_t)kPanelMaxCols * R;             // R x N, column-major (ldcs)
+    const int G = gridDim.x, g = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int r0 = g * R;
+    const int r1 = min(p.M, r0 + R);
+    GridBarrier bar{p.counter, p.err, (unsigned)G, 0u};
+    bar.status = p.status;
+    if (tid == 0) {
+        qtc::bar_init(&s_bar);
+        qtc::bar_init_fence();
+    }
+    __syncthreads();
+    // warp 0: the block's rows of the K columns of V and the N columns of C
+    if (warp == 0) {
+        const uint32_t bytes = r0 < r1 ? (uint32_t)(r1 - r0) * 4u : 0u;
+        if (lane == 0) qtc::arrive_tx(&s_bar, bytes * (uint32_t)(K + N));
+        __syncwarp();
+        if (bytes) {
+            for (int c = lane; c < K + N; c += 32) {
+                if (c < K) qtc::copy(sV + (size_t)c * R, p.V + (size_t)c * p.ldv + r0, bytes, &s_bar);
+                else qtc::copy(sC + (size_t)(c - K) * ldcs, p.C + (size_t)(c - K) * p.ldc + r0, bytes, &s_bar);
+            }
+        }
+    }
+    // rows past r1 (the last block) read as zeros; V's columns past K too
+    for (int e = tid; e < N * (r0 + R - max(r1, r0)); e += kThinThreads) {
+        const int nr = r0 + R - max(r1, r0);
+        sC[(size_t)(e / nr) * ldcs + (max(r1, r0) - r0) + e % nr] = 0.f;
+    }
+    for (int e = tid; e < kPanelMaxCols * R; e += kThinThreads) {
+        const int l = e / R, rr = r0 + e % R;
+        if (l >= K || rr >= r1) sV[e] = 0.f;
+    }
+    if (!qtc::wait(&s_bar, 0)) {
+        // the copies did not land in time: stop every block, let them finish (bounded)
+        atomicExch(p.err, (int)kStatusBarrierTimeout);
+        if (p.status) atomicExch(p.status, (int)kStatusBarrierTimeout);
+        qtc::wait(&s_bar, 0);
+        return;
+    }
+    // the triangle of V: zeros above the diagonal, ones on it
+    for (int e = tid; e < K * (min(r1, K) - r0); e += kThinThreads) {
+        const int nr = min(r1, K) - r0, l = e / nr, rr = r0 + e % nr;
+        if (rr <= l) sV[(size_t)l * R + (rr - r0)] = (rr == l) ? 1.f : 0.f;
+    }
+    __syncthreads();
+    const int ctiles = N / 4, nw = K * N;
+    float *mine = p.part + (size_t)g * kPanelMaxCols * N;
+    // 1. partial W = V^T C over own rows: tile t per half warp, reflectors
+    // 4 (t % 8) .., columns 4 (t / 8) ..
+    for (int t = 2 * warp + (lane >> 4); t < 8 * ctiles; t += 2 * kThinWarps) {
+        const int l0 = 4 * (t % 8), c0 = 4 * (t / 8);
+        float acc[16];
+#pragma unroll
+        for (int e = 0; e < 16; ++e) acc[e] = 0.f;
+        for (int r4 = r0 + 4 * (lane & 15); l0 < K && r4 < r1; r4 += 64) {
+            float4 v[4], c[4];
+#pragma unroll
+            for (int a = 0; a < 4; ++a) v[a] = *reinterpret_cast<const float4 *>(sV + (size_t)(l0 + a) * R + (r4 - r0));
+#pragma unroll
+            for (int qq = 0; qq < 4; ++qq) c[qq] = *reinterpret_cast<const float4 *>(sC + (size_t)(c0 + qq) * ldcs + (r4 - r0));
+#pragma unroll
+            for (int a = 0; a < 4; ++a)
+#pragma unroll
+                for (int qq = 0; qq < 4; ++qq) {
+                    float x = acc[4 * a + qq];
+                    x = fmaf(v[a].x, c[qq].x, x);
+                    x = fmaf(v[a].y, c[qq].y, x);
+                    x = fmaf(v[a].z, c[qq].z, x);
+                    acc[4 * a + qq] = fmaf(v[a].w, c[qq].w, x);
+                }
+        }
+#pragma unroll
+        for (int lvl = 0; lvl < 4; ++lvl) {
+            const int o = 8 >> lvl, mm = 8 >> lvl;
+            const bool up = (lane & o) != 0;
+#pragma unroll
+            for (int e = 0; e < mm; ++e) {
+                const float send = up ? acc[e] : acc[e + mm], keep = up ? acc[e + mm] : acc[e];
+                acc[e] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+            }
+        }
+        const int e = lane & 15, l = l0 + (e >> 2);
+        if (l < K) mine[l + (size_t)(c0 + (e & 3)) * kPanelMaxCols] = acc[0];
+    }
+    if (!bar.sync()) return;
+    // 2. this block's slice of the cross-block sum, fixed order over blocks
+    const int slice = (nw + G - 1) / G;
+    for (int e = g * slice + warp; e < min(nw, (g + 1) * slice); e += kThinWarps) {
+        const int idx = (e % K) + (e / K) * kPanelMaxCols;
+        float v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) v[u] = (lane + 32 * u < G) ? ldcg(&p.part[(size_t)(lane + 32 * u) * kPanelMaxCols * N + idx]) : 0.f;
+        float a = 0.f;
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+            if (lane + 32 * u < G) a += v[u];
+        a = warp_sum(a);
+        if (lane == 0) p.wred[idx] = a;
+    }
+    if (!bar.sync()) return;
+    // 3. Y = T^T W: Y(l, c) = sum_{j <= l} T(j, l) W(j, c)
+    for (int e = tid; e < nw; e += kThinThreads) {
+        const int l = e % K, c = e / K;
+        sW[l * N + c] = ldcg(&p.wred[l + c * kPanelMaxCols]);
+    }
+    __syncthreads();
+    for (int e = tid; e < kPanelMaxCols * N; e += kThinThreads) {
+        const int l = e / N, c = e % N;
+        float a0 = 0.f, a1 = 0.f;
+        if (l < K) {
+            const float *tl = p.T + (size_t)l * kPanelMaxCols;
+            int j = 0;
+            for (; j + 1 <= l; j += 2) {
+                a0 = fmaf(__ldg(tl + j), sW[j * N + c], a0);
+                a1 = fmaf(__ldg(tl + j + 1), sW[(j + 1) * N + c], a1);
+            }
+            if (j <= l) a0 = fmaf(__ldg(tl + j), sW[j * N + c], a0);
+        }
+        sY[l * N + c] = a0 + a1;
+    }
+    __syncthreads();
+    // 4. C -= V Y on own rows, then the rows back to global memory
+    const int nqr = (r1 - r0 + 3) / 4;
+    for (int u = tid; u < nqr * ctiles; u += kThinThreads) {
+        const int r4 = r0 + 4 * (u % nqr), c0 = 4 * (u / nqr);
+        float4 acc[4];
+#pragma unroll
+        for (int qq = 0; qq < 4; ++qq) acc[qq] = *reinterpret_cast<const float4 *>(sC + (size_t)(c0 + qq) * ldcs + (r4 - r0));
+        const int lmax = min(K, r4 + 4);  // V(r, l) = 0 for l > r
+        for (int l = 0; l < lmax; ++l) {
+            const float4 v = *reinterpret_cast<const float4 *>(sV + (size_t)l * R + (r4 - r0));
+            const float4 y = *reinterpret_cast<const float4 *>(sY + (size_t)l * N + c0);
+            const float yq[4] = {y.x, y.y, y.z, y.w};
+#pragma unroll
+            for (int qq = 0; qq < 4; ++qq) {
+                acc[qq].x = fmaf(-v.x, yq[qq], acc[qq].x);
+                acc[qq].y = fmaf(-v.y, yq[qq], acc[qq].y);
+                acc[qq].z = fmaf(-v.z, yq[qq], acc[qq].z);
+                acc[qq].w = fmaf(-v.w, yq[qq], acc[qq].w);
+            }
+        }
+#pragma unroll
+        for (int qq = 0; qq < 4; ++qq) *reinterpret_cast<float4 *>(sC + (size_t)(c0 + qq) * ldcs + (r4 - r0)) = acc[qq];
+    }
+    __syncthreads();
+    for (int c = 0; c < N; ++c)
+        for (int r = r0 + tid; r < r1; r += kThinThreads) p.C[r + (size_t)c * p.ldc] = sC[(size_t)c * ldcs + (r - r0)];
+}
+
 } // namespace rnpgpu

@@ -628,6 +628,8 @@ inline LookAhead *lookahead_ctx() {
 //
 // lookahead_ok = false keeps the serial order (no side stream or events are
 // created, nothing beyond the serial plan is asked of the work block).
+inline bool a32_usable(int M, int N, int K, const float *V, size_t ldv, const float *C, size_t ldc, const BlockWs<float> &ws, size_t p_floats, size_t w_floats);
+inline int apply32(int M, int N, int K, const float *V, size_t ldv, const float *Tm, float *C, size_t ldc, const BlockWs<float> &ws, cudaStream_t st);
 template <class T> int geqrf(size_t m, size_t n, T *a, size_t lda, T *tau, size_t *lwork, T *work, T *Tstore = nullptr, const CqrWs *cqr = nullptr, bool lookahead_ok = true) {
     if (lwork == nullptr) return -6;
     const size_t k = std::min(m, n);
@@ -708,10 +710,17 @@ template <class T> int geqrf(size_t m, size_t n, T *a, size_t lda, T *tau, size_
             if (wide_mode) {
                 const size_t j0 = i / wide::kNb * wide::kNb, jend = std::min(j0 + wide::kNb, n);
                 if (c1 < jend) {
-                    // the rest of the block: rank-32 passes (a one-launch thin
-                    // MultQ per 64 columns measured 86-92 us a launch at 65536
-                    // rows against 51 us for these three launches)
-                    rc = apply_block<T>(true, false, (int)(m - i), (int)(jend - c1), ib, Ai, lda, Tb, kPanelMaxCols, a + i + c1 * lda, lda, bw, st);
+                    // the rest of the block: one launch when it is at most 64
+                    // columns (k_apply32), else the three launches of the
+                    // rank-32 passes
+                    const int Mr = (int)(m - i), Nr = (int)(jend - c1);
+                    float *Cr = a + i + c1 * lda;
+                    // (two launches of 48 columns for the 96-column case measured
+                    // slower than the three-launch path)
+                    if (a32_usable(Mr, Nr, ib, Ai, lda, Cr, lda, bw, (size_t)bw.smax * n * kPanelMaxCols, n * kPanelMaxCols))
+                        rc = apply32(Mr, Nr, ib, Ai, lda, Tb, Cr, lda, bw, st);
+                    else
+                        rc = apply_block<T>(true, false, Mr, Nr, ib, Ai, lda, Tb, kPanelMaxCols, Cr, lda, bw, st);
                     if (rc) return rc;
                 }
                 const bool block_done = (c1 == j0 + wide::kNb) || (c1 == k);
@@ -942,6 +951,38 @@ inline int qtc_blocks(size_t m, size_t n, size_t k, const float *a, size_t lda, 
     void *args[] = {&p};
     KScope ks("multq_thin", st);
     return coop_launch("k_qtc_blocks", kern, G, kThinThreads, args, smem, st);
+}
+
+// C -= V (T^T (V^T C)) for a K <= 32 column block reflector and an FP32 C of
+// at most kA32MaxCols columns in one launch (k_apply32); false when the shapes
+// or the workspace do not suit it.  ws: the block-apply workspace (its
+// partial buffer and W buffer hold the partials, the sum and the barrier).
+inline bool a32_usable(int M, int N, int K, const float *V, size_t ldv, const float *C, size_t ldc, const BlockWs<float> &ws, size_t p_floats, size_t w_floats) {
+    const int G = std::max(1, device_facts().sm_count);
+    if (N <= 0 || N > kA32MaxCols || N % 4 != 0 || K <= 0 || K > kPanelMaxCols || M % 4 != 0 || M < 4096 || G > 256) return false;
+    if (((uintptr_t)V % 16) != 0 || ((uintptr_t)C % 16) != 0 || ldv % 4 != 0 || ldc % 4 != 0) return false;
+    if ((size_t)G * kPanelMaxCols * N > p_floats || (size_t)kPanelMaxCols * N + 64 > w_floats || ws.P == nullptr || ws.W == nullptr) return false;
+    return a32_smem_bytes(qtc_rows((size_t)M), N) <= kQtcSmemMax;
+}
+inline int apply32(int M, int N, int K, const float *V, size_t ldv, const float *Tm, float *C, size_t ldc, const BlockWs<float> &ws, cudaStream_t st) {
+    const int G = std::max(1, device_facts().sm_count);
+    const int R = qtc_rows((size_t)M);
+    const void *kern = (const void *)k_apply32<0>;
+    if (int rc = kernel_attr(kern, (int)kQtcSmemMax)) return rc;
+    A32Args p;
+    p.V = V; p.ldv = ldv; p.T = Tm; p.C = C; p.ldc = ldc;
+    p.M = M; p.N = N; p.K = K;
+    p.part = ws.P;
+    p.wred = ws.W;
+    unsigned *sync = reinterpret_cast<unsigned *>(ws.W + (size_t)kPanelMaxCols * N + 32);
+    p.counter = sync;
+    p.err = (int *)(sync + 1);
+    p.status = device_status_ptr();
+    p.rows_per_cta = R;
+    RNPGPU_CHECK(cudaMemsetAsync(sync, 0, 2 * sizeof(unsigned), st));
+    void *args[] = {&p};
+    KScope ks("larfb_update", st);
+    return coop_launch("k_apply32", kern, G, kThinThreads, args, a32_smem_bytes(R, N), st);
 }
 
 // ---------------------------------------------------------------------------
