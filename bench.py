@@ -728,7 +728,8 @@ def gpu_arm(args, rank, world, local):
     e1.record(stream)
     torch.cuda.synchronize()
     ms_e2e = e0.elapsed_time(e1) / args.steps
-    e2e_x_diff = float((x_h.to(dev) - X).abs().max())
+    x_e2e = x_h.to(dev)
+    e2e_x_diff = float((x_e2e - X).abs().max())
     del work_h
     if dist is not None:
         t = torch.tensor([ms_e2e], device=dev)
@@ -794,6 +795,7 @@ def gpu_arm(args, rank, world, local):
     # independent Karlson-Walden estimates of the LS backward error, from the
     # SVD of the plain FP64 factor's R
     kw_mixed = kw_backward_error(torch, A, b, x_mixed, R_plain)
+    kw_e2e = kw_backward_error(torch, A, b, x_e2e, R_plain)
     kw_fwd = kw_backward_error(torch, A, b, x_fwd, R_plain)
     kw_plain = kw_backward_error(torch, A, b, x_plain, R_plain)
 
@@ -854,7 +856,9 @@ def gpu_arm(args, rank, world, local):
         "e2e": {"value": world * 1e3 / ms_e2e, "unit": UNIT, "ms_per_step": ms_e2e,
                 "h2d_bytes_per_step": A.numel() * 8 + b.numel() * 8, "d2h_bytes_per_step": X.numel() * 8,
                 "call": "rnpgpu_dsgels_host (pinned host A, b in; x out; A staged in 128-column ranges)",
-                "x_max_abs_diff_vs_device_resident_solve": e2e_x_diff},
+                "x_max_abs_diff_vs_device_resident_solve": e2e_x_diff,
+                "backward_error": kw_e2e,
+                "note": "the staged call factors left-looking: its x meets the same LS backward-error bound as the device-resident solve; in the default mode both sit O(cond u32 |r|) from the FP64 solution, in different directions"},
         "gpu_launches": int(launches),
         "mixed": {"iterations": info["iterations"] if info else None, "converged": info["converged"] if info else None,
                   "backward_error": kw_mixed, "backward_error_bound": 10 * N * 2.0 ** -52,

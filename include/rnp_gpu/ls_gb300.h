@@ -66,13 +66,16 @@ typedef struct {
 int rnpgpu_dsgels(size_t m, size_t n, size_t nrhs, const double *a, size_t lda, const double *b, size_t ldb, double *x, size_t ldx, int max_iter, int flags, rnpgpu_refine_info *info, size_t *lwork, double *work);
 /* The same solve from HOST buffers a, b and x (pinned memory keeps the copies
  * asynchronous): A travels to the device in ranges of 128 columns on a copy
- * stream while the ranges already landed are prepared and the factorization
- * of the first 128 columns runs; b travels on the library's stream first and
- * x comes back on it last.  work (device) holds A, b and x (m n + m nrhs +
- * n nrhs elements, each rounded up to 256 bytes) and the workspace of
- * rnpgpu_dsgels; the query as rnpgpu_dsgels.  The call returns with x
- * enqueued (synchronize the library's stream before reading it); the
- * results are those of rnpgpu_dsgels on the same data. */
+ * stream while the ranges already landed are prepared and factored (the
+ * FP32 factor runs left-looking by 128-column blocks: each range is brought
+ * up to date by the blocks left of it once it has landed); b travels on the
+ * library's stream first and x comes back on it last.  work (device) holds
+ * A, b and x (m n + m nrhs + n nrhs elements, each rounded up to 256 bytes)
+ * and the workspace of rnpgpu_dsgels; the query as rnpgpu_dsgels.  The call
+ * returns with x enqueued (synchronize the library's stream before reading
+ * it).  The stopping tests and the info are those of rnpgpu_dsgels; x agrees
+ * with rnpgpu_dsgels's to the refinement's accuracy (the FP32 factor's
+ * operations run in another order), and repeated calls give the same bits. */
 int rnpgpu_dsgels_host(size_t m, size_t n, size_t nrhs, const double *a, size_t lda, const double *b, size_t ldb, double *x, size_t ldx, int max_iter, int flags, rnpgpu_refine_info *info, size_t *lwork, double *work);
 int rnpgpu_zcgels(size_t m, size_t n, size_t nrhs, const rnpgpu_complex_double *a, size_t lda, const rnpgpu_complex_double *b, size_t ldb, rnpgpu_complex_double *x, size_t ldx, int max_iter, int flags, rnpgpu_refine_info *info, size_t *lwork, rnpgpu_complex_double *work);
 

@@ -151,8 +151,8 @@ constexpr int kStageCols = 128;
 struct HostStage {
     cudaStream_t prep;        // prepares each range once it has landed
     const cudaEvent_t *ev_copy;
+    const cudaEvent_t *ev_prep;  // range c prepared (recorded by the staging)
     int nchunk;
-    cudaEvent_t ev_first;     // the first range prepared
     cudaEvent_t ev_all;       // every range prepared
 };
 
@@ -220,11 +220,16 @@ int gels_refine(size_t m, size_t n, size_t nrhs, const TH *a, size_t lda, const 
                 const int c0 = c * kStageCols, w = (int)std::min<size_t>(kStageCols, n - (size_t)c0);
                 RNPGPU_CHECK(cudaStreamWaitEvent(hs->prep, hs->ev_copy[c], 0));
                 if ((rc = oz_prepare_cols((int)m, (int)n, c0, w, a, lda, ow, dn, Af, m, hs->prep))) return rc;
-                if (c == 0) RNPGPU_CHECK(cudaEventRecord(hs->ev_first, hs->prep));
+                RNPGPU_CHECK(cudaEventRecord(hs->ev_prep[c], hs->prep));
             }
             RNPGPU_CHECK(cudaEventRecord(hs->ev_all, hs->prep));
-            RNPGPU_CHECK(cudaStreamWaitEvent(st, hs->ev_first, 0));
-            if constexpr (std::is_same<TL, float>::value) cw.rest_ready = hs->ev_all;
+            RNPGPU_CHECK(cudaStreamWaitEvent(st, hs->ev_prep[0], 0));
+            if constexpr (std::is_same<TL, float>::value) {
+                cw.range_ready = hs->ev_prep;
+                cw.nranges = hs->nchunk;
+            } else {
+                RNPGPU_CHECK(cudaStreamWaitEvent(st, hs->ev_all, 0));
+            }
         } else {
             if ((rc = oz_prepare_a((int)m, (int)n, a, lda, ow, dn, Af, m, st))) return rc;
         }
@@ -449,8 +454,8 @@ int gels_refine(size_t m, size_t n, size_t nrhs, const TH *a, size_t lda, const 
 // ---------------------------------------------------------------------------
 struct StageCtx {
     cudaStream_t copy = nullptr, prep = nullptr;
-    cudaEvent_t ev_start = nullptr, ev_first = nullptr, ev_all = nullptr;
-    std::vector<cudaEvent_t> ev_copy;
+    cudaEvent_t ev_start = nullptr, ev_all = nullptr;
+    std::vector<cudaEvent_t> ev_copy, ev_prep;
 };
 inline StageCtx *stage_ctx(int nchunk) {
     constexpr int kMaxDev = 16;
@@ -461,19 +466,20 @@ inline StageCtx *stage_ctx(int nchunk) {
     StageCtx &c = ctx[dev];
     if (state[dev] == 0) {
         const bool ok = cudaStreamCreateWithFlags(&c.copy, cudaStreamNonBlocking) == cudaSuccess && cudaStreamCreateWithFlags(&c.prep, cudaStreamNonBlocking) == cudaSuccess &&
-                        cudaEventCreateWithFlags(&c.ev_start, cudaEventDisableTiming) == cudaSuccess &&
-                        cudaEventCreateWithFlags(&c.ev_first, cudaEventDisableTiming) == cudaSuccess && cudaEventCreateWithFlags(&c.ev_all, cudaEventDisableTiming) == cudaSuccess;
+                        cudaEventCreateWithFlags(&c.ev_start, cudaEventDisableTiming) == cudaSuccess && cudaEventCreateWithFlags(&c.ev_all, cudaEventDisableTiming) == cudaSuccess;
         state[dev] = ok ? 1 : 2;
         if (!ok) cudaGetLastError();
     }
     if (state[dev] != 1) return nullptr;
-    while ((int)c.ev_copy.size() < nchunk) {
-        cudaEvent_t e;
-        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
-            cudaGetLastError();
-            return nullptr;
+    for (std::vector<cudaEvent_t> *v : {&c.ev_copy, &c.ev_prep}) {
+        while ((int)v->size() < nchunk) {
+            cudaEvent_t e;
+            if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+                cudaGetLastError();
+                return nullptr;
+            }
+            v->push_back(e);
         }
-        c.ev_copy.push_back(e);
     }
     return &c;
 }
@@ -523,7 +529,7 @@ int gels_refine_host(size_t m, size_t n, size_t nrhs, const TH *a, size_t lda, c
         RNPGPU_CHECK(cudaMemcpy2DAsync(dA + c0 * m, m * sizeof(TH), a + c0 * lda, lda * sizeof(TH), m * sizeof(TH), w, cudaMemcpyHostToDevice, sc->copy));
         RNPGPU_CHECK(cudaEventRecord(sc->ev_copy[c], sc->copy));
     }
-    HostStage hs{sc->prep, sc->ev_copy.data(), nchunk, sc->ev_first, sc->ev_all};
+    HostStage hs{sc->prep, sc->ev_copy.data(), sc->ev_prep.data(), nchunk, sc->ev_all};
     rc = gels_refine<TH, TL>(m, n, nrhs, dA, m, dB, m, dX, n, max_iter, flags, info, &lw, wrest, &hs);
     // the caller's stream also waits for every copy (a failed call may have
     // returned before it waited for them)

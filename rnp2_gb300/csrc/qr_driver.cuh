@@ -524,10 +524,14 @@ struct CqrWs {
     int *fail = nullptr;
     wide::WideWs wide;
     bool use_wide = false;
-    // when set, the matrix right of the first 128 columns may still be
-    // arriving (host staging): the factor waits for this event before its
-    // first update of those columns
-    cudaEvent_t rest_ready = nullptr;
+    // when set, the matrix may still be arriving (host staging), 128 columns
+    // at a time: range r (columns 128 r ..) is ready once range_ready[r] has
+    // completed.  The mixed factor then runs left-looking by 128-column
+    // blocks (each range is brought up to date by the blocks left of it when
+    // it is reached), so that it works on the ranges that have landed while
+    // the rest is still copied.
+    const cudaEvent_t *range_ready = nullptr;
+    int nranges = 0;
     // when set, the 128 x 128 T of every wide block is kept here (block b at
     // t128 + b * 128 * 128, row-major); geqrf reports in nwide how many
     // leading 128-column blocks have one
@@ -681,20 +685,37 @@ template <class T> int geqrf(size_t m, size_t n, T *a, size_t lda, T *tau, size_
     }
     if (cqr != nullptr) cqr->nwide = 0;
     bool big_pending = false;
-    bool rest_waited = cqr == nullptr || cqr->rest_ready == nullptr;
-    auto wait_rest = [&]() -> int {
-        if (!rest_waited) {
-            RNPGPU_CHECK(cudaStreamWaitEvent(st, cqr->rest_ready, 0));
-            if (la) RNPGPU_CHECK(cudaStreamWaitEvent(la->side, cqr->rest_ready, 0));
-            rest_waited = true;
+    // staged input: left-looking 128-column blocks in wide mode, else wait
+    // for every range up front
+    const bool staged = cqr != nullptr && cqr->range_ready != nullptr && cqr->nranges > 0;
+    const bool left_looking = staged && wide_mode;
+    if (staged && !left_looking) {
+        for (int r = 0; r < cqr->nranges; ++r) {
+            RNPGPU_CHECK(cudaStreamWaitEvent(st, cqr->range_ready[r], 0));
+            if (la) RNPGPU_CHECK(cudaStreamWaitEvent(la->side, cqr->range_ready[r], 0));
         }
-        return kOk;
-    };
+    }
     for (size_t i = 0; i < k; i += nb) {
         const int ib = (int)std::min(nb, k - i);
         T *Ai = a + i + i * lda;
         T *Tb = Tstore ? Tstore + (i / nb) * kPanelMaxCols * kPanelMaxCols : Tm[(i / nb) & 1];
         int rc;
+        if constexpr (std::is_same<T, float>::value) {
+            if (left_looking && i % wide::kNb == 0) {
+                // block jb's columns: once landed, updated by every block left of it
+                const int jb = (int)(i / wide::kNb);
+                if (jb < cqr->nranges) RNPGPU_CHECK(cudaStreamWaitEvent(st, cqr->range_ready[jb], 0));
+                const size_t cend = std::min(n, (size_t)(jb + 1) * wide::kNb);
+                for (int b0 = 0; b0 < jb; ++b0) {
+                    const size_t j0 = (size_t)b0 * wide::kNb;
+                    float *tsave = cqr->t128 ? cqr->t128 + (size_t)b0 * wide::kNb * wide::kNb : nullptr;
+                    rc = wide::apply(a, lda, (int)m, (int)cend, (int)j0, Tstore + (j0 / nb) * kPanelMaxCols * kPanelMaxCols, (size_t)kPanelMaxCols * kPanelMaxCols, cqr->wide, st, tsave,
+                                     (int)i);
+                    if (rc) return rc;
+                    if (tsave && cqr->nwide == b0) cqr->nwide = b0 + 1;
+                }
+            }
+        }
         if constexpr (std::is_same<T, float>::value) {
             if (cqr != nullptr && cqr_grid((int)(m - i), ib) > 0)
                 rc = panel_factor_cqr((int)(m - i), ib, Ai, lda, tau + i, Tb, kPanelMaxCols, pw, *cqr, st);
@@ -724,8 +745,7 @@ template <class T> int geqrf(size_t m, size_t n, T *a, size_t lda, T *tau, size_
                     if (rc) return rc;
                 }
                 const bool block_done = (c1 == j0 + wide::kNb) || (c1 == k);
-                if (block_done && jend < n) {
-                    if ((rc = wait_rest())) return rc;
+                if (block_done && jend < n && !left_looking) {
                     if (c1 == j0 + wide::kNb && m - j0 >= 128) {
                         const int wb = (int)(j0 / wide::kNb);
                         float *tsave = cqr->t128 ? cqr->t128 + (size_t)wb * wide::kNb * wide::kNb : nullptr;
@@ -744,7 +764,6 @@ template <class T> int geqrf(size_t m, size_t n, T *a, size_t lda, T *tau, size_
                 continue;
             }
         }
-        if ((rc = wait_rest())) return rc;
         if (!ahead) {
             rc = apply_block<T>(true, false, (int)(m - i), (int)(n - c1), ib, Ai, lda, Tb, kPanelMaxCols, a + i + c1 * lda, lda, bw, st);
             if (rc) return rc;

@@ -772,11 +772,13 @@ inline bool usable(size_t m, size_t n, const float *a, size_t lda) {
 }
 
 // C = A(r0:m, c1:n) -= V Y^T for the 128-column block V = A(r0:m, r0:r0+128)
-// (c1 = r0 + 128) with the four 32 x 32 panel factors at Tp (tstride apart).
-// The block's 128 x 128 T (row-major) goes to Tsave when given (kept for
-// later applications of Q), else to the workspace.
-inline int apply(float *A, size_t lda, int m, int n, int r0, const float *Tp, size_t tstride, const WideWs &w, cudaStream_t st, float *Tsave = nullptr) {
-    const int rows = m - r0, c1 = r0 + kNb, nc = n - c1;
+// (c1 = r0 + 128 unless given: any column right of the block, e.g. one
+// 128-column range of a left-looking order) with the four 32 x 32 panel
+// factors at Tp (tstride apart).  The block's 128 x 128 T (row-major) goes to
+// Tsave when given (kept for later applications of Q), else to the workspace.
+inline int apply(float *A, size_t lda, int m, int n, int r0, const float *Tp, size_t tstride, const WideWs &w, cudaStream_t st, float *Tsave = nullptr, int c1_at = -1) {
+    const int rows = m - r0, c1 = c1_at >= 0 ? c1_at : r0 + kNb, nc = n - c1;
+    if (c1 < r0 + kNb) return kErrDevice;
     if (rows <= 0 || nc <= 0) return kOk;
     const int sms = std::max(1, device_facts().sm_count);
     int *status = device_status_ptr();

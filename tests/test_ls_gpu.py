@@ -222,8 +222,9 @@ def test_mixed_fp32_factor_falls_back_to_householder_panels():
 @pytest.mark.parametrize("m,n,nrhs", [(4096, 300, 3), (2000, 130, 1), (1000, 100, 2), (8192, 512, 16)])
 def test_gels_refine_host_matches_device_solve(m, n, nrhs):
     """rnpgpu_dsgels_host (host buffers, A staged in 128-column ranges while
-    the GPU starts on the ranges already landed) gives the device solve's
-    result bit for bit."""
+    the GPU factors the ranges already landed, left-looking by 128-column
+    blocks) converges like the device solve, to the same solution within the
+    refinement's accuracy."""
     from rnp2_gb300 import ls as gls
     from rnp2_gb300.qr import to_colmajor
 
@@ -239,8 +240,16 @@ def test_gels_refine_host_matches_device_solve(m, n, nrhs):
     info_h = gls.gels_refine_host(A_h, B_h, X_h)
     torch.cuda.synchronize()
     assert bool(torch.isfinite(X).all()) and info["converged"] == 1, info
-    assert torch.equal(X_h, X.cpu())
-    assert info_h["iterations"] == info["iterations"] and info_h["converged"] == info["converged"]
+    assert info_h["converged"] == 1, info_h
+    bound = 10 * n * np.finfo(np.float64).eps
+    assert info_h["backward_error"] <= bound and info_h["normal_residual"] <= bound, info_h
+    Xd = X.cpu()
+    assert float((X_h - Xd).abs().max() / Xd.abs().max()) <= 1e-11
+    # the same staged call twice: the same bits
+    X_h2 = torch.full((nrhs, n), float("nan"), dtype=torch.float64).pin_memory().t()
+    gls.gels_refine_host(A_h, B_h, X_h2)
+    torch.cuda.synchronize()
+    assert torch.equal(X_h, X_h2)
 
 
 @pytest.mark.parametrize("m,n", [(2000, 130), (3000, 130), (1500, 70), (4096, 97)])
