@@ -154,7 +154,17 @@ struct HostStage {
     const cudaEvent_t *ev_prep;  // range c prepared (recorded by the staging)
     int nchunk;
     cudaEvent_t ev_all;       // every range prepared
+    unsigned char *vcache;    // per-block V slice images of the left-looking factor (or null)
+    size_t vstride;
 };
+// the left-looking factor's per-block V slice images (every 128-column block
+// but the last)
+inline size_t stage_vcache_stride(size_t m) { return wide::al256(wide::va_bytes((int)m)) + wide::al256(wide::vb_bytes((int)m)); }
+inline size_t stage_vcache_bytes(size_t m, size_t n) {
+    if (!wide::usable(m, n, reinterpret_cast<const float *>(256), m)) return 0;
+    const size_t nblk = (n + wide::kNb - 1) / wide::kNb;
+    return nblk > 1 ? (nblk - 1) * stage_vcache_stride(m) : 0;
+}
 
 template <class TH, class TL>
 int gels_refine(size_t m, size_t n, size_t nrhs, const TH *a, size_t lda, const TH *b, size_t ldb, TH *x, size_t ldx, int max_iter, int flags, RefineInfo *info, size_t *lwork, TH *work,
@@ -227,6 +237,8 @@ int gels_refine(size_t m, size_t n, size_t nrhs, const TH *a, size_t lda, const 
             if constexpr (std::is_same<TL, float>::value) {
                 cw.range_ready = hs->ev_prep;
                 cw.nranges = hs->nchunk;
+                cw.vcache = hs->vcache;
+                cw.vcache_stride = hs->vstride;
             } else {
                 RNPGPU_CHECK(cudaStreamWaitEvent(st, hs->ev_all, 0));
             }
@@ -496,10 +508,11 @@ int gels_refine_host(size_t m, size_t n, size_t nrhs, const TH *a, size_t lda, c
     if (m > (size_t)INT32_MAX || nrhs > (size_t)INT32_MAX) return -1;
     auto al = [](size_t bytes) { return (bytes + 255) / 256 * 256; };
     const size_t da = al(m * n * sizeof(TH)), db = al(m * nrhs * sizeof(TH)), dx = al(n * nrhs * sizeof(TH));
+    const size_t dvc = std::is_same<TL, float>::value ? al(stage_vcache_bytes(m, n)) : 0;
     size_t inner = 0;
     int rc = gels_refine<TH, TL>(m, n, nrhs, nullptr, m, nullptr, m, nullptr, n, max_iter, flags, nullptr, &inner, nullptr);
     if (rc) return rc;
-    const size_t need = elems_for<TH>(da + db + dx) + inner;
+    const size_t need = elems_for<TH>(da + db + dx + dvc) + inner;
     if (work == nullptr || *lwork == 0) {
         *lwork = need;
         return kOk;
@@ -516,6 +529,7 @@ int gels_refine_host(size_t m, size_t n, size_t nrhs, const TH *a, size_t lda, c
     TH *dA = cv.take<TH>(da / sizeof(TH));
     TH *dB = cv.take<TH>(db / sizeof(TH));
     TH *dX = cv.take<TH>(dx / sizeof(TH));
+    unsigned char *vcache = dvc ? cv.take<unsigned char>(dvc) : nullptr;
     TH *wrest = cv.take<TH>(0);
     size_t lw = *lwork - (size_t)(wrest - work);
     // the staging streams start after the caller's earlier work on this
@@ -529,7 +543,7 @@ int gels_refine_host(size_t m, size_t n, size_t nrhs, const TH *a, size_t lda, c
         RNPGPU_CHECK(cudaMemcpy2DAsync(dA + c0 * m, m * sizeof(TH), a + c0 * lda, lda * sizeof(TH), m * sizeof(TH), w, cudaMemcpyHostToDevice, sc->copy));
         RNPGPU_CHECK(cudaEventRecord(sc->ev_copy[c], sc->copy));
     }
-    HostStage hs{sc->prep, sc->ev_copy.data(), sc->ev_prep.data(), nchunk, sc->ev_all};
+    HostStage hs{sc->prep, sc->ev_copy.data(), sc->ev_prep.data(), nchunk, sc->ev_all, vcache, stage_vcache_stride(m)};
     rc = gels_refine<TH, TL>(m, n, nrhs, dA, m, dB, m, dX, n, max_iter, flags, info, &lw, wrest, &hs);
     // the caller's stream also waits for every copy (a failed call may have
     // returned before it waited for them)

@@ -532,6 +532,10 @@ struct CqrWs {
     // the rest is still copied.
     const cudaEvent_t *range_ready = nullptr;
     int nranges = 0;
+    // left-looking only: block b's V slice images at vcache + b * vcache_stride
+    // (made by its first application, reused by the later ones)
+    unsigned char *vcache = nullptr;
+    size_t vcache_stride = 0;
     // when set, the 128 x 128 T of every wide block is kept here (block b at
     // t128 + b * 128 * 128, row-major); geqrf reports in nwide how many
     // leading 128-column blocks have one
@@ -709,8 +713,9 @@ template <class T> int geqrf(size_t m, size_t n, T *a, size_t lda, T *tau, size_
                 for (int b0 = 0; b0 < jb; ++b0) {
                     const size_t j0 = (size_t)b0 * wide::kNb;
                     float *tsave = cqr->t128 ? cqr->t128 + (size_t)b0 * wide::kNb * wide::kNb : nullptr;
+                    unsigned char *vc = (cqr->vcache && tsave) ? cqr->vcache + (size_t)b0 * cqr->vcache_stride : nullptr;
                     rc = wide::apply(a, lda, (int)m, (int)cend, (int)j0, Tstore + (j0 / nb) * kPanelMaxCols * kPanelMaxCols, (size_t)kPanelMaxCols * kPanelMaxCols, cqr->wide, st, tsave,
-                                     (int)i);
+                                     (int)i, vc, vc != nullptr && jb > b0 + 1);
                     if (rc) return rc;
                     if (tsave && cqr->nwide == b0) cqr->nwide = b0 + 1;
                 }

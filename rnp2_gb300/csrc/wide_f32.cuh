@@ -776,18 +776,26 @@ inline bool usable(size_t m, size_t n, const float *a, size_t lda) {
 // 128-column range of a left-looking order) with the four 32 x 32 panel
 // factors at Tp (tstride apart).  The block's 128 x 128 T (row-major) goes to
 // Tsave when given (kept for later applications of Q), else to the workspace.
-inline int apply(float *A, size_t lda, int m, int n, int r0, const float *Tp, size_t tstride, const WideWs &w, cudaStream_t st, float *Tsave = nullptr, int c1_at = -1) {
+// vcache (optional): the block's own V slice images (va_bytes(rows) +
+// vb_bytes(rows) bytes) instead of the workspace's; with reuse they already
+// hold this block's slices and Tsave its T from an earlier call, so the
+// slicing and the T build are skipped.
+inline int apply(float *A, size_t lda, int m, int n, int r0, const float *Tp, size_t tstride, const WideWs &w, cudaStream_t st, float *Tsave = nullptr, int c1_at = -1,
+                 unsigned char *vcache = nullptr, bool reuse = false) {
     const int rows = m - r0, c1 = c1_at >= 0 ? c1_at : r0 + kNb, nc = n - c1;
     if (c1 < r0 + kNb) return kErrDevice;
+    if (reuse && (vcache == nullptr || Tsave == nullptr)) return kErrDevice;
     if (rows <= 0 || nc <= 0) return kOk;
     const int sms = std::max(1, device_facts().sm_count);
     int *status = device_status_ptr();
     int rc;
-    {
+    unsigned char *va = vcache ? vcache : w.va;
+    unsigned char *vb = vcache ? vcache + al256(va_bytes(rows)) : w.vb;
+    if (!reuse) {
         KScope ks("wide_vsplit", st);
         const int smem = 128 * 129 * 4;
         if ((rc = kernel_attr((const void *)k_wide_vsplit<0>, smem))) return rc;
-        k_wide_vsplit<0><<<(rows + 127) / 128, 256, smem, st>>>(A + r0 + (size_t)r0 * lda, lda, rows, w.va, w.vb);
+        k_wide_vsplit<0><<<(rows + 127) / 128, 256, smem, st>>>(A + r0 + (size_t)r0 * lda, lda, rows, va, vb);
         RNPGPU_CHECK_LAUNCH();
     }
     const int ntile = 1 + (nc + kNb - 1) / kNb;
@@ -802,7 +810,7 @@ inline int apply(float *A, size_t lda, int m, int n, int r0, const float *Tp, si
         if ((rc = kernel_attr((const void *)k_wide_w<0>, kWSmem))) return rc;
         WArgs wa;
         wa.rows = rows; wa.r0 = r0; wa.c1 = c1; wa.ntile = ntile; wa.nsplit = nsplit; wa.rows_per_split = rps;
-        wa.vb = w.vb; wa.P = w.P; wa.status = status;
+        wa.vb = vb; wa.P = w.P; wa.status = status;
         k_wide_w<0><<<dim3(nsplit, ntile), kWThreads, kWSmem, st>>>(map, wa);
         RNPGPU_CHECK_LAUNCH();
     }
@@ -810,10 +818,12 @@ inline int apply(float *A, size_t lda, int m, int n, int r0, const float *Tp, si
         KScope ks("wide_t", st);
         k_wide_reduce<0><<<ntile * 128, 128, 0, st>>>(w.P, nsplit, ntile, w.GW);
         RNPGPU_CHECK_LAUNCH();
-        if ((rc = kernel_attr((const void *)k_wide_t<0>, kTSmem))) return rc;
         float *Tb = Tsave ? Tsave : w.T;
-        k_wide_t<0><<<1, kTThreads, kTSmem, st>>>(w.GW, Tp, tstride, 4, Tb);
-        RNPGPU_CHECK_LAUNCH();
+        if (!reuse) {
+            if ((rc = kernel_attr((const void *)k_wide_t<0>, kTSmem))) return rc;
+            k_wide_t<0><<<1, kTThreads, kTSmem, st>>>(w.GW, Tp, tstride, 4, Tb);
+            RNPGPU_CHECK_LAUNCH();
+        }
         const int J = (nc + kUpdCols - 1) / kUpdCols;
         if ((rc = kernel_attr((const void *)k_wide_y<0>, kYSmem))) return rc;
         k_wide_y<0><<<J * kUpdCols / 16, 256, kYSmem, st>>>(w.GW, Tb, nc, w.y);
@@ -829,7 +839,7 @@ inline int apply(float *A, size_t lda, int m, int n, int r0, const float *Tp, si
         const int per = std::max(1, std::min(sms / J, ntr));
         UArgs ua;
         ua.rows = rows; ua.r0 = r0; ua.c1 = c1; ua.ntiles_r = ntr; ua.J = J;
-        ua.va = w.va; ua.yimg = w.y; ua.status = status;
+        ua.va = va; ua.yimg = w.y; ua.status = status;
         k_wide_update<0><<<J * per, kUThreads, kUSmem, st>>>(map, ua);
         RNPGPU_CHECK_LAUNCH();
     }
