@@ -70,8 +70,10 @@ int rnpgpu_dsgels(size_t m, size_t n, size_t nrhs, const double *a, size_t lda, 
  * FP32 factor runs left-looking by 128-column blocks: each range is brought
  * up to date by the blocks left of it once it has landed); b travels on the
  * library's stream first and x comes back on it last.  work (device) holds
- * A, b and x (m n + m nrhs + n nrhs elements, each rounded up to 256 bytes)
- * and the workspace of rnpgpu_dsgels; the query as rnpgpu_dsgels.  The call
+ * A, b and x (m n + m nrhs + n nrhs elements, each rounded up to 256 bytes),
+ * the tensor-core slice images of every 128-column block of the factor but
+ * the last (about 1.5 KB per row and block, so that each block is sliced
+ * once) and the workspace of rnpgpu_dsgels; the query as rnpgpu_dsgels.  The call
  * returns with x enqueued (synchronize the library's stream before reading
  * it).  The stopping tests and the info are those of rnpgpu_dsgels; x agrees
  * with rnpgpu_dsgels's to the refinement's accuracy (the FP32 factor's
