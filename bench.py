@@ -547,8 +547,9 @@ def other_configs(torch, dev, gq, lib, peak64, check=True, only_c2=False):
 # launch, and that launch's algorithmic bytes): the reported traffic is scaled
 # to the average launch by the algorithmic bytes (traffic grows with the
 # columns and rows processed).  Captured launches: the 65,408 x 32 panels, the
-# update and W of the 65,408-row step with 352 trailing columns, one residual
-# r = b - A x and one A^T r of the 65536 x 512 x 16 refinement; the
+# one-launch rank-32 apply on 64 columns at 65,440 rows (C's writes still in
+# L2 at the end), the W of the 65,408-row step with 352 trailing columns, one
+# residual r = b - A x and one A^T r of the 65536 x 512 x 16 refinement; the
 # tensor-core W and update of the first 128-column block at 32768 rows
 # (384 trailing columns; the update's writes of C were still in L2 when the
 # capture ended).
@@ -557,7 +558,7 @@ NCU_TRAFFIC = {
     "wide_update": (75.826944e6 + 2.329088e6, 2.0 * 32768 * 384 * 4 + 32768 * 128 * 4.0),
     "panel": (8.494080e6 + 0.003072e6, 2.0 * 65408 * 32 * 4),
     "panel_cqr": (8.489984e6 + 0.0, 2.0 * 65408 * 32 * 4),
-    "larfb_update": (100.581632e6 + 32.246784e6, 2.0 * 65408 * 352 * 4 + 65408 * 32 * 4.0),
+    "larfb_update": (25.059072e6 + 0.0, 65440 * (2.0 * 64 + 32) * 4),
     "larfb_w": (100.586240e6 + 3.193088e6, 65408 * 352 * 4.0 + 65408 * 32 * 4.0),
     "residual_fp64": (277.589248e6 + 5.319424e6, 65536 * 512 * 8.0 + 2.0 * 65536 * 16 * 8),
     "normal_eq_fp64": (285.316352e6 + 3.713280e6, 65536 * 512 * 8.0 + 65536 * 16 * 8.0 + 65536 * 256.0),
@@ -578,12 +579,14 @@ def kernel_rooflines(prof, tot_ms, top_name, peak64, steps):
     average CUDA-event duration per launch.  The FP32 factor runs in
     128-column blocks: 16 panels of 32 columns on 65536 - 32 i rows; inside
     each block the panels update the block's remaining 96, 64, 32 columns
-    with the rank-32 passes (12 updates); after each of the first three
-    blocks one tensor-core update covers the remaining 384, 256, 128
-    columns."""
+    with the rank-32 passes (12 updates: the 64- and 32-column ones in one
+    launch each, k_apply32, W included; the 96-column one as W partials, their
+    sum times T and the update); after each of the first three blocks one
+    tensor-core update covers the remaining 384, 256, 128 columns."""
     nb, wb = 32, 128
     panels = [(M - nb * i, nb) for i in range(N // nb)]
     inner = [(M - wb * j - nb * p, wb - nb * (p + 1)) for j in range(N // wb) for p in range(wb // nb - 1)]
+    inner_w = [(m, c) for m, c in inner if c > 64]  # the updates that still take separate W launches
     outer = [(M - wb * j, N - wb * (j + 1)) for j in range(N // wb - 1)]
     mean = lambda xs: sum(xs) / len(xs)
     hbm, hbm_src = measured_hbm_gbs()
@@ -593,9 +596,9 @@ def kernel_rooflines(prof, tot_ms, top_name, peak64, steps):
         "panel_cqr": ("hbm", mean([2.0 * m * c * 4 for m, c in panels]),
                       "k_panel_cqr: FP32 CholeskyQR2 panel with Householder reconstruction, rows read and written once (2 m 32 x 4 B)"),
         "larfb_update": ("hbm", mean([2.0 * m * c * 4 + m * nb * 4.0 for m, c in inner]),
-                         "k_update_f32: rank-32 update inside a 128-column block, C read and written once, V read once"),
-        "larfb_w": ("hbm", mean([m * c * 4.0 + m * nb * 4.0 for m, c in inner]),
-                    "k_w_f32 + k_reduce_times_t: W = C^T V partials inside a 128-column block, C and V read once"),
+                         "k_apply32 (64 and 32 columns, W included) and k_update_f32 (96 columns): rank-32 updates inside a 128-column block, C read and written once, V read once"),
+        "larfb_w": ("hbm", mean([m * c * 4.0 + m * nb * 4.0 for m, c in inner_w]),
+                    "k_w_f32 + k_reduce_times_t: W = C^T V partials of the 96-column update inside a 128-column block, C and V read once"),
         "wide_w": ("hbm", mean([m * c * 4.0 + m * wb * 4.0 for m, c in outer]),
                    "wide::k_wide_w: W = C^T V and V^T V for a 128-column block on tcgen05 (three BF16 slices), C and V read once"),
         "wide_update": ("hbm", mean([2.0 * m * c * 4 + m * wb * 4.0 for m, c in outer]),
