@@ -410,15 +410,16 @@ template <int kTag = 0> __global__ void __launch_bounds__(128) k_wide_reduce(con
 // factors Tp (column-major, 32 x 32 each, kTstride apart) and G = V^T V
 // (GW tile 0, G[v][c]).  T(0:32b, blk b) = -T(0:32b, 0:32b) G(0:32b, blk b) T_b.
 // ---------------------------------------------------------------------------
-constexpr int kTSmem = (128 * 129 + 2 * 96 * 33) * 4;
+constexpr int kTLd = 132, kTGld = 36;  // row strides (16-byte rows for float4 loads)
+constexpr int kTSmem = (128 * kTLd + 96 * kTGld + 96 * 33) * 4;
 constexpr int kTThreads = 1024;
 template <int kTag = 0> __global__ void __launch_bounds__(kTThreads) k_wide_t(const float *GW, const float *Tp, size_t tstride, int nblk, float *Tout) {
     extern __shared__ __align__(16) float s_t[];
-    float (*sT)[129] = reinterpret_cast<float (*)[129]>(s_t);
-    float (*sX)[33] = reinterpret_cast<float (*)[33]>(s_t + 128 * 129);
-    float (*sG)[33] = reinterpret_cast<float (*)[33]>(s_t + 128 * 129 + 96 * 33);
-    const int tid = threadIdx.x;
-    for (int idx = tid; idx < 128 * 128; idx += kTThreads) sT[idx >> 7][idx & 127] = 0.f;
+    float (*sT)[kTLd] = reinterpret_cast<float (*)[kTLd]>(s_t);
+    float (*sG)[kTGld] = reinterpret_cast<float (*)[kTGld]>(s_t + 128 * kTLd);
+    float (*sX)[33] = reinterpret_cast<float (*)[33]>(s_t + 128 * kTLd + 96 * kTGld);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int idx = tid; idx < 128 * kTLd; idx += kTThreads) (&sT[0][0])[idx] = 0.f;
     __syncthreads();
     // the panel factors: 4 x 1024 values, upper triangles only (the panels
     // leave whatever the workspace held below their diagonals)
@@ -435,6 +436,9 @@ template <int kTag = 0> __global__ void __launch_bounds__(kTThreads) k_wide_t(co
             if (b < nblk) sT[32 * b + (e & 31)][32 * b + (e >> 5)] = v[i];
         }
     }
+    // warp w forms rows w, w + 32, w + 64 of each product, lane = column:
+    // the row operand comes as float4 broadcasts, the column operand one
+    // value per lane (four FMAs per five shared loads instead of one per two)
     for (int b = 1; b < nblk; ++b) {
         const int nr = 32 * b;
         // G(0:nr, blk b)
@@ -452,32 +456,43 @@ template <int kTag = 0> __global__ void __launch_bounds__(kTThreads) k_wide_t(co
             }
         }
         __syncthreads();
-        // X = G(0:nr, blk b) T_b  (two partial sums per entry)
-        for (int idx = tid; idx < nr * 32; idx += kTThreads) {
-            const int r = idx >> 5, c = idx & 31;
-            float a0 = 0.f, a1 = 0.f;
-            int l = 0;
-            for (; l + 1 <= c; l += 2) {
-                a0 = fmaf(sG[r][l], sT[32 * b + l][32 * b + c], a0);
-                a1 = fmaf(sG[r][l + 1], sT[32 * b + l + 1][32 * b + c], a1);
+        // X = G(0:nr, blk b) T_b  (T_b upper: zeros below its diagonal in sT)
+        {
+            float x[3] = {0.f, 0.f, 0.f};
+            for (int l = 0; l < 32; l += 4) {
+                const float t0 = sT[32 * b + l][32 * b + lane], t1 = sT[32 * b + l + 1][32 * b + lane];
+                const float t2 = sT[32 * b + l + 2][32 * b + lane], t3 = sT[32 * b + l + 3][32 * b + lane];
+#pragma unroll
+                for (int i = 0; i < 3; ++i) {
+                    const int r = warp + 32 * i;
+                    if (r < nr) {
+                        const float4 gv = *reinterpret_cast<const float4 *>(&sG[r][l]);
+                        x[i] = fmaf(gv.w, t3, fmaf(gv.z, t2, fmaf(gv.y, t1, fmaf(gv.x, t0, x[i]))));
+                    }
+                }
             }
-            if (l <= c) a0 = fmaf(sG[r][l], sT[32 * b + l][32 * b + c], a0);
-            sX[r][c] = a0 + a1;
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+                if (warp + 32 * i < nr) sX[warp + 32 * i][lane] = x[i];
         }
         __syncthreads();
-        // T(0:nr, blk b) = -T(0:nr, 0:nr) X  (upper: l >= r), four partial sums
-        for (int idx = tid; idx < nr * 32; idx += kTThreads) {
-            const int r = idx >> 5, c = idx & 31;
-            float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
-            int l = r;
-            for (; l + 3 < nr; l += 4) {
-                a0 = fmaf(sT[r][l], sX[l][c], a0);
-                a1 = fmaf(sT[r][l + 1], sX[l + 1][c], a1);
-                a2 = fmaf(sT[r][l + 2], sX[l + 2][c], a2);
-                a3 = fmaf(sT[r][l + 3], sX[l + 3][c], a3);
+        // T(0:nr, blk b) = -T(0:nr, 0:nr) X  (T upper: zeros left of its diagonal)
+        {
+            float acc[3] = {0.f, 0.f, 0.f};
+            for (int l = (warp & ~3); l < nr; l += 4) {
+                const float x0 = sX[l][lane], x1 = sX[l + 1][lane], x2 = sX[l + 2][lane], x3 = sX[l + 3][lane];
+#pragma unroll
+                for (int i = 0; i < 3; ++i) {
+                    const int r = warp + 32 * i;
+                    if (r < nr && l + 3 >= r) {
+                        const float4 tv = *reinterpret_cast<const float4 *>(&sT[r][l]);
+                        acc[i] = fmaf(tv.w, x3, fmaf(tv.z, x2, fmaf(tv.y, x1, fmaf(tv.x, x0, acc[i]))));
+                    }
+                }
             }
-            for (; l < nr; ++l) a0 = fmaf(sT[r][l], sX[l][c], a0);
-            sT[r][32 * b + c] = -((a0 + a1) + (a2 + a3));
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+                if (warp + 32 * i < nr) sT[warp + 32 * i][32 * b + lane] = -acc[i];
         }
         __syncthreads();
     }
