@@ -250,6 +250,13 @@ int gels_refine(size_t m, size_t n, size_t nrhs, const TH *a, size_t lda, const 
         RNPGPU_CHECK_LAUNCH();
     }
     size_t lw = lwq;
+    std::vector<double> h(n + 6 * nrhs);
+    if constexpr (!use_oz) {
+        k_col_sumsq<TH><<<cb, 256, 0, st>>>((int)m, (int)n, a, lda, dn);
+        RNPGPU_CHECK_LAUNCH();
+    }
+    k_col_sumsq<TH><<<cb, 256, 0, st>>>((int)m, (int)nrhs, b, ldb, dn + n);
+    RNPGPU_CHECK_LAUNCH();
     if constexpr (std::is_same<TL, float>::value) {
         // FP32 factor with CholeskyQR2 panels; a panel whose Gram matrix is
         // too ill-conditioned for them sends the whole factorization back to
@@ -279,14 +286,8 @@ int gels_refine(size_t m, size_t n, size_t nrhs, const TH *a, size_t lda, const 
     }
 
     // ||A||_F (real FP64 data: from the FP32 working copy, which only scales
-    // the stopping test) and ||b_j|| in FP64
-    std::vector<double> h(n + 6 * nrhs);
-    if constexpr (!use_oz) {
-        k_col_sumsq<TH><<<cb, 256, 0, st>>>((int)m, (int)n, a, lda, dn);
-        RNPGPU_CHECK_LAUNCH();
-    }
-    k_col_sumsq<TH><<<cb, 256, 0, st>>>((int)m, (int)nrhs, b, ldb, dn + n);
-    RNPGPU_CHECK_LAUNCH();
+    // the stopping test) and ||b_j|| in FP64: computed before the factor, read
+    // back after it (one wait for the factor's flag and the norms)
     RNPGPU_CHECK(cudaMemcpyAsync(h.data(), dn, (n + nrhs) * sizeof(double), cudaMemcpyDeviceToHost, st));
     RNPGPU_CHECK(cudaStreamSynchronize(st));
     double asq = 0.0;
@@ -407,6 +408,12 @@ int gels_refine(size_t m, size_t n, size_t nrhs, const TH *a, size_t lda, const 
             if ((rc = launch_gemm(gr, 1, st, "residual_fp64"))) return rc;
         }
         ++it;
+        if (it == 1 && max_iter > 1) {
+            // from x = 0 the first correction is x itself (size 1): nothing
+            // to decide yet, so no read-back (and no host wait) here
+            prev_corr = corr = 1.0;
+            continue;
+        }
         if ((rc = correction_size(corr))) return rc;
         if (std::isnan(corr)) {
             if ((rc = check())) return rc;
