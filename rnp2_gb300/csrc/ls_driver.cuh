@@ -149,7 +149,8 @@ template <class TH, class TL> struct RefinePlan {
 // kStageCols columns on a copy stream, ev_copy[c] recorded after range c.
 constexpr int kStageCols = 128;
 struct HostStage {
-    cudaStream_t prep;        // prepares each range once it has landed
+    cudaStream_t prep;        // converts each range to FP32 once it has landed
+    cudaStream_t dig;         // (lower priority) the packed digits and norms of each range
     const cudaEvent_t *ev_copy;
     const cudaEvent_t *ev_prep;  // range c prepared (recorded by the staging)
     int nchunk;
@@ -226,13 +227,23 @@ int gels_refine(size_t m, size_t n, size_t nrhs, const TH *a, size_t lda, const 
             // stream once its copy has landed; the factor starts after the
             // first range and waits for the rest before it updates columns
             // past its first block
+            // the factor needs only the FP32 copy of a range: it is made first,
+            // on its own stream; the digits of the residual products and the
+            // column norms follow on a lower-priority stream, done long before
+            // the refinement reads them
             for (int c = 0; c < hs->nchunk; ++c) {
                 const int c0 = c * kStageCols, w = (int)std::min<size_t>(kStageCols, n - (size_t)c0);
                 RNPGPU_CHECK(cudaStreamWaitEvent(hs->prep, hs->ev_copy[c], 0));
-                if ((rc = oz_prepare_cols((int)m, (int)n, c0, w, a, lda, ow, dn, Af, m, hs->prep))) return rc;
+                k_convert<TH, TL><<<dim3((unsigned)std::min<size_t>((m + 255) / 256, 2048), (unsigned)w), 256, 0, hs->prep>>>((int)m, w, a + (size_t)c0 * lda, lda,
+                                                                                                                    Af + (size_t)c0 * m, m);
+                RNPGPU_CHECK_LAUNCH();
                 RNPGPU_CHECK(cudaEventRecord(hs->ev_prep[c], hs->prep));
+                RNPGPU_CHECK(cudaStreamWaitEvent(hs->dig, hs->ev_prep[c], 0));
+                if ((rc = oz_prepare_cols((int)m, (int)n, c0, w, a, lda, ow, nullptr, nullptr, m, hs->dig))) return rc;
+                oz::k_col_sumsq_f32<0><<<(unsigned)std::min(w, 8192), 256, 0, hs->dig>>>((int)m, w, Af + (size_t)c0 * m, m, dn + c0);
+                RNPGPU_CHECK_LAUNCH();
             }
-            RNPGPU_CHECK(cudaEventRecord(hs->ev_all, hs->prep));
+            RNPGPU_CHECK(cudaEventRecord(hs->ev_all, hs->dig));
             RNPGPU_CHECK(cudaStreamWaitEvent(st, hs->ev_prep[0], 0));
             if constexpr (std::is_same<TL, float>::value) {
                 cw.range_ready = hs->ev_prep;
@@ -472,7 +483,7 @@ int gels_refine(size_t m, size_t n, size_t nrhs, const TH *a, size_t lda, const 
 // Workspace: A, b and x on the device, then gels_refine's.
 // ---------------------------------------------------------------------------
 struct StageCtx {
-    cudaStream_t copy = nullptr, prep = nullptr;
+    cudaStream_t copy = nullptr, prep = nullptr, dig = nullptr;
     cudaEvent_t ev_start = nullptr, ev_all = nullptr;
     std::vector<cudaEvent_t> ev_copy, ev_prep;
 };
@@ -484,7 +495,13 @@ inline StageCtx *stage_ctx(int nchunk) {
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDev) return nullptr;
     StageCtx &c = ctx[dev];
     if (state[dev] == 0) {
+        int least = 0, greatest = 0;
+        if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) {
+            cudaGetLastError();
+            least = greatest = 0;
+        }
         const bool ok = cudaStreamCreateWithFlags(&c.copy, cudaStreamNonBlocking) == cudaSuccess && cudaStreamCreateWithFlags(&c.prep, cudaStreamNonBlocking) == cudaSuccess &&
+                        cudaStreamCreateWithPriority(&c.dig, cudaStreamNonBlocking, least) == cudaSuccess &&
                         cudaEventCreateWithFlags(&c.ev_start, cudaEventDisableTiming) == cudaSuccess && cudaEventCreateWithFlags(&c.ev_all, cudaEventDisableTiming) == cudaSuccess;
         state[dev] = ok ? 1 : 2;
         if (!ok) cudaGetLastError();
@@ -544,19 +561,22 @@ int gels_refine_host(size_t m, size_t n, size_t nrhs, const TH *a, size_t lda, c
     RNPGPU_CHECK(cudaEventRecord(sc->ev_start, st));
     RNPGPU_CHECK(cudaStreamWaitEvent(sc->copy, sc->ev_start, 0));
     RNPGPU_CHECK(cudaStreamWaitEvent(sc->prep, sc->ev_start, 0));
+    RNPGPU_CHECK(cudaStreamWaitEvent(sc->dig, sc->ev_start, 0));
     RNPGPU_CHECK(cudaMemcpy2DAsync(dB, m * sizeof(TH), b, ldb * sizeof(TH), m * sizeof(TH), nrhs, cudaMemcpyHostToDevice, st));
     for (int c = 0; c < nchunk; ++c) {
         const size_t c0 = (size_t)c * kStageCols, w = std::min<size_t>(kStageCols, n - c0);
         RNPGPU_CHECK(cudaMemcpy2DAsync(dA + c0 * m, m * sizeof(TH), a + c0 * lda, lda * sizeof(TH), m * sizeof(TH), w, cudaMemcpyHostToDevice, sc->copy));
         RNPGPU_CHECK(cudaEventRecord(sc->ev_copy[c], sc->copy));
     }
-    HostStage hs{sc->prep, sc->ev_copy.data(), sc->ev_prep.data(), nchunk, sc->ev_all, vcache, stage_vcache_stride(m)};
+    HostStage hs{sc->prep, sc->dig, sc->ev_copy.data(), sc->ev_prep.data(), nchunk, sc->ev_all, vcache, stage_vcache_stride(m)};
     rc = gels_refine<TH, TL>(m, n, nrhs, dA, m, dB, m, dX, n, max_iter, flags, info, &lw, wrest, &hs);
     // the caller's stream also waits for every copy (a failed call may have
     // returned before it waited for them)
     RNPGPU_CHECK(cudaEventRecord(sc->ev_start, sc->copy));
     RNPGPU_CHECK(cudaStreamWaitEvent(st, sc->ev_start, 0));
     RNPGPU_CHECK(cudaEventRecord(sc->ev_start, sc->prep));
+    RNPGPU_CHECK(cudaStreamWaitEvent(st, sc->ev_start, 0));
+    RNPGPU_CHECK(cudaEventRecord(sc->ev_start, sc->dig));
     RNPGPU_CHECK(cudaStreamWaitEvent(st, sc->ev_start, 0));
     if (rc) return rc;
     RNPGPU_CHECK(cudaMemcpy2DAsync(x, ldx * sizeof(TH), dX, n * sizeof(TH), n * sizeof(TH), nrhs, cudaMemcpyDeviceToHost, st));
