@@ -123,3 +123,19 @@ def test_consumer_arguments_are_rejected(lib):
     assert lib.rnpgpu_cgg_triangularize_b(10, 0, 10, None, 10, None, 10, None, 1, None, 1, None, None) == -12
     lw = C.c_size_t(0)
     assert lib.rnpgpu_zgg_triangularize_b(100, 0, 100, None, 100, None, 100, None, 1, None, 1, C.byref(lw), None) == 0 and lw.value > 100
+
+
+def test_host_buffer_solve_arguments_are_rejected(lib):
+    """rnpgpu_dsgels_host checks its shapes and leading dimensions before any
+    device call (argument positions as in ls_gb300.h)."""
+    lw = C.c_size_t(0)
+    # m < n, lda < m, ldb < m, ldx < n, no workspace length
+    assert lib.rnpgpu_dsgels_host(10, 11, 1, None, 10, None, 10, None, 11, 0, 0, None, C.byref(lw), None) == -2
+    assert lib.rnpgpu_dsgels_host(10, 4, 1, None, 9, None, 10, None, 4, 0, 0, None, C.byref(lw), None) == -5
+    assert lib.rnpgpu_dsgels_host(10, 4, 1, None, 10, None, 9, None, 4, 0, 0, None, C.byref(lw), None) == -7
+    assert lib.rnpgpu_dsgels_host(10, 4, 1, None, 10, None, 10, None, 3, 0, 0, None, C.byref(lw), None) == -9
+    assert lib.rnpgpu_dsgels_host(10, 4, 1, None, 10, None, 10, None, 4, 0, 0, None, None, None) == -13
+    # an empty problem returns at once and leaves the length alone
+    lw = C.c_size_t(5)
+    assert lib.rnpgpu_dsgels_host(0, 0, 1, None, 1, None, 1, None, 1, 0, 0, None, C.byref(lw), None) == 0
+    assert lw.value == 5
