@@ -219,7 +219,7 @@ def test_mixed_fp32_factor_falls_back_to_householder_panels():
         assert be <= 10 * n * np.finfo(np.float64).eps
 
 
-@pytest.mark.parametrize("m,n,nrhs", [(4096, 300, 3), (2000, 130, 1), (1000, 100, 2), (8192, 512, 16)])
+@pytest.mark.parametrize("m,n,nrhs", [(4096, 300, 3), (2000, 130, 1), (1000, 100, 2), (8192, 512, 16), (4096, 384, 20)])
 def test_gels_refine_host_matches_device_solve(m, n, nrhs):
     """rnpgpu_dsgels_host (host buffers, A staged in 128-column ranges while
     the GPU factors the ranges already landed, left-looking by 128-column
@@ -279,3 +279,28 @@ def test_refinement_reports_nonfinite_data():
     torch.cuda.synchronize()
     assert info["converged"] == 0, info
     assert not np.isfinite(info["backward_error"]), info
+
+
+def test_gels_refine_host_from_pageable_buffers():
+    """Host buffers that are not pinned: the copies are synchronous, the result
+    the same as from pinned buffers (same staged order, same bits)."""
+    m, n, nrhs = 3000, 260, 2
+    g = torch.Generator(device="cuda").manual_seed(11)
+    A = torch.randn((m, n), generator=g, dtype=torch.float64, device="cuda")
+    B = torch.randn((m, nrhs), generator=g, dtype=torch.float64, device="cuda")
+    A_p = torch.empty((n, m), dtype=torch.float64).pin_memory().t()
+    A_p.copy_(A)
+    B_p = torch.empty((nrhs, m), dtype=torch.float64).pin_memory().t()
+    B_p.copy_(B)
+    X_p = torch.empty((nrhs, n), dtype=torch.float64).pin_memory().t()
+    info_p = gls.gels_refine_host(A_p, B_p, X_p)
+    torch.cuda.synchronize()
+    A_u = torch.empty((n, m), dtype=torch.float64).t()
+    A_u.copy_(A)
+    B_u = torch.empty((nrhs, m), dtype=torch.float64).t()
+    B_u.copy_(B)
+    X_u = torch.empty((nrhs, n), dtype=torch.float64).t()
+    info_u = gls.gels_refine_host(A_u, B_u, X_u)
+    torch.cuda.synchronize()
+    assert info_p["converged"] == 1 and info_u == info_p, (info_p, info_u)
+    assert torch.equal(X_u, X_p)
