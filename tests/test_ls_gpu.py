@@ -304,3 +304,30 @@ def test_gels_refine_host_from_pageable_buffers():
     torch.cuda.synchronize()
     assert info_p["converged"] == 1 and info_u == info_p, (info_p, info_u)
     assert torch.equal(X_u, X_p)
+
+
+@pytest.mark.parametrize("rank32,forward", [(True, False), (False, True)])
+def test_gels_refine_host_modes(rank32, forward):
+    """The host-buffer solve with the rank-32 FP32 updates (its staged input
+    then waits for every range before the factor) and in forward mode meets
+    the same stopping tests as the device solve in the same mode."""
+    m, n, nrhs = 4096, 300, 2
+    g = torch.Generator(device="cuda").manual_seed(13 + rank32 + 2 * forward)
+    A = torch.randn((m, n), generator=g, dtype=torch.float64, device="cuda")
+    B = torch.randn((m, nrhs), generator=g, dtype=torch.float64, device="cuda")
+    from rnp2_gb300.qr import to_colmajor
+
+    X, info = gls.gels_refine(to_colmajor(A), to_colmajor(B), forward=forward, rank32=rank32)
+    A_h = torch.empty((n, m), dtype=torch.float64).pin_memory().t()
+    A_h.copy_(A)
+    B_h = torch.empty((nrhs, m), dtype=torch.float64).pin_memory().t()
+    B_h.copy_(B)
+    X_h = torch.empty((nrhs, n), dtype=torch.float64).pin_memory().t()
+    info_h = gls.gels_refine_host(A_h, B_h, X_h, forward=forward, rank32=rank32)
+    torch.cuda.synchronize()
+    assert info["converged"] == 1 and info_h["converged"] == 1, (info, info_h)
+    Xd = X.cpu()
+    assert float((X_h - Xd).abs().max() / Xd.abs().max()) <= 1e-11
+    if rank32:
+        # no left-looking order without the wide blocks: the same operations, the same bits
+        assert torch.equal(X_h, Xd)
